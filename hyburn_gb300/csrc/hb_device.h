@@ -1,0 +1,126 @@
+// hb_device.h — device-side network description shared by the host engine and the kernels.
+//
+// The host engine (hb_engine.cu) lowers a validated hb_sim_desc into these flat tables once per
+// engine (projections, CSR rows with packed per-edge delays) and once per run (per-point model
+// and coupling parameters, noise, BOLD schedules). Kernels receive a DevNet by value.
+#pragma once
+#include <cstdint>
+
+#define HB_MAX_SUB 8
+#define HB_MAX_PROJ 16
+#define HB_MAX_BOLD 4
+#define HB_PSTRIDE 32   // floats per (subnetwork, point) parameter row: params + derived constants
+#define HB_NCP 16       // floats per resolved coupling-function parameter row
+#define HB_MAX_THREADS 1024
+
+// model ids (order of the host registry)
+enum { HBM_G2DO = 0, HBM_MPR = 1, HBM_RWW = 2, HBM_KURAMOTO = 3, HBM_JR = 4, HBM_WC = 5 };
+
+// effective integrators (engine.rs:697-771); HBI_HEUN_DET is the deterministic Heun arm
+enum { HBI_HEUN_DET = 0, HBI_EULER = 1, HBI_EULER_STOCH = 2, HBI_HEUN_STOCH = 3, HBI_RK4 = 4, HBI_RK4_STOCH = 5 };
+
+// coupling functions (coupling.rs:52-71)
+enum { HBC_LINEAR = 0, HBC_SIGMOIDAL, HBC_DIFFERENCE, HBC_KURAMOTO, HBC_SCALED_LINEAR, HBC_TANH, HBC_SJR, HBC_PRESIG };
+
+// weighted-sum kinds
+enum { HBK_MEAN = 0, HBK_DIAG = 1, HBK_SPARSE = 2 };
+
+// delay read modes
+//  HBD_COMPAT: one delay per projection, batch engine shift window (engine.rs:541-589)
+//  HBD_RING:   one delay per projection, true ring (runtime.rs:235-252)
+//  HBD_EDGE:   per-edge delays, true ring, zero rows after pre() (runtime.rs:162-204)
+enum { HBD_COMPAT = 0, HBD_RING = 1, HBD_EDGE = 2 };
+
+// derived-constant slots in a parameter row (computed on the host in f32 with the C library)
+#define HB_D_WC_SIG_E_OFF 24
+#define HB_D_WC_SIG_I_OFF 25
+
+struct DevSub {
+    int model, nm, nvar, ncvar;
+    int thread_off;   // resident kernel: first thread of this subnetwork (warp aligned)
+    int col_off;      // first ring column (columns are [node][cvar])
+    int state_off;    // offset of this subnetwork in a point's packed state [nm][nvar]
+    int noise_off;    // offset in a noise row
+    int integ, sweep_form;
+    int n_in;
+    int in_idx[HB_MAX_PROJ];
+    const float* params;   // [B][HB_PSTRIDE]
+};
+
+struct DevProj {
+    int src, tgt, kind, dmode, delay, nsrc, ntgt;
+    int cfk, pre_cpu, ncv, pc, oc, has_rowsums;
+    int direct, ncm;
+    int cm_s[4], cm_cpl[4];
+    int mean_slot;        // MEAN: index of its partial-sum slot
+    int smem_edges;       // resident kernel: edge offset inside the shared-memory copy, -1 if global
+    float w;
+    float cp[HB_NCP];
+    const float* cp_pp;   // [B][HB_NCP] when the coupling parameters are swept, else nullptr
+    const int* rowptr;    // [ntgt + 1]
+    const uint32_t* edges; // (delay << 16) | src node
+    const float* ew;
+    const float* rowsums;
+};
+
+struct DevNet {
+    int n_sub, n_proj, n_mean;
+    int B;                // sweep points
+    int H;                // horizon (batch: max delay + 1 or 0; ring: max delay + 1)
+    int R;                // ring length (slots)
+    int cols;             // ring columns per point = sum nm * ncvar
+    int state_len;        // floats per point of packed state = sum nm * nvar
+    int noise_row;        // floats per step (per point) of the noise array
+    int total_edges;
+    float dt, dt_half, dt_sixth, dt_h2;
+    float noise_scale[8]; // sqrt(2*nsig[v]) * sqrt(dt)
+    DevSub sub[HB_MAX_SUB];
+    DevProj proj[HB_MAX_PROJ];
+};
+
+// BOLD emission schedule entry: emit output `out` when run-local sample `k` is produced
+struct BoldEmit {
+    int k;       // run-local sample index
+    int out;     // run-local output row
+    int interp;  // 1: prev + (cur - prev) * w ; 0: cur
+    float w;
+};
+
+struct DevBold {
+    int n;                 // number of monitors
+    int per_point;         // 1: one series per point
+    int period[HB_MAX_BOLD];
+    int n_full[HB_MAX_BOLD];      // full windows in this run
+    int partial[HB_MAX_BOLD];     // steps of the flushed partial window (0 if none)
+    float dt_full[HB_MAX_BOLD];   // BW step (s) of a full window
+    float dt_part[HB_MAX_BOLD];   // BW step (s) of the partial window
+    int n_emit[HB_MAX_BOLD];
+    const BoldEmit* emit[HB_MAX_BOLD];
+    float* out[HB_MAX_BOLD];      // per point: [B][n_out_run][N0]; batch mean: [n_out_run][N0]
+    int n_out_run[HB_MAX_BOLD];
+    float* bw[HB_MAX_BOLD];       // BW state [5][B or 1][N0]: s, f, v, q, previous signal
+    float* win[HB_MAX_BOLD];      // batch mean: window sums [W][B][N0]
+    float* acc[HB_MAX_BOLD];      // running window sum [B][N0] carried between launches
+    int n0;                       // nodes of subnetwork 0
+};
+
+// per-launch arguments of the simulation kernels
+struct RunArgs {
+    int64_t s0;           // absolute step of the first step of this launch
+    int n_steps;          // steps in this launch
+    int64_t run_s0;       // absolute step at which the current run started
+    int64_t run_steps;    // total steps of the run
+    float* state;         // [B][state_len]
+    float* tavg;          // [B][state_len]
+    float* ring;          // [B][R][cols] global ring (scratch)
+    const float* noise;   // noise rows of this launch: [n_steps][row] or [n_steps][B][row]
+    int noise_per_point;
+    float* traj;          // [n_steps][B][state_len] or nullptr
+    int ring_in_smem;     // resident kernel: ring cached in shared memory
+    int smem_edges;       // resident kernel: edges cached in shared memory
+    int load_ring;        // copy the global ring into shared memory at launch start
+    int store_ring;       // copy the shared ring back at launch end
+    int* flags;           // [0]: non-finite seen, [1]: bounds error
+    int check_finite;
+    DevBold bold;
+};

@@ -1,0 +1,1163 @@
+// hb_engine.cu — host engine behind the C ABI of include/hyburn_gb300.h.
+//
+// Replaces BatchHybridEngine::from_config / run_sweep* (src/engine/batch_engine/engine.rs) for
+// `--backend cuda`. The host side validates the descriptor with the reference's rules, lowers
+// every projection into one device form (mean-field, diagonal, or CSR rows with packed per-edge
+// delays), builds per-run parameter tables for the sweep, the BOLD emission schedule and the
+// noise upload, and launches the simulation kernels of hb_kernels.cu. There is no host
+// computation of the simulation itself and no fallback path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hb_device.h"
+#include "hyburn_gb300.h"
+
+cudaError_t hb_launch_resident(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
+int hb_resident_static_smem();
+
+namespace {
+
+thread_local std::string g_err;
+
+hb_status fail(hb_status st, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CUDA_TRY(x)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (x);                                                                         \
+        if (e_ != cudaSuccess) return fail(HB_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---- model registry (src/config.rs:43-72); the six batch-native models are supported ----
+struct ModelInfo { const char* name; int nvar, ncvar, nparams, native_sweep, cvar0; };
+const ModelInfo k_models[6] = {
+    {"Generic2dOscillator", 2, 1, 12, 1, 0}, {"MontbrioPazoRoxin", 2, 2, 7, 4, 0}, {"ReducedWongWang", 1, 1, 8, 7, 0},
+    {"Kuramoto", 1, 1, 1, 0, 0},             {"JansenRit", 6, 1, 13, 12, 1},     {"WilsonCowan", 2, 1, 22, 18, 0},
+};
+const char* k_other_models[] = {
+    "Linear", "SupHopf", "Hopfield", "CoombesByrne2D", "CoombesByrne", "GastSchmidtKnoscheSD", "GastSchmidtKnoscheSF",
+    "LarterBreakspear", "Epileptor2D", "Epileptor", "ReducedWongWangExcInh", "DecoBalancedExcInh", "EpileptorCodim3",
+    "EpileptorCodim3SlowMod", "EpileptorRestingState", "ZetterbergJansen", "ReducedSetFitzHughNagumo",
+    "ReducedSetHindmarshRose", "DumontGutkin", "ZerlautAdaptationFirstOrder", "ZerlautAdaptationSecondOrder", "KIonEx"};
+const int k_other_nvar[] = {1, 2, 2, 2, 4, 4, 4, 3, 2, 6, 2, 2, 3, 5, 8, 12, 4, 6, 8, 5, 8, 5};
+const int k_other_ncvar[] = {1, 2, 2, 2, 4, 4, 4, 1, 1, 2, 1, 1, 1, 1, 3, 1, 2, 2, 4, 1, 1, 1};
+const int k_other_np[] = {1, 2, 3, 4, 5, 9, 9, 32, 12, 17, 19, 20, 13, 27, 28, 18, 8, 12, 14, 50, 50, 14};
+
+int model_id(const char* name) {
+    if (!name) return -1;
+    for (int i = 0; i < 6; i++)
+        if (strcmp(name, k_models[i].name) == 0) return i;
+    return -1;
+}
+bool is_other_model(const char* name) {
+    if (!name) return false;
+    for (const char* m : k_other_models)
+        if (strcmp(name, m) == 0) return true;
+    return false;
+}
+
+// ---- coupling functions: CouplingFnConfig::from_name_and_params (coupling.rs:114-202) ----
+struct Cfn {
+    int kind = HBC_LINEAR;
+    float a = 1, b = 0, cmin = 0, cmax = 0, mid = 0, sigma = 1, r = 0, e0 = 0, v0 = 0;
+    int classic = 0;
+    float h = 1, q = 1, g = 1, p = 1, theta = 0.5f;
+    int dynamic = 0, global_t = 0;
+};
+
+bool cfn_parse(const char* name, const float* cp, int n, Cfn& f) {
+    f = Cfn();
+    auto P = [&](int i, float d) { return n > i ? cp[i] : d; };
+    if (!name) return false;
+    if (!strcmp(name, "Linear")) { f.kind = HBC_LINEAR; f.a = P(0, 1.0f); f.b = P(1, 0.0f); }
+    else if (!strcmp(name, "Sigmoidal")) {
+        f.kind = HBC_SIGMOIDAL;
+        if (n >= 5) { f.cmin = cp[0]; f.cmax = cp[1]; f.mid = cp[2]; f.a = cp[3]; f.sigma = cp[4]; }
+        else { f.cmin = -1.0f; f.cmax = P(0, 1.0f); f.mid = P(1, 0.0f); f.a = 1.0f; f.sigma = P(2, 1.0f); }
+    } else if (!strcmp(name, "Difference")) { f.kind = HBC_DIFFERENCE; f.a = P(0, 1.0f); }
+    else if (!strcmp(name, "Kuramoto")) { f.kind = HBC_KURAMOTO; f.a = P(0, 1.0f); }
+    else if (!strcmp(name, "ScaledLinear")) { f.kind = HBC_SCALED_LINEAR; f.a = P(0, 1.0f); f.b = P(1, 0.0f); }
+    else if (!strcmp(name, "HyperbolicTangent")) { f.kind = HBC_TANH; f.a = P(0, 1.0f); f.b = P(1, 1.0f); f.mid = P(2, 0.0f); f.sigma = P(3, 1.0f); }
+    else if (!strcmp(name, "SigmoidalJansenRit")) {
+        f.kind = HBC_SJR;
+        if (n >= 5) { f.a = cp[0]; f.classic = 1; f.cmin = cp[1]; f.cmax = cp[2]; f.r = cp[3]; f.mid = cp[4]; f.e0 = 0.005f; f.v0 = 6.0f; }
+        else { f.a = P(0, 1.0f); f.classic = 0; f.cmin = 0.0f; f.cmax = 0.005f; f.r = P(2, 0.56f); f.mid = 6.0f; f.e0 = P(1, 0.005f); f.v0 = P(3, 6.0f); }
+    } else if (!strcmp(name, "PreSigmoidal")) {
+        f.kind = HBC_PRESIG; f.h = P(0, 1.0f); f.q = P(1, 1.0f); f.g = P(2, 1.0f); f.p = P(3, 1.0f); f.theta = P(4, 0.5f);
+        f.dynamic = (n > 5 && cp[5] != 0.0f); f.global_t = (n > 6 && cp[6] != 0.0f);
+    } else return false;
+    return true;
+}
+
+struct HostSub {
+    int model, nnodes, nmodes, nm, nvar, ncvar, nparams;
+    std::vector<float> params, x0;
+};
+
+enum { W_MEAN = 0, W_DIAG = 1, W_SPARSE = 2 };
+
+struct HostProj {
+    int src, tgt, kind, dmode, delay, nsrc, ntgt;
+    std::string cf_name;
+    std::vector<float> cf_params;
+    int diff_mode = 0;   // 1: Difference became Linear{a,0}; 2: Difference with rowsums
+    Cfn cf;              // resolved with the configured parameters
+    float w = 0;
+    std::vector<int> rowptr;
+    std::vector<uint32_t> edges;
+    std::vector<float> ew, rowsums;
+    int direct = 0, ncm = 0, cm_s[4] = {0, 0, 0, 0}, cm_cpl[4] = {0, 0, 0, 0};
+    int ncv = 1, pc = 1, oc = 1, pre_cpu = 0;
+    // device copies
+    int* d_rowptr = nullptr;
+    uint32_t* d_edges = nullptr;
+    float* d_ew = nullptr;
+    float* d_rowsums = nullptr;
+    float* d_cp_pp = nullptr;
+    size_t cp_pp_cap = 0;
+};
+
+Cfn resolve_cfn(const HostProj& hp, const float* params, int n) {
+    Cfn f;
+    if (!cfn_parse(hp.cf_name.c_str(), params, n, f)) {
+        f = Cfn();  // engine.rs:277-279: unknown names fall back to Linear{a:1,b:0}
+        f.kind = HBC_LINEAR; f.a = 1.0f; f.b = 0.0f;
+    }
+    if (f.kind == HBC_DIFFERENCE && hp.diff_mode == 1) {
+        float a = f.a;
+        f = Cfn();
+        f.kind = HBC_LINEAR; f.a = a; f.b = 0.0f;
+    }
+    return f;
+}
+
+void cfn_to_cp(const Cfn& f, int n_src, float* cp) {
+    for (int i = 0; i < HB_NCP; i++) cp[i] = 0.0f;
+    switch (f.kind) {
+    case HBC_LINEAR: case HBC_SCALED_LINEAR: cp[0] = f.a; cp[1] = f.b; break;
+    case HBC_SIGMOIDAL: cp[0] = f.cmin; cp[1] = f.cmax; cp[2] = f.mid; cp[3] = f.a; cp[4] = f.sigma; break;
+    case HBC_DIFFERENCE: cp[0] = f.a; break;
+    case HBC_KURAMOTO: cp[0] = f.a; cp[1] = f.a / (float)n_src; break;
+    case HBC_TANH: cp[0] = f.a; cp[1] = f.b; cp[2] = f.mid; cp[3] = f.sigma; break;
+    case HBC_SJR: cp[0] = f.a; cp[1] = (float)f.classic; cp[2] = f.cmin; cp[3] = f.cmax; cp[4] = f.r; cp[5] = f.mid; cp[6] = f.e0; cp[7] = f.v0; break;
+    case HBC_PRESIG: cp[0] = f.h; cp[1] = f.q; cp[2] = f.g; cp[3] = f.p; cp[4] = f.theta; cp[5] = (float)f.dynamic; break;
+    }
+}
+
+int parse_cvar_map(const char* s, int* ps, int* pt, int maxn) {
+    int n = 0;
+    std::string str = s ? s : "0:0";
+    size_t pos = 0;
+    while (pos <= str.size() && n < maxn) {
+        size_t e = str.find(',', pos);
+        std::string part = str.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+        size_t a = part.find_first_not_of(" \t"), z = part.find_last_not_of(" \t");
+        if (a != std::string::npos) {
+            part = part.substr(a, z - a + 1);
+            int v1 = 0, v2 = 0;
+            size_t c = part.find(':');
+            if (c != std::string::npos && part.find(':', c + 1) == std::string::npos) {
+                char* endp;
+                std::string l = part.substr(0, c), r = part.substr(c + 1);
+                long x1 = strtol(l.c_str(), &endp, 10);
+                if (*endp || l.empty() || x1 < 0) x1 = 0;
+                long x2 = strtol(r.c_str(), &endp, 10);
+                if (*endp || r.empty() || x2 < 0) x2 = 0;
+                v1 = (int)x1; v2 = (int)x2;
+            }
+            ps[n] = v1; pt[n] = v2; n++;
+        }
+        if (e == std::string::npos) break;
+        pos = e + 1;
+    }
+    return n;
+}
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = std::max<size_t>(count, 1);
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+struct BoldHost {
+    int period;
+    double tr;
+    std::vector<double> times;   // all BOLD sample times so far (ms)
+    int64_t n_out = 0;           // TR outputs produced so far
+    std::vector<float> out;      // batch mean: [n_out][N0]; per point: [B][n_out][N0]
+    DBuf<float> bw, acc, win, out_run;
+    DBuf<BoldEmit> emit;
+};
+
+struct RunTables {
+    std::vector<std::vector<float>> params;  // per sub [B][PSTRIDE]
+    std::vector<int> sweep_form;
+    std::vector<std::vector<float>> cp_pp;   // per proj [B][NCP] or empty
+    std::vector<float> param_values;
+};
+
+}  // namespace
+
+struct hb_engine {
+    int B = 0;
+    double dt_ms = 0;
+    int integrator = 0;
+    uint32_t flags = 0;
+    std::vector<float> nsig;
+    std::vector<HostSub> subs;
+    std::vector<HostProj> projs;
+    std::vector<hb_bold_desc> bold_cfg;
+    bool bold_removed = false;   // run_sweep_multi drops the monitors (engine.rs:1330-1333)
+    int H = 0, R = 0, cols = 0, state_len = 0, noise_row = 0, threads = 0, n_mean = 0;
+    DevNet net;
+    DevNet* d_net = nullptr;
+    DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
+    std::vector<DBuf<float>> d_params;
+    DBuf<int> flags_buf;
+    std::vector<BoldHost> bold;
+    cudaStream_t own_stream = nullptr, user_stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t step = 0;
+    double last_ms = 0;
+    int64_t last_launches = 0;
+    int last_kind = 0;
+    // prepared run
+    bool prepared = false;
+    RunTables prep_tables;
+    int64_t prep_steps = 0;
+    uint32_t prep_flags = 0;
+    int64_t prep_noise_len = 0;
+
+    cudaStream_t stream() const { return user_stream ? user_stream : own_stream; }
+};
+
+struct hb_result {
+    int n_sweep = 0;
+    double elapsed_ms = 0;
+    std::vector<float> params;
+    std::vector<std::vector<float>> tavg, fin, traj;
+    bool has_traj = false;
+    std::vector<std::vector<float>> bold;
+    int n_bold = 0;
+};
+
+namespace {
+
+int eff_integrator(const hb_engine* e, int model) {
+    bool use_heun = (e->flags & HB_SEM_HYBRID_INTEGRATOR) ? (model == HBM_G2DO) : (e->integrator == HB_INT_HEUN);
+    if (use_heun) return HBI_HEUN_DET;
+    switch (e->integrator) {
+    case HB_INT_EULER: return HBI_EULER;
+    case HB_INT_EULER_STOCHASTIC: return HBI_EULER_STOCH;
+    case HB_INT_HEUN_STOCHASTIC: return HBI_HEUN_STOCH;
+    case HB_INT_RK4: return HBI_RK4;
+    case HB_INT_RK4_STOCHASTIC: return HBI_RK4_STOCH;
+    default: return HBI_EULER;  // `_ =>` arm: Heun under hybrid integration for non-oscillators
+    }
+}
+
+bool is_stochastic(int integ) { return integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH; }
+
+void fill_derived(int model, float* row) {
+    if (model == HBM_WC) {
+        row[HB_D_WC_SIG_E_OFF] = 1.0f / (1.0f + expf(row[6] * row[7]));
+        row[HB_D_WC_SIG_I_OFF] = 1.0f / (1.0f + expf(row[10] * row[11]));
+    }
+}
+
+// per-run tables for a sweep (engine.rs:477-535 single, 862-940 multi)
+hb_status build_tables(hb_engine* e, const hb_sweep_point* dims, int n_dims, bool multi, RunTables& T) {
+    const int B = e->B;
+    const int ns = (int)e->subs.size(), np = (int)e->projs.size();
+    T.params.assign(ns, std::vector<float>((size_t)B * HB_PSTRIDE, 0.0f));
+    T.sweep_form.assign(ns, 0);
+    T.cp_pp.assign(np, std::vector<float>());
+    for (int i = 0; i < ns; i++)
+        for (int b = 0; b < B; b++) {
+            float* row = &T.params[i][(size_t)b * HB_PSTRIDE];
+            for (int k = 0; k < e->subs[i].nparams; k++) row[k] = e->subs[i].params[k];
+        }
+    std::vector<int> cnt(ns, 0);
+    std::vector<char> proj_swept(np, 0);
+    for (int d = 0; d < n_dims; d++) {
+        int si = dims[d].sub_idx;
+        if (si >= ns || si < -np) return fail(HB_ERR_INVALID_CONFIG, "subnetwork index %d out of range", si);
+        if (si >= 0) cnt[si]++;
+        else {
+            int p = -1 - si;
+            if (dims[d].param_idx < 0 || dims[d].param_idx >= (int)e->projs[p].cf_params.size())
+                return fail(HB_ERR_INVALID_CONFIG, "projection %d has %d coupling params, cannot sweep index %d", p,
+                            (int)e->projs[p].cf_params.size(), dims[d].param_idx);
+            proj_swept[p] = 1;
+        }
+    }
+    // mode per subnetwork: 0 none, 1 native sweep form, 2 per-point parameters (dfun.rs:39-45, 99-133)
+    std::vector<int> mode(ns, 0);
+    for (int i = 0; i < ns; i++) {
+        if (!cnt[i]) continue;
+        if (cnt[i] == 1) {
+            int d0 = 0;
+            while (dims[d0].sub_idx != i) d0++;
+            mode[i] = (dims[d0].param_idx == k_models[e->subs[i].model].native_sweep) ? 1 : 0;
+        } else mode[i] = 2;
+        T.sweep_form[i] = (mode[i] == 1);
+    }
+    for (int p = 0; p < np; p++)
+        if (proj_swept[p]) T.cp_pp[p].assign((size_t)B * HB_NCP, 0.0f);
+    T.param_values.clear();
+    std::vector<float> vals(n_dims);
+    for (int b = 0; b < B; b++) {
+        int64_t rem = b;
+        for (int d = n_dims - 1; d >= 0; d--) {
+            int nv = multi ? dims[d].n_values : B;
+            int64_t idx = multi ? rem % nv : b;
+            if (multi) rem /= nv;
+            vals[d] = dims[d].values[idx];
+        }
+        for (int d = 0; d < n_dims; d++) T.param_values.push_back(vals[d]);
+        for (int d = 0; d < n_dims; d++) {
+            int si = dims[d].sub_idx;
+            if (si < 0 || mode[si] == 0) continue;
+            if (dims[d].param_idx >= 0 && dims[d].param_idx < e->subs[si].nparams)
+                T.params[si][(size_t)b * HB_PSTRIDE + dims[d].param_idx] = vals[d];
+        }
+        for (int p = 0; p < np; p++) {
+            if (!proj_swept[p]) continue;
+            HostProj& hp = e->projs[p];
+            std::vector<float> prm = hp.cf_params;
+            for (int d = 0; d < n_dims; d++)
+                if (dims[d].sub_idx == -1 - p) prm[dims[d].param_idx] = vals[d];
+            Cfn f = resolve_cfn(hp, prm.data(), (int)prm.size());
+            cfn_to_cp(f, hp.nsrc, &T.cp_pp[p][(size_t)b * HB_NCP]);
+        }
+    }
+    for (int i = 0; i < ns; i++)
+        for (int b = 0; b < B; b++) fill_derived(e->subs[i].model, &T.params[i][(size_t)b * HB_PSTRIDE]);
+    return HB_OK;
+}
+
+// BOLD sample times and TR outputs of a run of n_steps (bold_monitor.rs:72-227); fills the emit
+// schedule and returns the number of new outputs
+int64_t bold_schedule(const hb_engine* e, BoldHost& bh, int64_t n_steps, std::vector<BoldEmit>& emit,
+                      int& n_full, int& partial, std::vector<double>& new_times) {
+    const double dt_bold = e->dt_ms * (double)bh.period;
+    const double tr_ms = bh.tr * 1000.0;
+    n_full = (int)(n_steps / bh.period);
+    partial = (int)(n_steps % bh.period);
+    int64_t n_prev = (int64_t)bh.times.size();
+    new_times.clear();
+    for (int k = 0; k < n_full; k++) new_times.push_back((double)(n_prev + k) * dt_bold + dt_bold);
+    if (partial > 0) new_times.push_back((double)(n_prev + n_full) * dt_bold + e->dt_ms * (double)partial);
+    std::vector<double> times = bh.times;
+    times.insert(times.end(), new_times.begin(), new_times.end());
+    emit.clear();
+    const int64_t ns = (int64_t)times.size();
+    if (ns == 0) return 0;
+    if (tr_ms <= 0.0 || std::fabs(tr_ms - dt_bold) < 1e-6) {
+        // native sampling: every sample is an output
+        for (int64_t k = n_prev; k < ns; k++) emit.push_back({(int)(k - n_prev), (int)(k - n_prev), 0, 0.0f});
+        return ns - n_prev;
+    }
+    double max_t = times.back();
+    int64_t n_out = max_t >= tr_ms ? (int64_t)std::floor(max_t / tr_ms) : 0;
+    int64_t j0 = bh.n_out;
+    for (int64_t j = j0; j < n_out; j++) {
+        double tt = (double)(j + 1) * tr_ms;
+        BoldEmit em;
+        em.out = (int)(j - j0);
+        if (tt <= times[0]) { em.k = 0; em.interp = 0; em.w = 0; }
+        else {
+            int64_t idx = 0;
+            for (int64_t k = 1; k < ns; k++) {
+                if (times[k] > tt) { idx = k - 1; break; }
+                idx = k;
+            }
+            if (idx + 1 >= ns) { em.k = (int)idx; em.interp = 0; em.w = 0; }
+            else {
+                double t0 = times[idx], t1 = times[idx + 1];
+                double w = std::fabs(t1 - t0) < 1e-12 ? 0.0 : (tt - t0) / (t1 - t0);
+                w = std::min(1.0, std::max(0.0, w));
+                em.k = (int)(idx + 1); em.interp = 1; em.w = (float)w;
+            }
+        }
+        em.k -= (int)n_prev;  // run-local sample index
+        emit.push_back(em);
+    }
+    std::stable_sort(emit.begin(), emit.end(), [](const BoldEmit& a, const BoldEmit& b) { return a.k < b.k; });
+    return n_out - j0;
+}
+
+hb_status upload_net(hb_engine* e, const RunTables& T) {
+    cudaStream_t st = e->stream();
+    for (size_t i = 0; i < e->subs.size(); i++) {
+        CUDA_TRY(e->d_params[i].ensure(T.params[i].size()));
+        CUDA_TRY(cudaMemcpyAsync(e->d_params[i].p, T.params[i].data(), T.params[i].size() * 4, cudaMemcpyHostToDevice, st));
+        e->net.sub[i].params = e->d_params[i].p;
+        e->net.sub[i].sweep_form = T.sweep_form[i];
+    }
+    for (size_t p = 0; p < e->projs.size(); p++) {
+        HostProj& hp = e->projs[p];
+        if (T.cp_pp[p].empty()) { e->net.proj[p].cp_pp = nullptr; continue; }
+        if (hp.cp_pp_cap < T.cp_pp[p].size()) {
+            if (hp.d_cp_pp) cudaFree(hp.d_cp_pp);
+            CUDA_TRY(cudaMalloc(&hp.d_cp_pp, T.cp_pp[p].size() * 4));
+            hp.cp_pp_cap = T.cp_pp[p].size();
+        }
+        CUDA_TRY(cudaMemcpyAsync(hp.d_cp_pp, T.cp_pp[p].data(), T.cp_pp[p].size() * 4, cudaMemcpyHostToDevice, st));
+        e->net.proj[p].cp_pp = hp.d_cp_pp;
+    }
+    CUDA_TRY(cudaMemcpyAsync(e->d_net, &e->net, sizeof(DevNet), cudaMemcpyHostToDevice, st));
+    return HB_OK;
+}
+
+hb_status reset_bold_device(hb_engine* e) {
+    cudaStream_t st = e->stream();
+    const int N0 = e->subs[0].nnodes;
+    const bool pp = (e->flags & HB_SEM_BOLD_PER_POINT) != 0;
+    const size_t lanes = pp ? (size_t)e->B * N0 : (size_t)N0;
+    for (auto& bh : e->bold) {
+        bh.times.clear();
+        bh.n_out = 0;
+        bh.out.clear();
+        CUDA_TRY(bh.bw.ensure(5 * lanes));
+        std::vector<float> init(5 * lanes, 0.0f);
+        for (size_t i = 0; i < lanes; i++) { init[lanes + i] = 1.0f; init[2 * lanes + i] = 1.0f; init[3 * lanes + i] = 1.0f; }
+        CUDA_TRY(cudaMemcpyAsync(bh.bw.p, init.data(), init.size() * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(bh.acc.ensure((size_t)e->B * N0));
+    }
+    return HB_OK;
+}
+
+// the simulation of one run; noise is a host pointer (copied per launch) or a device pointer
+hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t run_flags, const float* noise_host,
+                     const float* noise_dev, hb_result* res) {
+    const bool noise_on_device = noise_dev != nullptr;
+    cudaStream_t st = e->stream();
+    const int B = e->B;
+    hb_status s = upload_net(e, T);
+    if (s) return s;
+    bool any_stoch = false;
+    for (auto& sb : e->subs) any_stoch |= is_stochastic(eff_integrator(e, sb.model));
+    const bool per_point_noise = (e->flags & HB_SEM_NOISE_PER_POINT) != 0;
+    const int64_t noise_rows_per_step = (int64_t)e->noise_row * (per_point_noise ? B : 1);
+
+    // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
+    const size_t smem_cap = 227 * 1024 - sizeof(DevNet) - 512;
+    const size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
+    const size_t ring_bytes = (size_t)e->R * e->cols * 4;
+    size_t edges = 0;
+    for (auto& hp : e->projs) if (hp.kind == W_SPARSE) edges += hp.edges.size();
+    const size_t edge_bytes = ((edges * 8) + 15) & ~(size_t)15;
+    int ring_in_smem = 0, edges_in_smem = 0;
+    bool force_global = (run_flags & HB_RUN_GLOBAL_RING) != 0;
+    if (!force_global && ring_bytes + 16 + edge_bytes + part_bytes <= smem_cap) { ring_in_smem = 1; edges_in_smem = 1; }
+    else if (!force_global && ring_bytes + 16 + part_bytes <= smem_cap) { ring_in_smem = 1; }
+    else if (edge_bytes + part_bytes <= smem_cap) { edges_in_smem = 1; }
+    size_t smem = (ring_in_smem ? ((ring_bytes + 15) & ~(size_t)15) : 0) + (edges_in_smem ? edge_bytes : 0) + part_bytes + 16;
+    {
+        size_t off = 0;
+        for (size_t p = 0; p < e->projs.size(); p++) {
+            if (e->projs[p].kind == W_SPARSE && edges_in_smem) { e->net.proj[p].smem_edges = (int)off; off += e->projs[p].edges.size(); }
+            else e->net.proj[p].smem_edges = -1;
+        }
+        CUDA_TRY(cudaMemcpyAsync(e->d_net, &e->net, sizeof(DevNet), cudaMemcpyHostToDevice, st));
+    }
+
+    // ---- BOLD schedule of this run ----
+    const int n_bold_active = e->bold_removed ? 0 : (int)e->bold.size();
+    const bool bold_pp = (e->flags & HB_SEM_BOLD_PER_POINT) != 0;
+    const int N0 = e->subs[0].nnodes;
+    DevBold db;
+    memset(&db, 0, sizeof db);
+    db.n = n_bold_active;
+    db.per_point = bold_pp ? 1 : 0;
+    db.n0 = N0;
+    std::vector<std::vector<double>> new_times(n_bold_active);
+    for (int m = 0; m < n_bold_active; m++) {
+        BoldHost& bh = e->bold[m];
+        std::vector<BoldEmit> emit;
+        int n_full, partial;
+        int64_t n_new = bold_schedule(e, bh, n_steps, emit, n_full, partial, new_times[m]);
+        db.period[m] = bh.period;
+        db.n_full[m] = n_full;
+        db.partial[m] = partial;
+        db.dt_full[m] = (float)((e->dt_ms * (double)bh.period) / 1000.0);
+        db.dt_part[m] = (float)((e->dt_ms * (double)partial) / 1000.0);
+        db.n_emit[m] = (int)emit.size();
+        CUDA_TRY(bh.emit.ensure(emit.size()));
+        if (!emit.empty()) CUDA_TRY(cudaMemcpyAsync(bh.emit.p, emit.data(), emit.size() * sizeof(BoldEmit), cudaMemcpyHostToDevice, st));
+        db.emit[m] = bh.emit.p;
+        db.n_out_run[m] = (int)n_new;
+        CUDA_TRY(bh.out_run.ensure((size_t)std::max<int64_t>(n_new, 1) * N0 * (bold_pp ? B : 1)));
+        db.out[m] = bh.out_run.p;
+        db.bw[m] = bh.bw.p;
+        db.acc[m] = bh.acc.p;
+        if (!bold_pp) {
+            int n_win = n_full + (partial > 0 ? 1 : 0);
+            CUDA_TRY(bh.win.ensure((size_t)std::max(n_win, 1) * B * N0));
+            db.win[m] = bh.win.p;
+        }
+        CUDA_TRY(cudaStreamSynchronize(st));  // the emit vector is released at scope end
+    }
+
+    // ---- chunking: one launch unless a trajectory or per-point noise must be streamed ----
+    const bool record = (run_flags & HB_RUN_TRAJECTORY) != 0;
+    int64_t chunk = n_steps;
+    const size_t traj_step_bytes = (size_t)B * e->state_len * 4;
+    if (record) chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, (int64_t)((512ull << 20) / std::max<size_t>(traj_step_bytes, 1))));
+    if (any_stoch && !noise_on_device) {
+        const size_t nb = (size_t)noise_rows_per_step * 4;
+        chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, (int64_t)((2048ull << 20) / std::max<size_t>(nb, 1))));
+    }
+    chunk = std::min<int64_t>(chunk, (int64_t)1 << 30);
+    if (record && res) {
+        CUDA_TRY(e->traj.ensure((size_t)chunk * B * e->state_len));
+        res->traj.assign(e->subs.size(), std::vector<float>());
+        for (size_t i = 0; i < e->subs.size(); i++) res->traj[i].resize((size_t)n_steps * B * e->subs[i].nm * e->subs[i].nvar);
+    }
+    if (any_stoch && !noise_on_device) CUDA_TRY(e->noise.ensure((size_t)chunk * noise_rows_per_step));
+    CUDA_TRY(e->flags_buf.ensure(2));
+    CUDA_TRY(cudaMemsetAsync(e->flags_buf.p, 0, 2 * sizeof(int), st));
+
+    RunArgs a;
+    memset(&a, 0, sizeof a);
+    a.run_s0 = e->step;
+    a.run_steps = n_steps;
+    a.state = e->state.p;
+    a.tavg = e->tavg.p;
+    a.ring = e->ring.p;
+    a.noise_per_point = per_point_noise ? 1 : 0;
+    a.ring_in_smem = ring_in_smem;
+    a.smem_edges = edges_in_smem ? (int)edges : 0;
+    a.flags = e->flags_buf.p;
+    a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
+    a.bold = db;
+
+    std::vector<float> traj_host;
+    e->last_launches = 0;
+    float kernel_ms_total = 0.0f;
+    for (int64_t c0 = 0; c0 < n_steps; c0 += chunk) {
+        const int n = (int)std::min<int64_t>(chunk, n_steps - c0);
+        a.s0 = e->step + c0;
+        a.n_steps = n;
+        a.load_ring = (a.s0 > 0) ? 1 : 0;
+        a.store_ring = 1;
+        if (any_stoch) {
+            if (noise_on_device) a.noise = noise_dev + (size_t)c0 * noise_rows_per_step;
+            else {
+                CUDA_TRY(cudaMemcpyAsync(e->noise.p, noise_host + (size_t)c0 * noise_rows_per_step,
+                                         (size_t)n * noise_rows_per_step * 4, cudaMemcpyHostToDevice, st));
+                a.noise = e->noise.p;
+            }
+        }
+        a.traj = record ? e->traj.p : nullptr;
+        CUDA_TRY(cudaEventRecord(e->ev0, st));
+        CUDA_TRY(hb_launch_resident(e->d_net, a, B, e->threads, smem, st));
+        CUDA_TRY(cudaEventRecord(e->ev1, st));
+        e->last_launches++;
+        if (record) {
+            traj_host.resize((size_t)n * B * e->state_len);
+            CUDA_TRY(cudaMemcpyAsync(traj_host.data(), e->traj.p, traj_host.size() * 4, cudaMemcpyDeviceToHost, st));
+        }
+        CUDA_TRY(cudaEventSynchronize(e->ev1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        kernel_ms_total += ms;
+        if (record) {
+            CUDA_TRY(cudaStreamSynchronize(st));
+            // [step][B][state_len] -> per subnetwork [step][B][nm*nvar]
+            for (int it = 0; it < n; it++)
+                for (int b = 0; b < B; b++)
+                    for (size_t i = 0; i < e->subs.size(); i++) {
+                        const int per = e->subs[i].nm * e->subs[i].nvar;
+                        const float* src = traj_host.data() + ((size_t)it * B + b) * e->state_len + e->net.sub[i].state_off;
+                        float* dst = res->traj[i].data() + (((size_t)(c0 + it)) * B + b) * per;
+                        memcpy(dst, src, per * 4);
+                    }
+        }
+    }
+    e->last_ms = kernel_ms_total;
+    e->last_kind = 1;
+
+    // ---- batch-mean BOLD: reduce windows over sweep points, then the BW ODE ----
+    for (int m = 0; m < n_bold_active && !bold_pp; m++) {
+        int n_win = db.n_full[m] + (db.partial[m] > 0 ? 1 : 0);
+        CUDA_TRY(e->means.ensure((size_t)std::max(n_win, 1) * N0));
+        CUDA_TRY(hb_launch_bold_batch_mean(db, m, n_win, B, e->means.p, st));
+    }
+    int flags_h[2] = {0, 0};
+    CUDA_TRY(cudaMemcpyAsync(flags_h, e->flags_buf.p, sizeof flags_h, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    e->step += n_steps;
+    // BOLD bookkeeping and outputs
+    for (int m = 0; m < n_bold_active; m++) {
+        BoldHost& bh = e->bold[m];
+        bh.times.insert(bh.times.end(), new_times[m].begin(), new_times[m].end());
+        int64_t n_new = db.n_out_run[m];
+        if (res && n_new > 0) {
+            std::vector<float> tmp((size_t)n_new * N0 * (bold_pp ? B : 1));
+            CUDA_TRY(cudaMemcpy(tmp.data(), bh.out_run.p, tmp.size() * 4, cudaMemcpyDeviceToHost));
+            if (!bold_pp) bh.out.insert(bh.out.end(), tmp.begin(), tmp.end());
+            else {
+                std::vector<float> merged((size_t)B * (bh.n_out + n_new) * N0);
+                for (int b = 0; b < B; b++) {
+                    if (bh.n_out) memcpy(&merged[(size_t)b * (bh.n_out + n_new) * N0], &bh.out[(size_t)b * bh.n_out * N0], (size_t)bh.n_out * N0 * 4);
+                    memcpy(&merged[((size_t)b * (bh.n_out + n_new) + bh.n_out) * N0], &tmp[(size_t)b * n_new * N0], (size_t)n_new * N0 * 4);
+                }
+                bh.out.swap(merged);
+            }
+        }
+        bh.n_out += n_new;
+    }
+    if (a.check_finite && flags_h[0]) return fail(HB_ERR_NONFINITE, "a state variable became NaN or Inf");
+    return HB_OK;
+}
+
+hb_status collect(hb_engine* e, int64_t n_steps, hb_result* r) {
+    const int B = e->B;
+    std::vector<float> st((size_t)B * e->state_len), ta((size_t)B * e->state_len);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), e->state.p, st.size() * 4, cudaMemcpyDeviceToHost, e->stream()));
+    CUDA_TRY(cudaMemcpyAsync(ta.data(), e->tavg.p, ta.size() * 4, cudaMemcpyDeviceToHost, e->stream()));
+    CUDA_TRY(cudaStreamSynchronize(e->stream()));
+    const float inv = 1.0f / (float)n_steps;  // engine.rs:514
+    r->tavg.assign(e->subs.size(), {});
+    r->fin.assign(e->subs.size(), {});
+    for (size_t i = 0; i < e->subs.size(); i++) {
+        const int per = e->subs[i].nm * e->subs[i].nvar;
+        r->tavg[i].resize((size_t)B * per);
+        r->fin[i].resize((size_t)B * per);
+        for (int b = 0; b < B; b++)
+            for (int k = 0; k < per; k++) {
+                size_t src = (size_t)b * e->state_len + e->net.sub[i].state_off + k;
+                r->tavg[i][(size_t)b * per + k] = ta[src] * inv;
+                r->fin[i][(size_t)b * per + k] = st[src];
+            }
+    }
+    const int n_bold_active = e->bold_removed ? 0 : (int)e->bold.size();
+    r->n_bold = n_bold_active;
+    r->bold.assign(n_bold_active, {});
+    for (int m = 0; m < n_bold_active; m++) r->bold[m] = e->bold[m].out;
+    r->n_sweep = B;
+    return HB_OK;
+}
+
+hb_status validate_noise(hb_engine* e, const float* noise, int64_t noise_len, int64_t n_steps) {
+    bool any = false;
+    for (auto& s : e->subs) any |= is_stochastic(eff_integrator(e, s.model));
+    if (!any) return HB_OK;
+    int64_t need = (int64_t)e->noise_row * ((e->flags & HB_SEM_NOISE_PER_POINT) ? e->B : 1) * n_steps;
+    if (!noise || noise_len < need)
+        return fail(HB_ERR_INVALID_STATE, "noise array too short: %lld < %lld", (long long)noise_len, (long long)need);
+    for (size_t i = 0; i < e->subs.size(); i++)
+        if (e->subs[i].nvar > (int)e->nsig.size())
+            return fail(HB_ERR_INVALID_CONFIG, "nsig has %d entries, subnetwork %d has nvar %d", (int)e->nsig.size(), (int)i, e->subs[i].nvar);
+    return HB_OK;
+}
+
+hb_status reset_state(hb_engine* e) {
+    CUDA_TRY(cudaMemcpyAsync(e->state.p, e->x0.p, (size_t)e->B * e->state_len * 4, cudaMemcpyDeviceToDevice, e->stream()));
+    e->step = 0;
+    return HB_OK;
+}
+
+}  // namespace
+
+// ======================================================================================
+// C ABI
+// ======================================================================================
+extern "C" {
+
+int32_t hb_abi_version(void) { return HB_ABI_VERSION; }
+const char* hb_last_error(void) { return g_err.c_str(); }
+
+hb_status hb_model_info(const char* model, int32_t* nvar, int32_t* ncvar, int32_t* n_params) {
+    int m = model_id(model);
+    if (m >= 0) { *nvar = k_models[m].nvar; *ncvar = k_models[m].ncvar; *n_params = k_models[m].nparams; return HB_OK; }
+    for (int i = 0; i < 22; i++)
+        if (model && !strcmp(model, k_other_models[i])) { *nvar = k_other_nvar[i]; *ncvar = k_other_ncvar[i]; *n_params = k_other_np[i]; return HB_OK; }
+    return fail(HB_ERR_INVALID_CONFIG, "Unknown model: %s", model ? model : "(null)");
+}
+
+hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** out) {
+    if (!out) return fail(HB_ERR_INVALID_STATE, "out is NULL");
+    *out = nullptr;
+    if (!d) return fail(HB_ERR_INVALID_CONFIG, "descriptor is NULL");
+    if (n_sweep < 1) return fail(HB_ERR_INVALID_CONFIG, "n_sweep must be >= 1");
+    if (d->n_subnets < 1) return fail(HB_ERR_INVALID_CONFIG, "At least one subnetwork required");
+    if (d->n_subnets > HB_MAX_SUB) return fail(HB_ERR_UNSUPPORTED, "at most %d subnetworks are supported", HB_MAX_SUB);
+    if (d->n_projections > HB_MAX_PROJ) return fail(HB_ERR_UNSUPPORTED, "at most %d projections are supported", HB_MAX_PROJ);
+    if (d->n_bold > HB_MAX_BOLD) return fail(HB_ERR_UNSUPPORTED, "at most %d BOLD monitors are supported", HB_MAX_BOLD);
+    if (!(d->dt > 0.0)) return fail(HB_ERR_INVALID_CONFIG, "dt must be positive");
+    if (d->integrator < 0 || d->integrator > 5) return fail(HB_ERR_INVALID_CONFIG, "unknown integrator kind: %d", d->integrator);
+    const bool ring = (d->flags & HB_SEM_DELAY_RING) != 0;
+
+    hb_engine* e = new hb_engine();
+    auto bail = [&](hb_status s) { hb_engine_destroy(e); return s; };
+    e->B = n_sweep;
+    e->dt_ms = d->dt;
+    e->integrator = d->integrator;
+    e->flags = d->flags;
+    e->nsig.assign(d->nsig, d->nsig + std::max(0, d->n_nsig));
+    memset(&e->net, 0, sizeof e->net);
+
+    // ---- subnetworks (engine.rs:153-247) ----
+    int thread_off = 0, col_off = 0, state_off = 0;
+    for (int i = 0; i < d->n_subnets; i++) {
+        const hb_subnet_desc& sd = d->subnets[i];
+        HostSub s;
+        s.model = model_id(sd.model);
+        if (s.model < 0) {
+            if (is_other_model(sd.model))
+                return bail(fail(HB_ERR_UNSUPPORTED, "model '%s' is not batch-native in the reference (per-point fallback); "
+                                 "this engine implements the six batch-native models", sd.model));
+            return bail(fail(HB_ERR_INVALID_CONFIG, "Unknown model: %s", sd.model ? sd.model : "(null)"));
+        }
+        if (sd.nnodes < 1 || sd.nmodes < 1) return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: nnodes and nmodes must be >= 1", i));
+        s.nnodes = sd.nnodes; s.nmodes = sd.nmodes; s.nm = sd.nnodes * sd.nmodes;
+        s.nvar = k_models[s.model].nvar; s.ncvar = k_models[s.model].ncvar;
+        if (sd.n_params < k_models[s.model].nparams || sd.n_params > 24)
+            return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: model '%s' expects %d params, got %d", i, sd.model,
+                             k_models[s.model].nparams, sd.n_params));
+        s.nparams = sd.n_params;
+        s.params.assign(sd.params, sd.params + sd.n_params);
+        if (sd.n_initial_state != (int64_t)s.nm * s.nvar)
+            return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: initial_state has %lld values, expected %d (nvar=%d * nnodes=%d * nmodes=%d)",
+                             i, (long long)sd.n_initial_state, s.nm * s.nvar, s.nvar, s.nnodes, s.nmodes));
+        s.x0.assign(sd.initial_state, sd.initial_state + s.nm * s.nvar);
+        if (ring && s.nmodes != 1) return bail(fail(HB_ERR_UNSUPPORTED, "ring-buffer delay semantics need nmodes == 1"));
+        if (s.nm > 65535) return bail(fail(HB_ERR_UNSUPPORTED, "subnetwork %d has %d nodes; at most 65535 are supported", i, s.nm));
+        DevSub& ds = e->net.sub[i];
+        ds.model = s.model; ds.nm = s.nm; ds.nvar = s.nvar; ds.ncvar = s.ncvar;
+        ds.thread_off = thread_off; ds.col_off = col_off; ds.state_off = state_off; ds.noise_off = state_off;
+        thread_off += (s.nm + 31) / 32 * 32;
+        col_off += s.nm * s.ncvar;
+        state_off += s.nm * s.nvar;
+        e->subs.push_back(s);
+    }
+    e->threads = thread_off;
+    e->cols = col_off;
+    e->state_len = state_off;
+    e->noise_row = state_off;
+    if (e->threads > HB_MAX_THREADS)
+        return bail(fail(HB_ERR_UNSUPPORTED, "a sweep point has %d node threads; the point-resident kernel supports %d", e->threads, HB_MAX_THREADS));
+
+    // ---- horizon: engine.rs:253-257 (batch) / construction.rs:596-601 (ring) ----
+    int max_delay = 0;
+    for (int p = 0; p < d->n_projections; p++)
+        for (int64_t k = 0; k < d->projections[p].n_delays; k++) max_delay = std::max<int>(max_delay, (int)d->projections[p].delays[k]);
+    if (max_delay > 65535) return bail(fail(HB_ERR_UNSUPPORTED, "delays above 65535 steps are not supported"));
+    e->H = ring ? max_delay + 1 : (max_delay == 0 ? 0 : max_delay + 1);
+    e->R = std::max(e->H, 1) + 1;
+
+    // ---- projections (engine.rs:272-417) ----
+    int n_mean = 0;
+    for (int p = 0; p < d->n_projections; p++) {
+        const hb_projection_desc& pd = d->projections[p];
+        if (pd.src < 0 || pd.src >= d->n_subnets) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: src %d >= number of subnetworks %d", p, pd.src, d->n_subnets));
+        if (pd.tgt < 0 || pd.tgt >= d->n_subnets) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: tgt %d >= number of subnetworks %d", p, pd.tgt, d->n_subnets));
+        HostProj hp;
+        hp.src = pd.src; hp.tgt = pd.tgt;
+        const HostSub& S = e->subs[pd.src];
+        const HostSub& Tg = e->subs[pd.tgt];
+        hp.nsrc = S.nm; hp.ntgt = Tg.nm;
+        hp.cf_name = pd.coupling_fn ? pd.coupling_fn : "Linear";
+        hp.cf_params.assign(pd.coupling_params, pd.coupling_params + std::max(0, pd.n_coupling_params));
+        if (hp.cf_params.size() > 16) return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: too many coupling params", p));
+        hp.delay = pd.n_delays > 0 ? (int)pd.delays[0] : 0;
+        Cfn cf0 = resolve_cfn(hp, hp.cf_params.data(), (int)hp.cf_params.size());
+        if (cf0.kind == HBC_PRESIG && cf0.global_t)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: PreSigmoidal global_t couples all sweep points; not supported", p));
+        // weights
+        std::vector<float> dense;  // only for Difference preprocessing of dense weights
+        bool per_edge = false;
+        if (pd.weights_kind == HB_WEIGHTS_SCALAR) {
+            hp.kind = (d->flags & HB_SEM_SCALAR_DIAGONAL) ? W_DIAG : W_MEAN;
+            hp.w = pd.scalar_weight;
+            if (hp.kind == W_DIAG && hp.nsrc != hp.ntgt)
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Scalar weights require src and tgt nnodes to match"));
+        } else if (pd.weights_kind == HB_WEIGHTS_DENSE) {
+            if (!pd.dense || pd.dense_rows != hp.ntgt || pd.dense_cols != hp.nsrc)
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: weights must be [%d x %d], got [%d x %d]", p, hp.ntgt, hp.nsrc, pd.dense_rows, pd.dense_cols));
+            hp.kind = W_SPARSE;
+            dense.assign(pd.dense, pd.dense + (size_t)hp.ntgt * hp.nsrc);
+        } else if (pd.weights_kind == HB_WEIGHTS_CSR) {
+            if (pd.n_indptr != hp.ntgt + 1)
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: CSR indptr length %lld != tgt_nnodes + 1 = %d", p, (long long)pd.n_indptr, hp.ntgt + 1));
+            if (pd.csr_indptr[0] != 0 || (int64_t)pd.csr_indptr[hp.ntgt] != pd.nnz)
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: CSR indptr must start at 0 and end at nnz", p));
+            for (int t = 0; t < hp.ntgt; t++)
+                if (pd.csr_indptr[t + 1] < pd.csr_indptr[t]) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: CSR indptr is not monotonic", p));
+            for (int64_t k = 0; k < pd.nnz; k++)
+                if ((int)pd.csr_indices[k] >= hp.nsrc) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: CSR index %u >= src nodes %d", p, pd.csr_indices[k], hp.nsrc));
+            hp.kind = W_SPARSE;
+            per_edge = ring && pd.n_delays == pd.nnz && pd.nnz > 0;
+            if (!ring) {
+                // densified by the batch engine (engine.rs:298-322)
+                dense.assign((size_t)hp.ntgt * hp.nsrc, 0.0f);
+                for (int t = 0; t < hp.ntgt; t++)
+                    for (uint32_t k = pd.csr_indptr[t]; k < pd.csr_indptr[t + 1]; k++) dense[(size_t)t * hp.nsrc + pd.csr_indices[k]] = pd.csr_data[k];
+            }
+        } else return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: unknown weights kind %d", p, pd.weights_kind));
+
+        // Difference preprocessing (engine.rs:327-368; CSR in ring mode follows construction.rs:700-730)
+        if (cf0.kind == HBC_DIFFERENCE) {
+            if (hp.kind == W_MEAN || hp.kind == W_DIAG) { hp.w = 0.0f; hp.diff_mode = 1; }
+            else if (!dense.empty()) {
+                if (hp.ntgt == hp.nsrc) {
+                    for (int i = 0; i < hp.ntgt; i++) {
+                        float rs = 0.0f;
+                        for (int j = 0; j < hp.nsrc; j++) rs = rs + dense[(size_t)i * hp.nsrc + j];
+                        dense[(size_t)i * hp.nsrc + i] -= rs;
+                    }
+                    hp.diff_mode = 1;
+                } else {
+                    hp.rowsums.resize(hp.ntgt);
+                    for (int i = 0; i < hp.ntgt; i++) {
+                        float rs = 0.0f;
+                        for (int j = 0; j < hp.nsrc; j++) rs = rs + dense[(size_t)i * hp.nsrc + j];
+                        hp.rowsums[i] = rs;
+                    }
+                    hp.diff_mode = 2;
+                }
+            } else hp.diff_mode = 1;
+        }
+        hp.cf = resolve_cfn(hp, hp.cf_params.data(), (int)hp.cf_params.size());
+        // CSR rows: dense rows keep only non-zero weights (exact for finite values), in source order
+        if (hp.kind == W_SPARSE) {
+            hp.rowptr.assign(hp.ntgt + 1, 0);
+            if (!dense.empty()) {
+                for (int t = 0; t < hp.ntgt; t++) {
+                    for (int j = 0; j < hp.nsrc; j++) {
+                        float w = dense[(size_t)t * hp.nsrc + j];
+                        if (w != 0.0f) { hp.edges.push_back((uint32_t)j); hp.ew.push_back(w); }
+                    }
+                    hp.rowptr[t + 1] = (int)hp.edges.size();
+                }
+            } else {
+                for (int t = 0; t < hp.ntgt; t++) {
+                    for (uint32_t k = pd.csr_indptr[t]; k < pd.csr_indptr[t + 1]; k++) {
+                        uint32_t dl = per_edge ? pd.delays[k] : 0;
+                        hp.edges.push_back((dl << 16) | pd.csr_indices[k]);
+                        hp.ew.push_back(pd.csr_data[k]);
+                    }
+                    hp.rowptr[t + 1] = (int)hp.edges.size();
+                }
+            }
+        }
+        hp.dmode = per_edge ? HBD_EDGE : (ring ? HBD_RING : HBD_COMPAT);
+        hp.pre_cpu = per_edge ? 1 : 0;
+        // channels and cvar map (engine.rs:370-392, 637-664)
+        hp.ncv = std::min(S.ncvar, S.nvar);
+        const Cfn& f = hp.cf;
+        hp.pc = (f.kind == HBC_KURAMOTO) ? 2 * hp.ncv : ((f.kind == HBC_SJR || (f.kind == HBC_PRESIG && f.dynamic)) ? 1 : hp.ncv);
+        hp.oc = (f.kind == HBC_KURAMOTO) ? Tg.ncvar : hp.pc;
+        if (f.kind == HBC_PRESIG && f.dynamic && hp.ncv < 2)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: PreSigmoidal dynamic needs two source coupling variables", p));
+        if (f.kind == HBC_KURAMOTO && hp.ncv != Tg.ncvar)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: Kuramoto coupling needs equal source and target cvar counts", p));
+        if (hp.diff_mode == 2 && hp.pc != Tg.ncvar)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: Difference rowsums need equal source and target cvar counts", p));
+        int cs[8], ct[8];
+        int ncm = parse_cvar_map(pd.cvar_map, cs, ct, 8);
+        if (ncm > 4) return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: at most 4 cvar_map pairs", p));
+        for (int k = 0; k < ncm; k++) {
+            if (cs[k] >= S.ncvar) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d cvar_map src index %d >= src_ncvar %d", p, cs[k], S.ncvar));
+            if (ct[k] >= Tg.ncvar) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d cvar_map tgt index %d >= tgt_ncvar %d", p, ct[k], Tg.ncvar));
+            hp.cm_s[k] = cs[k];
+            int pos = 0;
+            if (Tg.model == HBM_MPR) pos = (ct[k] == 1) ? 1 : 0;
+            else pos = (k_models[Tg.model].cvar0 == ct[k]) ? 0 : 0;
+            hp.cm_cpl[k] = pos;
+        }
+        hp.ncm = ncm;
+        hp.direct = (Tg.ncvar == S.ncvar && ncm == 1 && cs[0] == 0 && ct[0] == 0) ? 1 : 0;
+        if (hp.direct && hp.oc != Tg.ncvar)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: coupling produces %d channels for a target with %d cvars", p, hp.oc, Tg.ncvar));
+        if (!hp.direct && hp.oc != S.ncvar)
+            return bail(fail(HB_ERR_UNSUPPORTED, "projection %d: cvar remap of a %d-channel coupling output", p, hp.oc));
+        // device form
+        DevProj& dp = e->net.proj[p];
+        dp.src = hp.src; dp.tgt = hp.tgt; dp.kind = hp.kind; dp.dmode = hp.dmode; dp.delay = hp.delay;
+        dp.nsrc = hp.nsrc; dp.ntgt = hp.ntgt; dp.cfk = f.kind; dp.pre_cpu = hp.pre_cpu; dp.ncv = hp.ncv; dp.pc = hp.pc;
+        dp.oc = hp.oc; dp.has_rowsums = hp.diff_mode == 2; dp.direct = hp.direct; dp.ncm = ncm;
+        for (int k = 0; k < 4; k++) { dp.cm_s[k] = hp.cm_s[k]; dp.cm_cpl[k] = hp.cm_cpl[k]; }
+        dp.w = hp.w;
+        cfn_to_cp(f, hp.nsrc, dp.cp);
+        dp.mean_slot = (hp.kind == W_MEAN) ? n_mean++ : -1;
+        e->projs.push_back(hp);
+    }
+    e->n_mean = n_mean;
+    for (int i = 0; i < d->n_subnets; i++) {
+        DevSub& ds = e->net.sub[i];
+        ds.n_in = 0;
+        for (int p = 0; p < d->n_projections; p++)
+            if (e->projs[p].tgt == i) ds.in_idx[ds.n_in++] = p;
+        ds.integ = eff_integrator(e, e->subs[i].model);
+    }
+    // BOLD monitors (engine.rs:419-449)
+    for (int m = 0; m < d->n_bold; m++) {
+        if (e->subs[0].nmodes != 1) return bail(fail(HB_ERR_UNSUPPORTED, "BOLD monitors need nmodes == 1 on subnetwork 0"));
+        e->bold_cfg.push_back(d->bold[m]);
+        BoldHost bh;
+        bh.period = std::max(1, d->bold[m].bold_period);
+        bh.tr = d->bold[m].tr;
+        e->bold.push_back(std::move(bh));
+    }
+    // network-wide constants
+    DevNet& net = e->net;
+    net.n_sub = d->n_subnets; net.n_proj = d->n_projections; net.n_mean = n_mean;
+    net.B = e->B; net.H = e->H; net.R = e->R; net.cols = e->cols; net.state_len = e->state_len; net.noise_row = e->noise_row;
+    const float dt = (float)d->dt;
+    net.dt = dt; net.dt_half = dt * 0.5f; net.dt_sixth = dt / 6.0f; net.dt_h2 = dt / 2.0f;
+    const float sqrt_dt = sqrtf(dt);
+    for (int v = 0; v < 8; v++) net.noise_scale[v] = v < (int)e->nsig.size() ? sqrtf(2.0f * e->nsig[v]) * sqrt_dt : 0.0f;
+
+    // ---- device allocations ----
+    auto cu = [&](cudaError_t err, const char* what) -> hb_status {
+        if (err != cudaSuccess) return fail(HB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+        return HB_OK;
+    };
+    hb_status s;
+    if ((s = cu(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return bail(s);
+    if ((s = cu(cudaEventCreate(&e->ev0), "cudaEventCreate"))) return bail(s);
+    if ((s = cu(cudaEventCreate(&e->ev1), "cudaEventCreate"))) return bail(s);
+    if ((s = cu(cudaMalloc(&e->d_net, sizeof(DevNet)), "cudaMalloc(net)"))) return bail(s);
+    const size_t stn = (size_t)e->B * e->state_len;
+    if ((s = cu(e->state.ensure(stn), "cudaMalloc(state)"))) return bail(s);
+    if ((s = cu(e->x0.ensure(stn), "cudaMalloc(x0)"))) return bail(s);
+    if ((s = cu(e->tavg.ensure(stn), "cudaMalloc(tavg)"))) return bail(s);
+    if ((s = cu(e->ring.ensure((size_t)e->B * e->R * e->cols), "cudaMalloc(ring)"))) return bail(s);
+    {
+        std::vector<float> x0(stn);
+        for (int b = 0; b < e->B; b++)
+            for (size_t i = 0; i < e->subs.size(); i++)
+                memcpy(&x0[(size_t)b * e->state_len + e->net.sub[i].state_off], e->subs[i].x0.data(), e->subs[i].x0.size() * 4);
+        if ((s = cu(cudaMemcpy(e->x0.p, x0.data(), stn * 4, cudaMemcpyHostToDevice), "upload x0"))) return bail(s);
+        if ((s = cu(cudaMemcpy(e->state.p, x0.data(), stn * 4, cudaMemcpyHostToDevice), "upload state"))) return bail(s);
+    }
+    e->d_params.resize(e->subs.size());
+    for (size_t p = 0; p < e->projs.size(); p++) {
+        HostProj& hp = e->projs[p];
+        DevProj& dp = e->net.proj[p];
+        if (hp.kind == W_SPARSE) {
+            if ((s = cu(cudaMalloc(&hp.d_rowptr, hp.rowptr.size() * 4), "cudaMalloc(rowptr)"))) return bail(s);
+            if ((s = cu(cudaMemcpy(hp.d_rowptr, hp.rowptr.data(), hp.rowptr.size() * 4, cudaMemcpyHostToDevice), "upload rowptr"))) return bail(s);
+            size_t ne = std::max<size_t>(hp.edges.size(), 1);
+            if ((s = cu(cudaMalloc(&hp.d_edges, ne * 4), "cudaMalloc(edges)"))) return bail(s);
+            if ((s = cu(cudaMalloc(&hp.d_ew, ne * 4), "cudaMalloc(ew)"))) return bail(s);
+            if (!hp.edges.empty()) {
+                if ((s = cu(cudaMemcpy(hp.d_edges, hp.edges.data(), hp.edges.size() * 4, cudaMemcpyHostToDevice), "upload edges"))) return bail(s);
+                if ((s = cu(cudaMemcpy(hp.d_ew, hp.ew.data(), hp.ew.size() * 4, cudaMemcpyHostToDevice), "upload weights"))) return bail(s);
+            }
+            dp.rowptr = hp.d_rowptr; dp.edges = hp.d_edges; dp.ew = hp.d_ew;
+        }
+        if (!hp.rowsums.empty()) {
+            if ((s = cu(cudaMalloc(&hp.d_rowsums, hp.rowsums.size() * 4), "cudaMalloc(rowsums)"))) return bail(s);
+            if ((s = cu(cudaMemcpy(hp.d_rowsums, hp.rowsums.data(), hp.rowsums.size() * 4, cudaMemcpyHostToDevice), "upload rowsums"))) return bail(s);
+            dp.rowsums = hp.d_rowsums;
+        }
+    }
+    if ((s = reset_bold_device(e))) return bail(s);
+    *out = e;
+    return HB_OK;
+}
+
+void hb_engine_destroy(hb_engine* e) {
+    if (!e) return;
+    if (e->own_stream) cudaStreamSynchronize(e->own_stream);
+    for (auto& hp : e->projs) {
+        if (hp.d_rowptr) cudaFree(hp.d_rowptr);
+        if (hp.d_edges) cudaFree(hp.d_edges);
+        if (hp.d_ew) cudaFree(hp.d_ew);
+        if (hp.d_rowsums) cudaFree(hp.d_rowsums);
+        if (hp.d_cp_pp) cudaFree(hp.d_cp_pp);
+    }
+    for (auto& b : e->d_params) b.release();
+    for (auto& bh : e->bold) { bh.bw.release(); bh.acc.release(); bh.win.release(); bh.out_run.release(); bh.emit.release(); }
+    e->state.release(); e->x0.release(); e->tavg.release(); e->ring.release(); e->noise.release(); e->prep_noise.release();
+    e->traj.release();
+    e->means.release(); e->flags_buf.release();
+    if (e->d_net) cudaFree(e->d_net);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->own_stream) cudaStreamDestroy(e->own_stream);
+    delete e;
+}
+
+static hb_status run_common(hb_engine* e, const hb_sweep_point* dims, int n_dims, bool multi, int64_t n_steps,
+                            uint32_t run_flags, const float* noise, int64_t noise_len, hb_result** out) {
+    if (!e || !out) return fail(HB_ERR_INVALID_STATE, "NULL engine or result pointer");
+    *out = nullptr;
+    if (n_steps < 1) return fail(HB_ERR_INVALID_STATE, "n_steps must be >= 1");
+    hb_status s = validate_noise(e, noise, noise_len, n_steps);
+    if (s) return s;
+    RunTables T;
+    if ((s = build_tables(e, dims, n_dims, multi, T))) return s;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventRecord(t0, e->stream());
+    hb_result* r = new hb_result();
+    if (multi) {
+        // a fresh engine seeded by sweep point 0's current state, without BOLD (engine.rs:886-915)
+        cudaStream_t st = e->stream();
+        for (int b = 1; b < e->B; b++) {
+            cudaError_t err = cudaMemcpyAsync(e->state.p + (size_t)b * e->state_len, e->state.p, e->state_len * 4, cudaMemcpyDeviceToDevice, st);
+            if (err != cudaSuccess) { delete r; return fail(HB_ERR_CUDA, "reseed: %s", cudaGetErrorString(err)); }
+        }
+        e->step = 0;
+        e->bold_removed = true;
+    }
+    s = run_device(e, T, n_steps, run_flags, noise, nullptr, r);
+    if (!s) s = collect(e, n_steps, r);
+    cudaEventRecord(t1, e->stream());
+    cudaEventSynchronize(t1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (s) { delete r; return s; }
+    r->elapsed_ms = ms;
+    r->params = T.param_values;
+    r->has_traj = (run_flags & HB_RUN_TRAJECTORY) != 0;
+    *out = r;
+    return HB_OK;
+}
+
+hb_status hb_engine_run_sweep(hb_engine* e, int32_t sub_idx, int32_t param_idx, const float* values, int32_t n_values,
+                              int64_t n_steps, uint32_t run_flags, const float* noise, int64_t noise_len, hb_result** out) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (n_values != e->B || !values) return fail(HB_ERR_INVALID_STATE, "expected %d sweep values, got %d", e->B, n_values);
+    hb_sweep_point dim{sub_idx, param_idx, values, n_values};
+    return run_common(e, &dim, 1, false, n_steps, run_flags, noise, noise_len, out);
+}
+
+hb_status hb_engine_run_sweep_multi(hb_engine* e, const hb_sweep_point* dims, int32_t n_dims, int64_t n_steps,
+                                    uint32_t run_flags, const float* noise, int64_t noise_len, hb_result** out) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (!dims || n_dims < 1) return fail(HB_ERR_INVALID_STATE, "empty sweep");
+    int64_t n = 1;
+    for (int d = 0; d < n_dims; d++) n *= dims[d].n_values;
+    if (n != e->B) return fail(HB_ERR_INVALID_STATE, "Cartesian product has %lld points, engine has %d", (long long)n, e->B);
+    return run_common(e, dims, n_dims, true, n_steps, run_flags, noise, noise_len, out);
+}
+
+hb_status hb_engine_get_state(hb_engine* e, int32_t sub_idx, float* out, int64_t len) {
+    if (!e || !out) return fail(HB_ERR_INVALID_STATE, "NULL argument");
+    if (sub_idx < 0 || sub_idx >= (int)e->subs.size()) return fail(HB_ERR_INVALID_CONFIG, "subnetwork index %d out of range", sub_idx);
+    const int per = e->subs[sub_idx].nm * e->subs[sub_idx].nvar;
+    if (len < (int64_t)e->B * per) return fail(HB_ERR_INVALID_STATE, "output buffer too small");
+    std::vector<float> st((size_t)e->B * e->state_len);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), e->state.p, st.size() * 4, cudaMemcpyDeviceToHost, e->stream()));
+    CUDA_TRY(cudaStreamSynchronize(e->stream()));
+    for (int b = 0; b < e->B; b++) memcpy(out + (size_t)b * per, &st[(size_t)b * e->state_len + e->net.sub[sub_idx].state_off], per * 4);
+    return HB_OK;
+}
+
+int64_t hb_engine_step(const hb_engine* e) { return e ? e->step : -1; }
+
+hb_status hb_engine_reset(hb_engine* e) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    hb_status s = reset_state(e);
+    if (s) return s;
+    e->bold_removed = false;
+    return reset_bold_device(e);
+}
+
+hb_status hb_engine_last_kernel_time(const hb_engine* e, double* ms, int64_t* launches, int32_t* kind) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (ms) *ms = e->last_ms;
+    if (launches) *launches = e->last_launches;
+    if (kind) *kind = e->last_kind;
+    return HB_OK;
+}
+
+hb_status hb_engine_set_stream(hb_engine* e, void* stream) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (e->own_stream) CUDA_TRY(cudaStreamSynchronize(e->own_stream));
+    e->user_stream = (cudaStream_t)stream;
+    return HB_OK;
+}
+
+hb_status hb_engine_prepare(hb_engine* e, int32_t sub_idx, int32_t param_idx, const float* values, int32_t n_values,
+                            int64_t n_steps, uint32_t run_flags, const float* noise, int64_t noise_len) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (n_values != e->B || !values) return fail(HB_ERR_INVALID_STATE, "expected %d sweep values, got %d", e->B, n_values);
+    if (n_steps < 1) return fail(HB_ERR_INVALID_STATE, "n_steps must be >= 1");
+    hb_status s = validate_noise(e, noise, noise_len, n_steps);
+    if (s) return s;
+    hb_sweep_point dim{sub_idx, param_idx, values, n_values};
+    if ((s = build_tables(e, &dim, 1, false, e->prep_tables))) return s;
+    e->prep_steps = n_steps;
+    e->prep_flags = run_flags & ~HB_RUN_TRAJECTORY;
+    e->prep_noise_len = noise ? noise_len : 0;
+    if (noise) {
+        CUDA_TRY(e->prep_noise.ensure((size_t)noise_len));
+        CUDA_TRY(cudaMemcpy(e->prep_noise.p, noise, (size_t)noise_len * 4, cudaMemcpyHostToDevice));
+    }
+    e->prepared = true;
+    return HB_OK;
+}
+
+hb_status hb_engine_execute_prepared(hb_engine* e) {
+    if (!e || !e->prepared) return fail(HB_ERR_INVALID_STATE, "no prepared run");
+    hb_status s = reset_state(e);
+    if (s) return s;
+    e->bold_removed = false;
+    if ((s = reset_bold_device(e))) return s;
+    return run_device(e, e->prep_tables, e->prep_steps, e->prep_flags, nullptr,
+                      e->prep_noise_len ? e->prep_noise.p : e->x0.p, nullptr);
+}
+
+int32_t hb_result_n_sweep(const hb_result* r) { return r ? r->n_sweep : 0; }
+int32_t hb_result_n_subnets(const hb_result* r) { return r ? (int32_t)r->tavg.size() : 0; }
+int32_t hb_result_n_bold(const hb_result* r) { return r ? r->n_bold : 0; }
+double hb_result_elapsed_ms(const hb_result* r) { return r ? r->elapsed_ms : 0.0; }
+const float* hb_result_param_values(const hb_result* r, int64_t* len) {
+    if (len) *len = r ? (int64_t)r->params.size() : 0;
+    return r && !r->params.empty() ? r->params.data() : nullptr;
+}
+#define RESULT_VEC(fn, member)                                                             \
+    const float* fn(const hb_result* r, int32_t i, int64_t* len) {                         \
+        if (len) *len = 0;                                                                 \
+        if (!r || i < 0 || i >= (int32_t)r->member.size()) return nullptr;                  \
+        if (len) *len = (int64_t)r->member[i].size();                                      \
+        return r->member[i].data();                                                        \
+    }
+RESULT_VEC(hb_result_tavg, tavg)
+RESULT_VEC(hb_result_final_states, fin)
+RESULT_VEC(hb_result_bold, bold)
+const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
+    if (len) *len = 0;
+    if (!r || !r->has_traj || i < 0 || i >= (int32_t)r->traj.size()) return nullptr;
+    if (len) *len = (int64_t)r->traj[i].size();
+    return r->traj[i].data();
+}
+void hb_result_free(hb_result* r) { delete r; }
+
+}  // extern "C"

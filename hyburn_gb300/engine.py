@@ -1,0 +1,233 @@
+"""Host-side mirror of hyburn's ``BatchHybridEngine`` API over the GB300 C-ABI library.
+
+Names, arguments and result layouts follow src/engine/batch_engine/engine.rs so that code written
+against the reference reads the same:
+
+    engine = BatchHybridEngine.from_config(config, n_sweep=3)
+    result = engine.run_sweep(SweepParam(sub_idx=0, param_idx=1), [-0.5, 0.0, 0.5], 100)
+    result.tavg[0]      # flat [n_sweep, nnodes*nmodes, nvar]
+
+Every simulation step runs in the CUDA kernels of ``libhyburn_gb300.so``; there is no host
+fallback: if the library or a GPU is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from itertools import product
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _abi
+from .config import (BackendError, InvalidConfig, InvalidState, IOError_, NonFinite, SimConfig,
+                     SimulationError, Unsupported, resolve_initial_state)
+
+
+@dataclass
+class SweepParam:
+    """engine.rs:33-39."""
+
+    sub_idx: int
+    param_idx: int
+
+
+@dataclass
+class SweepPoint:
+    """engine.rs:41-50."""
+
+    sub_idx: int
+    param_idx: int
+    values: List[float]
+
+
+@dataclass
+class SweepSpec:
+    """engine.rs:52-91."""
+
+    points: List[SweepPoint]
+
+    def n_sweep(self) -> int:
+        n = 1
+        for p in self.points:
+            n *= len(p.values)
+        return n
+
+    def cartesian_product(self) -> List[List[Tuple[int, int, float]]]:
+        """Last dimension varies fastest (engine.rs:69-90)."""
+        out = []
+        for combo in product(*[range(len(p.values)) for p in self.points]):
+            out.append([(p.sub_idx, p.param_idx, p.values[i]) for p, i in zip(self.points, combo)])
+        return out
+
+
+@dataclass
+class BatchSweepResult:
+    """engine.rs:14-31; arrays are flat in the reference's memory order."""
+
+    param_values: np.ndarray
+    tavg: List[np.ndarray]
+    final_states: List[np.ndarray]
+    trajectories: Optional[List[np.ndarray]]
+    bold: Optional[List[np.ndarray]]
+    elapsed_ms: float
+    n_sweep: int
+
+
+_ERRORS = {
+    _abi.HB_ERR_INVALID_CONFIG: InvalidConfig,
+    _abi.HB_ERR_INVALID_STATE: InvalidState,
+    _abi.HB_ERR_BACKEND: BackendError,
+    _abi.HB_ERR_IO: IOError_,
+    _abi.HB_ERR_CUDA: BackendError,
+    _abi.HB_ERR_NONFINITE: NonFinite,
+    _abi.HB_ERR_TIMEOUT: BackendError,
+    _abi.HB_ERR_UNSUPPORTED: Unsupported,
+}
+
+
+def raise_for(status: int, message: str) -> None:
+    if status == _abi.HB_OK:
+        return
+    raise _ERRORS.get(status, SimulationError)(message)
+
+
+def noise_shape(config: SimConfig, n_steps: int, n_sweep: int, semantics: int = 0) -> Tuple[int, ...]:
+    """Shape of the standard-normal array a stochastic run consumes."""
+    row = 0
+    for s in config.network.subnetworks:
+        row += s.nnodes * s.nmodes * _abi.MODEL_INFO[s.model][0]
+    if semantics & _abi.HB_SEM_NOISE_PER_POINT:
+        return (n_steps, n_sweep, row)
+    return (n_steps, row)
+
+
+class BatchHybridEngine:
+    """src/engine/batch_engine/engine.rs:105-138, backed by the CUDA engine."""
+
+    def __init__(self, config: SimConfig, n_sweep: int, semantics: int = 0):
+        self._lib = _abi.load_library()
+        self.config = config
+        self.n_sweep = int(n_sweep)
+        self.semantics = int(semantics)
+        states = [resolve_initial_state(s) for s in config.network.subnetworks]
+        self._sd = _abi.build_sim_desc(config, states, semantics)
+        h = C.c_void_p()
+        st = self._lib.hb_engine_create(C.byref(self._sd.desc), self.n_sweep, C.byref(h))
+        raise_for(st, self._lib.hb_last_error().decode())
+        self._h = h
+        self.models = [s.model for s in config.network.subnetworks]
+
+    @classmethod
+    def from_config(cls, config: SimConfig, n_sweep: int, device=None, semantics: int = 0) -> "BatchHybridEngine":
+        """BatchHybridEngine::from_config (engine.rs:145-471)."""
+        return cls(config, n_sweep, semantics)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.hb_engine_destroy(h)
+            self._h = None
+
+    def close(self) -> None:
+        self.__del__()
+
+    # ---- runs ----
+    def _noise_args(self, noise, n_steps):
+        if noise is None:
+            return None, 0, None
+        a = np.ascontiguousarray(np.asarray(noise, dtype=np.float32))
+        return _abi.f32p(a), a.size, a
+
+    def _result(self, r, record_traj: bool) -> BatchSweepResult:
+        lib = self._lib
+        n = C.c_int64()
+        try:
+            nsub = lib.hb_result_n_subnets(r)
+            pv = _abi.copy_out(lib.hb_result_param_values(r, C.byref(n)), n.value)
+            tavg, fin, traj = [], [], []
+            for i in range(nsub):
+                tavg.append(_abi.copy_out(lib.hb_result_tavg(r, i, C.byref(n)), n.value))
+                fin.append(_abi.copy_out(lib.hb_result_final_states(r, i, C.byref(n)), n.value))
+                if record_traj:
+                    traj.append(_abi.copy_out(lib.hb_result_trajectory(r, i, C.byref(n)), n.value))
+            nb = lib.hb_result_n_bold(r)
+            bold = None
+            if nb > 0:
+                bold = []
+                for m in range(nb):
+                    p = lib.hb_result_bold(r, m, C.byref(n))
+                    bold.append(_abi.copy_out(p, n.value) if n.value > 0 else np.zeros(0, np.float32))
+            return BatchSweepResult(param_values=pv, tavg=tavg, final_states=fin,
+                                    trajectories=traj if record_traj else None, bold=bold,
+                                    elapsed_ms=lib.hb_result_elapsed_ms(r), n_sweep=lib.hb_result_n_sweep(r))
+        finally:
+            lib.hb_result_free(r)
+
+    def run_sweep(self, param: SweepParam, param_values: Sequence[float], n_steps: int,
+                  noise=None, run_flags: int = 0) -> BatchSweepResult:
+        """BatchHybridEngine::run_sweep (engine.rs:477-484)."""
+        vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
+        nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        r = C.c_void_p()
+        st = self._lib.hb_engine_run_sweep(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals),
+                                           vals.size, int(n_steps), int(run_flags), nptr, nlen, C.byref(r))
+        raise_for(st, self._lib.hb_last_error().decode())
+        return self._result(r, bool(run_flags & _abi.HB_RUN_TRAJECTORY))
+
+    def run_sweep_with_trajectory(self, param: SweepParam, param_values, n_steps: int, noise=None,
+                                  run_flags: int = 0) -> BatchSweepResult:
+        """BatchHybridEngine::run_sweep_with_trajectory (engine.rs:487-494)."""
+        return self.run_sweep(param, param_values, n_steps, noise, run_flags | _abi.HB_RUN_TRAJECTORY)
+
+    def run_sweep_multi(self, spec: SweepSpec, n_steps: int, noise=None, run_flags: int = 0) -> BatchSweepResult:
+        """BatchHybridEngine::run_sweep_multi (engine.rs:845-851)."""
+        arr, keep = _abi.sweep_points(spec.points)
+        nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        r = C.c_void_p()
+        st = self._lib.hb_engine_run_sweep_multi(self._h, arr, len(spec.points), int(n_steps), int(run_flags),
+                                                 nptr, nlen, C.byref(r))
+        raise_for(st, self._lib.hb_last_error().decode())
+        return self._result(r, bool(run_flags & _abi.HB_RUN_TRAJECTORY))
+
+    def run_sweep_multi_with_trajectory(self, spec: SweepSpec, n_steps: int, noise=None, run_flags: int = 0):
+        return self.run_sweep_multi(spec, n_steps, noise, run_flags | _abi.HB_RUN_TRAJECTORY)
+
+    # ---- state ----
+    @property
+    def step(self) -> int:
+        return int(self._lib.hb_engine_step(self._h))
+
+    @property
+    def states(self) -> List[np.ndarray]:
+        out = []
+        for i, s in enumerate(self.config.network.subnetworks):
+            nv = _abi.MODEL_INFO[s.model][0]
+            a = np.zeros((self.n_sweep, s.nnodes * s.nmodes, nv), dtype=np.float32)
+            st = self._lib.hb_engine_get_state(self._h, i, _abi.f32p(a), a.size)
+            raise_for(st, self._lib.hb_last_error().decode())
+            out.append(a)
+        return out
+
+    def reset(self) -> None:
+        raise_for(self._lib.hb_engine_reset(self._h), self._lib.hb_last_error().decode())
+
+    def set_stream(self, stream_handle: Optional[int]) -> None:
+        raise_for(self._lib.hb_engine_set_stream(self._h, C.c_void_p(stream_handle or 0)),
+                  self._lib.hb_last_error().decode())
+
+    def prepare(self, param: SweepParam, param_values, n_steps: int, noise=None, run_flags: int = 0) -> None:
+        vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
+        nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        st = self._lib.hb_engine_prepare(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals), vals.size,
+                                         int(n_steps), int(run_flags), nptr, nlen)
+        raise_for(st, self._lib.hb_last_error().decode())
+
+    def execute_prepared(self) -> None:
+        raise_for(self._lib.hb_engine_execute_prepared(self._h), self._lib.hb_last_error().decode())
+
+    def last_kernel_time(self) -> Tuple[float, int, int]:
+        ms, n, kind = C.c_double(), C.c_int64(), C.c_int32()
+        raise_for(self._lib.hb_engine_last_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(kind)),
+                  self._lib.hb_last_error().decode())
+        return ms.value, n.value, kind.value

@@ -1,0 +1,227 @@
+/*
+ * hyburn_gb300.h — C ABI of the GB300-native batched neural-mass simulation engine.
+ *
+ * This library replaces the `BatchHybridEngine` step of hyburn 0.2.0 (Rust crate) for
+ * `--backend cuda`. Every entry point below names the reference item it stands in for,
+ * by the file path inside the hyburn project.
+ *
+ * Conventions (mirroring the reference's engine contract, src/engine/batch_engine/engine.rs):
+ *   - All functions return an `hb_status`; the message of the last failure on the calling
+ *     thread is returned by `hb_last_error()` (thread-local, valid until the next call).
+ *   - Status codes mirror `SimulationError` (src/error.rs:6-25) plus CUDA/numeric/timeout codes.
+ *   - Engines are not thread-safe (one CUDA stream each); distinct engines may be driven from
+ *     distinct threads.
+ *   - Result buffers are owned by the library until `hb_result_free`.
+ *   - Layouts are those of `BatchSweepResult` (engine.rs:15-31): tavg / final states are
+ *     [n_sweep, nnodes*nmodes, nvar] (memory order of the batch engine's state tensor),
+ *     trajectories [n_steps, n_sweep, nnodes*nmodes, nvar], BOLD [n_tr, nnodes] per monitor in
+ *     batch-mean mode or [n_sweep, n_tr, nnodes] in per-point mode.
+ *   - All simulation arithmetic is FP32.
+ */
+#ifndef HYBURN_GB300_H
+#define HYBURN_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HB_ABI_VERSION 1
+
+/* ---- status codes: src/error.rs:6-25 (SimulationError) + device-side codes ---- */
+typedef int32_t hb_status;
+#define HB_OK                   0
+#define HB_ERR_INVALID_CONFIG   1  /* SimulationError::InvalidConfig */
+#define HB_ERR_INVALID_STATE    2  /* SimulationError::InvalidState */
+#define HB_ERR_BACKEND          3  /* SimulationError::BackendError */
+#define HB_ERR_IO               4  /* SimulationError::IOError */
+#define HB_ERR_CUDA             5  /* a CUDA runtime call failed */
+#define HB_ERR_NONFINITE        6  /* a state value became NaN/Inf on the device (checked runs) */
+#define HB_ERR_TIMEOUT          7  /* a bounded device-side wait gave up */
+#define HB_ERR_UNSUPPORTED      8  /* valid for the reference, not implemented by this engine */
+
+/* ---- integrators: src/engine/integrator.rs:14-23 (IntegratorKind, same order) ---- */
+#define HB_INT_HEUN              0
+#define HB_INT_EULER             1
+#define HB_INT_EULER_STOCHASTIC  2
+#define HB_INT_HEUN_STOCHASTIC   3
+#define HB_INT_RK4               4
+#define HB_INT_RK4_STOCHASTIC    5
+
+/* ---- weight kinds: src/config.rs (WeightsConfig) ---- */
+#define HB_WEIGHTS_SCALAR 0
+#define HB_WEIGHTS_DENSE  1
+#define HB_WEIGHTS_CSR    2
+
+/* ---- semantics flags (hb_sim_desc.flags) ----
+ * Default (0) reproduces the batch engine exactly, including its documented quirks:
+ * one delay per projection (`delays.first()`, engine.rs:410) read from the shift-window
+ * history (engine.rs:541-551, 565-589), Scalar weights as w*mean over source nodes
+ * (engine.rs:602-608), noise shared by all sweep points (engine.rs:729-745) and BOLD driven
+ * by the mean over sweep points (engine.rs:786-801). */
+#define HB_SEM_DELAY_RING       (1u << 0) /* true ring-buffer delays, per edge for CSR with
+                                             len(delays)==nnz (src/engine/runtime.rs:55-85,125-211) */
+#define HB_SEM_SCALAR_DIAGONAL  (1u << 1) /* Scalar weights as w*I (construction.rs:639-655) */
+#define HB_SEM_BOLD_PER_POINT   (1u << 2) /* one BOLD series per sweep point */
+#define HB_SEM_NOISE_PER_POINT  (1u << 3) /* noise array carries an independent draw per point */
+#define HB_SEM_HYBRID_INTEGRATOR (1u << 4) /* BatchHybridEngine::hybrid_integrator = true (engine.rs:697-702) */
+
+/* ---- run flags (hb_engine_run_* `run_flags`) ---- */
+#define HB_RUN_TRAJECTORY   (1u << 0) /* run_sweep_with_trajectory (engine.rs:487-494) */
+#define HB_RUN_CHECK_FINITE (1u << 1) /* fail with HB_ERR_NONFINITE if a state becomes NaN/Inf */
+#define HB_RUN_FORCE_RESIDENT (1u << 8) /* kernel choice: point-resident persistent kernel */
+#define HB_RUN_FORCE_BLOCKED  (1u << 9) /* kernel choice: time-blocked tiled kernel */
+#define HB_RUN_GLOBAL_RING    (1u << 10) /* resident kernel: keep the history ring in global memory */
+
+/* One subnetwork: SubnetworkConfig (src/config.rs:129-142) after the batch engine resolved its
+ * initial state (engine.rs:161-247). */
+typedef struct hb_subnet_desc {
+    const char*  model;          /* "Generic2dOscillator", "MontbrioPazoRoxin", "ReducedWongWang",
+                                    "Kuramoto", "JansenRit", "WilsonCowan" (config.rs:43-49) */
+    int32_t      nnodes;
+    int32_t      nmodes;
+    const float* params;         /* model parameters, config.rs:43-72 sizes */
+    int32_t      n_params;
+    const float* initial_state;  /* one point, [nnodes*nmodes, nvar] node-major (engine.rs:239-243) */
+    int64_t      n_initial_state;
+} hb_subnet_desc;
+
+/* One projection: ProjectionConfig (src/config.rs:158-184). */
+typedef struct hb_projection_desc {
+    int32_t         src;
+    int32_t         tgt;
+    int32_t         weights_kind;    /* HB_WEIGHTS_* */
+    float           scalar_weight;   /* HB_WEIGHTS_SCALAR */
+    const float*    dense;           /* HB_WEIGHTS_DENSE: [tgt_nodes, src_nodes] row-major */
+    int32_t         dense_rows;
+    int32_t         dense_cols;
+    const float*    csr_data;        /* HB_WEIGHTS_CSR: rows are target nodes */
+    const uint32_t* csr_indices;
+    const uint32_t* csr_indptr;      /* length n_indptr (tgt_nodes + 1) */
+    int64_t         nnz;
+    int64_t         n_indptr;
+    const uint32_t* delays;          /* integration steps; may be NULL when n_delays == 0 */
+    int64_t         n_delays;
+    const char*     coupling_fn;     /* CouplingFnConfig::from_name_and_params (coupling.rs:114-202) */
+    const float*    coupling_params;
+    int32_t         n_coupling_params;
+    const char*     cvar_map;        /* "0:0" or "0:0,1:1" (construction.rs:337-349) */
+} hb_projection_desc;
+
+/* One BOLD monitor: MonitorConfig with monitor_type == "Bold" (config.rs:206-229, engine.rs:419-449). */
+typedef struct hb_bold_desc {
+    int32_t bold_period;   /* neural steps per Balloon-Windkessel step */
+    double  tr;            /* repetition time in seconds */
+} hb_bold_desc;
+
+/* SimConfig (src/config.rs:83-114) as the batch engine consumes it. */
+typedef struct hb_sim_desc {
+    double                     dt;              /* ms */
+    int32_t                    integrator;      /* HB_INT_* */
+    const float*               nsig;            /* NsigConfig::to_vec(first nvar) (config.rs:16-24) */
+    int32_t                    n_nsig;
+    int32_t                    n_subnets;
+    const hb_subnet_desc*      subnets;
+    int32_t                    n_projections;
+    const hb_projection_desc*  projections;
+    int32_t                    n_bold;
+    const hb_bold_desc*        bold;
+    uint32_t                   flags;           /* HB_SEM_* */
+} hb_sim_desc;
+
+/* One sweep dimension: SweepPoint (engine.rs:41-50). */
+typedef struct hb_sweep_point {
+    int32_t      sub_idx;
+    int32_t      param_idx;
+    const float* values;
+    int32_t      n_values;
+} hb_sweep_point;
+
+typedef struct hb_engine hb_engine;
+typedef struct hb_result hb_result;
+
+/* ---- library ---- */
+int32_t     hb_abi_version(void);
+const char* hb_last_error(void);
+
+/* Number of state variables / coupling variables / parameters of a model name
+ * (config.rs:43-49, MODEL_REGISTRY); returns HB_ERR_INVALID_CONFIG for unknown names. */
+hb_status hb_model_info(const char* model, int32_t* nvar, int32_t* ncvar, int32_t* n_params);
+
+/* ---- engine lifecycle ---- */
+
+/* BatchHybridEngine::from_config(SimConfig, n_sweep, device) (engine.rs:145-471).
+ * Validates the descriptor, builds the device-side projection tables and uploads them. */
+hb_status hb_engine_create(const hb_sim_desc* desc, int32_t n_sweep, hb_engine** out);
+
+/* Drop of BatchHybridEngine. Accepts NULL. */
+void hb_engine_destroy(hb_engine* engine);
+
+/* BatchHybridEngine::run_sweep / run_sweep_with_trajectory (engine.rs:477-494, 496-842).
+ * `values` has n_sweep entries. `noise` holds standard-normal draws (the raw N(0,1) samples
+ * that generate_noise_reproducible scales by sqrt(2*nsig)*sqrt(dt), integrator.rs:170-198):
+ *   shared (default):  [n_steps, sum_over_subnets(nnodes*nmodes*nvar)]
+ *   HB_SEM_NOISE_PER_POINT: [n_steps, n_sweep, sum_over_subnets(nnodes*nmodes*nvar)]
+ * It is required for stochastic integrators and ignored otherwise (may be NULL).
+ * The engine keeps its state, history and step counter across calls, like the reference. */
+hb_status hb_engine_run_sweep(hb_engine* engine, int32_t sub_idx, int32_t param_idx,
+                              const float* values, int32_t n_values, int64_t n_steps,
+                              uint32_t run_flags, const float* noise, int64_t noise_len,
+                              hb_result** out);
+
+/* BatchHybridEngine::run_sweep_multi / run_sweep_multi_with_trajectory (engine.rs:845-1348):
+ * Cartesian product of the dimensions (last dimension fastest, engine.rs:69-90). Like the
+ * reference, this runs a fresh engine seeded from sweep point 0's current state, with no BOLD
+ * monitors. The product size must equal the engine's n_sweep. */
+hb_status hb_engine_run_sweep_multi(hb_engine* engine, const hb_sweep_point* dims, int32_t n_dims,
+                                    int64_t n_steps, uint32_t run_flags,
+                                    const float* noise, int64_t noise_len, hb_result** out);
+
+/* Current batched state of one subnetwork (BatchHybridEngine::states, engine.rs:109):
+ * [n_sweep, nnodes*nmodes, nvar] written into `out` (len floats). */
+hb_status hb_engine_get_state(hb_engine* engine, int32_t sub_idx, float* out, int64_t len);
+
+/* BatchHybridEngine::step (engine.rs:113). */
+int64_t   hb_engine_step(const hb_engine* engine);
+
+/* Restore the state, history, step counter and BOLD monitors of a freshly created engine
+ * (no reference counterpart: lets a caller repeat a run without re-uploading the network). */
+hb_status hb_engine_reset(hb_engine* engine);
+
+/* Milliseconds of device time of the last run's simulation kernels, measured with CUDA events
+ * on the engine's stream, and the number of kernel launches of that run. */
+hb_status hb_engine_last_kernel_time(const hb_engine* engine, double* ms, int64_t* launches,
+                                     int32_t* kernel_kind);
+
+/* Use a caller-provided CUDA stream (cudaStream_t passed as void*) for subsequent runs; NULL
+ * restores the engine's own stream. */
+hb_status hb_engine_set_stream(hb_engine* engine, void* cuda_stream);
+
+/* ---- device-resident runs (inputs already in HBM; used to time the kernels alone) ---- */
+
+/* Upload the sweep values and noise of a run once; later `hb_engine_execute_prepared` calls
+ * reset the engine and run all steps on the device without host transfers. */
+hb_status hb_engine_prepare(hb_engine* engine, int32_t sub_idx, int32_t param_idx,
+                            const float* values, int32_t n_values, int64_t n_steps,
+                            uint32_t run_flags, const float* noise, int64_t noise_len);
+hb_status hb_engine_execute_prepared(hb_engine* engine);
+
+/* ---- results: BatchSweepResult (engine.rs:15-31) ---- */
+int32_t      hb_result_n_sweep(const hb_result* r);
+int32_t      hb_result_n_subnets(const hb_result* r);
+int32_t      hb_result_n_bold(const hb_result* r);
+double       hb_result_elapsed_ms(const hb_result* r);
+const float* hb_result_param_values(const hb_result* r, int64_t* len);
+const float* hb_result_tavg(const hb_result* r, int32_t sub_idx, int64_t* len);
+const float* hb_result_final_states(const hb_result* r, int32_t sub_idx, int64_t* len);
+const float* hb_result_trajectory(const hb_result* r, int32_t sub_idx, int64_t* len); /* NULL if not recorded */
+const float* hb_result_bold(const hb_result* r, int32_t monitor_idx, int64_t* len);
+void         hb_result_free(hb_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYBURN_GB300_H */
