@@ -1,0 +1,297 @@
+"""Benchmark of the batched neural-mass simulation step on GB300.
+
+Workload (one "step" = one full run of the hot path over one batch):
+  Generic2dOscillator, 74 nodes, 128 sweep points over the Linear coupling scale a in
+  linspace(0, 0.05); symmetric 20%-dense connectome with log-normal(0,1) weights / max; tract
+  lengths U[10, 200] mm at 3 mm/ms with dt 0.1 ms -> per-edge integer delays (up to ~667 steps);
+  Heun-stochastic, nsig 1e-3 with a seeded N(0,1) draw array shared by all points, 20 000 steps,
+  FP32. All inputs are synthetic (numpy default_rng seeds), no dataset.
+Metric: node-steps/s (points x nodes x steps / time), whole job over all ranks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value: device-resident run (inputs already in HBM), CUDA events on the engine's stream, L2
+flushed between timed iterations. e2e: the public API call (host noise in pinned memory -> H2D,
+run, D2H of tavg / final states) timed on the host. The reference arm times the CPU oracle
+(restatement of the reference's NdArray path) on all host cores on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_NODES, N_POINTS, N_STEPS = 74, 128, 20_000
+WORKLOAD = "g2do-74n-128pt-csr20pct-per-edge-delays-heun-stochastic-20000steps"
+METRIC = "node-steps/s"
+# algorithmic bytes per node-step of the delayed sparse gather (mean in-degree 4 B reads + 4 B ring
+# write + 8 B of shared noise per node), see the design doc
+FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._thr = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                parts = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(parts) >= 7:
+                    self.samples.append(parts)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thr = threading.Thread(target=self._run, daemon=True)
+        self._thr.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._thr:
+            self._thr.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def workload(n_steps=N_STEPS, n_points=N_POINTS):
+    from hyburn_gb300 import inputs
+
+    cfg, meta = inputs.batched_sweep(n_steps=n_steps, n_points=n_points)
+    noise = inputs.standard_normal((n_steps, N_NODES * 2), 2)
+    return cfg, meta, noise
+
+
+def algorithmic_bytes_per_node_step(meta) -> float:
+    c = meta["connectome"]
+    return 4.0 * c.nnz / c.n + 4.0 + 8.0
+
+
+def cpu_reference(n_points, steps_sample, n_threads):
+    """Times the CPU oracle on a bounded sample of the workload; returns node-steps/s."""
+    from hyburn_gb300 import SweepParam
+    from hyburn_gb300._abi import HB_SEM_DELAY_RING
+    from oracle.hb_oracle import OracleEngine
+
+    cfg, meta, noise = workload(steps_sample, n_points)
+    eng = OracleEngine(cfg, n_points, semantics=HB_SEM_DELAY_RING, n_threads=n_threads)
+    t0 = time.perf_counter()
+    eng.run_sweep(SweepParam(-1, 0), meta["values"], steps_sample, noise=noise)
+    dt = time.perf_counter() - t0
+    return n_points * N_NODES * steps_sample / dt, dt
+
+
+def calibrated_cpu_reference(n_threads, target_s=12.0):
+    rate, dt = cpu_reference(N_POINTS, 100, n_threads)
+    steps = int(max(100, min(N_STEPS, rate * target_s / (N_POINTS * N_NODES))))
+    rate, dt = cpu_reference(N_POINTS, steps, n_threads)
+    sample = f"{N_POINTS} points x {N_NODES} nodes x {steps} steps of the same workload ({dt:.1f} s)"
+    return rate, sample
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int, backend_ready: bool) -> float:
+    if world == 1 or not backend_ready:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    n_threads = os.cpu_count() or 1
+    vals = []
+    sample = ""
+    for _ in range(args.warmup):
+        cpu_reference(N_POINTS, 50, n_threads)
+    for _ in range(args.steps):
+        rate, sample = calibrated_cpu_reference(n_threads, target_s=max(2.0, 30.0 / max(args.steps, 1)))
+        vals.append(rate)
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "node-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "points": N_POINTS, "nodes": N_NODES, "steps_per_run": N_STEPS},
+            "cpu_baseline": {"value": v, "unit": "node-steps/s", "cores": n_threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--run-steps", type=int, default=N_STEPS,
+                    help="integration steps per run (smaller values only for profiler captures)")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    backend_ready = False
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        backend_ready = True
+
+    from hyburn_gb300 import BatchHybridEngine, SweepParam
+    from hyburn_gb300._abi import HB_SEM_DELAY_RING
+
+    n_run = args.run_steps
+    cfg, meta, noise = workload(n_run)
+    param = SweepParam(-1, 0)
+    eng = BatchHybridEngine.from_config(cfg, N_POINTS, semantics=HB_SEM_DELAY_RING)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # ---- device-resident runs (value) ----
+    eng.prepare(param, meta["values"], n_run, noise=noise)
+    for _ in range(args.warmup):
+        eng.execute_prepared()
+    torch.cuda.synchronize()
+    if backend_ready:
+        torch.distributed.barrier()
+    times, kern = [], []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                eng.execute_prepared()
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            ms_k, launches, _ = eng.last_kernel_time()
+            kern.append((ms_k, launches))
+        torch.cuda.synchronize()
+    if backend_ready:
+        torch.distributed.barrier()
+    total_ms = reduce_max(sum(times), world, backend_ready)
+    node_steps = N_POINTS * N_NODES * n_run
+    value = world * node_steps * args.steps / (total_ms / 1e3)
+
+    # dominant kernel: the resident simulation kernel, its launches timed on the engine stream
+    kern_ms = sum(k for k, _ in kern) / max(1, sum(n for _, n in kern))
+    bpns = algorithmic_bytes_per_node_step(meta)
+    achieved = bpns * node_steps / (kern_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "resident_kernel_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # ---- end to end through the public API (pinned host noise, H2D, run, D2H) ----
+    e2e = None
+    h2d = noise.nbytes + 4 * N_POINTS
+    d2h = 2 * 4 * N_POINTS * N_NODES * 2
+    if not args.no_e2e:
+        pinned = torch.from_numpy(noise).pin_memory()
+        host_noise = pinned.numpy()
+        eng2 = BatchHybridEngine.from_config(cfg, N_POINTS, semantics=HB_SEM_DELAY_RING)
+        for _ in range(max(1, args.warmup)):
+            eng2.reset()
+            eng2.run_sweep(param, meta["values"], n_run, noise=host_noise)
+        torch.cuda.synchronize()
+        if backend_ready:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng2.reset()
+            r = eng2.run_sweep(param, meta["values"], n_run, noise=host_noise)
+        e2e_s = reduce_max(time.perf_counter() - t0, world, backend_ready)
+        e2e = world * node_steps * args.steps / e2e_s
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points_per_gpu": N_POINTS, "nodes": N_NODES, "steps_per_run": n_run,
+                   "delays": f"per edge {meta['min_delay']}-{meta['max_delay']} steps", "l2": "flushed (512 MiB write) between timed iterations",
+                   "kernel": "point-resident persistent (plain)", "parallelism": f"sweep points sharded, {world} replica(s)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_node_step": bpns,
+                     "kernel_ms_per_launch": kern_ms},
+        "e2e": {"value": e2e, "unit": "node-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(n for _, n in kern)),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, sample = calibrated_cpu_reference(os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "node-steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if backend_ready:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

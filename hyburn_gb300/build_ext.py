@@ -47,7 +47,7 @@ def build(verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    cmd = [nvcc, "-shared", "-cudart", "static"] + ARCH + ["-o", LIB] + objs
+    cmd = [nvcc, "-shared", "-cudart", "static", "-Xlinker", "--no-undefined"] + ARCH + ["-o", LIB] + objs + ["-lrt", "-lpthread", "-ldl"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.run(cmd, check=True)

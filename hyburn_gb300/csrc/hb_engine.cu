@@ -21,7 +21,7 @@
 
 cudaError_t hb_launch_resident(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
-int hb_resident_static_smem();
+int hb_resident_smem_budget(int threads);
 
 namespace {
 
@@ -467,7 +467,9 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     const int64_t noise_rows_per_step = (int64_t)e->noise_row * (per_point_noise ? B : 1);
 
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
-    const size_t smem_cap = 227 * 1024 - sizeof(DevNet) - 512;
+    const int budget = hb_resident_smem_budget(e->threads);
+    if (budget < 0) return fail(HB_ERR_CUDA, "cannot query the shared-memory limit of the resident kernel");
+    const size_t smem_cap = (size_t)budget - 64;
     const size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
     const size_t ring_bytes = (size_t)e->R * e->cols * 4;
     size_t edges = 0;

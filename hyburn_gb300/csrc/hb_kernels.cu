@@ -458,15 +458,28 @@ __global__ void bold_bw_kernel(DevBold bold, int m, const float* __restrict__ me
 }  // namespace hb
 
 // ---- launch wrappers (called by the host engine) ----
+// largest dynamic shared-memory request a resident_kernel<MAXT> launch may make on this device
+template <int MAXT>
+static int resident_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, hb::resident_kernel<MAXT>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(hb::resident_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
 template <int MAXT>
 static cudaError_t launch_resident_t(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(hb::resident_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(227 * 1024 - sizeof(DevNet)));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    int maxdyn = resident_max_dynamic_smem<MAXT>();
+    if (maxdyn < 0) return cudaGetLastError() != cudaSuccess ? cudaGetLastError() : cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn) return cudaErrorInvalidValue;
     hb::resident_kernel<MAXT><<<B, threads, smem, st>>>(d_net, a);
     return cudaGetLastError();
 }
@@ -474,6 +487,12 @@ static cudaError_t launch_resident_t(const DevNet* d_net, const RunArgs& a, int 
 cudaError_t hb_launch_resident(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
     if (threads <= 256) return launch_resident_t<256>(d_net, a, B, threads, smem, st);
     return launch_resident_t<1024>(d_net, a, B, threads, smem, st);
+}
+
+// dynamic shared memory available to the resident kernel for a CTA of `threads` threads
+int hb_resident_smem_budget(int threads) {
+    int v = threads <= 256 ? resident_max_dynamic_smem<256>() : resident_max_dynamic_smem<1024>();
+    return v;
 }
 
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st) {

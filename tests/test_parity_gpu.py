@@ -11,7 +11,7 @@ import pytest
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
 from hyburn_gb300._abi import (HB_RUN_GLOBAL_RING, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
-from hyburn_gb300.config import InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
+from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
 
 from cases import NATIVE_SWEEP, noise_for, single_model, sub, sweep_values, three_subnet_ring
@@ -139,11 +139,26 @@ def test_coupling_sweep_batched_workload_small():
     compare(cfg, 16, SweepParam(-1, 0), meta["values"], 400, semantics=HB_SEM_DELAY_RING, noise=nz)
 
 
-def test_three_subnet_ring_with_cvar_maps_and_noise_per_point():
+def test_three_subnet_ring_with_noise_per_point():
+    # nsig is sized by the first subnetwork's nvar (engine.rs:451-452): JansenRit (6 vars) goes first
     cfg = three_subnet_ring(12, "heun_stochastic", delays=(0, 0, 0))
+    net = cfg.network
+    net.subnetworks = [net.subnetworks[1], net.subnetworks[2], net.subnetworks[0]]
+    remap = {1: 0, 2: 1, 0: 2}
+    for p in net.projections:
+        p.src, p.tgt = remap[p.src], remap[p.tgt]
     cfg.nsig = 1e-4
     nz = noise_for(cfg, 60, 3, True, 5)
-    compare(cfg, 3, SweepParam(0, 1), [0.0, 0.1, 0.2], 60, semantics=HB_SEM_NOISE_PER_POINT, noise=nz)
+    compare(cfg, 3, SweepParam(2, 1), [0.0, 0.1, 0.2], 60, semantics=HB_SEM_NOISE_PER_POINT, noise=nz)
+
+
+def test_stochastic_subnetwork_wider_than_nsig_is_rejected():
+    cfg = three_subnet_ring(12, "heun_stochastic")
+    cfg.nsig = 1e-4
+    nz = noise_for(cfg, 10, 2, False, 5)
+    eng = BatchHybridEngine.from_config(cfg, 2)
+    with pytest.raises(InvalidConfig, match="nsig has 2 entries"):
+        eng.run_sweep(SweepParam(0, 1), [0.0, 0.1], 10, noise=nz)
 
 
 def test_mpr_to_kuramoto_cvar_remap():
