@@ -41,6 +41,11 @@ HB_RUN_FORCE_RESIDENT = 1 << 8
 HB_RUN_FORCE_BLOCKED = 1 << 9
 HB_RUN_GLOBAL_RING = 1 << 10
 
+
+def HB_RUN_LANES(n: int) -> int:
+    return {1: 1, 2: 2, 4: 3, 8: 4}.get(n, 0) << 12
+
+
 # MODEL_REGISTRY rows of the six hot-path models (src/config.rs:43-49): (nvar, ncvar, nparams)
 MODEL_INFO = {
     "Generic2dOscillator": (2, 1, 12),

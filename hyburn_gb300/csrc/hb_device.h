@@ -1,8 +1,9 @@
 // hb_device.h — device-side network description shared by the host engine and the kernels.
 //
 // The host engine (hb_engine.cu) lowers a validated hb_sim_desc into these flat tables once per
-// engine (projections, CSR rows with packed per-edge delays) and once per run (per-point model
-// and coupling parameters, noise, BOLD schedules). Kernels receive a DevNet by value.
+// engine (projections, CSR rows with packed per-edge delays and precomputed ring offsets) and
+// once per run (per-point model and coupling parameters, noise, BOLD schedules). Kernels read
+// the DevNet from global memory and keep a copy in shared memory.
 #pragma once
 #include <cstdint>
 
@@ -12,6 +13,7 @@
 #define HB_PSTRIDE 32   // floats per (subnetwork, point) parameter row: params + derived constants
 #define HB_NCP 16       // floats per resolved coupling-function parameter row
 #define HB_MAX_THREADS 1024
+#define HB_MAX_IN 4       // incoming projections per subnetwork
 
 // model ids (order of the host registry)
 enum { HBM_G2DO = 0, HBM_MPR = 1, HBM_RWW = 2, HBM_KURAMOTO = 3, HBM_JR = 4, HBM_WC = 5 };
@@ -42,8 +44,12 @@ struct DevSub {
     int state_off;    // offset of this subnetwork in a point's packed state [nm][nvar]
     int noise_off;    // offset in a noise row
     int integ, sweep_form;
+    int lanes;        // threads per node (edge lists split over `lanes` lanes, power of two <= 8)
+    int lanes_log2;
     int n_in;
-    int in_idx[HB_MAX_PROJ];
+    int in_idx[HB_MAX_IN];
+    int n_mean_out;   // mean-field projections whose source is this subnetwork
+    int mean_out[HB_MAX_PROJ];
     const float* params;   // [B][HB_PSTRIDE]
 };
 
@@ -54,11 +60,13 @@ struct DevProj {
     int cm_s[4], cm_cpl[4];
     int mean_slot;        // MEAN: index of its partial-sum slot
     int smem_edges;       // resident kernel: edge offset inside the shared-memory copy, -1 if global
+    int maxd;             // largest edge delay (per-edge mode)
     float w;
     float cp[HB_NCP];
     const float* cp_pp;   // [B][HB_NCP] when the coupling parameters are swept, else nullptr
     const int* rowptr;    // [ntgt + 1]
     const uint32_t* edges; // (delay << 16) | src node
+    const int* eoff;       // ring offset of each edge: src column - delay * cols (per-edge mode) or src column
     const float* ew;
     const float* rowsums;
 };

@@ -19,9 +19,9 @@
 #include "hb_device.h"
 #include "hyburn_gb300.h"
 
-cudaError_t hb_launch_resident(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_resident(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
-int hb_resident_smem_budget(int threads);
+int hb_resident_smem_budget(int model, int threads);
 
 namespace {
 
@@ -120,12 +120,15 @@ struct HostProj {
     float w = 0;
     std::vector<int> rowptr;
     std::vector<uint32_t> edges;
+    std::vector<int> eoff;
     std::vector<float> ew, rowsums;
+    int maxd = 0;
     int direct = 0, ncm = 0, cm_s[4] = {0, 0, 0, 0}, cm_cpl[4] = {0, 0, 0, 0};
     int ncv = 1, pc = 1, oc = 1, pre_cpu = 0;
     // device copies
     int* d_rowptr = nullptr;
     uint32_t* d_edges = nullptr;
+    int* d_eoff = nullptr;
     float* d_ew = nullptr;
     float* d_rowsums = nullptr;
     float* d_cp_pp = nullptr;
@@ -233,6 +236,7 @@ struct hb_engine {
     std::vector<hb_bold_desc> bold_cfg;
     bool bold_removed = false;   // run_sweep_multi drops the monitors (engine.rs:1330-1333)
     int H = 0, R = 0, cols = 0, state_len = 0, noise_row = 0, threads = 0, n_mean = 0;
+    int kernel_model = -1;   // the model all subnetworks share, or -1
     DevNet net;
     DevNet* d_net = nullptr;
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
@@ -466,8 +470,39 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     const bool per_point_noise = (e->flags & HB_SEM_NOISE_PER_POINT) != 0;
     const int64_t noise_rows_per_step = (int64_t)e->noise_row * (per_point_noise ? B : 1);
 
+    // ---- thread layout: `lanes` threads per node share its edge list ----
+    {
+        int forced = (int)((run_flags >> 12) & 0xf);
+        std::vector<int> lanes(e->subs.size(), 1);
+        for (size_t i = 0; i < e->subs.size(); i++) {
+            if (forced) { lanes[i] = 1 << (forced - 1); continue; }
+            double deg = 0;
+            for (auto& hp : e->projs)
+                if (hp.tgt == (int)i && hp.kind == W_SPARSE) deg = std::max(deg, (double)hp.edges.size() / std::max(1, hp.ntgt));
+            lanes[i] = deg < 6 ? 1 : deg < 12 ? 2 : deg < 32 ? 4 : 8;
+        }
+        auto total = [&]() { int t = 0; for (size_t i = 0; i < e->subs.size(); i++) t += (e->subs[i].nm * lanes[i] + 31) / 32 * 32; return t; };
+        while (total() > HB_MAX_THREADS) {
+            size_t imax = 0;
+            for (size_t i = 1; i < lanes.size(); i++) if (lanes[i] > lanes[imax]) imax = i;
+            if (lanes[imax] == 1) break;
+            lanes[imax] >>= 1;
+        }
+        if (total() > HB_MAX_THREADS)
+            return fail(HB_ERR_UNSUPPORTED, "a sweep point needs %d threads; the point-resident kernel supports %d", total(), HB_MAX_THREADS);
+        int off = 0;
+        for (size_t i = 0; i < e->subs.size(); i++) {
+            DevSub& ds = e->net.sub[i];
+            ds.lanes = lanes[i];
+            ds.lanes_log2 = 0;
+            while ((1 << ds.lanes_log2) < lanes[i]) ds.lanes_log2++;
+            ds.thread_off = off;
+            off += (e->subs[i].nm * lanes[i] + 31) / 32 * 32;
+        }
+        e->threads = off;
+    }
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
-    const int budget = hb_resident_smem_budget(e->threads);
+    const int budget = hb_resident_smem_budget(e->kernel_model, e->threads);
     if (budget < 0) return fail(HB_ERR_CUDA, "cannot query the shared-memory limit of the resident kernel");
     const size_t smem_cap = (size_t)budget - 64;
     const size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
@@ -579,7 +614,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
         a.traj = record ? e->traj.p : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        CUDA_TRY(hb_launch_resident(e->d_net, a, B, e->threads, smem, st));
+        CUDA_TRY(hb_launch_resident(e->kernel_model, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
         e->last_launches++;
         if (record) {
@@ -756,6 +791,7 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
         DevSub& ds = e->net.sub[i];
         ds.model = s.model; ds.nm = s.nm; ds.nvar = s.nvar; ds.ncvar = s.ncvar;
         ds.thread_off = thread_off; ds.col_off = col_off; ds.state_off = state_off; ds.noise_off = state_off;
+        ds.lanes = 1; ds.lanes_log2 = 0;
         thread_off += (s.nm + 31) / 32 * 32;
         col_off += s.nm * s.ncvar;
         state_off += s.nm * s.nvar;
@@ -917,10 +953,32 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
     for (int i = 0; i < d->n_subnets; i++) {
         DevSub& ds = e->net.sub[i];
         ds.n_in = 0;
-        for (int p = 0; p < d->n_projections; p++)
-            if (e->projs[p].tgt == i) ds.in_idx[ds.n_in++] = p;
+        ds.n_mean_out = 0;
+        for (int p = 0; p < d->n_projections; p++) {
+            if (e->projs[p].tgt == i) {
+                if (ds.n_in == HB_MAX_IN)
+                    return bail(fail(HB_ERR_UNSUPPORTED, "subnetwork %d receives more than %d projections", i, HB_MAX_IN));
+                ds.in_idx[ds.n_in++] = p;
+            }
+            if (e->projs[p].src == i && e->projs[p].kind == W_MEAN) ds.mean_out[ds.n_mean_out++] = p;
+        }
         ds.integ = eff_integrator(e, e->subs[i].model);
     }
+    e->kernel_model = e->subs[0].model;
+    for (auto& sb : e->subs)
+        if (sb.model != e->kernel_model) e->kernel_model = -1;
+    // ring offset of every edge: source column minus delay * cols (per-edge) or the source column
+    for (auto& hp : e->projs) {
+        if (hp.kind != W_SPARSE) continue;
+        const int scol = e->net.sub[hp.src].col_off, sncv = e->subs[hp.src].ncvar;
+        hp.eoff.resize(hp.edges.size());
+        for (size_t k2 = 0; k2 < hp.edges.size(); k2++) {
+            int src = (int)(hp.edges[k2] & 0xffffu), dl = (int)(hp.edges[k2] >> 16);
+            hp.eoff[k2] = scol + src * sncv - (hp.dmode == HBD_EDGE ? dl * e->cols : 0);
+            hp.maxd = std::max(hp.maxd, dl);
+        }
+    }
+    for (size_t p = 0; p < e->projs.size(); p++) e->net.proj[p].maxd = e->projs[p].maxd;
     // BOLD monitors (engine.rs:419-449)
     for (int m = 0; m < d->n_bold; m++) {
         if (e->subs[0].nmodes != 1) return bail(fail(HB_ERR_UNSUPPORTED, "BOLD monitors need nmodes == 1 on subnetwork 0"));
@@ -971,12 +1029,14 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
             if ((s = cu(cudaMemcpy(hp.d_rowptr, hp.rowptr.data(), hp.rowptr.size() * 4, cudaMemcpyHostToDevice), "upload rowptr"))) return bail(s);
             size_t ne = std::max<size_t>(hp.edges.size(), 1);
             if ((s = cu(cudaMalloc(&hp.d_edges, ne * 4), "cudaMalloc(edges)"))) return bail(s);
+            if ((s = cu(cudaMalloc(&hp.d_eoff, ne * 4), "cudaMalloc(eoff)"))) return bail(s);
             if ((s = cu(cudaMalloc(&hp.d_ew, ne * 4), "cudaMalloc(ew)"))) return bail(s);
             if (!hp.edges.empty()) {
                 if ((s = cu(cudaMemcpy(hp.d_edges, hp.edges.data(), hp.edges.size() * 4, cudaMemcpyHostToDevice), "upload edges"))) return bail(s);
+                if ((s = cu(cudaMemcpy(hp.d_eoff, hp.eoff.data(), hp.eoff.size() * 4, cudaMemcpyHostToDevice), "upload eoff"))) return bail(s);
                 if ((s = cu(cudaMemcpy(hp.d_ew, hp.ew.data(), hp.ew.size() * 4, cudaMemcpyHostToDevice), "upload weights"))) return bail(s);
             }
-            dp.rowptr = hp.d_rowptr; dp.edges = hp.d_edges; dp.ew = hp.d_ew;
+            dp.rowptr = hp.d_rowptr; dp.edges = hp.d_edges; dp.eoff = hp.d_eoff; dp.ew = hp.d_ew;
         }
         if (!hp.rowsums.empty()) {
             if ((s = cu(cudaMalloc(&hp.d_rowsums, hp.rowsums.size() * 4), "cudaMalloc(rowsums)"))) return bail(s);
@@ -995,6 +1055,7 @@ void hb_engine_destroy(hb_engine* e) {
     for (auto& hp : e->projs) {
         if (hp.d_rowptr) cudaFree(hp.d_rowptr);
         if (hp.d_edges) cudaFree(hp.d_edges);
+        if (hp.d_eoff) cudaFree(hp.d_eoff);
         if (hp.d_ew) cudaFree(hp.d_ew);
         if (hp.d_rowsums) cudaFree(hp.d_rowsums);
         if (hp.d_cp_pp) cudaFree(hp.d_cp_pp);

@@ -300,6 +300,24 @@ __device__ __forceinline__ int post(int cfk, const float* cp, int has_rowsums, c
     }
 }
 
+// compile-time model facts (MODEL = -1: decided at run time)
+__host__ __device__ constexpr int c_nvar(int m) { return m == HBM_G2DO ? 2 : m == HBM_MPR ? 2 : m == HBM_RWW ? 1 : m == HBM_KURAMOTO ? 1 : m == HBM_JR ? 6 : m == HBM_WC ? 2 : 6; }
+__host__ __device__ constexpr int c_ncvar(int m) { return m == HBM_MPR ? 2 : (m >= 0 ? 1 : 2); }
+// parameter-row entries a model reads (WilsonCowan also reads the two derived constants at 24, 25)
+__host__ __device__ constexpr int c_nparams_used(int m) {
+    return m == HBM_G2DO ? 12 : m == HBM_MPR ? 7 : m == HBM_RWW ? 8 : m == HBM_KURAMOTO ? 1 : m == HBM_JR ? 13 : m == HBM_WC ? 26 : HB_PSTRIDE;
+}
+
+template <int MODEL>
+__device__ __forceinline__ void dfun_m(int model, const float* p, int sweep_form, const float* x, const float* c, float* dx) {
+    dfun(MODEL >= 0 ? MODEL : model, p, sweep_form, x, c, dx);
+}
+
+template <int MODEL>
+__device__ __forceinline__ void clamp_m(int model, float* x) {
+    clamp(MODEL >= 0 ? MODEL : model, x);
+}
+
 __device__ __forceinline__ float pick4(const float* a, int i) {
     return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
 }

@@ -1,0 +1,570 @@
+// hb_resident.cuh — the point-resident persistent simulation kernel (the "plain" form).
+//
+// One CTA owns one sweep point for a whole launch: every node of every subnetwork, `lanes`
+// threads per node (warp aligned per subnetwork). State, temporal average and BOLD window sums
+// stay in registers across steps. The coupling-variable history ring ([R][cols], only the cvars)
+// stays in shared memory when it fits, otherwise in global memory. Each CSR edge carries a
+// precomputed ring offset (source column - delay * cols), so a delayed read is one add, one
+// wrap and one load. The edges of a node are split over its `lanes` lanes and the partial sums
+// are combined with a butterfly; the model update is evaluated identically by all lanes of the
+// node and lane 0 alone publishes results.
+//
+// Synchronisation: one __syncthreads per step separates publishing x_s into ring slot s % R
+// from the coupling gather; R >= H + 1 so the write of step s + 1 never hits a slot that a
+// slower thread may still read at step s.
+//
+// Template parameters: MODEL (a fixed model id, or -1 for networks mixing models) and MAXT
+// (the launch bound, which sets the register budget).
+#pragma once
+#include <cuda_runtime.h>
+#include "hb_models.cuh"
+
+namespace hb {
+
+enum { PRE_ID = 0, PRE_KURA = 1, PRE_GEN = 2 };
+
+__device__ __forceinline__ int wrap_add(int a, int wrap) { return a < 0 ? a + wrap : a; }
+
+// single-delay projection at step s: false when the source rows are the zero tensor (zeros before
+// pre(), engine.rs:580-584 / runtime.rs:246-249); dd is the read-back distance in steps
+__device__ __forceinline__ bool single_delay(const DevProj& P, int64_t s, int H, int& dd) {
+    int d = P.delay;
+    if (d == 0 || s == 0) { dd = 0; return true; }
+    if ((int64_t)d > s) return false;
+    if (P.dmode == HBD_COMPAT) {
+        // window index (s - d + H) % H of the shift-window history holds x_{s+1+idx-H}
+        dd = H - 1 - (int)((s - d) % H);
+        return (int64_t)dd <= s;
+    }
+    dd = d;
+    return true;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ int lower_bound_emit(const BoldEmit* e, int n, int k) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (e[mid].k < k) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// gx[c] += sum over edges e = e0 + lane, e0 + lane + L, ... of w_e * pre(ring[base + off_e])
+template <int PRE>
+__device__ __forceinline__ void gather(const float* __restrict__ ring, const int* __restrict__ eoff,
+                                       const float* __restrict__ ew, int e0, int e1, int lane, int L, int base,
+                                       int wrap, int ncv, int cfk, const float* cp, int cpu_form, float* gx) {
+    if (PRE == PRE_ID) {
+        float a0 = 0.0f, a1 = 0.0f;
+        if (ncv == 1) {
+#pragma unroll 4
+            for (int e = e0 + lane; e < e1; e += L) {
+                int a = wrap_add(base + eoff[e], wrap);
+                a0 += ew[e] * ring[a];
+            }
+        } else {
+#pragma unroll 2
+            for (int e = e0 + lane; e < e1; e += L) {
+                int a = wrap_add(base + eoff[e], wrap);
+                float w = ew[e];
+                a0 += w * ring[a];
+                a1 += w * ring[a + 1];
+            }
+        }
+        gx[0] += a0;
+        gx[1] += a1;
+    } else if (PRE == PRE_KURA) {  // one cvar: [sin, cos]
+        float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll 2
+        for (int e = e0 + lane; e < e1; e += L) {
+            int a = wrap_add(base + eoff[e], wrap);
+            float w = ew[e], v = ring[a];
+            a0 += w * sinf(v);
+            a1 += w * cosf(v);
+        }
+        gx[0] += a0;
+        gx[1] += a1;
+    } else {
+        for (int e = e0 + lane; e < e1; e += L) {
+            int a = wrap_add(base + eoff[e], wrap);
+            float cv[2] = {ring[a], ncv > 1 ? ring[a + 1] : 0.0f}, pv[4] = {0.f, 0.f, 0.f, 0.f};
+            pre(cfk, cp, cpu_form, cv, ncv, pv);
+            float w = ew[e];
+#pragma unroll
+            for (int c = 0; c < 4; c++) gx[c] += w * pv[c];
+        }
+    }
+}
+
+// per-edge delays during the first max-delay steps: the delay of every edge is checked (zero rows
+// after pre() for d > s, current state for d == 0 or s == 0, runtime.rs:166-176)
+__device__ __forceinline__ void gather_early(const float* __restrict__ ring, const DevProj& P, int e0, int e1,
+                                             int lane, int L, int64_t s, int slot, int R, int cols, int scol,
+                                             int sncv, const float* cp, float* gx) {
+    for (int e = e0 + lane; e < e1; e += L) {
+        uint32_t m = P.edges[e];
+        int d = (int)(m >> 16), src = (int)(m & 0xffffu);
+        int dd = d;
+        if (d == 0 || s == 0) dd = 0;
+        else if ((int64_t)d > s) continue;
+        int row = slot - dd;
+        row = row < 0 ? row + R : row;
+        const float* rr = ring + row * cols + scol + src * sncv;
+        float cv[2] = {rr[0], P.ncv > 1 ? rr[1] : 0.0f}, pv[4] = {0.f, 0.f, 0.f, 0.f};
+        pre(P.cfk, cp, P.pre_cpu, cv, P.ncv, pv);
+        float w = P.ew[e];
+#pragma unroll
+        for (int c = 0; c < 4; c++) gx[c] += w * pv[c];
+    }
+}
+
+template <int MODEL, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ DevNet net;
+    {
+        const int* src = reinterpret_cast<const int*>(gnet);
+        int* dst = reinterpret_cast<int*>(&net);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+
+    const int b = blockIdx.x;
+    const int t = threadIdx.x;
+    const int wlane = t & 31, warp = t >> 5;
+    const int R = net.R, cols = net.cols, H = net.H, B = net.B;
+    const int ring_words = R * cols;
+
+    size_t off = 0;
+    float* ring;
+    if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)ring_words * sizeof(float); }
+    else ring = a.ring + (size_t)b * ring_words;
+    off = (off + 15) & ~(size_t)15;
+    int* s_eoff = reinterpret_cast<int*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    float* s_ew = reinterpret_cast<float*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    off = (off + 15) & ~(size_t)15;
+    float* s_part = reinterpret_cast<float*>(smem + off);  // [2][n_mean][32 warps][4]
+
+    if (a.ring_in_smem && a.load_ring) {
+        const float4* g = reinterpret_cast<const float4*>(a.ring + (size_t)b * ring_words);
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += blockDim.x) r4[i] = g[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) ring[i] = a.ring[(size_t)b * ring_words + i];
+    }
+    for (int p = 0; p < net.n_proj; p++) {
+        const DevProj& P = net.proj[p];
+        if (P.kind != HBK_SPARSE || P.smem_edges < 0) continue;
+        const int nnz = P.rowptr[P.ntgt];
+        for (int i = t; i < nnz; i += blockDim.x) {
+            s_eoff[P.smem_edges + i] = P.eoff[i];
+            s_ew[P.smem_edges + i] = P.ew[i];
+        }
+    }
+
+    // ---- role: lane `lane` of node n of subnetwork k ----
+    int k = 0;
+    for (int i = 1; i < net.n_sub; i++)
+        if (t >= net.sub[i].thread_off) k = i;
+    const int model = MODEL >= 0 ? MODEL : net.sub[k].model;
+    const int nm = net.sub[k].nm, nvar = MODEL >= 0 ? c_nvar(MODEL) : net.sub[k].nvar;
+    const int ncvar = MODEL >= 0 ? c_ncvar(MODEL) : net.sub[k].ncvar;
+    const int L = net.sub[k].lanes;
+    const int local = t - net.sub[k].thread_off;
+    const int n = local >> net.sub[k].lanes_log2;
+    const int lane = local & (L - 1);
+    const bool active = n < nm;
+    const bool lead = active && lane == 0;
+    const int nn = active ? n : 0;
+    const int col_off = net.sub[k].col_off, integ = net.sub[k].integ, sweep_form = net.sub[k].sweep_form;
+    const int mycol = col_off + nn * ncvar;
+
+    float prm[HB_PSTRIDE];
+    {
+        const float* pr = net.sub[k].params + (size_t)b * HB_PSTRIDE;
+#pragma unroll
+        for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
+    }
+    float x[6], tv[6];
+    const size_t st_base = (size_t)b * net.state_len + net.sub[k].state_off + (size_t)nn * nvar;
+    const bool first_launch_of_run = (a.s0 == a.run_s0);
+#pragma unroll
+    for (int v = 0; v < 6; v++) {
+        x[v] = (active && v < nvar) ? a.state[st_base + v] : 0.0f;
+        tv[v] = (active && v < nvar && !first_launch_of_run) ? a.tavg[st_base + v] : 0.0f;
+    }
+    // row bounds of the incoming sparse projections
+    const int n_in = net.sub[k].n_in;
+    int re0[HB_MAX_IN], re1[HB_MAX_IN];
+#pragma unroll
+    for (int q = 0; q < HB_MAX_IN; q++) {
+        re0[q] = re1[q] = 0;
+        if (q < n_in) {
+            const DevProj& P = net.proj[net.sub[k].in_idx[q]];
+            if (P.kind == HBK_SPARSE && active) { re0[q] = P.rowptr[n]; re1[q] = P.rowptr[n + 1]; }
+        }
+    }
+    // noise stream of this node
+    const bool stoch = (integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH);
+    const float* nptr = a.noise + (a.noise_per_point ? (size_t)b * net.noise_row : 0) + net.sub[k].noise_off + (size_t)nn * nvar;
+    const size_t nstride = (size_t)(a.noise_per_point ? B : 1) * net.noise_row;
+    float nz_next[6];
+#pragma unroll
+    for (int v = 0; v < 6; v++) nz_next[v] = (stoch && active && v < nvar) ? __ldcs(nptr + v) : 0.0f;
+    // BOLD (subnetwork 0, nmodes == 1)
+    const bool bold_thread = (k == 0) && lead && a.bold.n > 0;
+    const int N0 = a.bold.n0;
+    float bacc[HB_MAX_BOLD];
+    int bcnt[HB_MAX_BOLD];
+#pragma unroll
+    for (int m = 0; m < HB_MAX_BOLD; m++) {
+        bacc[m] = 0.0f;
+        bcnt[m] = 0;
+        if (m < a.bold.n) {
+            bcnt[m] = (int)((a.s0 - a.run_s0) % a.bold.period[m]);
+            if (bold_thread && !first_launch_of_run) bacc[m] = a.bold.acc[m][(size_t)b * N0 + n];
+        }
+    }
+    __syncthreads();
+
+    int64_t s = a.s0;
+    int slot = (int)(s % R);
+    const int n_mean = net.n_mean;
+    for (int it = 0; it < a.n_steps; ++it, ++s) {
+        const int buf = it & 1;
+        // ---- 1. publish x_s (first ncvar state vars, engine.rs:570) into ring slot s % R ----
+        if (lead) {
+            ring[slot * cols + mycol] = x[0];
+            if (ncvar > 1) ring[slot * cols + mycol + 1] = x[1];
+        }
+        // ---- mean-field partial sums of projections whose source is this subnetwork ----
+        for (int q = 0; q < net.sub[k].n_mean_out; q++) {
+            const DevProj& P = net.proj[net.sub[k].mean_out[q]];
+            const float* cp = P.cp_pp ? P.cp_pp + (size_t)b * HB_NCP : P.cp;
+            float pv[4] = {0.f, 0.f, 0.f, 0.f};
+            int dd;
+            bool ok = single_delay(P, s, H, dd);
+            if (lead) {
+                float cv[2] = {0.0f, 0.0f};
+                if (ok) {
+                    int row = slot - dd;
+                    row = row < 0 ? row + R : row;
+                    cv[0] = dd == 0 ? x[0] : ring[row * cols + mycol];
+                    if (P.ncv > 1) cv[1] = dd == 0 ? x[1] : ring[row * cols + mycol + 1];
+                }
+                pre(P.cfk, cp, 0, cv, P.ncv, pv);
+            }
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                if (c < P.pc) {
+                    float sum = warp_sum(pv[c]);
+                    if (wlane == 0) s_part[((buf * n_mean + P.mean_slot) * 32 + warp) * 4 + c] = sum;
+                }
+            }
+        }
+        // noise of this step was prefetched one step ahead
+        float nz[6];
+#pragma unroll
+        for (int v = 0; v < 6; v++) nz[v] = nz_next[v] * net.noise_scale[v];
+        if (stoch && it + 1 < a.n_steps) {
+            nptr += nstride;
+#pragma unroll
+            for (int v = 0; v < 6; v++) nz_next[v] = (active && v < nvar) ? __ldcs(nptr + v) : 0.0f;
+        }
+        __syncthreads();
+
+        // ---- 2. coupling into this subnetwork (engine.rs:557-674) ----
+        float cc[2] = {0.0f, 0.0f};
+#pragma unroll
+        for (int q = 0; q < HB_MAX_IN; q++) {
+            if (q >= n_in) break;
+            const DevProj& P = net.proj[net.sub[k].in_idx[q]];
+            const float* cp = P.cp_pp ? P.cp_pp + (size_t)b * HB_NCP : P.cp;
+            const int scol = net.sub[P.src].col_off, sncv = net.sub[P.src].ncvar;
+            float gx[4] = {0.f, 0.f, 0.f, 0.f};
+            if (P.kind == HBK_MEAN) {
+                const int w0 = net.sub[P.src].thread_off >> 5;
+                const int w1 = (net.sub[P.src].thread_off + P.nsrc * net.sub[P.src].lanes + 31) >> 5;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    if (c < P.pc) {
+                        float acc = 0.0f;
+                        for (int w = w0; w < w1; w++) acc += s_part[((buf * n_mean + P.mean_slot) * 32 + w) * 4 + c];
+                        gx[c] = (acc / (float)P.nsrc) * P.w;
+                    }
+                }
+            } else if (P.kind == HBK_DIAG) {
+                int dd;
+                bool ok = single_delay(P, s, H, dd);
+                int row = slot - (ok ? dd : 0);
+                row = row < 0 ? row + R : row;
+                const float* rr = ring + row * cols + scol + nn * sncv;
+                float cv[2] = {ok ? rr[0] : 0.0f, (ok && P.ncv > 1) ? rr[1] : 0.0f}, pv[4] = {0.f, 0.f, 0.f, 0.f};
+                pre(P.cfk, cp, 0, cv, P.ncv, pv);
+#pragma unroll
+                for (int c = 0; c < 4; c++) gx[c] = P.w * pv[c];
+            } else {
+                const int* eo = P.smem_edges >= 0 ? s_eoff + P.smem_edges : P.eoff;
+                const float* ew = P.smem_edges >= 0 ? s_ew + P.smem_edges : P.ew;
+                const int pk = (P.cfk == HBC_KURAMOTO && P.ncv == 1) ? PRE_KURA
+                             : ((P.cfk == HBC_TANH || P.cfk == HBC_SJR || P.cfk == HBC_PRESIG || P.cfk == HBC_KURAMOTO) ? PRE_GEN : PRE_ID);
+                if (P.dmode == HBD_EDGE) {
+                    if (s < (int64_t)P.maxd || s == 0) {
+                        gather_early(ring, P, re0[q], re1[q], lane, L, s, slot, R, cols, scol, sncv, cp, gx);
+                    } else {
+                        const int base = slot * cols;
+                        if (pk == PRE_ID) gather<PRE_ID>(ring, eo, ew, re0[q], re1[q], lane, L, base, ring_words, P.ncv, P.cfk, cp, P.pre_cpu, gx);
+                        else if (pk == PRE_KURA) gather<PRE_KURA>(ring, eo, ew, re0[q], re1[q], lane, L, base, ring_words, P.ncv, P.cfk, cp, P.pre_cpu, gx);
+                        else gather<PRE_GEN>(ring, eo, ew, re0[q], re1[q], lane, L, base, ring_words, P.ncv, P.cfk, cp, P.pre_cpu, gx);
+                    }
+                } else {
+                    int dd;
+                    bool ok = single_delay(P, s, H, dd);
+                    if (ok) {
+                        int row = slot - dd;
+                        row = row < 0 ? row + R : row;
+                        const int base = row * cols;
+                        if (pk == PRE_ID) gather<PRE_ID>(ring, eo, ew, re0[q], re1[q], lane, L, base, 0, P.ncv, P.cfk, cp, 0, gx);
+                        else if (pk == PRE_KURA) gather<PRE_KURA>(ring, eo, ew, re0[q], re1[q], lane, L, base, 0, P.ncv, P.cfk, cp, 0, gx);
+                        else gather<PRE_GEN>(ring, eo, ew, re0[q], re1[q], lane, L, base, 0, P.ncv, P.cfk, cp, 0, gx);
+                    } else {
+                        // every source row is the zero tensor: sum of w_e * pre(0) in edge order
+                        float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
+                        pre(P.cfk, cp, 0, zero, P.ncv, pz);
+                        for (int e = re0[q] + lane; e < re1[q]; e += L) {
+                            float w = ew[e];
+#pragma unroll
+                            for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
+                        }
+                    }
+                }
+                // combine the lanes of this node
+                for (int o = L >> 1; o > 0; o >>= 1) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) gx[c] += __shfl_xor_sync(0xffffffffu, gx[c], o);
+                }
+            }
+            if (active) {
+                float out[4] = {0.f, 0.f, 0.f, 0.f};
+                float rs = P.has_rowsums ? P.rowsums[n] : 0.0f;
+                int oc = post(P.cfk, cp, P.has_rowsums, gx, P.pc, x, ncvar, rs, out);
+                if (P.direct) {
+                    cc[0] = cc[0] + out[0];
+                    if (ncvar > 1 && oc > 1) cc[1] = cc[1] + out[1];
+                } else {
+                    float t0 = 0.0f, t1 = 0.0f;
+                    for (int j = 0; j < P.ncm; j++) {
+                        int sidx = P.cm_s[j], cpl = P.cm_cpl[j];
+                        if (sidx < sncv && cpl < ncvar) {
+                            float o = pick4(out, sidx);
+                            if (cpl == 0) t0 += o; else t1 += o;
+                        }
+                    }
+                    cc[0] = cc[0] + t0;
+                    if (ncvar > 1) cc[1] = cc[1] + t1;
+                }
+            }
+        }
+
+        // ---- 3. integrate (engine.rs:677-783) ----
+        if (active) {
+            float k1[6], k2[6], tmp[6];
+            const float dt = net.dt;
+            dfun_m<MODEL>(model, prm, sweep_form, x, cc, k1);
+            switch (integ) {
+            case HBI_HEUN_DET:
+#pragma unroll
+                for (int v = 0; v < 6; v++) tmp[v] = x[v] + k1[v] * dt;
+                clamp_m<MODEL>(model, tmp);
+                dfun_m<MODEL>(model, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < 6; v++) x[v] = x[v] + (k1[v] + k2[v]) * net.dt_half;
+                break;
+            case HBI_EULER:
+#pragma unroll
+                for (int v = 0; v < 6; v++) x[v] = x[v] + k1[v] * dt;
+                break;
+            case HBI_EULER_STOCH:
+#pragma unroll
+                for (int v = 0; v < 6; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
+                break;
+            case HBI_HEUN_STOCH:
+#pragma unroll
+                for (int v = 0; v < 6; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+                clamp_m<MODEL>(model, tmp);
+                dfun_m<MODEL>(model, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < 6; v++) x[v] = (x[v] + (k1[v] + k2[v]) * net.dt_half) + nz[v];
+                break;
+            default: {  // RK4 / RK4 stochastic
+                float k3[6], k4[6];
+                const float h2 = net.dt_h2, h6 = net.dt_sixth;
+#pragma unroll
+                for (int v = 0; v < 6; v++) tmp[v] = x[v] + k1[v] * h2;
+                clamp_m<MODEL>(model, tmp);
+                dfun_m<MODEL>(model, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < 6; v++) tmp[v] = x[v] + k2[v] * h2;
+                clamp_m<MODEL>(model, tmp);
+                dfun_m<MODEL>(model, prm, sweep_form, tmp, cc, k3);
+#pragma unroll
+                for (int v = 0; v < 6; v++) tmp[v] = x[v] + k3[v] * dt;
+                clamp_m<MODEL>(model, tmp);
+                dfun_m<MODEL>(model, prm, sweep_form, tmp, cc, k4);
+#pragma unroll
+                for (int v = 0; v < 6; v++) {
+                    float sacc = k1[v] + k2[v] * 2.0f;
+                    sacc = sacc + k3[v] * 2.0f;
+                    sacc = sacc + k4[v];
+                    x[v] = x[v] + sacc * h6;
+                }
+                if (integ == HBI_RK4_STOCH) {
+#pragma unroll
+                    for (int v = 0; v < 6; v++) x[v] = x[v] + nz[v];
+                }
+                break;
+            }
+            }
+            clamp_m<MODEL>(model, x);
+#pragma unroll
+            for (int v = 0; v < 6; v++) tv[v] = tv[v] + x[v];
+            if (a.traj && lane == 0) {
+                float* tr = a.traj + ((size_t)it * B + b) * net.state_len + net.sub[k].state_off + (size_t)n * nvar;
+#pragma unroll
+                for (int v = 0; v < 6; v++) if (v < nvar) __stcs(tr + v, x[v]);
+            }
+        }
+
+        // ---- 4. BOLD monitors on var0 of subnetwork 0 (engine.rs:786-801) ----
+        if (bold_thread) {
+            const int64_t rel = s - a.run_s0;
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++) {
+                if (m >= a.bold.n) break;
+                bacc[m] = bacc[m] + x[0];
+                bcnt[m] += 1;
+                bool full = bcnt[m] >= a.bold.period[m];
+                bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
+                if (!(full || last_partial)) continue;
+                int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
+                if (a.bold.per_point) {
+                    float avg = bacc[m] / (float)bcnt[m];
+                    float* bw = a.bold.bw[m];
+                    const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
+                    float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
+                    float prev = bw[4 * stride + idx];
+                    bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
+                    float cur = bw_signal(bv, bq);
+                    const BoldEmit* em = a.bold.emit[m];
+                    for (int j = lower_bound_emit(em, a.bold.n_emit[m], kk); j < a.bold.n_emit[m] && em[j].k == kk; j++) {
+                        float val = em[j].interp ? prev + (cur - prev) * em[j].w : cur;
+                        a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[j].out) * N0 + n] = val;
+                    }
+                    bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
+                    bw[4 * stride + idx] = cur;
+                } else {
+                    a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
+                }
+                bacc[m] = 0.0f;
+                bcnt[m] = 0;
+            }
+        }
+        slot = (slot + 1 == R) ? 0 : slot + 1;
+    }
+
+    // ---- launch end: persist state, running sums and the shared ring ----
+    if (lead) {
+        bool bad = false;
+#pragma unroll
+        for (int v = 0; v < 6; v++) {
+            if (v < nvar) {
+                a.state[st_base + v] = x[v];
+                a.tavg[st_base + v] = tv[v];
+                bad |= !isfinite(x[v]);
+            }
+        }
+        if (a.check_finite && bad) atomicOr(a.flags, 1);
+    }
+    if (bold_thread) {
+#pragma unroll
+        for (int m = 0; m < HB_MAX_BOLD; m++)
+            if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + n] = bacc[m];
+    }
+    if (a.ring_in_smem && a.store_ring) {
+        __syncthreads();
+        float4* g = reinterpret_cast<float4*>(a.ring + (size_t)b * ring_words);
+        const float4* r4 = reinterpret_cast<const float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += blockDim.x) g[i] = r4[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) a.ring[(size_t)b * ring_words + i] = ring[i];
+    }
+}
+
+// dynamic shared memory available to resident_kernel<MODEL, MAXT> on this device (sets the opt-in)
+template <int MODEL, int MAXT>
+int resident_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, resident_kernel<MODEL, MAXT>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(resident_kernel<MODEL, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
+template <int MODEL, int MAXT>
+cudaError_t launch_resident(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
+    int maxdyn = resident_max_dynamic_smem<MODEL, MAXT>();
+    if (maxdyn < 0) return cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn) return cudaErrorInvalidValue;
+    resident_kernel<MODEL, MAXT><<<B, threads, smem, st>>>(d_net, a);
+    return cudaGetLastError();
+}
+
+}  // namespace hb
+
+// per-MAXT entry points (one translation unit each)
+cudaError_t hb_launch_resident_256(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_resident_512(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_resident_1024(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_resident_budget_256(int model);
+int hb_resident_budget_512(int model);
+int hb_resident_budget_1024(int model);
+
+#define HB_RESIDENT_UNIT(MAXT)                                                                                      \
+    cudaError_t hb_launch_resident_##MAXT(int model, const DevNet* d_net, const RunArgs& a, int B, int threads,     \
+                                          size_t smem, cudaStream_t st) {                                            \
+        switch (model) {                                                                                             \
+        case 0: return hb::launch_resident<0, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        case 1: return hb::launch_resident<1, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        case 2: return hb::launch_resident<2, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        case 3: return hb::launch_resident<3, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        case 4: return hb::launch_resident<4, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        case 5: return hb::launch_resident<5, MAXT>(d_net, a, B, threads, smem, st);                                 \
+        default: return hb::launch_resident<-1, MAXT>(d_net, a, B, threads, smem, st);                               \
+        }                                                                                                            \
+    }                                                                                                                \
+    int hb_resident_budget_##MAXT(int model) {                                                                       \
+        switch (model) {                                                                                             \
+        case 0: return hb::resident_max_dynamic_smem<0, MAXT>();                                                     \
+        case 1: return hb::resident_max_dynamic_smem<1, MAXT>();                                                     \
+        case 2: return hb::resident_max_dynamic_smem<2, MAXT>();                                                     \
+        case 3: return hb::resident_max_dynamic_smem<3, MAXT>();                                                     \
+        case 4: return hb::resident_max_dynamic_smem<4, MAXT>();                                                     \
+        case 5: return hb::resident_max_dynamic_smem<5, MAXT>();                                                     \
+        default: return hb::resident_max_dynamic_smem<-1, MAXT>();                                                   \
+        }                                                                                                            \
+    }

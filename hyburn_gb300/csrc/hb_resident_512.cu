@@ -1,0 +1,4 @@
+// Point-resident kernel instantiations with launch bound 512 (see hb_resident.cuh).
+#include "hb_resident.cuh"
+
+HB_RESIDENT_UNIT(512)

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
-from hyburn_gb300._abi import (HB_RUN_GLOBAL_RING, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
+from hyburn_gb300._abi import (HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
 from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
@@ -129,6 +129,19 @@ def test_ring_per_edge_global_ring_matches_shared_ring():
     e2 = BatchHybridEngine.from_config(cfg, 3, semantics=HB_SEM_DELAY_RING)
     g2 = e2.run_sweep(SweepParam(-1, 0), [0.0, 0.1, 0.2], 100, noise=nz, run_flags=HB_RUN_GLOBAL_RING)
     assert np.array_equal(g1.final_states[0], g2.final_states[0])
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+@pytest.mark.parametrize("semantics", [0, HB_SEM_DELAY_RING])
+def test_lane_split_gather(lanes, semantics):
+    """The edge list of a node split over 1-8 lanes gives the oracle's coupling (summation order
+    differs only by the final lane combine)."""
+    cfg = single_model("Kuramoto", 30, "heun", "Kuramoto", (1.5,), weights="csr", delays="per_edge"
+                       if semantics else [3], density=0.5)
+    compare(cfg, 3, SweepParam(0, 0), [0.8, 1.0, 1.2], 120, semantics=semantics, run_flags=HB_RUN_LANES(lanes))
+    cfg = single_model("MontbrioPazoRoxin", 30, "rk4", "Linear", (0.3,), weights="csr", delays="per_edge"
+                       if semantics else [2], density=0.5, dt=0.05)
+    compare(cfg, 2, SweepParam(0, 4), [0.0, 0.5], 120, semantics=semantics, run_flags=HB_RUN_LANES(lanes))
 
 
 def test_coupling_sweep_batched_workload_small():
