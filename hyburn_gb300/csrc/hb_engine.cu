@@ -1011,7 +1011,7 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
     if ((s = cu(e->state.ensure(stn), "cudaMalloc(state)"))) return bail(s);
     if ((s = cu(e->x0.ensure(stn), "cudaMalloc(x0)"))) return bail(s);
     if ((s = cu(e->tavg.ensure(stn), "cudaMalloc(tavg)"))) return bail(s);
-    if ((s = cu(e->ring.ensure((size_t)e->B * e->R * e->cols), "cudaMalloc(ring)"))) return bail(s);
+    if ((s = cu(e->ring.ensure((size_t)e->B * (((size_t)e->R * e->cols + 3) & ~(size_t)3)), "cudaMalloc(ring)"))) return bail(s);
     {
         std::vector<float> x0(stn);
         for (int b = 0; b < e->B; b++)

@@ -140,11 +140,12 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
     const int wlane = t & 31, warp = t >> 5;
     const int R = net.R, cols = net.cols, H = net.H, B = net.B;
     const int ring_words = R * cols;
+    const size_t ring_stride = (size_t)((ring_words + 3) & ~3);  // per-point stride, 16-byte aligned
 
     size_t off = 0;
     float* ring;
     if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)ring_words * sizeof(float); }
-    else ring = a.ring + (size_t)b * ring_words;
+    else ring = a.ring + (size_t)b * ring_stride;
     off = (off + 15) & ~(size_t)15;
     int* s_eoff = reinterpret_cast<int*>(smem + off);
     off += (size_t)a.smem_edges * 4;
@@ -154,11 +155,11 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
     float* s_part = reinterpret_cast<float*>(smem + off);  // [2][n_mean][32 warps][4]
 
     if (a.ring_in_smem && a.load_ring) {
-        const float4* g = reinterpret_cast<const float4*>(a.ring + (size_t)b * ring_words);
+        const float4* g = reinterpret_cast<const float4*>(a.ring + (size_t)b * ring_stride);
         float4* r4 = reinterpret_cast<float4*>(ring);
         const int n4 = ring_words >> 2;
         for (int i = t; i < n4; i += blockDim.x) r4[i] = g[i];
-        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) ring[i] = a.ring[(size_t)b * ring_words + i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) ring[i] = a.ring[(size_t)b * ring_stride + i];
     }
     for (int p = 0; p < net.n_proj; p++) {
         const DevProj& P = net.proj[p];
@@ -500,11 +501,11 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
     }
     if (a.ring_in_smem && a.store_ring) {
         __syncthreads();
-        float4* g = reinterpret_cast<float4*>(a.ring + (size_t)b * ring_words);
+        float4* g = reinterpret_cast<float4*>(a.ring + (size_t)b * ring_stride);
         const float4* r4 = reinterpret_cast<const float4*>(ring);
         const int n4 = ring_words >> 2;
         for (int i = t; i < n4; i += blockDim.x) g[i] = r4[i];
-        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) a.ring[(size_t)b * ring_words + i] = ring[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) a.ring[(size_t)b * ring_stride + i] = ring[i];
     }
 }
 
