@@ -19,9 +19,9 @@ LIB = os.path.join(OUT_DIR, "libhyburn_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
-    ("hb_resident_1024.cu", ["--fmad=false", "-lineinfo"]),
-    ("hb_resident_512.cu", ["--fmad=false", "-lineinfo"]),
-    ("hb_resident_256.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_fast_1024.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_fast_512.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_resident_generic.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_kernels.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_engine.cu", []),
 ]

@@ -19,9 +19,10 @@
 #include "hb_device.h"
 #include "hyburn_gb300.h"
 
-cudaError_t hb_launch_resident(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_resident(int model, int fast, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem,
+                               cudaStream_t st);
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
-int hb_resident_smem_budget(int model, int threads);
+int hb_resident_smem_budget(int model, int fast, int threads);
 
 namespace {
 
@@ -501,8 +502,16 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
         e->threads = off;
     }
+    // ---- kernel choice: the specialised single-projection form when the network allows it ----
+    int fast = -1;
+    if (e->subs.size() == 1 && e->projs.size() == 1 && e->projs[0].kind == W_SPARSE && !(run_flags & HB_RUN_GENERIC)) {
+        const int k = e->projs[0].cf.kind;
+        if (k == HBC_LINEAR || k == HBC_SIGMOIDAL || k == HBC_SCALED_LINEAR || k == HBC_DIFFERENCE) fast = 0;  // PRE_ID
+        else if (k == HBC_KURAMOTO && e->projs[0].ncv == 1) fast = 1;                                     // PRE_KURA
+    }
+    e->last_kind = fast >= 0 ? 2 : 1;
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
-    const int budget = hb_resident_smem_budget(e->kernel_model, e->threads);
+    const int budget = hb_resident_smem_budget(e->kernel_model, fast, e->threads);
     if (budget < 0) return fail(HB_ERR_CUDA, "cannot query the shared-memory limit of the resident kernel");
     const size_t smem_cap = (size_t)budget - 64;
     const size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
@@ -614,7 +623,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
         a.traj = record ? e->traj.p : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        CUDA_TRY(hb_launch_resident(e->kernel_model, e->d_net, a, B, e->threads, smem, st));
+        CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
         e->last_launches++;
         if (record) {
@@ -639,7 +648,6 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
     }
     e->last_ms = kernel_ms_total;
-    e->last_kind = 1;
 
     // ---- batch-mean BOLD: reduce windows over sweep points, then the BW ODE ----
     for (int m = 0; m < n_bold_active && !bold_pp; m++) {

@@ -56,14 +56,26 @@ int hb_resident_budget_256(int model);
 int hb_resident_budget_512(int model);
 int hb_resident_budget_1024(int model);
 
-cudaError_t hb_launch_resident(int model, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
+cudaError_t hb_launch_fast_512(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_fast_1024(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_fast_budget_512(int model, int pre);
+int hb_fast_budget_1024(int model, int pre);
+
+// fast >= 0 selects the specialised single-projection kernel with that pre() kind
+cudaError_t hb_launch_resident(int model, int fast, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem,
+                               cudaStream_t st) {
+    if (fast >= 0) {
+        if (threads <= 512) return hb_launch_fast_512(model, fast, d_net, a, B, threads, smem, st);
+        return hb_launch_fast_1024(model, fast, d_net, a, B, threads, smem, st);
+    }
     if (threads <= 256) return hb_launch_resident_256(model, d_net, a, B, threads, smem, st);
     if (threads <= 512) return hb_launch_resident_512(model, d_net, a, B, threads, smem, st);
     return hb_launch_resident_1024(model, d_net, a, B, threads, smem, st);
 }
 
 // dynamic shared memory available to a resident launch of `threads` threads
-int hb_resident_smem_budget(int model, int threads) {
+int hb_resident_smem_budget(int model, int fast, int threads) {
+    if (fast >= 0) return threads <= 512 ? hb_fast_budget_512(model, fast) : hb_fast_budget_1024(model, fast);
     if (threads <= 256) return hb_resident_budget_256(model);
     if (threads <= 512) return hb_resident_budget_512(model);
     return hb_resident_budget_1024(model);

@@ -509,6 +509,319 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Specialised form for the dominant network shape: one subnetwork coupled to itself through one
+// sparse (CSR or dense) projection whose pre() is the identity or Kuramoto's [sin, cos]. The
+// projection's constants, the point's coupling parameters and the node's row bounds live in
+// registers; the step is publish -> barrier -> lane-split gather -> butterfly -> post -> update.
+// ---------------------------------------------------------------------------------------------
+template <int MODEL, int PRE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) resident_fast_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ DevNet net;
+    {
+        const int* src = reinterpret_cast<const int*>(gnet);
+        int* dst = reinterpret_cast<int*>(&net);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
+    const int b = blockIdx.x, t = threadIdx.x;
+    const int R = net.R, cols = net.cols, H = net.H, B = net.B;
+    const int ring_words = R * cols;
+    const size_t ring_stride = (size_t)((ring_words + 3) & ~3);
+    const DevProj& P = net.proj[0];
+
+    size_t off = 0;
+    float* ring;
+    if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)ring_words * sizeof(float); }
+    else ring = a.ring + (size_t)b * ring_stride;
+    off = (off + 15) & ~(size_t)15;
+    int* s_eoff = reinterpret_cast<int*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    float* s_ew = reinterpret_cast<float*>(smem + off);
+
+    if (a.ring_in_smem && a.load_ring) {
+        const float4* g = reinterpret_cast<const float4*>(a.ring + (size_t)b * ring_stride);
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += blockDim.x) r4[i] = g[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) ring[i] = a.ring[(size_t)b * ring_stride + i];
+    }
+    const bool edges_smem = P.smem_edges >= 0;
+    if (edges_smem) {
+        const int nnz = P.rowptr[P.ntgt];
+        for (int i = t; i < nnz; i += blockDim.x) { s_eoff[i] = P.eoff[i]; s_ew[i] = P.ew[i]; }
+    }
+    const int* __restrict__ eo = edges_smem ? s_eoff : P.eoff;
+    const float* __restrict__ ew = edges_smem ? s_ew : P.ew;
+
+    const int L = net.sub[0].lanes;
+    const int n = t >> net.sub[0].lanes_log2;
+    const int lane = t & (L - 1);
+    const int nm = net.sub[0].nm;
+    const bool active = n < nm;
+    const bool lead = active && lane == 0;
+    const int nn = active ? n : 0;
+    const int mycol = nn * NCV;
+    const int integ = net.sub[0].integ, sweep_form = net.sub[0].sweep_form;
+    const int cfk = P.cfk, pc = P.pc, direct = P.direct, dmode = P.dmode, maxd = P.maxd, has_rowsums = P.has_rowsums;
+
+    float prm[HB_PSTRIDE];
+    {
+        const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+#pragma unroll
+        for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
+    }
+    float cp[8];
+    {
+        const float* c = P.cp_pp ? P.cp_pp + (size_t)b * HB_NCP : P.cp;
+#pragma unroll
+        for (int i = 0; i < 8; i++) cp[i] = c[i];
+    }
+    const float rowsum = (has_rowsums && active) ? P.rowsums[n] : 0.0f;
+    const int e0 = active ? P.rowptr[n] : 0, e1 = active ? P.rowptr[n + 1] : 0;
+
+    float x[NVAR], tv[NVAR];
+    const size_t st_base = (size_t)b * net.state_len + (size_t)nn * NVAR;
+    const bool first_launch_of_run = (a.s0 == a.run_s0);
+#pragma unroll
+    for (int v = 0; v < NVAR; v++) {
+        x[v] = active ? a.state[st_base + v] : 0.0f;
+        tv[v] = (active && !first_launch_of_run) ? a.tavg[st_base + v] : 0.0f;
+    }
+    const bool stoch = (integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH);
+    const float* nptr = a.noise + (a.noise_per_point ? (size_t)b * net.noise_row : 0) + (size_t)nn * NVAR;
+    const size_t nstride = (size_t)(a.noise_per_point ? B : 1) * net.noise_row;
+    float nscale[NVAR], nz_next[NVAR];
+#pragma unroll
+    for (int v = 0; v < NVAR; v++) {
+        nscale[v] = net.noise_scale[v];
+        nz_next[v] = (stoch && active) ? __ldcs(nptr + v) : 0.0f;
+    }
+    const bool bold_thread = lead && a.bold.n > 0;
+    const int N0 = a.bold.n0;
+    float bacc[HB_MAX_BOLD];
+    int bcnt[HB_MAX_BOLD];
+#pragma unroll
+    for (int m = 0; m < HB_MAX_BOLD; m++) {
+        bacc[m] = 0.0f;
+        bcnt[m] = 0;
+        if (m < a.bold.n) {
+            bcnt[m] = (int)((a.s0 - a.run_s0) % a.bold.period[m]);
+            if (bold_thread && !first_launch_of_run) bacc[m] = a.bold.acc[m][(size_t)b * N0 + n];
+        }
+    }
+    const float dt = net.dt, dt_half = net.dt_half, h2 = net.dt_h2, h6 = net.dt_sixth;
+    __syncthreads();
+
+    int64_t s = a.s0;
+    int slot = (int)(s % R);
+    for (int it = 0; it < a.n_steps; ++it, ++s) {
+        if (lead) {
+            ring[slot * cols + mycol] = x[0];
+            if (NCV > 1) ring[slot * cols + mycol + 1] = x[1];
+        }
+        float nz[NVAR];
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v] * nscale[v];
+        if (stoch && it + 1 < a.n_steps) {
+            nptr += nstride;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) nz_next[v] = active ? __ldcs(nptr + v) : 0.0f;
+        }
+        __syncthreads();
+
+        // ---- coupling ----
+        float gx[4] = {0.f, 0.f, 0.f, 0.f};
+        if (dmode == HBD_EDGE) {
+            if (s < (int64_t)maxd || s == 0) gather_early(ring, P, e0, e1, lane, L, s, slot, R, cols, 0, NCV, cp, gx);
+            else gather<PRE>(ring, eo, ew, e0, e1, lane, L, slot * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
+        } else {
+            int dd;
+            if (single_delay(P, s, H, dd)) {
+                int row = slot - dd;
+                row = row < 0 ? row + R : row;
+                gather<PRE>(ring, eo, ew, e0, e1, lane, L, row * cols, 0, NCV, cfk, cp, 0, gx);
+            } else {
+                float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
+                pre(cfk, cp, 0, zero, NCV, pz);
+                for (int e = e0 + lane; e < e1; e += L) {
+                    float w = ew[e];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
+                }
+            }
+        }
+        constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
+        for (int o = L >> 1; o > 0; o >>= 1) {
+#pragma unroll
+            for (int c = 0; c < PCH; c++) gx[c] += __shfl_xor_sync(0xffffffffu, gx[c], o);
+        }
+        float cc[2] = {0.0f, 0.0f};
+        {
+            float out[4] = {0.f, 0.f, 0.f, 0.f};
+            float xi[2] = {x[0], NCV > 1 ? x[NCV - 1] : 0.0f};
+            int oc = post(cfk, cp, has_rowsums, gx, pc, xi, NCV, rowsum, out);
+            if (direct) {
+                cc[0] = out[0];
+                if (NCV > 1 && oc > 1) cc[1] = out[1];
+            } else {
+                for (int j = 0; j < P.ncm; j++) {
+                    int sidx = P.cm_s[j], cpl = P.cm_cpl[j];
+                    if (sidx < NCV && cpl < NCV) {
+                        float o = pick4(out, sidx);
+                        if (cpl == 0) cc[0] += o; else cc[1] += o;
+                    }
+                }
+            }
+        }
+
+        // ---- integrate ----
+        {
+            float k1[NVAR], k2[NVAR], tmp[NVAR];
+            dfun(MODEL, prm, sweep_form, x, cc, k1);
+            if (integ == HBI_HEUN_STOCH) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+                clamp(MODEL, tmp);
+                dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
+            } else if (integ == HBI_HEUN_DET) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
+                clamp(MODEL, tmp);
+                dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+            } else if (integ == HBI_EULER) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = x[v] + k1[v] * dt;
+            } else if (integ == HBI_EULER_STOCH) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
+            } else {
+                float k3[NVAR], k4[NVAR];
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * h2;
+                clamp(MODEL, tmp);
+                dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k2[v] * h2;
+                clamp(MODEL, tmp);
+                dfun(MODEL, prm, sweep_form, tmp, cc, k3);
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k3[v] * dt;
+                clamp(MODEL, tmp);
+                dfun(MODEL, prm, sweep_form, tmp, cc, k4);
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) {
+                    float sacc = k1[v] + k2[v] * 2.0f;
+                    sacc = sacc + k3[v] * 2.0f;
+                    sacc = sacc + k4[v];
+                    x[v] = x[v] + sacc * h6;
+                }
+                if (integ == HBI_RK4_STOCH) {
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) x[v] = x[v] + nz[v];
+                }
+            }
+            clamp(MODEL, x);
+        }
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
+        if (a.traj && lead) {
+            float* tr = a.traj + ((size_t)it * B + b) * net.state_len + (size_t)n * NVAR;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[v]);
+        }
+        if (bold_thread) {
+            const int64_t rel = s - a.run_s0;
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++) {
+                if (m >= a.bold.n) break;
+                bacc[m] = bacc[m] + x[0];
+                bcnt[m] += 1;
+                bool full = bcnt[m] >= a.bold.period[m];
+                bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
+                if (!(full || last_partial)) continue;
+                int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
+                if (a.bold.per_point) {
+                    float avg = bacc[m] / (float)bcnt[m];
+                    float* bw = a.bold.bw[m];
+                    const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
+                    float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
+                    float prev = bw[4 * stride + idx];
+                    bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
+                    float cur = bw_signal(bv, bq);
+                    const BoldEmit* em = a.bold.emit[m];
+                    for (int j = lower_bound_emit(em, a.bold.n_emit[m], kk); j < a.bold.n_emit[m] && em[j].k == kk; j++) {
+                        float val = em[j].interp ? prev + (cur - prev) * em[j].w : cur;
+                        a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[j].out) * N0 + n] = val;
+                    }
+                    bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
+                    bw[4 * stride + idx] = cur;
+                } else {
+                    a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
+                }
+                bacc[m] = 0.0f;
+                bcnt[m] = 0;
+            }
+        }
+        slot = (slot + 1 == R) ? 0 : slot + 1;
+    }
+
+    if (lead) {
+        bool bad = false;
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) {
+            a.state[st_base + v] = x[v];
+            a.tavg[st_base + v] = tv[v];
+            bad |= !isfinite(x[v]);
+        }
+        if (a.check_finite && bad) atomicOr(a.flags, 1);
+    }
+    if (bold_thread) {
+#pragma unroll
+        for (int m = 0; m < HB_MAX_BOLD; m++)
+            if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + n] = bacc[m];
+    }
+    if (a.ring_in_smem && a.store_ring) {
+        __syncthreads();
+        float4* g = reinterpret_cast<float4*>(a.ring + (size_t)b * ring_stride);
+        const float4* r4 = reinterpret_cast<const float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += blockDim.x) g[i] = r4[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += blockDim.x) a.ring[(size_t)b * ring_stride + i] = ring[i];
+    }
+}
+
+template <int MODEL, int PRE, int MAXT>
+int fast_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, resident_fast_kernel<MODEL, PRE, MAXT>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(resident_fast_kernel<MODEL, PRE, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
+template <int MODEL, int PRE, int MAXT>
+cudaError_t launch_fast(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
+    int maxdyn = fast_max_dynamic_smem<MODEL, PRE, MAXT>();
+    if (maxdyn < 0) return cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn) return cudaErrorInvalidValue;
+    resident_fast_kernel<MODEL, PRE, MAXT><<<B, threads, smem, st>>>(d_net, a);
+    return cudaGetLastError();
+}
+
 // dynamic shared memory available to resident_kernel<MODEL, MAXT> on this device (sets the opt-in)
 template <int MODEL, int MAXT>
 int resident_max_dynamic_smem() {
@@ -548,24 +861,57 @@ int hb_resident_budget_1024(int model);
 #define HB_RESIDENT_UNIT(MAXT)                                                                                      \
     cudaError_t hb_launch_resident_##MAXT(int model, const DevNet* d_net, const RunArgs& a, int B, int threads,     \
                                           size_t smem, cudaStream_t st) {                                            \
-        switch (model) {                                                                                             \
-        case 0: return hb::launch_resident<0, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        case 1: return hb::launch_resident<1, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        case 2: return hb::launch_resident<2, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        case 3: return hb::launch_resident<3, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        case 4: return hb::launch_resident<4, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        case 5: return hb::launch_resident<5, MAXT>(d_net, a, B, threads, smem, st);                                 \
-        default: return hb::launch_resident<-1, MAXT>(d_net, a, B, threads, smem, st);                               \
-        }                                                                                                            \
+        (void)model;                                                                                                 \
+        return hb::launch_resident<-1, MAXT>(d_net, a, B, threads, smem, st);                                        \
     }                                                                                                                \
     int hb_resident_budget_##MAXT(int model) {                                                                       \
-        switch (model) {                                                                                             \
-        case 0: return hb::resident_max_dynamic_smem<0, MAXT>();                                                     \
-        case 1: return hb::resident_max_dynamic_smem<1, MAXT>();                                                     \
-        case 2: return hb::resident_max_dynamic_smem<2, MAXT>();                                                     \
-        case 3: return hb::resident_max_dynamic_smem<3, MAXT>();                                                     \
-        case 4: return hb::resident_max_dynamic_smem<4, MAXT>();                                                     \
-        case 5: return hb::resident_max_dynamic_smem<5, MAXT>();                                                     \
-        default: return hb::resident_max_dynamic_smem<-1, MAXT>();                                                   \
+        (void)model;                                                                                                 \
+        return hb::resident_max_dynamic_smem<-1, MAXT>();                                                            \
+    }
+
+cudaError_t hb_launch_fast_512(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_fast_1024(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_fast_budget_512(int model, int pre);
+int hb_fast_budget_1024(int model, int pre);
+
+#define HB_FAST_UNIT(MAXT)                                                                                          \
+    cudaError_t hb_launch_fast_##MAXT(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, \
+                                      size_t smem, cudaStream_t st) {                                                \
+        constexpr int MAXT_ = MAXT;                                                                                  \
+        using F = cudaError_t (*)(const DevNet*, const RunArgs&, int, int, size_t, cudaStream_t);                   \
+        F f = nullptr;                                                                                               \
+        switch (model * 2 + (pre == hb::PRE_KURA ? 1 : 0)) {                                                         \
+        case 0: f = hb::launch_fast<0, hb::PRE_ID, MAXT_>; break;                                                    \
+        case 1: f = hb::launch_fast<0, hb::PRE_KURA, MAXT_>; break;                                                  \
+        case 2: f = hb::launch_fast<1, hb::PRE_ID, MAXT_>; break;                                                    \
+        case 3: f = hb::launch_fast<1, hb::PRE_KURA, MAXT_>; break;                                                  \
+        case 4: f = hb::launch_fast<2, hb::PRE_ID, MAXT_>; break;                                                    \
+        case 5: f = hb::launch_fast<2, hb::PRE_KURA, MAXT_>; break;                                                  \
+        case 6: f = hb::launch_fast<3, hb::PRE_ID, MAXT_>; break;                                                    \
+        case 7: f = hb::launch_fast<3, hb::PRE_KURA, MAXT_>; break;                                                  \
+        case 8: f = hb::launch_fast<4, hb::PRE_ID, MAXT_>; break;                                                    \
+        case 9: f = hb::launch_fast<4, hb::PRE_KURA, MAXT_>; break;                                                  \
+        case 10: f = hb::launch_fast<5, hb::PRE_ID, MAXT_>; break;                                                   \
+        case 11: f = hb::launch_fast<5, hb::PRE_KURA, MAXT_>; break;                                                 \
+        default: return cudaErrorInvalidValue;                                                                       \
+        }                                                                                                            \
+        return f(d_net, a, B, threads, smem, st);                                                                    \
+    }                                                                                                                \
+    int hb_fast_budget_##MAXT(int model, int pre) {                                                                  \
+        constexpr int MAXT_ = MAXT;                                                                                  \
+        switch (model * 2 + (pre == hb::PRE_KURA ? 1 : 0)) {                                                         \
+        case 0: return hb::fast_max_dynamic_smem<0, hb::PRE_ID, MAXT_>();                                            \
+        case 1: return hb::fast_max_dynamic_smem<0, hb::PRE_KURA, MAXT_>();                                          \
+        case 2: return hb::fast_max_dynamic_smem<1, hb::PRE_ID, MAXT_>();                                            \
+        case 3: return hb::fast_max_dynamic_smem<1, hb::PRE_KURA, MAXT_>();                                          \
+        case 4: return hb::fast_max_dynamic_smem<2, hb::PRE_ID, MAXT_>();                                            \
+        case 5: return hb::fast_max_dynamic_smem<2, hb::PRE_KURA, MAXT_>();                                          \
+        case 6: return hb::fast_max_dynamic_smem<3, hb::PRE_ID, MAXT_>();                                            \
+        case 7: return hb::fast_max_dynamic_smem<3, hb::PRE_KURA, MAXT_>();                                          \
+        case 8: return hb::fast_max_dynamic_smem<4, hb::PRE_ID, MAXT_>();                                            \
+        case 9: return hb::fast_max_dynamic_smem<4, hb::PRE_KURA, MAXT_>();                                          \
+        case 10: return hb::fast_max_dynamic_smem<5, hb::PRE_ID, MAXT_>();                                           \
+        case 11: return hb::fast_max_dynamic_smem<5, hb::PRE_KURA, MAXT_>();                                         \
+        default: return -1;                                                                                          \
         }                                                                                                            \
     }

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
-from hyburn_gb300._abi import (HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
+from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
 from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
@@ -83,9 +83,12 @@ def test_models_integrators_mean_field(model, integrator):
     ("NotACouplingFunction", (), "Generic2dOscillator"),
 ])
 @pytest.mark.parametrize("weights", ["scalar", "dense", "csr"])
-def test_coupling_functions(coupling, cparams, model, weights):
+@pytest.mark.parametrize("generic", [False, True])
+def test_coupling_functions(coupling, cparams, model, weights, generic):
+    """generic=True forces the general resident kernel for networks the specialised kernel serves."""
     cfg = single_model(model, 16, "heun", coupling, cparams, weights=weights)
-    compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 100)
+    compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 100,
+            run_flags=HB_RUN_GENERIC if generic else 0)
 
 
 @pytest.mark.parametrize("weights", ["scalar", "dense", "csr"])
@@ -114,11 +117,12 @@ def test_ring_single_delay(weights):
     ("MontbrioPazoRoxin", "Linear", (0.5,)),
     ("WilsonCowan", "HyperbolicTangent", (0.2, 1.0, 0.0, 1.0)),
 ])
-def test_ring_per_edge_delays(model, coupling, cparams):
+@pytest.mark.parametrize("generic", [False, True])
+def test_ring_per_edge_delays(model, coupling, cparams, generic):
     """runtime.rs:125-211: CSR with one delay per edge, zero rows after pre()."""
     cfg = single_model(model, 24, "heun", coupling, cparams, weights="csr", delays="per_edge", density=0.3)
     compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 150,
-            semantics=HB_SEM_DELAY_RING, traj=True)
+            semantics=HB_SEM_DELAY_RING, traj=True, run_flags=HB_RUN_GENERIC if generic else 0)
 
 
 def test_ring_per_edge_global_ring_matches_shared_ring():
