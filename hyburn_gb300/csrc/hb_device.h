@@ -126,6 +126,7 @@ struct RunArgs {
     float* traj;          // [n_steps][B][state_len] or nullptr
     int ring_in_smem;     // resident kernel: ring cached in shared memory
     int smem_edges;       // resident kernel: edges cached in shared memory
+    int sync_every;       // specialised kernel: steps between CTA barriers (<= smallest delay, R >= H + sync_every)
     int load_ring;        // copy the global ring into shared memory at launch start
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error

@@ -238,6 +238,7 @@ struct hb_engine {
     bool bold_removed = false;   // run_sweep_multi drops the monitors (engine.rs:1330-1333)
     int H = 0, R = 0, cols = 0, state_len = 0, noise_row = 0, threads = 0, n_mean = 0;
     int kernel_model = -1;   // the model all subnetworks share, or -1
+    int sync_every = 1;      // barrier interval of the specialised kernel (<= smallest delay)
     DevNet net;
     DevNet* d_net = nullptr;
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
@@ -599,6 +600,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     a.ring = e->ring.p;
     a.noise_per_point = per_point_noise ? 1 : 0;
     a.ring_in_smem = ring_in_smem;
+    a.sync_every = fast >= 0 ? e->sync_every : 1;
     a.smem_edges = edges_in_smem ? (int)edges : 0;
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
@@ -818,7 +820,7 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
         for (int64_t k = 0; k < d->projections[p].n_delays; k++) max_delay = std::max<int>(max_delay, (int)d->projections[p].delays[k]);
     if (max_delay > 65535) return bail(fail(HB_ERR_UNSUPPORTED, "delays above 65535 steps are not supported"));
     e->H = ring ? max_delay + 1 : (max_delay == 0 ? 0 : max_delay + 1);
-    e->R = std::max(e->H, 1) + 1;
+    e->R = std::max(e->H, 1) + 1;  // widened below when the barrier interval allows
 
     // ---- projections (engine.rs:272-417) ----
     int n_mean = 0;
@@ -972,6 +974,21 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
         }
         ds.integ = eff_integrator(e, e->subs[i].model);
     }
+    // Barrier interval of the specialised kernel: one subnetwork, one sparse projection with
+    // per-edge delays, all >= 1. The ring then needs H + K slots; K shrinks (to 1) when the wider
+    // ring would no longer fit the shared-memory budget that fits it at K = 1.
+    if (d->n_subnets == 1 && d->n_projections == 1 && e->projs[0].kind == W_SPARSE && e->projs[0].dmode == HBD_EDGE) {
+        int dmin = 1 << 30;
+        for (uint32_t m : e->projs[0].edges) dmin = std::min(dmin, (int)(m >> 16));
+        if (e->projs[0].edges.empty()) dmin = 1;
+        int K = std::max(1, std::min(dmin, 32));
+        const size_t budget = 216 * 1024, edges_b = e->projs[0].edges.size() * 8;
+        auto fits = [&](int k) { return (size_t)(std::max(e->H, 1) + k) * e->cols * 4 + edges_b <= budget; };
+        if (fits(1)) while (K > 1 && !fits(K)) K >>= 1;
+        e->sync_every = K;
+        e->R = std::max(e->H, 1) + std::max(K, 1);
+    }
+    e->net.R = e->R;
     e->kernel_model = e->subs[0].model;
     for (auto& sb : e->subs)
         if (sb.model != e->kernel_model) e->kernel_model = -1;

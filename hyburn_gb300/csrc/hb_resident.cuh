@@ -25,6 +25,11 @@ enum { PRE_ID = 0, PRE_KURA = 1, PRE_GEN = 2 };
 
 __device__ __forceinline__ int wrap_add(int a, int wrap) { return a < 0 ? a + wrap : a; }
 
+// noise rows are fetched into L2 this many steps ahead of their use
+#define HB_NOISE_L2_AHEAD 8
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // single-delay projection at step s: false when the source rows are the zero tensor (zeros before
 // pre(), engine.rs:580-584 / runtime.rs:246-249); dd is the read-back distance in steps
 __device__ __forceinline__ bool single_delay(const DevProj& P, int64_t s, int H, int& dd) {
@@ -279,6 +284,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
             nptr += nstride;
 #pragma unroll
             for (int v = 0; v < 6; v++) nz_next[v] = (active && v < nvar) ? __ldcs(nptr + v) : 0.0f;
+            if (lead && it + HB_NOISE_L2_AHEAD < a.n_steps) prefetch_l2(nptr + (HB_NOISE_L2_AHEAD - 1) * nstride);
         }
         __syncthreads();
 
@@ -617,11 +623,22 @@ __global__ void __launch_bounds__(MAXT, 1) resident_fast_kernel(const DevNet* __
 
     int64_t s = a.s0;
     int slot = (int)(s % R);
+    // Barriers only every `sync_every` steps: every edge delay is >= sync_every, so the reads of a
+    // block of steps [s0, s0 + K) only touch times < s0 (or time 0 at s == 0), all published
+    // before the block's barrier; R >= H + K keeps the writes of a warp that runs ahead off the
+    // slots a slower warp still reads.
+    const int K = a.sync_every;
+    int until_sync = 0;
     for (int it = 0; it < a.n_steps; ++it, ++s) {
         if (lead) {
             ring[slot * cols + mycol] = x[0];
             if (NCV > 1) ring[slot * cols + mycol + 1] = x[1];
         }
+        if (until_sync == 0) {
+            __syncthreads();
+            until_sync = K;
+        }
+        --until_sync;
         float nz[NVAR];
 #pragma unroll
         for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v] * nscale[v];
@@ -629,8 +646,8 @@ __global__ void __launch_bounds__(MAXT, 1) resident_fast_kernel(const DevNet* __
             nptr += nstride;
 #pragma unroll
             for (int v = 0; v < NVAR; v++) nz_next[v] = active ? __ldcs(nptr + v) : 0.0f;
+            if (lead && it + HB_NOISE_L2_AHEAD < a.n_steps) prefetch_l2(nptr + (HB_NOISE_L2_AHEAD - 1) * nstride);
         }
-        __syncthreads();
 
         // ---- coupling ----
         float gx[4] = {0.f, 0.f, 0.f, 0.f};
