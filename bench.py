@@ -179,6 +179,7 @@ def main():
     ap.add_argument("--run-steps", type=int, default=N_STEPS,
                     help="integration steps per run (smaller values only for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0, help="threads per node (0: the engine's choice)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -207,7 +208,9 @@ def main():
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     # ---- device-resident runs (value) ----
-    eng.prepare(param, meta["values"], n_run, noise=noise)
+    from hyburn_gb300._abi import HB_RUN_LANES
+    run_flags = HB_RUN_LANES(args.lanes) if args.lanes else 0
+    eng.prepare(param, meta["values"], n_run, noise=noise, run_flags=run_flags)
     for _ in range(args.warmup):
         eng.execute_prepared()
     torch.cuda.synchronize()
@@ -257,14 +260,14 @@ def main():
         eng2 = BatchHybridEngine.from_config(cfg, N_POINTS, semantics=HB_SEM_DELAY_RING)
         for _ in range(max(1, args.warmup)):
             eng2.reset()
-            eng2.run_sweep(param, meta["values"], n_run, noise=host_noise)
+            eng2.run_sweep(param, meta["values"], n_run, noise=host_noise, run_flags=run_flags)
         torch.cuda.synchronize()
         if backend_ready:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             eng2.reset()
-            r = eng2.run_sweep(param, meta["values"], n_run, noise=host_noise)
+            r = eng2.run_sweep(param, meta["values"], n_run, noise=host_noise, run_flags=run_flags)
         e2e_s = reduce_max(time.perf_counter() - t0, world, backend_ready)
         e2e = world * node_steps * args.steps / e2e_s
 
