@@ -41,6 +41,7 @@ HB_RUN_FORCE_RESIDENT = 1 << 8
 HB_RUN_FORCE_BLOCKED = 1 << 9
 HB_RUN_GLOBAL_RING = 1 << 10
 HB_RUN_GENERIC = 1 << 11
+HB_RUN_TWO_PHASE = 1 << 16
 
 
 def HB_RUN_LANES(n: int) -> int:

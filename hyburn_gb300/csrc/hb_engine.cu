@@ -601,6 +601,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     a.noise_per_point = per_point_noise ? 1 : 0;
     a.ring_in_smem = ring_in_smem;
     a.sync_every = fast >= 0 ? e->sync_every : 1;
+    a.two_phase = (run_flags & HB_RUN_TWO_PHASE) ? 1 : 0;
     a.smem_edges = edges_in_smem ? (int)edges : 0;
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;

@@ -618,212 +618,242 @@ __global__ void __launch_bounds__(MAXT, 1) resident_fast_kernel(const DevNet* __
     const float dt = net.dt, dt_half = net.dt_half, h2 = net.dt_h2, h6 = net.dt_sixth;
     __syncthreads();
 
-    // ---- block-phased time loop ----
-    // Every edge delay is >= sync_every, so the coupling of a block of KB' <= sync_every steps
-    // [s0, s0 + KB') reads only times < s0 (or time 0 at s == 0), all published before the block's
-    // barrier. Phase A issues every gather and noise load of the block at once (independent of the
-    // block's own updates); phase B runs the serial model updates from registers and publishes
-    // x_{s+1} after each step. R >= H + KB' keeps a warp that runs ahead off the slots a slower
-    // warp still reads.
+    // ---- time loop ----
+    // Every edge delay is >= sync_every, so the coupling of a block of KBLK <= sync_every steps
+    // [s0, s0 + KBLK) reads only times < s0 (or time 0 at s == 0), all published before the block's
+    // barrier, and R >= H + KBLK keeps a warp that runs ahead off the slots a slower warp still
+    // reads. Two loop shapes: per-step (gather then update, one step at a time) and two-phase
+    // (phase A issues all gathers and noise loads of the block at once, phase B runs the serial
+    // updates from a register queue).
     constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
     constexpr int KB = (NVAR <= 2) ? 8 : 4;
-    const int KBLK = a.sync_every < KB ? a.sync_every : KB;
+    const bool two_phase = a.two_phase != 0;
+    const int KBLK = two_phase ? (a.sync_every < KB ? a.sync_every : KB) : a.sync_every;
     int64_t s = a.s0;
     int slot = (int)(s % R);
     if (lead) {
         ring[slot * cols + mycol] = x[0];
         if (NCV > 1) ring[slot * cols + mycol + 1] = x[1];
     }
-    for (int it0 = 0; it0 < a.n_steps; it0 += KBLK) {
-        const int nb = (a.n_steps - it0) < KBLK ? (a.n_steps - it0) : KBLK;
-        __syncthreads();
-        // ---- phase A: coupling sums and noise of the block ----
-        float gxs[KB][PCH];
-        float nzs[KB][NVAR];
+    auto coupling_sum = [&](int64_t sj, int sl, float* gx) {
+        if (dmode == HBD_EDGE) {
+            if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, lane, L, sj, sl, R, cols, 0, NCV, cp, gx);
+            else gather<PRE>(ring, eo, ew, e0, e1, lane, L, sl * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
+        } else {
+            int dd;
+            if (single_delay(P, sj, H, dd)) {
+                int row = sl - dd;
+                row = row < 0 ? row + R : row;
+                gather<PRE>(ring, eo, ew, e0, e1, lane, L, row * cols, 0, NCV, cfk, cp, 0, gx);
+            } else {
+                float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
+                pre(cfk, cp, 0, zero, NCV, pz);
+                for (int e = e0 + lane; e < e1; e += L) {
+                    float w = ew[e];
 #pragma unroll
-        for (int j = 0; j < KB; j++) {
-            if (j < nb) {
-                const int64_t sj = s + j;
-                int sl = slot + j;
-                sl = sl >= R ? sl - R : sl;
-                float gx[4] = {0.f, 0.f, 0.f, 0.f};
-                if (dmode == HBD_EDGE) {
-                    if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, lane, L, sj, sl, R, cols, 0, NCV, cp, gx);
-                    else gather<PRE>(ring, eo, ew, e0, e1, lane, L, sl * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
-                } else {
-                    int dd;
-                    if (single_delay(P, sj, H, dd)) {
-                        int row = sl - dd;
-                        row = row < 0 ? row + R : row;
-                        gather<PRE>(ring, eo, ew, e0, e1, lane, L, row * cols, 0, NCV, cfk, cp, 0, gx);
-                    } else {
-                        float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
-                        pre(cfk, cp, 0, zero, NCV, pz);
-                        for (int e = e0 + lane; e < e1; e += L) {
-                            float w = ew[e];
-#pragma unroll
-                            for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
-                        }
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < PCH; c++) gxs[j][c] = gx[c];
-                if (stoch) {
-                    const float* np = nptr + (size_t)(it0 + j) * nstride;
-#pragma unroll
-                    for (int v = 0; v < NVAR; v++) nzs[j][v] = active ? __ldcs(np + v) * nscale[v] : 0.0f;
-                } else {
-#pragma unroll
-                    for (int v = 0; v < NVAR; v++) nzs[j][v] = 0.0f;
+                    for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
                 }
             }
         }
-        if (stoch && lead && it0 + KBLK * HB_NOISE_L2_AHEAD < a.n_steps)
-            prefetch_l2(nptr + (size_t)(it0 + KBLK * HB_NOISE_L2_AHEAD) * nstride);
-        if (L > 1) {
+    };
+    // one model step from the coupling sums gx and the scaled noise nz; publishes x_{s+1}
+    auto update = [&](const float* gx, const float* nz, int it, int64_t sj, int sl_next) {
+        float cc[2] = {0.0f, 0.0f};
+        {
+            float out[4] = {0.f, 0.f, 0.f, 0.f};
+            float xi[2] = {x[0], NCV > 1 ? x[NCV - 1] : 0.0f};
+            int oc = post(cfk, cp, has_rowsums, gx, pc, xi, NCV, rowsum, out);
+            if (direct) {
+                cc[0] = out[0];
+                if (NCV > 1 && oc > 1) cc[1] = out[1];
+            } else {
+                for (int jj = 0; jj < P.ncm; jj++) {
+                    int sidx = P.cm_s[jj], cpl = P.cm_cpl[jj];
+                    if (sidx < NCV && cpl < NCV) {
+                        float o = pick4(out, sidx);
+                        if (cpl == 0) cc[0] += o; else cc[1] += o;
+                    }
+                }
+            }
+        }
+        float k1[NVAR], k2[NVAR], tmp[NVAR];
+        dfun(MODEL, prm, sweep_form, x, cc, k1);
+        if (integ == HBI_HEUN_STOCH) {
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
+        } else if (integ == HBI_HEUN_DET) {
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+        } else if (integ == HBI_EULER) {
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) x[v] = x[v] + k1[v] * dt;
+        } else if (integ == HBI_EULER_STOCH) {
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
+        } else {
+            float k3[NVAR], k4[NVAR];
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * h2;
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k2[v] * h2;
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, sweep_form, tmp, cc, k3);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k3[v] * dt;
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, sweep_form, tmp, cc, k4);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) {
+                float sacc = k1[v] + k2[v] * 2.0f;
+                sacc = sacc + k3[v] * 2.0f;
+                sacc = sacc + k4[v];
+                x[v] = x[v] + sacc * h6;
+            }
+            if (integ == HBI_RK4_STOCH) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = x[v] + nz[v];
+            }
+        }
+        clamp(MODEL, x);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
+        if (a.traj && lead) {
+            float* tr = a.traj + ((size_t)it * B + b) * net.state_len + (size_t)n * NVAR;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[v]);
+        }
+        if (bold_thread) {
+            const int64_t rel = sj - a.run_s0;
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++) {
+                if (m >= a.bold.n) break;
+                bacc[m] = bacc[m] + x[0];
+                bcnt[m] += 1;
+                bool full = bcnt[m] >= a.bold.period[m];
+                bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
+                if (!(full || last_partial)) continue;
+                int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
+                if (a.bold.per_point) {
+                    float avg = bacc[m] / (float)bcnt[m];
+                    float* bw = a.bold.bw[m];
+                    const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
+                    float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
+                    float prev = bw[4 * stride + idx];
+                    bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
+                    float cur = bw_signal(bv, bq);
+                    const BoldEmit* em = a.bold.emit[m];
+                    for (int q = lower_bound_emit(em, a.bold.n_emit[m], kk); q < a.bold.n_emit[m] && em[q].k == kk; q++) {
+                        float val = em[q].interp ? prev + (cur - prev) * em[q].w : cur;
+                        a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[q].out) * N0 + n] = val;
+                    }
+                    bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
+                    bw[4 * stride + idx] = cur;
+                } else {
+                    a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
+                }
+                bacc[m] = 0.0f;
+                bcnt[m] = 0;
+            }
+        }
+        if (lead) {
+            ring[sl_next * cols + mycol] = x[0];
+            if (NCV > 1) ring[sl_next * cols + mycol + 1] = x[1];
+        }
+    };
+
+    if (!two_phase) {
+        int until_sync = 0;
+        for (int it = 0; it < a.n_steps; ++it, ++s) {
+            if (until_sync == 0) {
+                __syncthreads();
+                until_sync = KBLK;
+            }
+            --until_sync;
+            float gx[4] = {0.f, 0.f, 0.f, 0.f};
+            coupling_sum(s, slot, gx);
+            float nz[NVAR];
+            if (stoch) {
+                const float* np = nptr + (size_t)it * nstride;
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) nz[v] = active ? __ldcs(np + v) * nscale[v] : 0.0f;
+                if (lead && it + HB_NOISE_L2_AHEAD < a.n_steps) prefetch_l2(np + HB_NOISE_L2_AHEAD * nstride);
+            } else {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) nz[v] = 0.0f;
+            }
+            for (int o = L >> 1; o > 0; o >>= 1) {
+#pragma unroll
+                for (int c = 0; c < PCH; c++) gx[c] += __shfl_xor_sync(0xffffffffu, gx[c], o);
+            }
+            const int sl1 = (slot + 1 == R) ? 0 : slot + 1;
+            update(gx, nz, it, s, sl1);
+            slot = sl1;
+        }
+    } else {
+        for (int it0 = 0; it0 < a.n_steps; it0 += KBLK) {
+            const int nb = (a.n_steps - it0) < KBLK ? (a.n_steps - it0) : KBLK;
+            __syncthreads();
+            // phase A: coupling sums and noise of the block, into a register queue
+            float gxs[KB][PCH];
+            float nzs[KB][NVAR];
 #pragma unroll
             for (int j = 0; j < KB; j++) {
+                float gx[4] = {0.f, 0.f, 0.f, 0.f};
                 if (j < nb) {
+                    int sl = slot + j;
+                    sl = sl >= R ? sl - R : sl;
+                    coupling_sum(s + j, sl, gx);
+                }
+#pragma unroll
+                for (int c = 0; c < PCH; c++) gxs[j][c] = gx[c];
+#pragma unroll
+                for (int v = 0; v < NVAR; v++)
+                    nzs[j][v] = (stoch && active && j < nb) ? __ldcs(nptr + (size_t)(it0 + j) * nstride + v) * nscale[v] : 0.0f;
+            }
+            if (stoch && lead && it0 + KBLK * HB_NOISE_L2_AHEAD < a.n_steps)
+                prefetch_l2(nptr + (size_t)(it0 + KBLK * HB_NOISE_L2_AHEAD) * nstride);
+            if (L > 1) {
+#pragma unroll
+                for (int j = 0; j < KB; j++) {
                     for (int o = L >> 1; o > 0; o >>= 1) {
 #pragma unroll
                         for (int c = 0; c < PCH; c++) gxs[j][c] += __shfl_xor_sync(0xffffffffu, gxs[j][c], o);
                     }
                 }
             }
-        }
-        // ---- phase B: serial model updates ----
+            // phase B: serial updates, popping the queue front (not unrolled: one copy of the update)
+#pragma unroll 1
+            for (int j = 0; j < nb; j++) {
+                float gx[4] = {0.f, 0.f, 0.f, 0.f}, nz[NVAR];
 #pragma unroll
-        for (int j = 0; j < KB; j++) {
-            if (j < nb) {
-                float gx[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int c = 0; c < PCH; c++) gx[c] = gxs[0][c];
 #pragma unroll
-                for (int c = 0; c < PCH; c++) gx[c] = gxs[j][c];
-                float cc[2] = {0.0f, 0.0f};
-                {
-                    float out[4] = {0.f, 0.f, 0.f, 0.f};
-                    float xi[2] = {x[0], NCV > 1 ? x[NCV - 1] : 0.0f};
-                    int oc = post(cfk, cp, has_rowsums, gx, pc, xi, NCV, rowsum, out);
-                    if (direct) {
-                        cc[0] = out[0];
-                        if (NCV > 1 && oc > 1) cc[1] = out[1];
-                    } else {
-                        for (int jj = 0; jj < P.ncm; jj++) {
-                            int sidx = P.cm_s[jj], cpl = P.cm_cpl[jj];
-                            if (sidx < NCV && cpl < NCV) {
-                                float o = pick4(out, sidx);
-                                if (cpl == 0) cc[0] += o; else cc[1] += o;
-                            }
-                        }
-                    }
+                for (int v = 0; v < NVAR; v++) nz[v] = nzs[0][v];
+#pragma unroll
+                for (int q = 0; q < KB - 1; q++) {
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) gxs[q][c] = gxs[q + 1][c];
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) nzs[q][v] = nzs[q + 1][v];
                 }
-                float nz[NVAR];
-#pragma unroll
-                for (int v = 0; v < NVAR; v++) nz[v] = nzs[j][v];
-                {
-                    float k1[NVAR], k2[NVAR], tmp[NVAR];
-                    dfun(MODEL, prm, sweep_form, x, cc, k1);
-                    if (integ == HBI_HEUN_STOCH) {
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
-                        clamp(MODEL, tmp);
-                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
-                    } else if (integ == HBI_HEUN_DET) {
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
-                        clamp(MODEL, tmp);
-                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
-                    } else if (integ == HBI_EULER) {
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) x[v] = x[v] + k1[v] * dt;
-                    } else if (integ == HBI_EULER_STOCH) {
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
-                    } else {
-                        float k3[NVAR], k4[NVAR];
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * h2;
-                        clamp(MODEL, tmp);
-                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k2[v] * h2;
-                        clamp(MODEL, tmp);
-                        dfun(MODEL, prm, sweep_form, tmp, cc, k3);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k3[v] * dt;
-                        clamp(MODEL, tmp);
-                        dfun(MODEL, prm, sweep_form, tmp, cc, k4);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) {
-                            float sacc = k1[v] + k2[v] * 2.0f;
-                            sacc = sacc + k3[v] * 2.0f;
-                            sacc = sacc + k4[v];
-                            x[v] = x[v] + sacc * h6;
-                        }
-                        if (integ == HBI_RK4_STOCH) {
-#pragma unroll
-                            for (int v = 0; v < NVAR; v++) x[v] = x[v] + nz[v];
-                        }
-                    }
-                    clamp(MODEL, x);
-                }
-#pragma unroll
-                for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
-                const int it = it0 + j;
-                const int64_t sj = s + j;
-                if (a.traj && lead) {
-                    float* tr = a.traj + ((size_t)it * B + b) * net.state_len + (size_t)n * NVAR;
-#pragma unroll
-                    for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[v]);
-                }
-                if (bold_thread) {
-                    const int64_t rel = sj - a.run_s0;
-#pragma unroll
-                    for (int m = 0; m < HB_MAX_BOLD; m++) {
-                        if (m >= a.bold.n) break;
-                        bacc[m] = bacc[m] + x[0];
-                        bcnt[m] += 1;
-                        bool full = bcnt[m] >= a.bold.period[m];
-                        bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
-                        if (!(full || last_partial)) continue;
-                        int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
-                        if (a.bold.per_point) {
-                            float avg = bacc[m] / (float)bcnt[m];
-                            float* bw = a.bold.bw[m];
-                            const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
-                            float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
-                            float prev = bw[4 * stride + idx];
-                            bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
-                            float cur = bw_signal(bv, bq);
-                            const BoldEmit* em = a.bold.emit[m];
-                            for (int q = lower_bound_emit(em, a.bold.n_emit[m], kk); q < a.bold.n_emit[m] && em[q].k == kk; q++) {
-                                float val = em[q].interp ? prev + (cur - prev) * em[q].w : cur;
-                                a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[q].out) * N0 + n] = val;
-                            }
-                            bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
-                            bw[4 * stride + idx] = cur;
-                        } else {
-                            a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
-                        }
-                        bacc[m] = 0.0f;
-                        bcnt[m] = 0;
-                    }
-                }
-                // publish x_{s+1}
                 int sl1 = slot + j + 1;
                 sl1 = sl1 >= R ? sl1 - R : sl1;
-                if (lead) {
-                    ring[sl1 * cols + mycol] = x[0];
-                    if (NCV > 1) ring[sl1 * cols + mycol + 1] = x[1];
-                }
+                update(gx, nz, it0 + j, s + j, sl1);
             }
+            s += nb;
+            slot += nb;
+            slot = slot >= R ? slot - R : slot;
         }
-        s += nb;
-        slot += nb;
-        slot = slot >= R ? slot - R : slot;
     }
 
     if (lead) {

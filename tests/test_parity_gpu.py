@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
-from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
+from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_RUN_TWO_PHASE, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
 from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
@@ -117,12 +117,13 @@ def test_ring_single_delay(weights):
     ("MontbrioPazoRoxin", "Linear", (0.5,)),
     ("WilsonCowan", "HyperbolicTangent", (0.2, 1.0, 0.0, 1.0)),
 ])
-@pytest.mark.parametrize("generic", [False, True])
-def test_ring_per_edge_delays(model, coupling, cparams, generic):
+@pytest.mark.parametrize("variant", ["generic", "per_step", "two_phase"])
+def test_ring_per_edge_delays(model, coupling, cparams, variant):
     """runtime.rs:125-211: CSR with one delay per edge, zero rows after pre()."""
     cfg = single_model(model, 24, "heun", coupling, cparams, weights="csr", delays="per_edge", density=0.3)
+    flags = {"generic": HB_RUN_GENERIC, "per_step": 0, "two_phase": HB_RUN_TWO_PHASE}[variant]
     compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 150,
-            semantics=HB_SEM_DELAY_RING, traj=True, run_flags=HB_RUN_GENERIC if generic else 0)
+            semantics=HB_SEM_DELAY_RING, traj=True, run_flags=flags)
 
 
 def test_ring_per_edge_global_ring_matches_shared_ring():
@@ -148,12 +149,15 @@ def test_lane_split_gather(lanes, semantics):
     compare(cfg, 2, SweepParam(0, 4), [0.0, 0.5], 120, semantics=semantics, run_flags=HB_RUN_LANES(lanes))
 
 
-def test_coupling_sweep_batched_workload_small():
-    """The batched-sweep workload (coupling scale sweep, per-edge delays, Heun-stochastic), 16 points."""
+@pytest.mark.parametrize("flags", [0, HB_RUN_TWO_PHASE, HB_RUN_TWO_PHASE | HB_RUN_LANES(1), HB_RUN_LANES(2)])
+def test_coupling_sweep_batched_workload_small(flags):
+    """The batched-sweep workload (coupling scale sweep, per-edge delays, Heun-stochastic), 16 points,
+    across the specialised kernel's loop shapes (barriers every K <= min-delay steps)."""
     from hyburn_gb300 import inputs
-    cfg, meta = inputs.batched_sweep(n_steps=400, n_points=16)
-    nz = inputs.standard_normal((400, 74 * 2), 4)
-    compare(cfg, 16, SweepParam(-1, 0), meta["values"], 400, semantics=HB_SEM_DELAY_RING, noise=nz)
+    cfg, meta = inputs.batched_sweep(n_steps=900, n_points=16)
+    nz = inputs.standard_normal((900, 74 * 2), 4)
+    compare(cfg, 16, SweepParam(-1, 0), meta["values"], 900, semantics=HB_SEM_DELAY_RING, noise=nz, run_flags=flags,
+            traj=True)
 
 
 def test_three_subnet_ring_with_noise_per_point():
