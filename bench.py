@@ -181,6 +181,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="threads per node (0: the engine's choice)")
     ap.add_argument("--two-phase", action="store_true", help="batch each block's gathers before its updates")
+    ap.add_argument("--no-pipe", action="store_true", help="do not use the warp-specialised pipeline")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -210,8 +211,9 @@ def main():
 
     # ---- device-resident runs (value) ----
     from hyburn_gb300._abi import HB_RUN_LANES
-    from hyburn_gb300._abi import HB_RUN_TWO_PHASE
-    run_flags = (HB_RUN_LANES(args.lanes) if args.lanes else 0) | (HB_RUN_TWO_PHASE if args.two_phase else 0)
+    from hyburn_gb300._abi import HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE
+    run_flags = ((HB_RUN_LANES(args.lanes) if args.lanes else 0) | (HB_RUN_TWO_PHASE if args.two_phase else 0)
+                 | (HB_RUN_NO_PIPE if args.no_pipe else 0))
     eng.prepare(param, meta["values"], n_run, noise=noise, run_flags=run_flags)
     for _ in range(args.warmup):
         eng.execute_prepared()

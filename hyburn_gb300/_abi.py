@@ -42,6 +42,7 @@ HB_RUN_FORCE_BLOCKED = 1 << 9
 HB_RUN_GLOBAL_RING = 1 << 10
 HB_RUN_GENERIC = 1 << 11
 HB_RUN_TWO_PHASE = 1 << 16
+HB_RUN_NO_PIPE = 1 << 17
 
 
 def HB_RUN_LANES(n: int) -> int:

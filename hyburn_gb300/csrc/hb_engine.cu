@@ -23,6 +23,8 @@ cudaError_t hb_launch_resident(int model, int fast, const DevNet* d_net, const R
                                cudaStream_t st);
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
 int hb_resident_smem_budget(int model, int fast, int threads);
+cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_pipe_budget(int model, int pre);
 
 namespace {
 
@@ -239,6 +241,7 @@ struct hb_engine {
     int H = 0, R = 0, cols = 0, state_len = 0, noise_row = 0, threads = 0, n_mean = 0;
     int kernel_model = -1;   // the model all subnetworks share, or -1
     int sync_every = 1;      // barrier interval of the specialised kernel (<= smallest delay)
+    int dmin = 0;            // smallest edge delay of a one-projection network (0: not applicable)
     DevNet net;
     DevNet* d_net = nullptr;
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
@@ -511,11 +514,25 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         else if (k == HBC_KURAMOTO && e->projs[0].ncv == 1) fast = 1;                                     // PRE_KURA
     }
     e->last_kind = fast >= 0 ? 2 : 1;
+    // warp-specialised pipeline: one thread per node for the updates plus 8 producer warps
+    int pipe = -1;
+    if (fast >= 0 && e->dmin >= 15 && e->R >= std::max(e->H, 1) + 16 && !(run_flags & HB_RUN_NO_PIPE) &&
+        ((e->subs[0].nm + 31) / 32 * 32 + 256) <= 512 && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE))
+        pipe = fast;
+    if (pipe >= 0) {
+        e->threads = (e->subs[0].nm + 31) / 32 * 32 + 256;
+        e->last_kind = 3;
+    }
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
-    const int budget = hb_resident_smem_budget(e->kernel_model, fast, e->threads);
+    const int budget = pipe >= 0 ? hb_pipe_budget(e->kernel_model, pipe) : hb_resident_smem_budget(e->kernel_model, fast, e->threads);
     if (budget < 0) return fail(HB_ERR_CUDA, "cannot query the shared-memory limit of the resident kernel");
     const size_t smem_cap = (size_t)budget - 64;
-    const size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
+    size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
+    if (pipe >= 0) {
+        // gx and noise double buffers: [2][8][nm][channels] + [2][8][nm*nvar]
+        const int pch = (pipe == 1) ? 2 : e->subs[0].ncvar;
+        part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + e->subs[0].nvar) * 4 + 16;
+    }
     const size_t ring_bytes = (size_t)e->R * e->cols * 4;
     size_t edges = 0;
     for (auto& hp : e->projs) if (hp.kind == W_SPARSE) edges += hp.edges.size();
@@ -626,7 +643,8 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
         a.traj = record ? e->traj.p : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
+        if (pipe >= 0) CUDA_TRY(hb_launch_pipe(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
+        else CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
         e->last_launches++;
         if (record) {
@@ -978,16 +996,22 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
     // Barrier interval of the specialised kernel: one subnetwork, one sparse projection with
     // per-edge delays, all >= 1. The ring then needs H + K slots; K shrinks (to 1) when the wider
     // ring would no longer fit the shared-memory budget that fits it at K = 1.
-    if (d->n_subnets == 1 && d->n_projections == 1 && e->projs[0].kind == W_SPARSE && e->projs[0].dmode == HBD_EDGE) {
+    if (d->n_subnets == 1 && d->n_projections == 1 && e->projs[0].kind == W_SPARSE &&
+        (e->projs[0].dmode == HBD_EDGE || (e->projs[0].dmode == HBD_RING && e->projs[0].delay > 0))) {
         int dmin = 1 << 30;
-        for (uint32_t m : e->projs[0].edges) dmin = std::min(dmin, (int)(m >> 16));
-        if (e->projs[0].edges.empty()) dmin = 1;
+        if (e->projs[0].dmode == HBD_EDGE) {
+            for (uint32_t m : e->projs[0].edges) dmin = std::min(dmin, (int)(m >> 16));
+            if (e->projs[0].edges.empty()) dmin = 1;
+        } else dmin = e->projs[0].delay;
+        e->dmin = dmin;
         int K = std::max(1, std::min(dmin, 32));
         const size_t budget = 216 * 1024, edges_b = e->projs[0].edges.size() * 8;
         auto fits = [&](int k) { return (size_t)(std::max(e->H, 1) + k) * e->cols * 4 + edges_b <= budget; };
         if (fits(1)) while (K > 1 && !fits(K)) K >>= 1;
         e->sync_every = K;
-        e->R = std::max(e->H, 1) + std::max(K, 1);
+        // the warp-specialised pipeline needs H + 2 * 8 slots
+        const int want = std::max(K, dmin >= 15 ? 16 : 1);
+        e->R = std::max(e->H, 1) + want;
     }
     e->net.R = e->R;
     e->kernel_model = e->subs[0].model;

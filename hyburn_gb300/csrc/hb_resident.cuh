@@ -906,6 +906,367 @@ cudaError_t launch_fast(const DevNet* d_net, const RunArgs& a, int B, int thread
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Warp-specialised pipeline for the same network shape when every edge delay is >= 2 * PK - 1.
+// Consumer warps (one thread per node) run the serial model updates of block i from a shared
+// double buffer while producer warps compute the coupling sums and stage the noise of block
+// i + 1. Producers of block i + 1 read times <= s0(i+1) + PK - 1 - dmin <= s0(i) - 1... that is,
+// only ring entries published by consumers no later than block i - 1, which the named barrier
+// EMPTY[buf] orders before the producers start. Named barriers: FULL[buf] (producers arrive,
+// consumers wait) and EMPTY[buf] (consumers arrive, producers wait). The ring holds H + 2*PK
+// slots so a consumer's writes never land on a slot a producer may still read.
+// ---------------------------------------------------------------------------------------------
+#define HB_PIPE_K 8
+#define HB_PIPE_PRODUCER_WARPS 8
+#define HB_BAR_FULL0 1
+#define HB_BAR_EMPTY0 3
+
+__device__ __forceinline__ void named_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+__device__ __forceinline__ void named_arrive(int id, int count) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+
+template <int MODEL, int PRE>
+__global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ DevNet net;
+    {
+        const int* src = reinterpret_cast<const int*>(gnet);
+        int* dst = reinterpret_cast<int*>(&net);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
+    constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
+    constexpr int PK = HB_PIPE_K;
+    const int b = blockIdx.x, t = threadIdx.x, nthreads = blockDim.x;
+    const int R = net.R, cols = net.cols, H = net.H, B = net.B;
+    const int ring_words = R * cols;
+    const size_t ring_stride = (size_t)((ring_words + 3) & ~3);
+    const DevProj& P = net.proj[0];
+    const int nm = net.sub[0].nm;
+    const int n_cons = ((nm + 31) >> 5) << 5;      // consumer threads (warp aligned)
+    const int n_prod = nthreads - n_cons;
+
+    // shared layout: ring | gx buffers [2][PK][nm][PCH] | noise buffers [2][PK][nm*NVAR] | edges
+    size_t off = 0;
+    float* ring;
+    if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)ring_words * sizeof(float); }
+    else ring = a.ring + (size_t)b * ring_stride;
+    off = (off + 15) & ~(size_t)15;
+    float* gxbuf = reinterpret_cast<float*>(smem + off);
+    off += (size_t)2 * PK * nm * PCH * sizeof(float);
+    float* nzbuf = reinterpret_cast<float*>(smem + off);
+    off += (size_t)2 * PK * nm * NVAR * sizeof(float);
+    off = (off + 15) & ~(size_t)15;
+    int* s_eoff = reinterpret_cast<int*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    float* s_ew = reinterpret_cast<float*>(smem + off);
+
+    if (a.ring_in_smem && a.load_ring) {
+        const float4* g = reinterpret_cast<const float4*>(a.ring + (size_t)b * ring_stride);
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += nthreads) r4[i] = g[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += nthreads) ring[i] = a.ring[(size_t)b * ring_stride + i];
+    }
+    const bool edges_smem = P.smem_edges >= 0;
+    if (edges_smem) {
+        const int nnz = P.rowptr[P.ntgt];
+        for (int i = t; i < nnz; i += nthreads) { s_eoff[i] = P.eoff[i]; s_ew[i] = P.ew[i]; }
+    }
+    const int* __restrict__ eo = edges_smem ? s_eoff : P.eoff;
+    const float* __restrict__ ew = edges_smem ? s_ew : P.ew;
+    const int cfk = P.cfk, maxd = P.maxd, dmode = P.dmode;
+    const int integ = net.sub[0].integ;
+    const bool stoch = (integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH);
+    float cp[8];
+    {
+        const float* c = P.cp_pp ? P.cp_pp + (size_t)b * HB_NCP : P.cp;
+#pragma unroll
+        for (int i = 0; i < 8; i++) cp[i] = c[i];
+    }
+    const float* noise_base = a.noise + (a.noise_per_point ? (size_t)b * net.noise_row : 0);
+    const size_t nstride = (size_t)(a.noise_per_point ? B : 1) * net.noise_row;
+    const int n_blocks = (a.n_steps + PK - 1) / PK;
+    const bool is_consumer = t < n_cons;
+
+    // consumers publish x_{s0} before the first barrier
+    const int n = t;
+    const bool active = is_consumer && n < nm;
+    float x[NVAR], tv[NVAR];
+    const size_t st_base = (size_t)b * net.state_len + (size_t)(active ? n : 0) * NVAR;
+    const bool first_launch_of_run = (a.s0 == a.run_s0);
+    int slot = (int)(a.s0 % R);
+#pragma unroll
+    for (int v = 0; v < NVAR; v++) {
+        x[v] = active ? a.state[st_base + v] : 0.0f;
+        tv[v] = (active && !first_launch_of_run) ? a.tavg[st_base + v] : 0.0f;
+    }
+    if (active) {
+        ring[slot * cols + n * NCV] = x[0];
+        if (NCV > 1) ring[slot * cols + n * NCV + 1] = x[1];
+    }
+    __syncthreads();
+
+    if (!is_consumer) {
+        // ================= producers =================
+        const int p = t - n_cons;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
+            const int it0 = blk * PK;
+            const int nb = (a.n_steps - it0) < PK ? (a.n_steps - it0) : PK;
+            const int64_t sb = a.s0 + it0;
+            int slb = (int)(sb % R);
+            float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
+            for (int item = p; item < nb * nm; item += n_prod) {
+                const int j = item / nm, nd = item - j * nm;
+                const int64_t sj = sb + j;
+                int sl = slb + j;
+                sl = sl >= R ? sl - R : sl;
+                const int e0 = P.rowptr[nd], e1 = P.rowptr[nd + 1];
+                float gx[4] = {0.f, 0.f, 0.f, 0.f};
+                if (dmode == HBD_EDGE) {
+                    if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, 0, 1, sj, sl, R, cols, 0, NCV, cp, gx);
+                    else gather<PRE>(ring, eo, ew, e0, e1, 0, 1, sl * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
+                } else {
+                    int dd;
+                    if (single_delay(P, sj, H, dd)) {
+                        int row = sl - dd;
+                        row = row < 0 ? row + R : row;
+                        gather<PRE>(ring, eo, ew, e0, e1, 0, 1, row * cols, 0, NCV, cfk, cp, 0, gx);
+                    } else {
+                        float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
+                        pre(cfk, cp, 0, zero, NCV, pz);
+                        for (int e = e0; e < e1; e++) {
+                            float w = ew[e];
+#pragma unroll
+                            for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + nd) * PCH + c] = gx[c];
+            }
+            if (stoch) {
+                float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR;
+                const int row_len = nm * NVAR;
+                for (int i = p; i < nb * row_len; i += n_prod) {
+                    const int j = i / row_len, k = i - j * row_len;
+                    nbuf[i] = __ldcs(noise_base + (size_t)(it0 + j) * nstride + k) * net.noise_scale[k % NVAR];
+                }
+            }
+            named_arrive(HB_BAR_FULL0 + buf, nthreads);
+        }
+    } else {
+        // ================= consumers =================
+        const int sweep_form = net.sub[0].sweep_form;
+        const int pc = P.pc, direct = P.direct, has_rowsums = P.has_rowsums;
+        const float rowsum = (has_rowsums && active) ? P.rowsums[n] : 0.0f;
+        float prm[HB_PSTRIDE];
+        {
+            const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+#pragma unroll
+            for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
+        }
+        const float dt = net.dt, dt_half = net.dt_half, h2 = net.dt_h2, h6 = net.dt_sixth;
+        const bool bold_thread = active && a.bold.n > 0;
+        const int N0 = a.bold.n0;
+        float bacc[HB_MAX_BOLD];
+        int bcnt[HB_MAX_BOLD];
+#pragma unroll
+        for (int m = 0; m < HB_MAX_BOLD; m++) {
+            bacc[m] = 0.0f;
+            bcnt[m] = 0;
+            if (m < a.bold.n) {
+                bcnt[m] = (int)((a.s0 - a.run_s0) % a.bold.period[m]);
+                if (bold_thread && !first_launch_of_run) bacc[m] = a.bold.acc[m][(size_t)b * N0 + n];
+            }
+        }
+        int64_t s = a.s0;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            named_sync(HB_BAR_FULL0 + buf, nthreads);
+            const int it0 = blk * PK;
+            const int nb = (a.n_steps - it0) < PK ? (a.n_steps - it0) : PK;
+            const float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
+            const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR;
+#pragma unroll 1
+            for (int j = 0; j < nb; j++, s++) {
+                if (active) {
+                    float gx[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
+                    float nz[NVAR];
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) nz[v] = stoch ? nbuf[(size_t)j * nm * NVAR + n * NVAR + v] : 0.0f;
+                    float cc[2] = {0.0f, 0.0f};
+                    {
+                        float out[4] = {0.f, 0.f, 0.f, 0.f};
+                        float xi[2] = {x[0], NCV > 1 ? x[NCV - 1] : 0.0f};
+                        int oc = post(cfk, cp, has_rowsums, gx, pc, xi, NCV, rowsum, out);
+                        if (direct) {
+                            cc[0] = out[0];
+                            if (NCV > 1 && oc > 1) cc[1] = out[1];
+                        } else {
+                            for (int jj = 0; jj < P.ncm; jj++) {
+                                int sidx = P.cm_s[jj], cpl = P.cm_cpl[jj];
+                                if (sidx < NCV && cpl < NCV) {
+                                    float o = pick4(out, sidx);
+                                    if (cpl == 0) cc[0] += o; else cc[1] += o;
+                                }
+                            }
+                        }
+                    }
+                    float k1[NVAR], k2[NVAR], tmp[NVAR];
+                    dfun(MODEL, prm, sweep_form, x, cc, k1);
+                    if (integ == HBI_HEUN_STOCH) {
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+                        clamp(MODEL, tmp);
+                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
+                    } else if (integ == HBI_HEUN_DET) {
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
+                        clamp(MODEL, tmp);
+                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+                    } else if (integ == HBI_EULER) {
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) x[v] = x[v] + k1[v] * dt;
+                    } else if (integ == HBI_EULER_STOCH) {
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
+                    } else {
+                        float k3[NVAR], k4[NVAR];
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * h2;
+                        clamp(MODEL, tmp);
+                        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k2[v] * h2;
+                        clamp(MODEL, tmp);
+                        dfun(MODEL, prm, sweep_form, tmp, cc, k3);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k3[v] * dt;
+                        clamp(MODEL, tmp);
+                        dfun(MODEL, prm, sweep_form, tmp, cc, k4);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) {
+                            float sacc = k1[v] + k2[v] * 2.0f;
+                            sacc = sacc + k3[v] * 2.0f;
+                            sacc = sacc + k4[v];
+                            x[v] = x[v] + sacc * h6;
+                        }
+                        if (integ == HBI_RK4_STOCH) {
+#pragma unroll
+                            for (int v = 0; v < NVAR; v++) x[v] = x[v] + nz[v];
+                        }
+                    }
+                    clamp(MODEL, x);
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
+                    const int it = it0 + j;
+                    if (a.traj) {
+                        float* tr = a.traj + ((size_t)it * B + b) * net.state_len + (size_t)n * NVAR;
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[v]);
+                    }
+                    if (bold_thread) {
+                        const int64_t rel = s - a.run_s0;
+#pragma unroll
+                        for (int m = 0; m < HB_MAX_BOLD; m++) {
+                            if (m >= a.bold.n) break;
+                            bacc[m] = bacc[m] + x[0];
+                            bcnt[m] += 1;
+                            bool full = bcnt[m] >= a.bold.period[m];
+                            bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
+                            if (!(full || last_partial)) continue;
+                            int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
+                            if (a.bold.per_point) {
+                                float avg = bacc[m] / (float)bcnt[m];
+                                float* bw = a.bold.bw[m];
+                                const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
+                                float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
+                                float prev = bw[4 * stride + idx];
+                                bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
+                                float cur = bw_signal(bv, bq);
+                                const BoldEmit* em = a.bold.emit[m];
+                                for (int q = lower_bound_emit(em, a.bold.n_emit[m], kk); q < a.bold.n_emit[m] && em[q].k == kk; q++) {
+                                    float val = em[q].interp ? prev + (cur - prev) * em[q].w : cur;
+                                    a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[q].out) * N0 + n] = val;
+                                }
+                                bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
+                                bw[4 * stride + idx] = cur;
+                            } else {
+                                a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
+                            }
+                            bacc[m] = 0.0f;
+                            bcnt[m] = 0;
+                        }
+                    }
+                    int sl1 = slot + 1;
+                    sl1 = sl1 >= R ? sl1 - R : sl1;
+                    ring[sl1 * cols + n * NCV] = x[0];
+                    if (NCV > 1) ring[sl1 * cols + n * NCV + 1] = x[1];
+                }
+                slot = (slot + 1 == R) ? 0 : slot + 1;
+            }
+            named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+        }
+        if (active) {
+            bool bad = false;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) {
+                a.state[st_base + v] = x[v];
+                a.tavg[st_base + v] = tv[v];
+                bad |= !isfinite(x[v]);
+            }
+            if (a.check_finite && bad) atomicOr(a.flags, 1);
+        }
+        if (bold_thread) {
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++)
+                if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + n] = bacc[m];
+        }
+    }
+    __syncthreads();
+    if (a.ring_in_smem && a.store_ring) {
+        float4* g = reinterpret_cast<float4*>(a.ring + (size_t)b * ring_stride);
+        const float4* r4 = reinterpret_cast<const float4*>(ring);
+        const int n4 = ring_words >> 2;
+        for (int i = t; i < n4; i += nthreads) g[i] = r4[i];
+        for (int i = (n4 << 2) + t; i < ring_words; i += nthreads) a.ring[(size_t)b * ring_stride + i] = ring[i];
+    }
+}
+
+template <int MODEL, int PRE>
+int pipe_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, resident_pipe_kernel<MODEL, PRE>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(resident_pipe_kernel<MODEL, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
+template <int MODEL, int PRE>
+cudaError_t launch_pipe(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
+    int maxdyn = pipe_max_dynamic_smem<MODEL, PRE>();
+    if (maxdyn < 0) return cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn) return cudaErrorInvalidValue;
+    resident_pipe_kernel<MODEL, PRE><<<B, threads, smem, st>>>(d_net, a);
+    return cudaGetLastError();
+}
+
 // dynamic shared memory available to resident_kernel<MODEL, MAXT> on this device (sets the opt-in)
 template <int MODEL, int MAXT>
 int resident_max_dynamic_smem() {
@@ -998,4 +1359,34 @@ int hb_fast_budget_1024(int model, int pre);
         case 11: return hb::fast_max_dynamic_smem<5, hb::PRE_KURA, MAXT_>();                                         \
         default: return -1;                                                                                          \
         }                                                                                                            \
+    }
+
+cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_pipe_budget(int model, int pre);
+
+#define HB_PIPE_UNIT                                                                                                \
+    cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads,       \
+                               size_t smem, cudaStream_t st) {                                                       \
+        using F = cudaError_t (*)(const DevNet*, const RunArgs&, int, int, size_t, cudaStream_t);                   \
+        static const F table[12] = {                                                                                 \
+            hb::launch_pipe<0, hb::PRE_ID>, hb::launch_pipe<0, hb::PRE_KURA>, hb::launch_pipe<1, hb::PRE_ID>,        \
+            hb::launch_pipe<1, hb::PRE_KURA>, hb::launch_pipe<2, hb::PRE_ID>, hb::launch_pipe<2, hb::PRE_KURA>,      \
+            hb::launch_pipe<3, hb::PRE_ID>, hb::launch_pipe<3, hb::PRE_KURA>, hb::launch_pipe<4, hb::PRE_ID>,        \
+            hb::launch_pipe<4, hb::PRE_KURA>, hb::launch_pipe<5, hb::PRE_ID>, hb::launch_pipe<5, hb::PRE_KURA>};     \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (model < 0 || i >= 12) return cudaErrorInvalidValue;                                                      \
+        return table[i](d_net, a, B, threads, smem, st);                                                             \
+    }                                                                                                                \
+    int hb_pipe_budget(int model, int pre) {                                                                         \
+        using G = int (*)();                                                                                         \
+        static const G table[12] = {                                                                                 \
+            hb::pipe_max_dynamic_smem<0, hb::PRE_ID>, hb::pipe_max_dynamic_smem<0, hb::PRE_KURA>,                    \
+            hb::pipe_max_dynamic_smem<1, hb::PRE_ID>, hb::pipe_max_dynamic_smem<1, hb::PRE_KURA>,                    \
+            hb::pipe_max_dynamic_smem<2, hb::PRE_ID>, hb::pipe_max_dynamic_smem<2, hb::PRE_KURA>,                    \
+            hb::pipe_max_dynamic_smem<3, hb::PRE_ID>, hb::pipe_max_dynamic_smem<3, hb::PRE_KURA>,                    \
+            hb::pipe_max_dynamic_smem<4, hb::PRE_ID>, hb::pipe_max_dynamic_smem<4, hb::PRE_KURA>,                    \
+            hb::pipe_max_dynamic_smem<5, hb::PRE_ID>, hb::pipe_max_dynamic_smem<5, hb::PRE_KURA>};                   \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (model < 0 || i >= 12) return -1;                                                                         \
+        return table[i]();                                                                                           \
     }

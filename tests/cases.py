@@ -51,6 +51,8 @@ def single_model(model: str, n: int = 20, integrator: str = "heun", coupling: st
         w = c.csr_weights()
         if delays == "per_edge":
             delays = tract_lengths_to_delays(c.lengths, 30.0, dt)
+        elif delays == "per_edge_long":  # every delay >= 17 steps
+            delays = tract_lengths_to_delays(c.lengths, 6.0, dt)
     return SimConfig(sim_length=1000.0, dt=dt, integrator=integrator, nsig=nsig, monitors=list(monitors or []),
                      network=NetworkConfig([sub(model, n, seed)],
                                            [ProjectionConfig(0, 0, w, coupling_fn=coupling,

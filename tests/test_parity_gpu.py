@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
-from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_RUN_TWO_PHASE, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
+from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
 from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
@@ -117,12 +117,15 @@ def test_ring_single_delay(weights):
     ("MontbrioPazoRoxin", "Linear", (0.5,)),
     ("WilsonCowan", "HyperbolicTangent", (0.2, 1.0, 0.0, 1.0)),
 ])
-@pytest.mark.parametrize("variant", ["generic", "per_step", "two_phase"])
+@pytest.mark.parametrize("variant", ["generic", "per_step", "two_phase", "pipeline"])
 def test_ring_per_edge_delays(model, coupling, cparams, variant):
     """runtime.rs:125-211: CSR with one delay per edge, zero rows after pre()."""
-    cfg = single_model(model, 24, "heun", coupling, cparams, weights="csr", delays="per_edge", density=0.3)
-    flags = {"generic": HB_RUN_GENERIC, "per_step": 0, "two_phase": HB_RUN_TWO_PHASE}[variant]
-    compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 150,
+    long = variant == "pipeline"
+    cfg = single_model(model, 24, "heun", coupling, cparams, weights="csr",
+                       delays="per_edge_long" if long else "per_edge", density=0.3)
+    flags = {"generic": HB_RUN_GENERIC, "per_step": HB_RUN_NO_PIPE, "two_phase": HB_RUN_TWO_PHASE,
+             "pipeline": 0}[variant]
+    compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 400 if long else 150,
             semantics=HB_SEM_DELAY_RING, traj=True, run_flags=flags)
 
 
@@ -149,7 +152,8 @@ def test_lane_split_gather(lanes, semantics):
     compare(cfg, 2, SweepParam(0, 4), [0.0, 0.5], 120, semantics=semantics, run_flags=HB_RUN_LANES(lanes))
 
 
-@pytest.mark.parametrize("flags", [0, HB_RUN_TWO_PHASE, HB_RUN_TWO_PHASE | HB_RUN_LANES(1), HB_RUN_LANES(2)])
+@pytest.mark.parametrize("flags", [0, HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE, HB_RUN_TWO_PHASE | HB_RUN_LANES(1),
+                                   HB_RUN_LANES(2), HB_RUN_GENERIC])
 def test_coupling_sweep_batched_workload_small(flags):
     """The batched-sweep workload (coupling scale sweep, per-edge delays, Heun-stochastic), 16 points,
     across the specialised kernel's loop shapes (barriers every K <= min-delay steps)."""
@@ -292,6 +296,25 @@ def test_noise_too_short_is_an_error():
     eng = BatchHybridEngine.from_config(cfg, 2)
     with pytest.raises(InvalidState, match="noise array too short"):
         eng.run_sweep(SweepParam(0, 1), [0.0, 0.1], 10, noise=np.zeros(5, np.float32))
+
+
+@pytest.mark.parametrize("integrator", INTEGRATORS)
+def test_pipeline_integrators_bold_and_chunked_runs(integrator):
+    """Warp-specialised pipeline (all delays >= 17): every integrator, per-point BOLD, and runs
+    split across calls (the ring and running sums carry over between launches)."""
+    mons = [MonitorConfig("Bold", tr=0.003, bold_period=10)]
+    cfg = single_model("Generic2dOscillator", 40, integrator, "Linear", (0.2,), weights="csr",
+                       delays="per_edge_long", nsig=1e-3, monitors=mons)
+    eng = BatchHybridEngine.from_config(cfg, 3, semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT)
+    ora = OracleEngine.from_config(cfg, 3, semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT)
+    for n in (333, 201):
+        nz = noise_for(cfg, n, 3, False, n)
+        g = eng.run_sweep(SweepParam(-1, 0), [0.0, 0.1, 0.2], n, noise=nz)
+        o = ora.run_sweep(SweepParam(-1, 0), [0.0, 0.1, 0.2], n, noise=nz)
+        close(g.final_states[0], o.final_states[0], what=f"final after {n}")
+        close(g.tavg[0], o.tavg[0], what=f"tavg after {n}")
+        close(g.bold[0], o.bold[0], what=f"bold after {n}")
+    assert eng.last_kernel_time()[2] == 3  # the pipeline ran
 
 
 def test_prepared_run_matches_host_run():
