@@ -531,7 +531,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     if (pipe >= 0) {
         // gx and noise double buffers: [2][8][nm][channels] + [2][8][nm*nvar]
         const int pch = (pipe == 1) ? 2 : e->subs[0].ncvar;
-        part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + e->subs[0].nvar) * 4 + 16;
+        part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + e->subs[0].nvar) * 4 + (size_t)(e->subs[0].nm + 1) * 4 + 48;
     }
     const size_t ring_bytes = (size_t)e->R * e->cols * 4;
     size_t edges = 0;

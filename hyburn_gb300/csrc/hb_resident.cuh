@@ -957,6 +957,9 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
     float* nzbuf = reinterpret_cast<float*>(smem + off);
     off += (size_t)2 * PK * nm * NVAR * sizeof(float);
     off = (off + 15) & ~(size_t)15;
+    int* s_rowptr = reinterpret_cast<int*>(smem + off);
+    off += (size_t)(nm + 1) * 4;
+    off = (off + 15) & ~(size_t)15;
     int* s_eoff = reinterpret_cast<int*>(smem + off);
     off += (size_t)a.smem_edges * 4;
     float* s_ew = reinterpret_cast<float*>(smem + off);
@@ -968,6 +971,7 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
         for (int i = t; i < n4; i += nthreads) r4[i] = g[i];
         for (int i = (n4 << 2) + t; i < ring_words; i += nthreads) ring[i] = a.ring[(size_t)b * ring_stride + i];
     }
+    for (int i = t; i <= nm; i += nthreads) s_rowptr[i] = P.rowptr[i];
     const bool edges_smem = P.smem_edges >= 0;
     if (edges_smem) {
         const int nnz = P.rowptr[P.ntgt];
@@ -1010,6 +1014,7 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
     if (!is_consumer) {
         // ================= producers =================
         const int p = t - n_cons;
+        const int row_len = nm * NVAR;
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
@@ -1018,12 +1023,13 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
             const int64_t sb = a.s0 + it0;
             int slb = (int)(sb % R);
             float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
-            for (int item = p; item < nb * nm; item += n_prod) {
-                const int j = item / nm, nd = item - j * nm;
+            // items (j, node) = p, p + n_prod, ... in [0, nb * nm), walked without divisions
+            int j = p / nm, nd = p - (p / nm) * nm;
+            while (j < nb) {
                 const int64_t sj = sb + j;
                 int sl = slb + j;
                 sl = sl >= R ? sl - R : sl;
-                const int e0 = P.rowptr[nd], e1 = P.rowptr[nd + 1];
+                const int e0 = s_rowptr[nd], e1 = s_rowptr[nd + 1];
                 float gx[4] = {0.f, 0.f, 0.f, 0.f};
                 if (dmode == HBD_EDGE) {
                     if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, 0, 1, sj, sl, R, cols, 0, NCV, cp, gx);
@@ -1046,13 +1052,23 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
                 }
 #pragma unroll
                 for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + nd) * PCH + c] = gx[c];
+                nd += n_prod;
+                while (nd >= nm) { nd -= nm; j++; }
             }
             if (stoch) {
-                float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR;
-                const int row_len = nm * NVAR;
-                for (int i = p; i < nb * row_len; i += n_prod) {
-                    const int j = i / row_len, k = i - j * row_len;
-                    nbuf[i] = __ldcs(noise_base + (size_t)(it0 + j) * nstride + k) * net.noise_scale[k % NVAR];
+                // raw draws of the block's rows; consumers apply the per-variable scale
+                float* nbuf = nzbuf + (size_t)buf * PK * row_len;
+                const float* src = noise_base + (size_t)it0 * nstride;
+                if (!a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    const int total = nb * row_len, n4 = total >> 2;
+                    const float4* s4 = reinterpret_cast<const float4*>(src);
+                    float4* d4 = reinterpret_cast<float4*>(nbuf);
+                    for (int i = p; i < n4; i += n_prod) d4[i] = __ldcs(s4 + i);
+                    for (int i = (n4 << 2) + p; i < total; i += n_prod) nbuf[i] = __ldcs(src + i);
+                    if (p == 0 && it0 + 4 * PK < a.n_steps) prefetch_l2(src + (size_t)4 * PK * nstride);
+                } else {
+                    for (int jj = 0; jj < nb; jj++)
+                        for (int i = p; i < row_len; i += n_prod) nbuf[jj * row_len + i] = __ldcs(src + (size_t)jj * nstride + i);
                 }
             }
             named_arrive(HB_BAR_FULL0 + buf, nthreads);
@@ -1098,7 +1114,7 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
                     for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
                     float nz[NVAR];
 #pragma unroll
-                    for (int v = 0; v < NVAR; v++) nz[v] = stoch ? nbuf[(size_t)j * nm * NVAR + n * NVAR + v] : 0.0f;
+                    for (int v = 0; v < NVAR; v++) nz[v] = stoch ? nbuf[(size_t)j * nm * NVAR + n * NVAR + v] * net.noise_scale[v] : 0.0f;
                     float cc[2] = {0.0f, 0.0f};
                     {
                         float out[4] = {0.f, 0.f, 0.f, 0.f};
