@@ -182,6 +182,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=0, help="threads per node (0: the engine's choice)")
     ap.add_argument("--two-phase", action="store_true", help="batch each block's gathers before its updates")
     ap.add_argument("--no-pipe", action="store_true", help="do not use the warp-specialised pipeline")
+    ap.add_argument("--pipe-lanes", type=int, default=0, help="pipeline producer threads per node (0: engine's choice)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -211,9 +212,9 @@ def main():
 
     # ---- device-resident runs (value) ----
     from hyburn_gb300._abi import HB_RUN_LANES
-    from hyburn_gb300._abi import HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE
+    from hyburn_gb300._abi import HB_RUN_NO_PIPE, HB_RUN_PIPE_LANES, HB_RUN_TWO_PHASE
     run_flags = ((HB_RUN_LANES(args.lanes) if args.lanes else 0) | (HB_RUN_TWO_PHASE if args.two_phase else 0)
-                 | (HB_RUN_NO_PIPE if args.no_pipe else 0))
+                 | (HB_RUN_NO_PIPE if args.no_pipe else 0) | HB_RUN_PIPE_LANES(args.pipe_lanes))
     eng.prepare(param, meta["values"], n_run, noise=noise, run_flags=run_flags)
     for _ in range(args.warmup):
         eng.execute_prepared()

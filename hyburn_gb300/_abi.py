@@ -45,6 +45,11 @@ HB_RUN_TWO_PHASE = 1 << 16
 HB_RUN_NO_PIPE = 1 << 17
 
 
+def HB_RUN_PIPE_LANES(n: int) -> int:
+    return (n & 0xf) << 20
+
+
+
 def HB_RUN_LANES(n: int) -> int:
     return {1: 1, 2: 2, 4: 3, 8: 4}.get(n, 0) << 12
 

@@ -128,6 +128,7 @@ struct RunArgs {
     int smem_edges;       // resident kernel: edges cached in shared memory
     int sync_every;       // specialised kernel: steps between CTA barriers (<= smallest delay, R >= H + sync_every)
     int two_phase;        // specialised kernel: batch the gathers of a block before its serial updates
+    int pipe_lanes;       // pipeline kernel: producer threads per node in the steady state
     int load_ring;        // copy the global ring into shared memory at launch start
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error

@@ -519,8 +519,16 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     if (fast >= 0 && e->dmin >= 15 && e->R >= std::max(e->H, 1) + 16 && !(run_flags & HB_RUN_NO_PIPE) &&
         ((e->subs[0].nm + 31) / 32 * 32 + 256) <= 512 && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE))
         pipe = fast;
+    int pipe_lanes = 1;
     if (pipe >= 0) {
-        e->threads = (e->subs[0].nm + 31) / 32 * 32 + 256;
+        // producer warps: PL lanes per node with nm * PL <= 256, rounded up to whole warps
+        const int nm0 = e->subs[0].nm;
+        int forced_pl = (int)((run_flags >> 20) & 0xf);
+        pipe_lanes = forced_pl ? forced_pl : 1;
+        if (!forced_pl)
+            while (pipe_lanes < 8 && nm0 * pipe_lanes * 2 <= 256) pipe_lanes *= 2;
+        const int prod = std::max(64, (nm0 * pipe_lanes + 31) / 32 * 32);
+        e->threads = (nm0 + 31) / 32 * 32 + std::min(prod, 256);
         e->last_kind = 3;
     }
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
@@ -619,6 +627,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     a.ring_in_smem = ring_in_smem;
     a.sync_every = fast >= 0 ? e->sync_every : 1;
     a.two_phase = (run_flags & HB_RUN_TWO_PHASE) ? 1 : 0;
+    a.pipe_lanes = pipe_lanes;
     a.smem_edges = edges_in_smem ? (int)edges : 0;
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;

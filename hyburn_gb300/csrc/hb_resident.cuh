@@ -1015,6 +1015,13 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
         // ================= producers =================
         const int p = t - n_cons;
         const int row_len = nm * NVAR;
+        // node-major assignment for the steady state: node p / PL, lane p % PL (PL a power of two)
+        const int PL = a.pipe_lanes;
+        const int pnode = p / PL, plane = p - (p / PL) * PL;
+        const bool pactive = pnode < nm;
+        const int pe0 = pactive ? s_rowptr[pnode] : 0, pe1 = pactive ? s_rowptr[pnode + 1] : 0;
+        const int early_until = (dmode == HBD_EDGE) ? maxd : P.delay;
+        const int doff = (dmode == HBD_RING) ? -P.delay * cols : 0;  // single delay: uniform row offset
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
@@ -1023,37 +1030,90 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
             const int64_t sb = a.s0 + it0;
             int slb = (int)(sb % R);
             float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
-            // items (j, node) = p, p + n_prod, ... in [0, nb * nm), walked without divisions
-            int j = p / nm, nd = p - (p / nm) * nm;
-            while (j < nb) {
-                const int64_t sj = sb + j;
-                int sl = slb + j;
-                sl = sl >= R ? sl - R : sl;
-                const int e0 = s_rowptr[nd], e1 = s_rowptr[nd + 1];
-                float gx[4] = {0.f, 0.f, 0.f, 0.f};
-                if (dmode == HBD_EDGE) {
-                    if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, 0, 1, sj, sl, R, cols, 0, NCV, cp, gx);
-                    else gather<PRE>(ring, eo, ew, e0, e1, 0, 1, sl * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
-                } else {
-                    int dd;
-                    if (single_delay(P, sj, H, dd)) {
-                        int row = sl - dd;
-                        row = row < 0 ? row + R : row;
-                        gather<PRE>(ring, eo, ew, e0, e1, 0, 1, row * cols, 0, NCV, cfk, cp, 0, gx);
-                    } else {
-                        float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
-                        pre(cfk, cp, 0, zero, NCV, pz);
-                        for (int e = e0; e < e1; e++) {
-                            float w = ew[e];
+            const bool early = (sb < (int64_t)early_until) || sb == 0 || dmode == HBD_COMPAT;
+            if (!early) {
+                // every edge reads PK consecutive rows at its column: one offset/weight load per edge
+                float acc[PK][PCH];
 #pragma unroll
-                            for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
+                for (int j = 0; j < PK; j++)
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
+                const int base = slb * cols + doff;
+                for (int e = pe0 + plane; e < pe1; e += PL) {
+                    int a0 = base + eo[e];
+                    a0 = a0 < 0 ? a0 + ring_words : a0;
+                    const float w = ew[e];
+                    if (a0 + (PK - 1) * cols < ring_words) {
+#pragma unroll
+                        for (int j = 0; j < PK; j++) {
+                            const float v = ring[a0 + j * cols];
+                            if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
+                            else {
+                                acc[j][0] += w * v;
+                                if (NCV > 1) acc[j][PCH - 1] += w * ring[a0 + j * cols + 1];
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < PK; j++) {
+                            int aj = a0 + j * cols;
+                            aj = aj >= ring_words ? aj - ring_words : aj;
+                            const float v = ring[aj];
+                            if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
+                            else {
+                                acc[j][0] += w * v;
+                                if (NCV > 1) acc[j][PCH - 1] += w * ring[aj + 1];
+                            }
                         }
                     }
                 }
+                for (int o = PL >> 1; o > 0; o >>= 1) {
 #pragma unroll
-                for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + nd) * PCH + c] = gx[c];
-                nd += n_prod;
-                while (nd >= nm) { nd -= nm; j++; }
+                    for (int j = 0; j < PK; j++)
+#pragma unroll
+                        for (int c = 0; c < PCH; c++) acc[j][c] += __shfl_xor_sync(0xffffffffu, acc[j][c], o);
+                }
+                if (pactive && plane == 0) {
+#pragma unroll
+                    for (int j = 0; j < PK; j++)
+                        if (j < nb) {
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + pnode) * PCH + c] = acc[j][c];
+                        }
+                }
+            } else {
+                // early steps: per (step, node) items with the delay checks of each edge
+                int j = p / nm, nd = p - (p / nm) * nm;
+                while (j < nb) {
+                    const int64_t sj = sb + j;
+                    int sl = slb + j;
+                    sl = sl >= R ? sl - R : sl;
+                    const int e0 = s_rowptr[nd], e1 = s_rowptr[nd + 1];
+                    float gx[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (dmode == HBD_EDGE) {
+                        if (sj < (int64_t)maxd || sj == 0) gather_early(ring, P, e0, e1, 0, 1, sj, sl, R, cols, 0, NCV, cp, gx);
+                        else gather<PRE>(ring, eo, ew, e0, e1, 0, 1, sl * cols, ring_words, NCV, cfk, cp, P.pre_cpu, gx);
+                    } else {
+                        int dd;
+                        if (single_delay(P, sj, H, dd)) {
+                            int row = sl - dd;
+                            row = row < 0 ? row + R : row;
+                            gather<PRE>(ring, eo, ew, e0, e1, 0, 1, row * cols, 0, NCV, cfk, cp, 0, gx);
+                        } else {
+                            float zero[2] = {0.0f, 0.0f}, pz[4] = {0.f, 0.f, 0.f, 0.f};
+                            pre(cfk, cp, 0, zero, NCV, pz);
+                            for (int e = e0; e < e1; e++) {
+                                float w = ew[e];
+#pragma unroll
+                                for (int c = 0; c < 4; c++) gx[c] += w * pz[c];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + nd) * PCH + c] = gx[c];
+                    nd += n_prod;
+                    while (nd >= nm) { nd -= nm; j++; }
+                }
             }
             if (stoch) {
                 // raw draws of the block's rows; consumers apply the per-variable scale

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam, SweepPoint, SweepSpec
-from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
+from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_GLOBAL_RING, HB_RUN_LANES, HB_RUN_NO_PIPE, HB_RUN_PIPE_LANES,
+                               HB_RUN_TWO_PHASE, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING,
                                HB_SEM_HYBRID_INTEGRATOR, HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL)
 from hyburn_gb300.config import InvalidConfig, InvalidState, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig
 from oracle.hb_oracle import OracleEngine
@@ -156,8 +157,8 @@ def test_lane_split_gather(lanes, semantics):
     compare(cfg, 2, SweepParam(0, 4), [0.0, 0.5], 120, semantics=semantics, run_flags=HB_RUN_LANES(lanes))
 
 
-@pytest.mark.parametrize("flags", [0, HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE, HB_RUN_TWO_PHASE | HB_RUN_LANES(1),
-                                   HB_RUN_LANES(2), HB_RUN_GENERIC])
+@pytest.mark.parametrize("flags", [0, HB_RUN_PIPE_LANES(1), HB_RUN_PIPE_LANES(4), HB_RUN_NO_PIPE, HB_RUN_TWO_PHASE,
+                                   HB_RUN_TWO_PHASE | HB_RUN_LANES(1), HB_RUN_LANES(2), HB_RUN_GENERIC])
 def test_coupling_sweep_batched_workload_small(flags):
     """The batched-sweep workload (coupling scale sweep, per-edge delays, Heun-stochastic), 16 points,
     across the specialised kernel's loop shapes (barriers every K <= min-delay steps)."""
