@@ -521,14 +521,21 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         pipe = fast;
     int pipe_lanes = 1;
     if (pipe >= 0) {
-        // producer warps: PL lanes per node with nm * PL <= 256, rounded up to whole warps
+        // producer threads: PL lanes per node (a power of two), every node covered, and consumer
+        // plus producer threads within the kernel's 512-thread bound
         const int nm0 = e->subs[0].nm;
+        const int n_cons = (nm0 + 31) / 32 * 32;
+        const int max_prod = 512 - n_cons;
         int forced_pl = (int)((run_flags >> 20) & 0xf);
         pipe_lanes = forced_pl ? forced_pl : 1;
         if (!forced_pl)
-            while (pipe_lanes < 8 && nm0 * pipe_lanes * 2 <= 256) pipe_lanes *= 2;
+            while (pipe_lanes < 8 && nm0 * pipe_lanes * 2 <= max_prod) pipe_lanes *= 2;
+        if ((pipe_lanes & (pipe_lanes - 1)) != 0 || pipe_lanes > 8)
+            return fail(HB_ERR_INVALID_STATE, "pipeline producer lanes must be 1, 2, 4 or 8");
         const int prod = std::max(64, (nm0 * pipe_lanes + 31) / 32 * 32);
-        e->threads = (nm0 + 31) / 32 * 32 + std::min(prod, 256);
+        if (prod > max_prod)
+            return fail(HB_ERR_UNSUPPORTED, "pipeline: %d nodes x %d producer lanes exceed the thread budget", nm0, pipe_lanes);
+        e->threads = n_cons + prod;
         e->last_kind = 3;
     }
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
