@@ -34,9 +34,9 @@ sys.path.insert(0, ROOT)
 N_NODES, N_POINTS, N_STEPS = 74, 128, 20_000
 WORKLOAD = "g2do-74n-128pt-csr20pct-per-edge-delays-heun-stochastic-20000steps"
 METRIC = "node-steps/s"
-# algorithmic bytes per node-step of the delayed sparse gather (mean in-degree 4 B reads + 4 B ring
-# write + 8 B of shared noise per node), see the design doc
 FLUSH_BYTES = 512 << 20
+KERNEL_NAMES = {1: "point-resident persistent (generic)", 2: "point-resident persistent (single projection)",
+                3: "point-resident warp-specialised pipeline"}
 
 
 def peaks():
@@ -70,7 +70,7 @@ class ClockSampler:
                     self.samples.append(parts)
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(0.05)
 
     def __enter__(self):
         self._thr = threading.Thread(target=self._run, daemon=True)
@@ -101,9 +101,11 @@ def workload(n_steps=N_STEPS, n_points=N_POINTS):
     return cfg, meta, noise
 
 
-def algorithmic_bytes_per_node_step(meta) -> float:
+def algorithmic_bytes_per_node_step(meta, n_points=N_POINTS) -> float:
+    """Delayed reads of the coupling variable (4 B per in-edge), the ring write (4 B) and the
+    shared noise draws (2 x 4 B per node per step, read once for all points)."""
     c = meta["connectome"]
-    return 4.0 * c.nnz / c.n + 4.0 + 8.0
+    return 4.0 * c.nnz / c.n + 4.0 + 8.0 / n_points
 
 
 def cpu_reference(n_points, steps_sample, n_threads):
@@ -172,7 +174,7 @@ def run_reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -233,7 +235,7 @@ def main():
                 e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            ms_k, launches, _ = eng.last_kernel_time()
+            ms_k, launches, kind = eng.last_kernel_time()
             kern.append((ms_k, launches))
         torch.cuda.synchronize()
     if backend_ready:
@@ -248,7 +250,7 @@ def main():
     achieved = bpns * node_steps / (kern_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "resident_kernel_traffic.json")
+    prof = os.path.join(ROOT, "profiles", "resident_pipe_kernel_traffic.json")
     if os.path.exists(prof):
         try:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch")
@@ -283,7 +285,7 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points_per_gpu": N_POINTS, "nodes": N_NODES, "steps_per_run": n_run,
                    "delays": f"per edge {meta['min_delay']}-{meta['max_delay']} steps", "l2": "flushed (512 MiB write) between timed iterations",
-                   "kernel": "point-resident persistent (plain)", "parallelism": f"sweep points sharded, {world} replica(s)"},
+                   "kernel": KERNEL_NAMES.get(kind, str(kind)), "parallelism": f"sweep points sharded, {world} replica(s)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_node_step": bpns,
                      "kernel_ms_per_launch": kern_ms},
