@@ -25,6 +25,7 @@ UNITS = [
     ("hb_resident_generic.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_kernels.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_engine.cu", []),
+    ("hb_noalloc.cu", ["--fmad=false"]),
 ]
 
 

@@ -769,6 +769,9 @@ hb_status reset_state(hb_engine* e) {
 
 }  // namespace
 
+// error message setter for the other translation units of the library (not exported)
+__attribute__((visibility("hidden"))) void hb_internal_set_error(const char* msg) { g_err = msg ? msg : ""; }
+
 // ======================================================================================
 // C ABI
 // ======================================================================================

@@ -215,6 +215,34 @@ hb_status hb_engine_prepare(hb_engine* engine, int32_t sub_idx, int32_t param_id
                             uint32_t run_flags, const float* noise, int64_t noise_len);
 hb_status hb_engine_execute_prepared(hb_engine* engine);
 
+/* ---- one sweep without any device allocation (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc: a host framework whose own arena owns all device
+ * memory, or a loop that must not pay cudaMalloc's implicit device synchronisation. It runs the
+ * hot-path shape — one subnetwork coupled to itself through one CSR projection with one delay
+ * per edge (ring-buffer semantics of HB_SEM_DELAY_RING), shared noise, no monitors — on inputs
+ * and outputs the caller already holds in device memory:
+ *   d_x0 [nnodes*nvar] (one point, node-major), CSR rows = target nodes: d_indptr [nnodes+1]
+ *   (int32), d_indices / d_delays / d_weights [nnz], d_noise [n_steps, nnodes*nvar] standard
+ *   normal draws (stochastic integrators only), outputs d_final_states / d_tavg
+ *   [n_sweep, nnodes, nvar]. Host arrays: model and coupling parameters, nsig, sweep_values.
+ * sweep_sub_idx 0 sweeps model parameter sweep_param_idx (the model's native sweep index only,
+ * as the batch engine), -1 sweeps coupling parameter sweep_param_idx.
+ * Network tables and the history ring live in one static device array of
+ * HB_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit; sweeps needing
+ * more are rejected with HB_ERR_UNSUPPORTED. The first call on a device resolves that array's
+ * address and should come before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. Returns after the work is
+ * enqueued on cuda_stream (the inputs' validation waits for a small packing kernel). */
+#define HB_NOALLOC_SCRATCH_BYTES (64u << 20)
+hb_status hb_noalloc_run_csr_sweep(
+    const char* model, const float* params, int32_t n_params, int32_t nnodes, const float* d_x0,
+    const int32_t* d_indptr, const uint32_t* d_indices, const uint32_t* d_delays, const float* d_weights,
+    int64_t nnz, int32_t max_delay, const char* coupling_fn, const float* coupling_params,
+    int32_t n_coupling_params, int32_t sweep_sub_idx, int32_t sweep_param_idx, const float* sweep_values,
+    int32_t n_sweep, double dt, int32_t integrator, const float* nsig, int32_t n_nsig,
+    const float* d_noise, int64_t noise_len, int64_t n_steps, float* d_final_states, float* d_tavg,
+    void* cuda_stream);
+
 /* ---- results: BatchSweepResult (engine.rs:15-31) ---- */
 int32_t      hb_result_n_sweep(const hb_result* r);
 int32_t      hb_result_n_subnets(const hb_result* r);
