@@ -43,6 +43,8 @@ HB_RUN_GLOBAL_RING = 1 << 10
 HB_RUN_GENERIC = 1 << 11
 HB_RUN_TWO_PHASE = 1 << 16
 HB_RUN_NO_PIPE = 1 << 17
+HB_RUN_STREAM = 1 << 18
+HB_RUN_NO_STREAM = 1 << 19
 
 
 def HB_RUN_PIPE_LANES(n: int) -> int:

@@ -19,6 +19,8 @@ LIB = os.path.join(OUT_DIR, "libhyburn_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
+    ("hb_stream_1.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_stream_2.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_pipe.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_1024.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_512.cu", ["--fmad=false", "-lineinfo"]),

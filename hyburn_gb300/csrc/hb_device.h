@@ -14,6 +14,7 @@
 #define HB_NCP 16       // floats per resolved coupling-function parameter row
 #define HB_MAX_THREADS 1024
 #define HB_MAX_IN 4       // incoming projections per subnetwork
+#define HB_STREAM_K 8     // steps per block of the streamed-history kernel (needs every delay >= 2K - 1)
 
 // model ids (order of the host registry)
 enum { HBM_G2DO = 0, HBM_MPR = 1, HBM_RWW = 2, HBM_KURAMOTO = 3, HBM_JR = 4, HBM_WC = 5 };
@@ -128,7 +129,9 @@ struct RunArgs {
     int smem_edges;       // resident kernel: edges cached in shared memory
     int sync_every;       // specialised kernel: steps between CTA barriers (<= smallest delay, R >= H + sync_every)
     int two_phase;        // specialised kernel: batch the gathers of a block before its serial updates
-    int pipe_lanes;       // pipeline kernel: producer threads per node in the steady state
+    int pipe_lanes;       // pipeline kernels: producer threads per node in the steady state
+    int stream_rp;        // streamed-history kernel: ring positions per node (time t at t mod stream_rp)
+    int stream_noise_smem;// streamed-history kernel: noise rows staged through shared memory
     int load_ring;        // copy the global ring into shared memory at launch start
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error

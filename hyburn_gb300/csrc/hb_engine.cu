@@ -25,6 +25,10 @@ cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows,
 int hb_resident_smem_budget(int model, int fast, int threads);
 cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 int hb_pipe_budget(int model, int pre);
+cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_stream_budget_1(int model, int pre);
+int hb_stream_budget_2(int model, int pre);
 
 namespace {
 
@@ -245,6 +249,10 @@ struct hb_engine {
     DevNet net;
     DevNet* d_net = nullptr;
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
+    // streamed-history kernel: its own ring [B][nm][rp + K][channels]; the layout of the history
+    // a run leaves behind (0: time-major ring, 1: streamed) must match the next run's kernel
+    DBuf<float> sring;
+    int hist_layout = 0, hist_rp = 0;
     std::vector<DBuf<float>> d_params;
     DBuf<int> flags_buf;
     std::vector<BoldHost> bold;
@@ -558,6 +566,48 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     else if (!force_global && ring_bytes + 16 + part_bytes <= smem_cap) { ring_in_smem = 1; }
     else if (edge_bytes + part_bytes <= smem_cap) { edges_in_smem = 1; }
     size_t smem = (ring_in_smem ? ((ring_bytes + 15) & ~(size_t)15) : 0) + (edges_in_smem ? edge_bytes : 0) + part_bytes + 16;
+    // ---- streamed-history pipeline: per-edge delays whose history does not fit shared memory ----
+    int stream_npt = 0, stream_pl = 1, stream_rp = 0, stream_noise_smem = 0, stream_edges = 0;
+    size_t stream_smem = 0;
+    if (fast >= 0 && e->projs[0].dmode == HBD_EDGE && e->dmin >= 2 * HB_STREAM_K - 1 && !(run_flags & HB_RUN_NO_STREAM) &&
+        (!ring_in_smem || (run_flags & HB_RUN_STREAM)) && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE) &&
+        !(run_flags & HB_RUN_GLOBAL_RING)) {
+        const int nm0 = e->subs[0].nm, nvar0 = e->subs[0].nvar;
+        const int pch = (fast == 1) ? 2 : e->subs[0].ncvar;
+        int npt = 0, threads = 0;
+        if ((nm0 + 31) / 32 * 32 + 128 <= 512) { npt = 1; threads = 512; }
+        else if (((nm0 + 1) / 2 + 31) / 32 * 32 + 256 <= 1024) { npt = 2; threads = 1024; }
+        const int sbudget = npt ? (npt == 1 ? hb_stream_budget_1(e->kernel_model, fast) : hb_stream_budget_2(e->kernel_model, fast)) : -1;
+        if (npt && sbudget > 0) {
+            const size_t cap = (size_t)sbudget - 64;
+            const size_t gx_b = (size_t)2 * HB_STREAM_K * nm0 * pch * 4;
+            const size_t nz_b = any_stoch ? (size_t)2 * HB_STREAM_K * nm0 * nvar0 * 4 : 0;
+            const size_t rp_b = ((size_t)(nm0 + 1) * 4 + 15) & ~(size_t)15;
+            const size_t ed_b = e->projs[0].edges.size() * 8;
+            if (gx_b + rp_b + 16 <= cap) {
+                stream_npt = npt;
+                stream_noise_smem = (nz_b > 0 && gx_b + nz_b + rp_b + 16 <= cap) ? 1 : 0;
+                size_t used = gx_b + (stream_noise_smem ? nz_b : 0) + rp_b + 16;
+                if (used + ed_b <= cap) { stream_edges = (int)e->projs[0].edges.size(); used += ed_b; }
+                stream_smem = used;
+                const int n_cons = ((nm0 + npt - 1) / npt + 31) / 32 * 32;
+                const int n_prod = threads - n_cons;
+                while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
+                e->threads = threads;
+                stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
+                const size_t words = (size_t)B * nm0 * (stream_rp + HB_STREAM_K) * pch;
+                CUDA_TRY(e->sring.ensure(words));
+                e->last_kind = 4;
+            }
+        }
+    }
+    {
+        const int layout = stream_npt ? 1 : 0;
+        if (e->step > 0 && (layout != e->hist_layout || (layout == 1 && stream_rp != e->hist_rp)))
+            return fail(HB_ERR_UNSUPPORTED, "this run would change the history layout of a started simulation; reset the engine first");
+        e->hist_layout = layout;
+        e->hist_rp = stream_rp;
+    }
     {
         size_t off = 0;
         for (size_t p = 0; p < e->projs.size(); p++) {
@@ -634,8 +684,11 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     a.ring_in_smem = ring_in_smem;
     a.sync_every = fast >= 0 ? e->sync_every : 1;
     a.two_phase = (run_flags & HB_RUN_TWO_PHASE) ? 1 : 0;
-    a.pipe_lanes = pipe_lanes;
-    a.smem_edges = edges_in_smem ? (int)edges : 0;
+    a.pipe_lanes = stream_npt ? stream_pl : pipe_lanes;
+    a.smem_edges = stream_npt ? stream_edges : (edges_in_smem ? (int)edges : 0);
+    a.stream_rp = stream_rp;
+    a.stream_noise_smem = stream_noise_smem;
+    if (stream_npt) { a.ring = e->sring.p; a.ring_in_smem = 0; }
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
     a.bold = db;
@@ -659,7 +712,9 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
         a.traj = record ? e->traj.p : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        if (pipe >= 0) CUDA_TRY(hb_launch_pipe(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
+        if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
+        else if (stream_npt == 2) CUDA_TRY(hb_launch_stream_2(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
+        else if (pipe >= 0) CUDA_TRY(hb_launch_pipe(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
         else CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
         e->last_launches++;

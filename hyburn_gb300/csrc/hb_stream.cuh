@@ -1,0 +1,474 @@
+// hb_stream.cuh — point-resident pipeline whose delayed history lives in HBM.
+//
+// For one subnetwork coupled to itself through one CSR projection with per-edge delays
+// (ring semantics of runtime.rs:125-211) when the history ring of a point does not fit shared
+// memory (hundreds of nodes, delays of hundreds to thousands of steps). One CTA owns one sweep
+// point. The history is stored per point as [node][RP + K][PCH] floats: for each source node the
+// coupling-function pre() channels (PCH = ncvar for identity pre, 2 = sin, cos for Kuramoto) of
+// consecutive time steps are adjacent, so the K = 8 delayed values an edge contributes to a block
+// of 8 steps are one contiguous 32·PCH-byte run that touches one or two 32-byte sectors, not eight.
+// Time t sits at position t mod RP; positions [RP, RP + K) mirror [0, K) so that a run of K
+// positions never wraps. Negative times read zero: the ring is zeroed at the start of a fresh
+// run and RP > max delay + 2K keeps a position from being reused before its last reader.
+//
+// Warp specialisation as in resident_pipe_kernel: consumer threads (NPT nodes each) run the
+// serial model updates of block i from a shared-memory double buffer while producer threads
+// gather the coupling sums (and stage the noise draws) of block i + 1. With every delay >= 2K - 1
+// the producers of block i + 1 read only times published by the consumers before they finished
+// block i - 1, which the named barrier EMPTY[buf] orders before the producers start.
+#pragma once
+#include <cuda_runtime.h>
+#include "hb_resident.cuh"
+
+namespace hb {
+
+// one model step of node state x from the coupling sums gx and the scaled noise nz
+// (post() then the integrator stages of engine.rs:697-771 and the final clamp)
+template <int MODEL>
+__device__ __forceinline__ void stream_node_step(const DevProj& P, const float* cp, int integ, const float* prm,
+                                                 int sweep_form, float rowsum, const float* gx, const float* nz,
+                                                 float* x, float dt, float dt_half, float h2, float h6) {
+    constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
+    float cc[2] = {0.0f, 0.0f};
+    {
+        float out[4] = {0.f, 0.f, 0.f, 0.f};
+        float xi[2] = {x[0], NCV > 1 ? x[NCV - 1] : 0.0f};
+        int oc = post(P.cfk, cp, P.has_rowsums, gx, P.pc, xi, NCV, rowsum, out);
+        if (P.direct) {
+            cc[0] = out[0];
+            if (NCV > 1 && oc > 1) cc[1] = out[1];
+        } else {
+            for (int jj = 0; jj < P.ncm; jj++) {
+                int sidx = P.cm_s[jj], cpl = P.cm_cpl[jj];
+                if (sidx < NCV && cpl < NCV) {
+                    float o = pick4(out, sidx);
+                    if (cpl == 0) cc[0] += o; else cc[1] += o;
+                }
+            }
+        }
+    }
+    float k1[NVAR], k2[NVAR], tmp[NVAR];
+    dfun(MODEL, prm, sweep_form, x, cc, k1);
+    if (integ == HBI_HEUN_STOCH) {
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+        clamp(MODEL, tmp);
+        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
+    } else if (integ == HBI_HEUN_DET) {
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
+        clamp(MODEL, tmp);
+        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+    } else if (integ == HBI_EULER) {
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) x[v] = x[v] + k1[v] * dt;
+    } else if (integ == HBI_EULER_STOCH) {
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) x[v] = (x[v] + k1[v] * dt) + nz[v];
+    } else {
+        float k3[NVAR], k4[NVAR];
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * h2;
+        clamp(MODEL, tmp);
+        dfun(MODEL, prm, sweep_form, tmp, cc, k2);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k2[v] * h2;
+        clamp(MODEL, tmp);
+        dfun(MODEL, prm, sweep_form, tmp, cc, k3);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k3[v] * dt;
+        clamp(MODEL, tmp);
+        dfun(MODEL, prm, sweep_form, tmp, cc, k4);
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) {
+            float sacc = k1[v] + k2[v] * 2.0f;
+            sacc = sacc + k3[v] * 2.0f;
+            sacc = sacc + k4[v];
+            x[v] = x[v] + sacc * h6;
+        }
+        if (integ == HBI_RK4_STOCH) {
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) x[v] = x[v] + nz[v];
+        }
+    }
+    clamp(MODEL, x);
+}
+
+// BOLD input of node n at absolute step s (bold_monitor.rs:72-227): window sums, and per point the
+// Balloon-Windkessel step and the TR emissions of a completed window
+__device__ __forceinline__ void stream_bold_sample(const RunArgs& a, int b, int B, int n, int64_t s, float x0,
+                                                   float* bacc, int* bcnt) {
+    const int N0 = a.bold.n0;
+    const int64_t rel = s - a.run_s0;
+#pragma unroll
+    for (int m = 0; m < HB_MAX_BOLD; m++) {
+        if (m >= a.bold.n) break;
+        bacc[m] = bacc[m] + x0;
+        bcnt[m] += 1;
+        bool full = bcnt[m] >= a.bold.period[m];
+        bool last_partial = !full && (rel == a.run_steps - 1) && a.bold.partial[m] > 0;
+        if (!(full || last_partial)) continue;
+        int kk = full ? (int)((rel + 1) / a.bold.period[m] - 1) : a.bold.n_full[m];
+        if (a.bold.per_point) {
+            float avg = bacc[m] / (float)bcnt[m];
+            float* bw = a.bold.bw[m];
+            const size_t stride = (size_t)B * N0, idx = (size_t)b * N0 + n;
+            float bs = bw[idx], bf = bw[stride + idx], bv = bw[2 * stride + idx], bq = bw[3 * stride + idx];
+            float prev = bw[4 * stride + idx];
+            bw_step(bs, bf, bv, bq, avg, full ? a.bold.dt_full[m] : a.bold.dt_part[m]);
+            float cur = bw_signal(bv, bq);
+            const BoldEmit* em = a.bold.emit[m];
+            for (int q = lower_bound_emit(em, a.bold.n_emit[m], kk); q < a.bold.n_emit[m] && em[q].k == kk; q++) {
+                float val = em[q].interp ? prev + (cur - prev) * em[q].w : cur;
+                a.bold.out[m][((size_t)b * a.bold.n_out_run[m] + em[q].out) * N0 + n] = val;
+            }
+            bw[idx] = bs; bw[stride + idx] = bf; bw[2 * stride + idx] = bv; bw[3 * stride + idx] = bq;
+            bw[4 * stride + idx] = cur;
+        } else {
+            a.bold.win[m][((size_t)kk * B + b) * N0 + n] = bacc[m];
+        }
+        bacc[m] = 0.0f;
+        bcnt[m] = 0;
+    }
+}
+
+// pre() channels of a node's new value at ring position pos (and its mirror below K)
+template <int PRE, int NCV, int PCH>
+__device__ __forceinline__ void stream_publish(float* ring, int n, int RPX, int RP, int pos, const float* x) {
+    float v[PCH];
+    if (PRE == PRE_KURA) { v[0] = sinf(x[0]); v[PCH - 1] = cosf(x[0]); }
+    else {
+#pragma unroll
+        for (int c = 0; c < PCH; c++) v[c] = x[c];
+    }
+    float* r = ring + ((size_t)n * RPX + pos) * PCH;
+    if (PCH == 2) *reinterpret_cast<float2*>(r) = make_float2(v[0], v[PCH - 1]);
+    else r[0] = v[0];
+    if (pos < HB_STREAM_K) {
+        float* m = r + (size_t)RP * PCH;
+        if (PCH == 2) *reinterpret_cast<float2*>(m) = make_float2(v[0], v[PCH - 1]);
+        else m[0] = v[0];
+    }
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ DevNet net;
+    {
+        const int* src = reinterpret_cast<const int*>(gnet);
+        int* dst = reinterpret_cast<int*>(&net);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
+    constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
+    constexpr int K = HB_STREAM_K;
+    constexpr int UNR = (MAXT > 512) ? 1 : 2;  // edges in flight per producer thread (register budget)
+    const int b = blockIdx.x, t = threadIdx.x, nthreads = blockDim.x;
+    const int nm = gnet->sub[0].nm;
+    const int RP = a.stream_rp, RPX = RP + K;
+    const int n_cons = (((nm + NPT - 1) / NPT + 31) >> 5) << 5;
+    const int n_prod = nthreads - n_cons;
+    float* ring = a.ring + (size_t)b * nm * RPX * PCH;
+
+    // shared layout: gx buffers [2][K][nm][PCH] | noise buffers [2][K][nm*NVAR] | rowptr | edges | weights
+    size_t off = 0;
+    float* gxbuf = reinterpret_cast<float*>(smem);
+    off += (size_t)2 * K * nm * PCH * sizeof(float);
+    float* nzbuf = reinterpret_cast<float*>(smem + off);
+    if (a.stream_noise_smem) off += (size_t)2 * K * nm * NVAR * sizeof(float);
+    off = (off + 15) & ~(size_t)15;
+    int* s_rowptr = reinterpret_cast<int*>(smem + off);
+    off += (size_t)(nm + 1) * 4;
+    off = (off + 15) & ~(size_t)15;
+    uint32_t* s_edges = reinterpret_cast<uint32_t*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    float* s_ew = reinterpret_cast<float*>(smem + off);
+
+    // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176)
+    if (a.s0 == 0) {
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const size_t n4 = ((size_t)nm * RPX * PCH) >> 2;
+        for (size_t i = t; i < n4; i += nthreads) r4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const DevProj& P = net.proj[0];
+    for (int i = t; i <= nm; i += nthreads) s_rowptr[i] = P.rowptr[i];
+    const bool edges_smem = a.smem_edges > 0;
+    if (edges_smem) {
+        const int nnz = P.rowptr[P.ntgt];
+        for (int i = t; i < nnz; i += nthreads) { s_edges[i] = P.edges[i]; s_ew[i] = P.ew[i]; }
+    }
+    const uint32_t* __restrict__ ed = edges_smem ? s_edges : P.edges;
+    const float* __restrict__ ew = edges_smem ? s_ew : P.ew;
+    const int integ = net.sub[0].integ;
+    const bool stoch = (integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH);
+    float cp[8];
+    {
+        const float* c = P.cp_pp ? P.cp_pp + (size_t)b * HB_NCP : P.cp;
+#pragma unroll
+        for (int i = 0; i < 8; i++) cp[i] = c[i];
+    }
+    const int B = net.B;
+    const float* noise_base = a.noise + (a.noise_per_point ? (size_t)b * net.noise_row : 0);
+    const size_t nstride = (size_t)(a.noise_per_point ? B : 1) * net.noise_row;
+    const int n_blocks = (a.n_steps + K - 1) / K;
+    const bool is_consumer = t < n_cons;
+    const bool first_launch_of_run = (a.s0 == a.run_s0);
+
+    // consumer state: nodes t, t + n_cons, ...
+    float x[NPT][NVAR], tv[NPT][NVAR];
+    size_t st_base[NPT];
+    bool active[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; q++) {
+        const int n = t + q * n_cons;
+        active[q] = is_consumer && n < nm;
+        st_base[q] = (size_t)b * net.state_len + (size_t)(active[q] ? n : 0) * NVAR;
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) {
+            x[q][v] = active[q] ? a.state[st_base[q] + v] : 0.0f;
+            tv[q][v] = (active[q] && !first_launch_of_run) ? a.tavg[st_base[q] + v] : 0.0f;
+        }
+        if (active[q]) stream_publish<PRE, NCV, PCH>(ring, n, RPX, RP, (int)(a.s0 % RP), x[q]);
+    }
+    __syncthreads();
+
+    if (!is_consumer) {
+        // ================= producers =================
+        const int p = t - n_cons;
+        const int PL = a.pipe_lanes;  // threads per node (power of two <= 8)
+        const int items = nm * PL;
+        const int rounds = (items + n_prod - 1) / n_prod;
+        const int row_len = nm * NVAR;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
+            const int it0 = blk * K;
+            const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
+            const int64_t sb = a.s0 + it0;
+            const int sbm = (int)(sb % RP);
+            float* gb = gxbuf + (size_t)buf * K * nm * PCH;
+            for (int r = 0; r < rounds; r++) {
+                const int item = p + r * n_prod;
+                const int node = item / PL, lane = item - (item / PL) * PL;
+                float acc[K][PCH];
+#pragma unroll
+                for (int j = 0; j < K; j++)
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
+                if (node < nm) {
+                    const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
+#pragma unroll UNR
+                    for (int e = e0 + lane; e < e1; e += PL) {
+                        const uint32_t m = ed[e];
+                        const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
+                        const float w = ew[e];
+                        int pos = sbm - d;
+                        pos += (pos < 0) ? RP : 0;
+                        const float* q = ring + ((size_t)src * RPX + pos) * PCH;
+                        float v[K][PCH];
+#pragma unroll
+                        for (int j = 0; j < K; j++) {
+                            if (PCH == 2) {
+                                const float2 u = *reinterpret_cast<const float2*>(q + 2 * j);
+                                v[j][0] = u.x;
+                                v[j][PCH - 1] = u.y;
+                            } else {
+                                v[j][0] = q[j];
+                            }
+                        }
+#pragma unroll
+                        for (int j = 0; j < K; j++)
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) acc[j][c] += w * v[j][c];
+                        if (sb == 0) {
+                            // step 0 reads the current state through every edge (runtime.rs:166-170)
+                            const float* q0 = ring + (size_t)src * RPX * PCH;
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) acc[0][c] += w * q0[c];
+                        }
+                    }
+                }
+                for (int o = PL >> 1; o > 0; o >>= 1) {
+#pragma unroll
+                    for (int j = 0; j < K; j++)
+#pragma unroll
+                        for (int c = 0; c < PCH; c++) acc[j][c] += __shfl_xor_sync(0xffffffffu, acc[j][c], o);
+                }
+                if (node < nm && lane == 0) {
+#pragma unroll
+                    for (int j = 0; j < K; j++)
+                        if (j < nb) {
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + node) * PCH + c] = acc[j][c];
+                        }
+                }
+            }
+            if (stoch && a.stream_noise_smem) {
+                float* nbuf = nzbuf + (size_t)buf * K * row_len;
+                const float* src = noise_base + (size_t)it0 * nstride;
+                if (!a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    const int total = nb * row_len, n4 = total >> 2;
+                    const float4* s4 = reinterpret_cast<const float4*>(src);
+                    float4* d4 = reinterpret_cast<float4*>(nbuf);
+                    for (int i = p; i < n4; i += n_prod) d4[i] = __ldcs(s4 + i);
+                    for (int i = (n4 << 2) + p; i < total; i += n_prod) nbuf[i] = __ldcs(src + i);
+                } else {
+                    for (int jj = 0; jj < nb; jj++)
+                        for (int i = p; i < row_len; i += n_prod) nbuf[jj * row_len + i] = __ldcs(src + (size_t)jj * nstride + i);
+                }
+            }
+            named_arrive(HB_BAR_FULL0 + buf, nthreads);
+        }
+    } else {
+        // ================= consumers =================
+        const int sweep_form = net.sub[0].sweep_form;
+        float prm[HB_PSTRIDE];
+        {
+            const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+#pragma unroll
+            for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
+        }
+        float rowsum[NPT];
+#pragma unroll
+        for (int q = 0; q < NPT; q++) rowsum[q] = (P.has_rowsums && active[q]) ? P.rowsums[t + q * n_cons] : 0.0f;
+        const float dt = net.dt, dt_half = net.dt_half, h2 = net.dt_h2, h6 = net.dt_sixth;
+        const int N0 = a.bold.n0;
+        float bacc[NPT][HB_MAX_BOLD];
+        int bcnt[NPT][HB_MAX_BOLD];
+#pragma unroll
+        for (int q = 0; q < NPT; q++)
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++) {
+                bacc[q][m] = 0.0f;
+                bcnt[q][m] = 0;
+                if (m < a.bold.n) {
+                    bcnt[q][m] = (int)((a.s0 - a.run_s0) % a.bold.period[m]);
+                    if (active[q] && !first_launch_of_run) bacc[q][m] = a.bold.acc[m][(size_t)b * N0 + t + q * n_cons];
+                }
+            }
+        int64_t s = a.s0;
+        int wpos = (int)((a.s0 + 1) % RP);
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            named_sync(HB_BAR_FULL0 + buf, nthreads);
+            const int it0 = blk * K;
+            const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
+            const float* gb = gxbuf + (size_t)buf * K * nm * PCH;
+            const float* nbuf = nzbuf + (size_t)buf * K * nm * NVAR;
+#pragma unroll 1
+            for (int j = 0; j < nb; j++, s++) {
+#pragma unroll
+                for (int q = 0; q < NPT; q++) {
+                    if (!active[q]) continue;
+                    const int n = t + q * n_cons;
+                    float gx[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
+                    float nz[NVAR];
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) {
+                        if (!stoch) nz[v] = 0.0f;
+                        else if (a.stream_noise_smem) nz[v] = nbuf[(size_t)j * nm * NVAR + n * NVAR + v] * net.noise_scale[v];
+                        else nz[v] = __ldcs(noise_base + (size_t)(it0 + j) * nstride + n * NVAR + v) * net.noise_scale[v];
+                    }
+                    stream_node_step<MODEL>(P, cp, integ, prm, sweep_form, rowsum[q], gx, nz, x[q], dt, dt_half, h2, h6);
+#pragma unroll
+                    for (int v = 0; v < NVAR; v++) tv[q][v] = tv[q][v] + x[q][v];
+                    if (a.traj) {
+                        float* tr = a.traj + ((size_t)(it0 + j) * B + b) * net.state_len + (size_t)n * NVAR;
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[q][v]);
+                    }
+                    if (a.bold.n > 0) stream_bold_sample(a, b, B, n, s, x[q][0], bacc[q], bcnt[q]);
+                    stream_publish<PRE, NCV, PCH>(ring, n, RPX, RP, wpos, x[q]);
+                }
+                wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
+            }
+            __threadfence_block();
+            named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+        }
+#pragma unroll
+        for (int q = 0; q < NPT; q++) {
+            if (!active[q]) continue;
+            bool bad = false;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) {
+                a.state[st_base[q] + v] = x[q][v];
+                a.tavg[st_base[q] + v] = tv[q][v];
+                bad |= !isfinite(x[q][v]);
+            }
+            if (a.check_finite && bad) atomicOr(a.flags, 1);
+#pragma unroll
+            for (int m = 0; m < HB_MAX_BOLD; m++)
+                if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + t + q * n_cons] = bacc[q][m];
+        }
+    }
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
+int stream_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, stream_pipe_kernel<MODEL, PRE, NPT, MAXT>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(stream_pipe_kernel<MODEL, PRE, NPT, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
+cudaError_t launch_stream(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
+    int maxdyn = stream_max_dynamic_smem<MODEL, PRE, NPT, MAXT>();
+    if (maxdyn < 0) return cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn || threads > MAXT) return cudaErrorInvalidValue;
+    stream_pipe_kernel<MODEL, PRE, NPT, MAXT><<<B, threads, smem, st>>>(d_net, a);
+    return cudaGetLastError();
+}
+
+}  // namespace hb
+
+// one translation unit per (NPT, MAXT): nodes per consumer thread and the launch bound
+cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_stream_budget_1(int model, int pre);
+int hb_stream_budget_2(int model, int pre);
+
+#define HB_STREAM_UNIT(NPT_, MAXT_)                                                                                  \
+    cudaError_t hb_launch_stream_##NPT_(int model, int pre, const DevNet* d_net, const RunArgs& a, int B,            \
+                                        int threads, size_t smem, cudaStream_t st) {                                 \
+        using F = cudaError_t (*)(const DevNet*, const RunArgs&, int, int, size_t, cudaStream_t);                    \
+        static const F tab[12] = {                                                                                   \
+            hb::launch_stream<0, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<0, hb::PRE_KURA, NPT_, MAXT_>,          \
+            hb::launch_stream<1, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<1, hb::PRE_KURA, NPT_, MAXT_>,          \
+            hb::launch_stream<2, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<2, hb::PRE_KURA, NPT_, MAXT_>,          \
+            hb::launch_stream<3, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<3, hb::PRE_KURA, NPT_, MAXT_>,          \
+            hb::launch_stream<4, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<4, hb::PRE_KURA, NPT_, MAXT_>,          \
+            hb::launch_stream<5, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream<5, hb::PRE_KURA, NPT_, MAXT_>};         \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (i < 0 || i >= 12) return cudaErrorInvalidValue;                                                          \
+        return tab[i](d_net, a, B, threads, smem, st);                                                               \
+    }                                                                                                                \
+    int hb_stream_budget_##NPT_(int model, int pre) {                                                                \
+        using G = int (*)();                                                                                         \
+        static const G tab[12] = {                                                                                   \
+            hb::stream_max_dynamic_smem<0, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<0, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_max_dynamic_smem<1, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<1, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_max_dynamic_smem<2, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<2, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_max_dynamic_smem<3, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<3, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_max_dynamic_smem<4, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<4, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_max_dynamic_smem<5, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<5, hb::PRE_KURA, NPT_, MAXT_>}; \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (i < 0 || i >= 12) return -1;                                                                             \
+        return tab[i]();                                                                                             \
+    }

@@ -77,6 +77,8 @@ typedef int32_t hb_status;
 #define HB_RUN_GENERIC        (1u << 11) /* resident kernel: use the general form even for one-projection networks */
 #define HB_RUN_TWO_PHASE      (1u << 16) /* specialised kernel: batch a block's gathers before its serial updates */
 #define HB_RUN_NO_PIPE        (1u << 17) /* do not use the warp-specialised producer/consumer pipeline */
+#define HB_RUN_STREAM         (1u << 18) /* keep the history in HBM (streamed-history pipeline) even when it fits shared memory */
+#define HB_RUN_NO_STREAM      (1u << 19) /* never use the streamed-history pipeline */
 /* pipeline kernel: producer threads per node (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_PIPE_LANES(n)  ((uint32_t)((n) & 0xf) << 20)
 /* resident kernel: threads per node sharing its edge list (1, 2, 4 or 8); 0 lets the engine choose */
