@@ -7,10 +7,10 @@ from the in-tree C-ABI library ``hyburn_gb300/_lib/libhyburn_gb300.so``.
 from .config import (BackendError, InvalidConfig, InvalidState, IOError_, MonitorConfig, NetworkConfig,
                      NonFinite, ProjectionConfig, SimConfig, SimulationError, SubnetworkConfig, SweepConfig,
                      Unsupported, parse_sweep_param)
-from .engine import BatchHybridEngine, BatchSweepResult, SweepParam, SweepPoint, SweepSpec, noise_shape
+from .engine import BatchHybridEngine, BatchSweepResult, GroupedSweep, SweepParam, SweepPoint, SweepSpec, noise_shape
 
 __all__ = [
-    "BatchHybridEngine", "BatchSweepResult", "SweepParam", "SweepPoint", "SweepSpec", "SimConfig",
+    "BatchHybridEngine", "BatchSweepResult", "GroupedSweep", "SweepParam", "SweepPoint", "SweepSpec", "SimConfig",
     "NetworkConfig", "SubnetworkConfig", "ProjectionConfig", "MonitorConfig", "SweepConfig",
     "parse_sweep_param", "noise_shape", "SimulationError", "InvalidConfig", "InvalidState", "BackendError",
     "IOError_", "NonFinite", "Unsupported",

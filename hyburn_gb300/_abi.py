@@ -51,6 +51,12 @@ def HB_RUN_PIPE_LANES(n: int) -> int:
     return (n & 0xf) << 20
 
 
+def HB_RUN_STREAM_NPT(n: int) -> int:
+    return (n & 0x7) << 24
+
+
+HB_RUN_STREAM_PREFETCH = 1 << 27
+
 
 def HB_RUN_LANES(n: int) -> int:
     return {1: 1, 2: 2, 4: 3, 8: 4}.get(n, 0) << 12
@@ -262,6 +268,12 @@ _LIB = None
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libhyburn_gb300.so")
 
 
+class hb_group_member(C.Structure):
+    _fields_ = [("engine", C.c_void_p), ("sub_idx", C.c_int32), ("param_idx", C.c_int32),
+                ("values", C.POINTER(C.c_float)), ("n_values", C.c_int32), ("n_steps", C.c_int64),
+                ("run_flags", C.c_uint32), ("noise", C.POINTER(C.c_float)), ("noise_len", C.c_int64)]
+
+
 def load_library():
     """Load the in-tree engine library; raises if it has not been built."""
     global _LIB
@@ -289,6 +301,11 @@ def load_library():
         "hb_engine_set_stream": (I32, [P, P]),
         "hb_engine_prepare": (I32, [P, I32, I32, FP, I32, I64, U32, FP, I64]),
         "hb_engine_execute_prepared": (I32, [P]),
+        "hb_group_prepare": (I32, [C.POINTER(hb_group_member), I32, P, C.POINTER(P)]),
+        "hb_group_execute": (I32, [P]),
+        "hb_group_result": (I32, [P, I32, C.POINTER(P)]),
+        "hb_group_last_kernel_time": (I32, [P, C.POINTER(D)]),
+        "hb_group_destroy": (None, [P]),
         "hb_result_n_sweep": (I32, [P]),
         "hb_result_n_subnets": (I32, [P]),
         "hb_result_n_bold": (I32, [P]),

@@ -21,6 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("hb_stream_1.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_2.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_stream_4.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_pipe.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_1024.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_512.cu", ["--fmad=false", "-lineinfo"]),

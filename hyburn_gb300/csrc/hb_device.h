@@ -132,9 +132,18 @@ struct RunArgs {
     int pipe_lanes;       // pipeline kernels: producer threads per node in the steady state
     int stream_rp;        // streamed-history kernel: ring positions per node (time t at t mod stream_rp)
     int stream_noise_smem;// streamed-history kernel: noise rows staged through shared memory
+    int stream_prefetch;  // streamed-history kernel: prefetch the history run of the edge this many lane strides ahead (0: off)
     int load_ring;        // copy the global ring into shared memory at launch start
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error
     int check_finite;
     DevBold bold;
+};
+
+// one network's sweep inside a grouped launch of the streamed-history kernel
+struct StreamJob {
+    const DevNet* net;
+    RunArgs args;
+    int first_block;   // first block of this job in the grouped grid
+    int n_points;      // its sweep points (one block each)
 };

@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -27,8 +28,16 @@ cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArg
 int hb_pipe_budget(int model, int pre);
 cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
+int hb_stream_budget_4(int model, int pre);
+cudaError_t hb_launch_stream_group_1(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_group_2(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_group_budget_1(int model, int pre);
+int hb_stream_group_budget_2(int model, int pre);
+int hb_stream_group_budget_4(int model, int pre);
 
 namespace {
 
@@ -470,9 +479,23 @@ hb_status reset_bold_device(hb_engine* e) {
     return HB_OK;
 }
 
-// the simulation of one run; noise is a host pointer (copied per launch) or a device pointer
-hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t run_flags, const float* noise_host,
-                     const float* noise_dev, hb_result* res) {
+// Everything a run needs between its setup (tables, kernel choice, BOLD schedule, launch
+// arguments) and its completion (BOLD reductions, flags, bookkeeping).
+struct RunPlan {
+    int64_t n_steps = 0;
+    uint32_t run_flags = 0;
+    const float* noise_host = nullptr;
+    const float* noise_dev = nullptr;
+    bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false;
+    int64_t noise_rows_per_step = 0, chunk = 0;
+    int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1;
+    size_t smem = 0, stream_smem = 0;
+    RunArgs a;
+    std::vector<std::vector<double>> new_times;
+};
+
+hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t run_flags, const float* noise_host,
+                    const float* noise_dev, hb_result* res, RunPlan& P) {
     const bool noise_on_device = noise_dev != nullptr;
     cudaStream_t st = e->stream();
     const int B = e->B;
@@ -574,10 +597,17 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         !(run_flags & HB_RUN_GLOBAL_RING)) {
         const int nm0 = e->subs[0].nm, nvar0 = e->subs[0].nvar;
         const int pch = (fast == 1) ? 2 : e->subs[0].ncvar;
+        // nodes per consumer thread: one (512 threads) for up to 96 nodes, else two (1024 threads, at
+        // least 256 producers); four on request
+        auto fits = [&](int k, int nt) { return ((nm0 + k - 1) / k + 31) / 32 * 32 + (nt == 512 ? 128 : 256) <= nt; };
+        const int want = (int)((run_flags >> 24) & 0x7);
         int npt = 0, threads = 0;
-        if ((nm0 + 31) / 32 * 32 + 128 <= 512) { npt = 1; threads = 512; }
-        else if (((nm0 + 1) / 2 + 31) / 32 * 32 + 256 <= 1024) { npt = 2; threads = 1024; }
-        const int sbudget = npt ? (npt == 1 ? hb_stream_budget_1(e->kernel_model, fast) : hb_stream_budget_2(e->kernel_model, fast)) : -1;
+        if (want == 1 || (want == 0 && nm0 <= 96)) { if (fits(1, 512)) { npt = 1; threads = 512; } }
+        else if (want == 4) { if (fits(4, 1024)) { npt = 4; threads = 1024; } }
+        else if (fits(2, 1024)) { npt = 2; threads = 1024; }
+        const int sbudget = npt == 1 ? hb_stream_budget_1(e->kernel_model, fast)
+                          : npt == 2 ? hb_stream_budget_2(e->kernel_model, fast)
+                          : npt == 4 ? hb_stream_budget_4(e->kernel_model, fast) : -1;
         if (npt && sbudget > 0) {
             const size_t cap = (size_t)sbudget - 64;
             const size_t gx_b = (size_t)2 * HB_STREAM_K * nm0 * pch * 4;
@@ -595,7 +625,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
                 while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
                 e->threads = threads;
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
-                const size_t words = (size_t)B * nm0 * (stream_rp + HB_STREAM_K) * pch;
+                const size_t words = (size_t)B * nm0 * (stream_rp + 2 * HB_STREAM_K) * pch;
                 CUDA_TRY(e->sring.ensure(words));
                 e->last_kind = 4;
             }
@@ -688,11 +718,46 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     a.smem_edges = stream_npt ? stream_edges : (edges_in_smem ? (int)edges : 0);
     a.stream_rp = stream_rp;
     a.stream_noise_smem = stream_noise_smem;
+    a.stream_prefetch = (run_flags & HB_RUN_STREAM_PREFETCH) ? 2 : 0;
     if (stream_npt) { a.ring = e->sring.p; a.ring_in_smem = 0; }
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
     a.bold = db;
 
+    P.n_steps = n_steps;
+    P.run_flags = run_flags;
+    P.noise_host = noise_host;
+    P.noise_dev = noise_dev;
+    P.noise_on_device = noise_on_device;
+    P.any_stoch = any_stoch;
+    P.record = record;
+    P.bold_pp = bold_pp;
+    P.noise_rows_per_step = noise_rows_per_step;
+    P.chunk = chunk;
+    P.B = B;
+    P.N0 = N0;
+    P.n_bold_active = n_bold_active;
+    P.stream_npt = stream_npt;
+    P.fast = fast;
+    P.pipe = pipe;
+    P.smem = smem;
+    P.stream_smem = stream_smem;
+    P.a = a;
+    P.new_times.swap(new_times);
+    return HB_OK;
+}
+
+// the launches of a run: one, or one per chunk when a trajectory or host noise is streamed
+hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
+    cudaStream_t st = e->stream();
+    const int B = P.B;
+    const int64_t n_steps = P.n_steps, chunk = P.chunk, noise_rows_per_step = P.noise_rows_per_step;
+    const bool any_stoch = P.any_stoch, noise_on_device = P.noise_on_device, record = P.record;
+    const float* noise_dev = P.noise_dev;
+    const float* noise_host = P.noise_host;
+    const int stream_npt = P.stream_npt, fast = P.fast, pipe = P.pipe;
+    const size_t smem = P.smem, stream_smem = P.stream_smem;
+    RunArgs& a = P.a;
     std::vector<float> traj_host;
     e->last_launches = 0;
     float kernel_ms_total = 0.0f;
@@ -714,6 +779,7 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         CUDA_TRY(cudaEventRecord(e->ev0, st));
         if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 2) CUDA_TRY(hb_launch_stream_2(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
+        else if (stream_npt == 4) CUDA_TRY(hb_launch_stream_4(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (pipe >= 0) CUDA_TRY(hb_launch_pipe(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
         else CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
@@ -740,9 +806,21 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
         }
     }
     e->last_ms = kernel_ms_total;
+    return HB_OK;
+}
+
+// completion of a run after its launches: batch-mean BOLD, flags, step counter, BOLD outputs
+hb_status run_finish(hb_engine* e, RunPlan& P, hb_result* res, bool device_part = true) {
+    cudaStream_t st = e->stream();
+    const int B = P.B, N0 = P.N0, n_bold_active = P.n_bold_active;
+    const bool bold_pp = P.bold_pp;
+    const int64_t n_steps = P.n_steps;
+    const DevBold& db = P.a.bold;
+    const RunArgs& a = P.a;
+    std::vector<std::vector<double>>& new_times = P.new_times;
 
     // ---- batch-mean BOLD: reduce windows over sweep points, then the BW ODE ----
-    for (int m = 0; m < n_bold_active && !bold_pp; m++) {
+    for (int m = 0; m < n_bold_active && !bold_pp && device_part; m++) {
         int n_win = db.n_full[m] + (db.partial[m] > 0 ? 1 : 0);
         CUDA_TRY(e->means.ensure((size_t)std::max(n_win, 1) * N0));
         CUDA_TRY(hb_launch_bold_batch_mean(db, m, n_win, B, e->means.p, st));
@@ -773,6 +851,17 @@ hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t
     }
     if (a.check_finite && flags_h[0]) return fail(HB_ERR_NONFINITE, "a state variable became NaN or Inf");
     return HB_OK;
+}
+
+// the simulation of one run; noise is a host pointer (copied per launch) or a device pointer
+hb_status run_device(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t run_flags, const float* noise_host,
+                     const float* noise_dev, hb_result* res) {
+    RunPlan P;
+    hb_status s = run_setup(e, T, n_steps, run_flags, noise_host, noise_dev, res, P);
+    if (s) return s;
+    s = run_launch(e, P, res);
+    if (s) return s;
+    return run_finish(e, P, res);
 }
 
 hb_status collect(hb_engine* e, int64_t n_steps, hb_result* r) {
@@ -1348,3 +1437,205 @@ const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
 void hb_result_free(hb_result* r) { delete r; }
 
 }  // extern "C"
+
+// ======================================================================================
+// Grouped launch: several engines' sweeps in one kernel launch, replayed from a CUDA graph
+// ======================================================================================
+
+struct hb_group {
+    struct Member {
+        hb_engine* e = nullptr;
+        RunTables T;
+        RunPlan P;
+        DBuf<float> noise;
+        std::vector<DBuf<float>> bw_init;  // per BOLD monitor: the Balloon-Windkessel start state
+    };
+    std::vector<Member> m;
+    DBuf<StreamJob> jobs;
+    cudaStream_t own = nullptr, user = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0;
+    bool executed = false;
+    cudaStream_t stream() const { return user ? user : own; }
+    ~hb_group() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        for (auto& mm : m) { mm.noise.release(); for (auto& b : mm.bw_init) b.release(); }
+        jobs.release();
+        if (own) cudaStreamDestroy(own);
+    }
+};
+
+hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda_stream, hb_group** out) {
+    if (!members || n < 1 || !out) return fail(HB_ERR_INVALID_STATE, "empty group");
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        if (!members[i].engine) return fail(HB_ERR_INVALID_STATE, "group member %d has no engine", i);
+        for (int j = 0; j < i; j++)
+            if (members[j].engine == members[i].engine) return fail(HB_ERR_INVALID_STATE, "engine of member %d appears twice", i);
+        if (members[i].run_flags & HB_RUN_TRAJECTORY) return fail(HB_ERR_UNSUPPORTED, "grouped launches record no trajectories");
+        if (members[i].n_steps < 1) return fail(HB_ERR_INVALID_STATE, "member %d: n_steps must be >= 1", i);
+        if (members[i].n_values != members[i].engine->B || !members[i].values)
+            return fail(HB_ERR_INVALID_STATE, "member %d: expected %d sweep values", i, members[i].engine->B);
+    }
+    // one kernel instantiation for all: nodes per consumer thread from the largest member
+    int max_nm = 0;
+    for (int i = 0; i < n; i++) max_nm = std::max(max_nm, members[i].engine->subs[0].nm);
+    const int npt = max_nm <= 96 ? 1 : 2;
+    std::unique_ptr<hb_group> g(new hb_group());
+    if (cuda_stream) g->user = (cudaStream_t)cuda_stream;
+    else CUDA_TRY(cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&g->ev0));
+    CUDA_TRY(cudaEventCreate(&g->ev1));
+    g->m.resize(n);
+    int model = -2, fast = -2;
+    size_t smem = 0;
+    for (int i = 0; i < n; i++) {
+        const hb_group_member& mb = members[i];
+        hb_group::Member& gm = g->m[i];
+        hb_engine* e = gm.e = mb.engine;
+        hb_status s = validate_noise(e, mb.noise, mb.noise_len, mb.n_steps);
+        if (s) return s;
+        hb_sweep_point dim{mb.sub_idx, mb.param_idx, mb.values, mb.n_values};
+        if ((s = build_tables(e, &dim, 1, false, gm.T))) return s;
+        if ((s = reset_state(e))) return s;
+        e->bold_removed = false;
+        if ((s = reset_bold_device(e))) return s;
+        const float* noise_dev = nullptr;
+        if (mb.noise && mb.noise_len > 0) {
+            CUDA_TRY(gm.noise.ensure((size_t)mb.noise_len));
+            CUDA_TRY(cudaMemcpy(gm.noise.p, mb.noise, (size_t)mb.noise_len * 4, cudaMemcpyHostToDevice));
+            noise_dev = gm.noise.p;
+        }
+        const uint32_t flags = (mb.run_flags & ~(uint32_t)(0x7u << 24)) | HB_RUN_STREAM | HB_RUN_STREAM_NPT(npt);
+        if ((s = run_setup(e, gm.T, mb.n_steps, flags, nullptr, noise_dev ? noise_dev : e->x0.p, nullptr, gm.P))) return s;
+        if (gm.P.stream_npt != npt)
+            return fail(HB_ERR_UNSUPPORTED, "member %d cannot run in the streamed-history kernel (one subnetwork, one sparse "
+                        "projection with per-edge delays >= %d steps)", i, 2 * HB_STREAM_K - 1);
+        if (model == -2) { model = e->kernel_model; fast = gm.P.fast; }
+        else if (model != e->kernel_model || fast != gm.P.fast)
+            return fail(HB_ERR_UNSUPPORTED, "group members must share the model and the coupling pre() form");
+        smem = std::max(smem, gm.P.stream_smem);
+        gm.P.a.s0 = 0;
+        gm.P.a.n_steps = (int)mb.n_steps;
+        gm.P.a.load_ring = 0;
+        gm.P.a.store_ring = 1;
+        gm.P.a.traj = nullptr;
+        if (gm.P.any_stoch) gm.P.a.noise = noise_dev;
+        // Balloon-Windkessel start state for the graph's reset
+        gm.bw_init.resize(e->bold.size());
+        for (size_t k = 0; k < e->bold.size(); k++) {
+            const size_t words = 5 * (size_t)((e->flags & HB_SEM_BOLD_PER_POINT) ? e->B : 1) * e->subs[0].nnodes;
+            CUDA_TRY(gm.bw_init[k].ensure(words));
+            CUDA_TRY(cudaMemcpyAsync(gm.bw_init[k].p, e->bold[k].bw.p, words * 4, cudaMemcpyDeviceToDevice, e->stream()));
+        }
+        for (int mo = 0; mo < gm.P.n_bold_active && !gm.P.bold_pp; mo++) {
+            int n_win = gm.P.a.bold.n_full[mo] + (gm.P.a.bold.partial[mo] > 0 ? 1 : 0);
+            CUDA_TRY(e->means.ensure((size_t)std::max(n_win, 1) * gm.P.N0));
+        }
+        CUDA_TRY(cudaStreamSynchronize(e->stream()));
+    }
+    const int budget = npt == 1 ? hb_stream_group_budget_1(model, fast) : hb_stream_group_budget_2(model, fast);
+    if (budget < 0 || smem + 64 > (size_t)budget) return fail(HB_ERR_UNSUPPORTED, "grouped launch: shared memory budget exceeded");
+    // jobs, longest points first
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return (double)g->m[x].e->subs[0].nm * members[x].n_steps > (double)g->m[y].e->subs[0].nm * members[y].n_steps;
+    });
+    std::vector<StreamJob> jobs(n);
+    int blocks = 0;
+    for (int k = 0; k < n; k++) {
+        hb_group::Member& gm = g->m[order[k]];
+        jobs[k].net = gm.e->d_net;
+        jobs[k].args = gm.P.a;
+        jobs[k].first_block = blocks;
+        jobs[k].n_points = gm.e->B;
+        blocks += gm.e->B;
+    }
+    CUDA_TRY(g->jobs.ensure(n));
+    CUDA_TRY(cudaMemcpy(g->jobs.p, jobs.data(), n * sizeof(StreamJob), cudaMemcpyHostToDevice));
+    const int threads = npt == 1 ? 512 : 1024;
+    // the whole run as one graph: member resets, the grouped launch, batch-mean BOLD reductions
+    cudaStream_t st = g->stream();
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaSuccess;
+    for (auto& gm : g->m) {
+        hb_engine* e = gm.e;
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(e->state.p, e->x0.p, (size_t)e->B * e->state_len * 4, cudaMemcpyDeviceToDevice, st);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(e->flags_buf.p, 0, 2 * sizeof(int), st);
+        for (size_t k = 0; k < gm.bw_init.size() && ce == cudaSuccess; k++)
+            ce = cudaMemcpyAsync(e->bold[k].bw.p, gm.bw_init[k].p, gm.bw_init[k].n * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    // external event records become nodes of the graph, so the replay times the launch itself
+    if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev0, st, cudaEventRecordExternal);
+    if (ce == cudaSuccess)
+        ce = npt == 1 ? hb_launch_stream_group_1(model, fast, g->jobs.p, n, blocks, threads, smem, st)
+                      : hb_launch_stream_group_2(model, fast, g->jobs.p, n, blocks, threads, smem, st);
+    if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev1, st, cudaEventRecordExternal);
+    for (auto& gm : g->m) {
+        for (int mo = 0; mo < gm.P.n_bold_active && !gm.P.bold_pp && ce == cudaSuccess; mo++) {
+            int n_win = gm.P.a.bold.n_full[mo] + (gm.P.a.bold.partial[mo] > 0 ? 1 : 0);
+            ce = hb_launch_bold_batch_mean(gm.P.a.bold, mo, n_win, gm.e->B, gm.e->means.p, st);
+        }
+    }
+    cudaError_t ce2 = cudaStreamEndCapture(st, &g->graph);
+    if (ce != cudaSuccess) return fail(HB_ERR_CUDA, "capturing the grouped launch: %s", cudaGetErrorString(ce));
+    if (ce2 != cudaSuccess) return fail(HB_ERR_CUDA, "capturing the grouped launch: %s", cudaGetErrorString(ce2));
+    CUDA_TRY(cudaGraphInstantiate(&g->exec, g->graph, 0));
+    for (auto& gm : g->m) gm.e->last_kind = 5;
+    *out = g.release();
+    return HB_OK;
+}
+
+hb_status hb_group_execute(hb_group* g) {
+    if (!g || !g->exec) return fail(HB_ERR_INVALID_STATE, "group not prepared");
+    for (auto& gm : g->m) {
+        hb_engine* e = gm.e;
+        e->step = 0;
+        e->bold_removed = false;
+        for (auto& bh : e->bold) { bh.times.clear(); bh.n_out = 0; bh.out.clear(); }
+    }
+    CUDA_TRY(cudaGraphLaunch(g->exec, g->stream()));
+    CUDA_TRY(cudaStreamSynchronize(g->stream()));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+    g->last_ms = ms;
+    for (auto& gm : g->m) {
+        hb_result sink;  // run_finish copies the BOLD outputs of the run when given a result
+        hb_status s = run_finish(gm.e, gm.P, &sink, false);
+        gm.e->last_ms = ms;
+        gm.e->last_launches = 1;
+        if (s) return s;
+    }
+    g->executed = true;
+    return HB_OK;
+}
+
+hb_status hb_group_result(hb_group* g, int32_t i, hb_result** out) {
+    if (!g || !out) return fail(HB_ERR_INVALID_STATE, "NULL argument");
+    *out = nullptr;
+    if (i < 0 || i >= (int)g->m.size()) return fail(HB_ERR_INVALID_STATE, "member %d out of range", i);
+    if (!g->executed) return fail(HB_ERR_INVALID_STATE, "group not executed");
+    hb_group::Member& gm = g->m[i];
+    hb_result* r = new hb_result();
+    hb_status s = collect(gm.e, gm.P.n_steps, r);
+    if (s) { delete r; return s; }
+    r->elapsed_ms = g->last_ms;
+    r->params = gm.T.param_values;
+    r->has_traj = false;
+    *out = r;
+    return HB_OK;
+}
+
+hb_status hb_group_last_kernel_time(const hb_group* g, double* ms) {
+    if (!g || !ms) return fail(HB_ERR_INVALID_STATE, "NULL argument");
+    *ms = g->last_ms;
+    return HB_OK;
+}
+
+void hb_group_destroy(hb_group* g) { delete g; }

@@ -3,12 +3,12 @@
 // For one subnetwork coupled to itself through one CSR projection with per-edge delays
 // (ring semantics of runtime.rs:125-211) when the history ring of a point does not fit shared
 // memory (hundreds of nodes, delays of hundreds to thousands of steps). One CTA owns one sweep
-// point. The history is stored per point as [node][RP + K][PCH] floats: for each source node the
+// point. The history is stored per point as [node][RP + 2K][PCH] floats: for each source node the
 // coupling-function pre() channels (PCH = ncvar for identity pre, 2 = sin, cos for Kuramoto) of
 // consecutive time steps are adjacent, so the K = 8 delayed values an edge contributes to a block
 // of 8 steps are one contiguous 32·PCH-byte run that touches one or two 32-byte sectors, not eight.
 // Time t sits at position t mod RP; positions [RP, RP + K) mirror [0, K) so that a run of K
-// positions never wraps. Negative times read zero: the ring is zeroed at the start of a fresh
+// positions never wraps, and [RP + K, RP + 2K) pads the row for aligned vector reads. Negative times read zero: the ring is zeroed at the start of a fresh
 // run and RP > max delay + 2K keeps a position from being reused before its last reader.
 //
 // Warp specialisation as in resident_pipe_kernel: consumer threads (NPT nodes each) run the
@@ -155,8 +155,46 @@ __device__ __forceinline__ void stream_publish(float* ring, int n, int RPX, int 
     }
 }
 
+// The K = 8 consecutive history entries (PCH channels each) starting at q, read with 16-byte
+// aligned vector loads from the aligned address at or below q and realigned in registers: 3 loads
+// instead of 8 for one channel, 5 instead of 8 for two. Rows are padded by 2K positions, so
+// the widest read stays inside the node's own row.
+template <int PCH>
+__device__ __forceinline__ void stream_window(const float* q, float (&v)[HB_STREAM_K][PCH]) {
+    constexpr int K = HB_STREAM_K;
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(q);
+    const float4* b4 = reinterpret_cast<const float4*>(addr & ~(uintptr_t)15);
+    const int sh = (int)((addr >> 2) & 3);  // floats between the aligned base and q
+    if (PCH == 1) {
+        float f[12];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float4 u = b4[i];
+            f[4 * i] = u.x; f[4 * i + 1] = u.y; f[4 * i + 2] = u.z; f[4 * i + 3] = u.w;
+        }
+        float g[10];
+#pragma unroll
+        for (int i = 0; i < 10; i++) g[i] = (sh & 1) ? f[i + 1] : f[i];
+#pragma unroll
+        for (int j = 0; j < K; j++) v[j][0] = (sh & 2) ? g[j + 2] : g[j];
+    } else {
+        // q is 8-byte aligned: sh is 0 or 2
+        float f[20];
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+            const float4 u = b4[i];
+            f[4 * i] = u.x; f[4 * i + 1] = u.y; f[4 * i + 2] = u.z; f[4 * i + 3] = u.w;
+        }
+#pragma unroll
+        for (int j = 0; j < K; j++)
+#pragma unroll
+            for (int c = 0; c < PCH; c++) v[j][c] = sh ? f[2 * j + c + 2] : f[2 * j + c];
+    }
+}
+
+// the whole run of sweep point b of one network (one CTA)
 template <int MODEL, int PRE, int NPT, int MAXT>
-__global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+__device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, const RunArgs& a, const int b) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ DevNet net;
     {
@@ -168,9 +206,9 @@ __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __re
     constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
     constexpr int K = HB_STREAM_K;
     constexpr int UNR = (MAXT > 512) ? 1 : 2;  // edges in flight per producer thread (register budget)
-    const int b = blockIdx.x, t = threadIdx.x, nthreads = blockDim.x;
+    const int t = threadIdx.x, nthreads = blockDim.x;
     const int nm = gnet->sub[0].nm;
-    const int RP = a.stream_rp, RPX = RP + K;
+    const int RP = a.stream_rp, RPX = RP + 2 * K;
     const int n_cons = (((nm + NPT - 1) / NPT + 31) >> 5) << 5;
     const int n_prod = nthreads - n_cons;
     float* ring = a.ring + (size_t)b * nm * RPX * PCH;
@@ -242,6 +280,7 @@ __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __re
         // ================= producers =================
         const int p = t - n_cons;
         const int PL = a.pipe_lanes;  // threads per node (power of two <= 8)
+        const int pf = a.stream_prefetch;
         const int items = nm * PL;
         const int rounds = (items + n_prod - 1) / n_prod;
         const int row_len = nm * NVAR;
@@ -265,23 +304,24 @@ __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __re
                     const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
 #pragma unroll UNR
                     for (int e = e0 + lane; e < e1; e += PL) {
+                        if (pf) {
+                            const int ep = e + pf * PL;
+                            if (ep < e1) {
+                                const uint32_t mp = ed[ep];
+                                int pp = sbm - (int)(mp >> 16);
+                                pp += (pp < 0) ? RP : 0;
+                                const float* qp = ring + ((size_t)(mp & 0xffffu) * RPX + pp) * PCH;
+                                prefetch_l2(qp);
+                                prefetch_l2(qp + (K * PCH - 1));
+                            }
+                        }
                         const uint32_t m = ed[e];
                         const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
                         const float w = ew[e];
                         int pos = sbm - d;
                         pos += (pos < 0) ? RP : 0;
-                        const float* q = ring + ((size_t)src * RPX + pos) * PCH;
                         float v[K][PCH];
-#pragma unroll
-                        for (int j = 0; j < K; j++) {
-                            if (PCH == 2) {
-                                const float2 u = *reinterpret_cast<const float2*>(q + 2 * j);
-                                v[j][0] = u.x;
-                                v[j][PCH - 1] = u.y;
-                            } else {
-                                v[j][0] = q[j];
-                            }
-                        }
+                        stream_window<PCH>(ring + ((size_t)src * RPX + pos) * PCH, v);
 #pragma unroll
                         for (int j = 0; j < K; j++)
 #pragma unroll
@@ -412,6 +452,59 @@ __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __re
 }
 
 template <int MODEL, int PRE, int NPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+    stream_point<MODEL, PRE, NPT, MAXT>(gnet, a, (int)blockIdx.x);
+}
+
+// Several networks' sweeps in one launch: block i runs point i - first_block of the job whose
+// range holds i. Jobs are ordered by decreasing work per point, so the block scheduler starts the
+// longest points first and fills the machine with the short ones as SMs free up.
+template <int MODEL, int PRE, int NPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) stream_group_kernel(const StreamJob* __restrict__ jobs, int n_jobs) {
+    __shared__ RunArgs sa;
+    __shared__ int sj;
+    if (threadIdx.x == 0) {
+        int j = 0;
+        while (j + 1 < n_jobs && (int)blockIdx.x >= jobs[j + 1].first_block) j++;
+        sj = j;
+    }
+    __syncthreads();
+    const StreamJob* J = jobs + sj;
+    {
+        const int* src = reinterpret_cast<const int*>(&J->args);
+        int* dst = reinterpret_cast<int*>(&sa);
+        for (int i = threadIdx.x; i < (int)(sizeof(RunArgs) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    stream_point<MODEL, PRE, NPT, MAXT>(J->net, sa, (int)blockIdx.x - J->first_block);
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
+int stream_group_max_dynamic_smem() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, stream_group_kernel<MODEL, PRE, NPT, MAXT>) != cudaSuccess) return -1;
+    int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(stream_group_kernel<MODEL, PRE, NPT, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return -1;
+    cached = maxdyn;
+    return cached;
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
+cudaError_t launch_stream_group(const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st) {
+    int maxdyn = stream_group_max_dynamic_smem<MODEL, PRE, NPT, MAXT>();
+    if (maxdyn < 0) return cudaErrorInvalidConfiguration;
+    if ((long long)smem > maxdyn || threads > MAXT) return cudaErrorInvalidValue;
+    stream_group_kernel<MODEL, PRE, NPT, MAXT><<<blocks, threads, smem, st>>>(d_jobs, n_jobs);
+    return cudaGetLastError();
+}
+
+template <int MODEL, int PRE, int NPT, int MAXT>
 int stream_max_dynamic_smem() {
     static int cached = -1;
     if (cached >= 0) return cached;
@@ -441,8 +534,16 @@ cudaError_t launch_stream(const DevNet* d_net, const RunArgs& a, int B, int thre
 // one translation unit per (NPT, MAXT): nodes per consumer thread and the launch bound
 cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
+int hb_stream_budget_4(int model, int pre);
+cudaError_t hb_launch_stream_group_1(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_group_2(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_group_budget_1(int model, int pre);
+int hb_stream_group_budget_2(int model, int pre);
+int hb_stream_group_budget_4(int model, int pre);
 
 #define HB_STREAM_UNIT(NPT_, MAXT_)                                                                                  \
     cudaError_t hb_launch_stream_##NPT_(int model, int pre, const DevNet* d_net, const RunArgs& a, int B,            \
@@ -468,6 +569,33 @@ int hb_stream_budget_2(int model, int pre);
             hb::stream_max_dynamic_smem<3, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<3, hb::PRE_KURA, NPT_, MAXT_>, \
             hb::stream_max_dynamic_smem<4, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<4, hb::PRE_KURA, NPT_, MAXT_>, \
             hb::stream_max_dynamic_smem<5, hb::PRE_ID, NPT_, MAXT_>, hb::stream_max_dynamic_smem<5, hb::PRE_KURA, NPT_, MAXT_>}; \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (i < 0 || i >= 12) return -1;                                                                             \
+        return tab[i]();                                                                                             \
+    }                                                                                                                \
+    cudaError_t hb_launch_stream_group_##NPT_(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks,   \
+                                              int threads, size_t smem, cudaStream_t st) {                           \
+        using F = cudaError_t (*)(const StreamJob*, int, int, int, size_t, cudaStream_t);                            \
+        static const F tab[12] = {                                                                                   \
+            hb::launch_stream_group<0, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<0, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::launch_stream_group<1, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<1, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::launch_stream_group<2, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<2, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::launch_stream_group<3, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<3, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::launch_stream_group<4, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<4, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::launch_stream_group<5, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<5, hb::PRE_KURA, NPT_, MAXT_>}; \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (i < 0 || i >= 12) return cudaErrorInvalidValue;                                                          \
+        return tab[i](d_jobs, n_jobs, blocks, threads, smem, st);                                                    \
+    }                                                                                                                \
+    int hb_stream_group_budget_##NPT_(int model, int pre) {                                                          \
+        using G = int (*)();                                                                                         \
+        static const G tab[12] = {                                                                                   \
+            hb::stream_group_max_dynamic_smem<0, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<0, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_group_max_dynamic_smem<1, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<1, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_group_max_dynamic_smem<2, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<2, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_group_max_dynamic_smem<3, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<3, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_group_max_dynamic_smem<4, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<4, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_group_max_dynamic_smem<5, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<5, hb::PRE_KURA, NPT_, MAXT_>}; \
         int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
         if (i < 0 || i >= 12) return -1;                                                                             \
         return tab[i]();                                                                                             \

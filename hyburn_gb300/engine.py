@@ -231,3 +231,63 @@ class BatchHybridEngine:
         raise_for(self._lib.hb_engine_last_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(kind)),
                   self._lib.hb_last_error().decode())
         return ms.value, n.value, kind.value
+
+
+class GroupedSweep:
+    """Several engines' sweeps in one kernel launch replayed from a CUDA graph (hb_group_*).
+
+    ``members`` is a list of ``(engine, SweepParam, values, n_steps, noise)`` tuples; the engines
+    may differ in node count, connectome, delays, sweep values and step count but share the model
+    and the coupling function's pre() form. ``execute()`` restarts every member from its initial
+    state and runs all of them; ``results()`` returns one BatchSweepResult per member.
+    """
+
+    def __init__(self, members, run_flags: int = 0, stream_handle: Optional[int] = None):
+        self._lib = _abi.load_library()
+        self._engines = [m[0] for m in members]
+        keep = []
+        arr = (_abi.hb_group_member * len(members))()
+        for i, (eng, param, values, n_steps, noise) in enumerate(members):
+            vals = np.ascontiguousarray(np.asarray(values, dtype=np.float32))
+            keep.append(vals)
+            nptr, nlen, nk = eng._noise_args(noise, n_steps)
+            keep.append(nk)
+            arr[i].engine = eng._h
+            arr[i].sub_idx, arr[i].param_idx = int(param.sub_idx), int(param.param_idx)
+            arr[i].values, arr[i].n_values = _abi.f32p(vals), vals.size
+            arr[i].n_steps, arr[i].run_flags = int(n_steps), int(run_flags)
+            arr[i].noise = nptr if nptr is not None else C.POINTER(C.c_float)()
+            arr[i].noise_len = nlen
+        h = C.c_void_p()
+        st = self._lib.hb_group_prepare(arr, len(members), C.c_void_p(stream_handle) if stream_handle else None,
+                                        C.byref(h))
+        raise_for(st, self._lib.hb_last_error().decode())
+        self._h = h
+
+    def execute(self) -> None:
+        raise_for(self._lib.hb_group_execute(self._h), self._lib.hb_last_error().decode())
+
+    def results(self) -> List[BatchSweepResult]:
+        out = []
+        for i, eng in enumerate(self._engines):
+            r = C.c_void_p()
+            raise_for(self._lib.hb_group_result(self._h, i, C.byref(r)), self._lib.hb_last_error().decode())
+            out.append(eng._result(r, False))
+        return out
+
+    def last_kernel_time(self) -> float:
+        ms = C.c_double()
+        raise_for(self._lib.hb_group_last_kernel_time(self._h, C.byref(ms)), self._lib.hb_last_error().decode())
+        return ms.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hb_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

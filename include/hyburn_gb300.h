@@ -81,6 +81,10 @@ typedef int32_t hb_status;
 #define HB_RUN_NO_STREAM      (1u << 19) /* never use the streamed-history pipeline */
 /* pipeline kernel: producer threads per node (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_PIPE_LANES(n)  ((uint32_t)((n) & 0xf) << 20)
+/* streamed-history kernel: nodes per consumer thread (1, 2 or 4; 0 lets the engine choose) */
+#define HB_RUN_STREAM_NPT(n)  ((uint32_t)((n) & 0x7) << 24)
+/* streamed-history kernel: prefetch the history runs of upcoming edges into L2 */
+#define HB_RUN_STREAM_PREFETCH (1u << 27)
 /* resident kernel: threads per node sharing its edge list (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_LANES(n) ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : 0) << 12)
 
@@ -244,6 +248,37 @@ hb_status hb_noalloc_run_csr_sweep(
     int32_t n_sweep, double dt, int32_t integrator, const float* nsig, int32_t n_nsig,
     const float* d_noise, int64_t noise_len, int64_t n_steps, float* d_final_states, float* d_tavg,
     void* cuda_stream);
+
+/* ---- grouped launch: several engines' sweeps in one kernel launch (no counterpart in the reference) ----
+ * The reference runs each network size as its own BatchHybridEngine, one after the other. A grouped
+ * launch runs the sweeps of several engines — different node counts, connectomes, delays, sweep
+ * values and step counts, one model and coupling pre() form — as one launch of the
+ * streamed-history kernel (one block per sweep point, longest points first), so short points fill
+ * the SMs that long ones leave free. Every member needs one subnetwork coupled to itself through
+ * one CSR projection with per-edge delays (HB_SEM_DELAY_RING) of at least 15 steps.
+ * hb_group_prepare resets every member engine, uploads its tables and noise, and captures the
+ * member resets, the launch and the batch-mean BOLD reductions in a CUDA graph;
+ * hb_group_execute replays it (each member restarts from its initial state) and completes the
+ * members' BOLD series; hb_group_result returns member i's BatchSweepResult of the last execute.
+ * The member engines must not be used elsewhere while the group exists. */
+typedef struct hb_group_member {
+    hb_engine*   engine;
+    int32_t      sub_idx;      /* SweepParam of this member's sweep (as hb_engine_run_sweep) */
+    int32_t      param_idx;
+    const float* values;       /* n_values == the engine's n_sweep */
+    int32_t      n_values;
+    int64_t      n_steps;
+    uint32_t     run_flags;    /* HB_RUN_CHECK_FINITE; no trajectories */
+    const float* noise;        /* host standard-normal draws as for hb_engine_run_sweep, or NULL */
+    int64_t      noise_len;
+} hb_group_member;
+typedef struct hb_group hb_group;
+
+hb_status hb_group_prepare(const hb_group_member* members, int32_t n_members, void* cuda_stream, hb_group** out);
+hb_status hb_group_execute(hb_group* group);
+hb_status hb_group_result(hb_group* group, int32_t member, hb_result** out);
+hb_status hb_group_last_kernel_time(const hb_group* group, double* ms);
+void      hb_group_destroy(hb_group* group);
 
 /* ---- results: BatchSweepResult (engine.rs:15-31) ---- */
 int32_t      hb_result_n_sweep(const hb_result* r);

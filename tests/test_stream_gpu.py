@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam
-from hyburn_gb300._abi import HB_RUN_STREAM, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING, HB_SEM_NOISE_PER_POINT
+from hyburn_gb300._abi import (HB_RUN_STREAM, HB_RUN_STREAM_NPT, HB_RUN_STREAM_PREFETCH, HB_SEM_BOLD_PER_POINT,
+                               HB_SEM_DELAY_RING, HB_SEM_NOISE_PER_POINT)
 from hyburn_gb300.config import MonitorConfig
 from oracle.hb_oracle import OracleEngine
 
@@ -79,12 +80,14 @@ def test_stream_coupling_sweep_batched_workload_small():
     assert kind(eng) == STREAM_KIND
 
 
-def test_stream_selected_when_history_exceeds_shared_memory():
-    """MPR, 500 nodes, delays up to ~700 steps: the ring (2.8 MB per point) only fits HBM; two
-    nodes per consumer thread."""
+@pytest.mark.parametrize("flags", [0, HB_RUN_STREAM_NPT(4), HB_RUN_STREAM_PREFETCH, HB_RUN_STREAM_NPT(4) | HB_RUN_STREAM_PREFETCH])
+def test_stream_selected_when_history_exceeds_shared_memory(flags):
+    """MPR, 500 nodes, delays up to ~1330 steps: the ring (5.3 MB per point) only fits HBM; two or
+    four nodes per consumer thread, with and without L2 prefetch of upcoming edges."""
     from hyburn_gb300 import inputs
     cfg, meta = inputs.mpr_grid(500, 3, 150, seed=3)
-    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 0.5, 1.0], 150, semantics=HB_SEM_DELAY_RING)
+    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 0.5, 1.0], 150, semantics=HB_SEM_DELAY_RING,
+                           run_flags=flags)
     assert kind(eng) == STREAM_KIND
 
 
