@@ -274,6 +274,13 @@ class hb_group_member(C.Structure):
                 ("run_flags", C.c_uint32), ("noise", C.POINTER(C.c_float)), ("noise_len", C.c_int64)]
 
 
+class hb_adjoint_out(C.Structure):
+    _fields_ = [("loss", C.POINTER(C.c_double)), ("d_gain", C.POINTER(C.c_double)), ("d_A", C.POINTER(C.c_double)),
+                ("d_B", C.POINTER(C.c_double)), ("d_a", C.POINTER(C.c_double)), ("fc", C.POINTER(C.c_float)),
+                ("y", C.POINTER(C.c_float)), ("forward_ms", C.c_float), ("statistics_ms", C.c_float),
+                ("reverse_ms", C.c_float)]
+
+
 def load_library():
     """Load the in-tree engine library; raises if it has not been built."""
     global _LIB
@@ -306,6 +313,7 @@ def load_library():
         "hb_group_result": (I32, [P, I32, C.POINTER(P)]),
         "hb_group_last_kernel_time": (I32, [P, C.POINTER(D)]),
         "hb_group_destroy": (None, [P]),
+        "hb_engine_adjoint_fc": (I32, [P, FP, I32, I64, FP, I32, C.POINTER(hb_adjoint_out)]),
         "hb_result_n_sweep": (I32, [P]),
         "hb_result_n_subnets": (I32, [P]),
         "hb_result_n_bold": (I32, [P]),

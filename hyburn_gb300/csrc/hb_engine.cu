@@ -38,6 +38,18 @@ cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs
 int hb_stream_group_budget_1(int model, int pre);
 int hb_stream_group_budget_2(int model, int pre);
 int hb_stream_group_budget_4(int model, int pre);
+struct HbAdjointLaunch {
+    int B, N, T, R, K, CK, n_ck, cfk, gain_idx;
+    float dt, dt_half;
+    const float* x0;
+    const int* rowptr; const uint32_t* edges; const float* ew;
+    const int* cptr; const int* ctgt; const int* cdel; const float* cw;
+    float *Y, *S, *ck_state, *ck_ring, *scratch, *mu_ring;
+    const float* target;
+    float *mean, *sdev, *coef, *rk, *M, *fc;
+    double *loss, *gG, *gA, *gB, *ga;
+};
+cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st);
 
 namespace {
 
@@ -1639,3 +1651,130 @@ hb_status hb_group_last_kernel_time(const hb_group* g, double* ms) {
 }
 
 void hb_group_destroy(hb_group* g) { delete g; }
+
+// ======================================================================================
+// Adjoint of a functional-connectivity loss (no counterpart in the reference)
+// ======================================================================================
+
+struct AdjWorkspace {
+    DBuf<int> cptr, ctgt, cdel;
+    DBuf<float> cw, Y, S, ck_state, ck_ring, scratch, mu_ring, target, mean, sdev, coef, rk, M, fc;
+    DBuf<double> loss, gG, gA, gB, ga;
+};
+
+hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n_values, int64_t n_steps,
+                               const float* target_fc, int32_t checkpoint_every, hb_adjoint_out* out) {
+    if (!e || !gain_values || !target_fc || !out) return fail(HB_ERR_INVALID_STATE, "NULL argument");
+    if (n_values != e->B) return fail(HB_ERR_INVALID_STATE, "expected %d gain values, got %d", e->B, n_values);
+    if (n_steps < 2 || n_steps > (1 << 30)) return fail(HB_ERR_INVALID_STATE, "n_steps must be in [2, 2^30]");
+    if (e->subs.size() != 1 || e->projs.size() != 1 || e->subs[0].model != HBM_JR || e->subs[0].nmodes != 1)
+        return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs one JansenRit subnetwork (one mode) and one projection");
+    HostProj& hp = e->projs[0];
+    if (hp.kind != W_SPARSE || hp.dmode != HBD_EDGE)
+        return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs a CSR projection with per-edge delays (HB_SEM_DELAY_RING)");
+    if (hp.cf.kind != HBC_SIGMOIDAL && hp.cf.kind != HBC_LINEAR)
+        return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports Sigmoidal and Linear coupling");
+    if (hp.ncv != 1 || !hp.direct) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs the coupling from and into the first coupling variable");
+    if (eff_integrator(e, HBM_JR) != HBI_HEUN_DET) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint differentiates deterministic Heun");
+    const int N = e->subs[0].nm, B = e->B;
+    if (N > 200) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports up to 200 nodes");
+    int dmin = 1 << 30;
+    for (uint32_t m : hp.edges) dmin = std::min(dmin, (int)(m >> 16));
+    if (hp.edges.empty()) dmin = 8;
+    if (dmin < 1) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs every edge delay >= 1");
+    const int K = std::min(dmin, 8);
+    const int R = hp.maxd + 2 * K + 1;
+    int dev = 0, optin = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if ((size_t)R * N * 4 + 1024 > (size_t)optin) return fail(HB_ERR_UNSUPPORTED, "the delay ring of one point does not fit shared memory");
+    int CK = std::max(K, (checkpoint_every + K - 1) / K * K);
+    const int T = (int)n_steps;
+    const int n_ck = (T + CK - 1) / CK;
+    // tables of the gain sweep (Sigmoidal a = parameter 3, Linear a = parameter 0)
+    const int gain_param = hp.cf.kind == HBC_SIGMOIDAL ? 3 : 0;
+    hb_sweep_point dim{-1, gain_param, gain_values, n_values};
+    RunTables Tb;
+    hb_status s = build_tables(e, &dim, 1, false, Tb);
+    if (s) return s;
+    if ((s = upload_net(e, Tb))) return s;
+    if ((s = reset_state(e))) return s;
+    // out-edges of every source node (transpose of the CSR rows)
+    std::vector<int> cptr(N + 1, 0), ctgt(hp.edges.size()), cdel(hp.edges.size());
+    std::vector<float> cw(hp.edges.size());
+    for (uint32_t m : hp.edges) cptr[(m & 0xffffu) + 1]++;
+    for (int j = 0; j < N; j++) cptr[j + 1] += cptr[j];
+    {
+        std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+        for (int i = 0; i < N; i++)
+            for (int k = hp.rowptr[i]; k < hp.rowptr[i + 1]; k++) {
+                const int src = (int)(hp.edges[k] & 0xffffu), q = fill[src]++;
+                ctgt[q] = i; cdel[q] = (int)(hp.edges[k] >> 16); cw[q] = hp.ew[k];
+            }
+    }
+    std::unique_ptr<AdjWorkspace> W(new AdjWorkspace());
+    cudaStream_t st = e->stream();
+    const size_t nnz = std::max<size_t>(hp.edges.size(), 1);
+    CUDA_TRY(W->cptr.ensure(N + 1)); CUDA_TRY(W->ctgt.ensure(nnz)); CUDA_TRY(W->cdel.ensure(nnz)); CUDA_TRY(W->cw.ensure(nnz));
+    CUDA_TRY(cudaMemcpyAsync(W->cptr.p, cptr.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
+    if (!hp.edges.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(W->ctgt.p, ctgt.data(), ctgt.size() * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(W->cdel.p, cdel.data(), cdel.size() * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(W->cw.p, cw.data(), cw.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    const size_t TBN = (size_t)T * B * N;
+    CUDA_TRY(W->Y.ensure(TBN)); CUDA_TRY(W->S.ensure(TBN));
+    CUDA_TRY(W->ck_state.ensure((size_t)n_ck * B * N * 6));
+    CUDA_TRY(W->ck_ring.ensure((size_t)n_ck * B * R * N));
+    CUDA_TRY(W->scratch.ensure((size_t)B * CK * N * 8));
+    CUDA_TRY(W->mu_ring.ensure((size_t)B * R * N));
+    CUDA_TRY(W->target.ensure((size_t)N * N));
+    CUDA_TRY(cudaMemcpyAsync(W->target.p, target_fc, (size_t)N * N * 4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(W->mean.ensure((size_t)B * N)); CUDA_TRY(W->sdev.ensure((size_t)B * N)); CUDA_TRY(W->coef.ensure((size_t)B * N));
+    CUDA_TRY(W->rk.ensure((size_t)B * N)); CUDA_TRY(W->M.ensure((size_t)B * N * N)); CUDA_TRY(W->fc.ensure((size_t)B * N * N));
+    CUDA_TRY(W->loss.ensure(B)); CUDA_TRY(W->gG.ensure(B));
+    CUDA_TRY(W->gA.ensure((size_t)B * N)); CUDA_TRY(W->gB.ensure((size_t)B * N)); CUDA_TRY(W->ga.ensure((size_t)B * N));
+    HbAdjointLaunch L;
+    L.B = B; L.N = N; L.T = T; L.R = R; L.K = K; L.CK = CK; L.n_ck = n_ck;
+    L.cfk = hp.cf.kind; L.gain_idx = gain_param;
+    L.dt = e->net.dt; L.dt_half = e->net.dt_half;
+    L.x0 = e->x0.p; L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
+    L.cptr = W->cptr.p; L.ctgt = W->ctgt.p; L.cdel = W->cdel.p; L.cw = W->cw.p;
+    L.Y = W->Y.p; L.S = W->S.p; L.ck_state = W->ck_state.p; L.ck_ring = W->ck_ring.p; L.scratch = W->scratch.p;
+    L.mu_ring = W->mu_ring.p; L.target = W->target.p; L.mean = W->mean.p; L.sdev = W->sdev.p; L.coef = W->coef.p;
+    L.rk = W->rk.p; L.M = W->M.p; L.fc = W->fc.p; L.loss = W->loss.p; L.gG = W->gG.p; L.gA = W->gA.p; L.gB = W->gB.p;
+    L.ga = W->ga.p;
+    cudaEvent_t ev[4];
+    for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
+    cudaError_t ce = cudaEventRecord(ev[0], st);
+    if (ce == cudaSuccess) ce = hb_launch_adjoint(e->d_net, L, 0, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev[1], st);
+    if (ce == cudaSuccess) ce = hb_launch_adjoint(e->d_net, L, 1, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev[2], st);
+    if (ce == cudaSuccess) ce = hb_launch_adjoint(e->d_net, L, 2, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev[3], st);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(ev[3]);
+    float ms[3] = {0, 0, 0};
+    for (int k = 0; k < 3 && ce == cudaSuccess; k++) ce = cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]);
+    for (auto& v : ev) cudaEventDestroy(v);
+    if (ce != cudaSuccess) return fail(HB_ERR_CUDA, "adjoint: %s", cudaGetErrorString(ce));
+    e->last_ms = (double)ms[0] + ms[1] + ms[2];
+    e->last_launches = 5;
+    e->last_kind = 6;
+    out->forward_ms = ms[0];
+    out->statistics_ms = ms[1];
+    out->reverse_ms = ms[2];
+    if (out->loss) CUDA_TRY(cudaMemcpy(out->loss, W->loss.p, B * 8, cudaMemcpyDeviceToHost));
+    if (out->d_gain) CUDA_TRY(cudaMemcpy(out->d_gain, W->gG.p, B * 8, cudaMemcpyDeviceToHost));
+    if (out->d_A) CUDA_TRY(cudaMemcpy(out->d_A, W->gA.p, (size_t)B * N * 8, cudaMemcpyDeviceToHost));
+    if (out->d_B) CUDA_TRY(cudaMemcpy(out->d_B, W->gB.p, (size_t)B * N * 8, cudaMemcpyDeviceToHost));
+    if (out->d_a) CUDA_TRY(cudaMemcpy(out->d_a, W->ga.p, (size_t)B * N * 8, cudaMemcpyDeviceToHost));
+    if (out->fc) CUDA_TRY(cudaMemcpy(out->fc, W->fc.p, (size_t)B * N * N * 4, cudaMemcpyDeviceToHost));
+    if (out->y) CUDA_TRY(cudaMemcpy(out->y, W->Y.p, TBN * 4, cudaMemcpyDeviceToHost));
+    for (auto* b : {&W->Y, &W->S, &W->ck_state, &W->ck_ring, &W->scratch, &W->mu_ring, &W->target, &W->mean, &W->sdev,
+                    &W->coef, &W->rk, &W->M, &W->fc, &W->cw})
+        b->release();
+    W->cptr.release(); W->ctgt.release(); W->cdel.release();
+    W->loss.release(); W->gG.release(); W->gA.release(); W->gB.release(); W->ga.release();
+    return HB_OK;
+}

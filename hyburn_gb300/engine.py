@@ -102,6 +102,21 @@ def noise_shape(config: SimConfig, n_steps: int, n_sweep: int, semantics: int = 
     return (n_steps, row)
 
 
+@dataclass
+class AdjointResult:
+    """Loss and gradients of a functional-connectivity fit (hb_engine_adjoint_fc)."""
+    loss: np.ndarray          # [n_sweep]
+    d_gain: np.ndarray        # [n_sweep]
+    d_A: np.ndarray           # [n_sweep, nnodes]
+    d_B: np.ndarray           # [n_sweep, nnodes]
+    d_a: np.ndarray           # [n_sweep, nnodes]
+    fc: np.ndarray            # [n_sweep, nnodes, nnodes]
+    y: Optional[np.ndarray]   # [n_steps, n_sweep, nnodes] or None
+    forward_ms: float = 0.0
+    statistics_ms: float = 0.0
+    reverse_ms: float = 0.0
+
+
 class BatchHybridEngine:
     """src/engine/batch_engine/engine.rs:105-138, backed by the CUDA engine."""
 
@@ -215,6 +230,29 @@ class BatchHybridEngine:
     def set_stream(self, stream_handle: Optional[int]) -> None:
         raise_for(self._lib.hb_engine_set_stream(self._h, C.c_void_p(stream_handle or 0)),
                   self._lib.hb_last_error().decode())
+
+    def adjoint_fc(self, gain_values, n_steps: int, target_fc, checkpoint_every: int = 500,
+                   return_y: bool = False) -> AdjointResult:
+        """Loss mean((FC - target_fc)^2) of y1 - y2 per sweep point and its gradients with respect to
+        the coupling gain and the per-node JansenRit A, B, a (discrete adjoint, FP64 accumulation)."""
+        vals = np.ascontiguousarray(np.asarray(gain_values, dtype=np.float32))
+        n = self.config.network.subnetworks[0].nnodes
+        tgt = np.ascontiguousarray(np.asarray(target_fc, dtype=np.float32).reshape(n, n))
+        B = vals.size
+        loss, dg = np.zeros(B), np.zeros(B)
+        dA, dB, da = np.zeros((B, n)), np.zeros((B, n)), np.zeros((B, n))
+        fc = np.zeros((B, n, n), np.float32)
+        y = np.zeros((n_steps, B, n), np.float32) if return_y else None
+        dp = C.POINTER(C.c_double)
+        out = _abi.hb_adjoint_out()
+        out.loss, out.d_gain = loss.ctypes.data_as(dp), dg.ctypes.data_as(dp)
+        out.d_A, out.d_B, out.d_a = dA.ctypes.data_as(dp), dB.ctypes.data_as(dp), da.ctypes.data_as(dp)
+        out.fc = _abi.f32p(fc)
+        out.y = _abi.f32p(y) if y is not None else C.POINTER(C.c_float)()
+        st = self._lib.hb_engine_adjoint_fc(self._h, _abi.f32p(vals), B, int(n_steps), _abi.f32p(tgt),
+                                            int(checkpoint_every), C.byref(out))
+        raise_for(st, self._lib.hb_last_error().decode())
+        return AdjointResult(loss, dg, dA, dB, da, fc, y, out.forward_ms, out.statistics_ms, out.reverse_ms)
 
     def prepare(self, param: SweepParam, param_values, n_steps: int, noise=None, run_flags: int = 0) -> None:
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))

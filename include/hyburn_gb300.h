@@ -280,6 +280,32 @@ hb_status hb_group_result(hb_group* group, int32_t member, hb_result** out);
 hb_status hb_group_last_kernel_time(const hb_group* group, double* ms);
 void      hb_group_destroy(hb_group* group);
 
+/* ---- adjoint of a functional-connectivity loss (no counterpart in the reference, which has no adjoint) ----
+ * For an engine with one JansenRit subnetwork coupled to itself through one CSR projection with
+ * per-edge delays (HB_SEM_DELAY_RING), Sigmoidal or Linear coupling and the deterministic Heun
+ * integrator: sweep point b runs n_steps from the engine's initial state with the coupling gain
+ * gain_values[b] (Sigmoidal `a`, Linear `a`); y = y1 - y2; FC = Pearson correlation over the
+ * post-step states t = 1..n_steps; loss_b = mean over i, j of (FC_ij - target_fc_ij)^2 with a
+ * symmetric target_fc [nnodes][nnodes]. Outputs (any pointer may be NULL): loss [n_sweep],
+ * d_gain [n_sweep], d_A / d_B / d_a [n_sweep][nnodes] (the JansenRit A, B, a taken per node),
+ * fc [n_sweep][nnodes][nnodes], y [n_steps][n_sweep][nnodes]. The gradients are those of the
+ * discrete FP32 step (discrete adjoint), accumulated in FP64, with the forward run re-computed
+ * from checkpoints taken every checkpoint_every steps. The engine's state is left reset. */
+typedef struct hb_adjoint_out {
+    double* loss;
+    double* d_gain;
+    double* d_A;
+    double* d_B;
+    double* d_a;
+    float*  fc;
+    float*  y;
+    float   forward_ms;     /* device time of the forward run with checkpoints */
+    float   statistics_ms;  /* FC, loss and the per-step loss sources */
+    float   reverse_ms;     /* re-computation and reverse sweep */
+} hb_adjoint_out;
+hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,
+                               const float* target_fc, int32_t checkpoint_every, hb_adjoint_out* out);
+
 /* ---- results: BatchSweepResult (engine.rs:15-31) ---- */
 int32_t      hb_result_n_sweep(const hb_result* r);
 int32_t      hb_result_n_subnets(const hb_result* r);
