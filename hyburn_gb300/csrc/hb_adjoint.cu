@@ -19,8 +19,9 @@
 // ring like the forward history, and source node j adds sum over its out-edges e of
 // w_e * mu_tgt(e)(s + d_e) to its lambda at time s. With every delay >= K the values pulled at
 // step s were written at least K reverse steps earlier, so one barrier per K steps suffices, as in
-// the forward kernels. The result is deterministic (no atomics). Parameter gradients accumulate in
-// FP64 over the run.
+// the forward kernels. The result is deterministic (no atomics). Parameter gradients are summed in
+// FP32 within a checkpoint segment and in FP64 across segments (FP64 arithmetic is slow on this
+// part, so it is kept out of the per-step work).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -34,6 +35,7 @@ constexpr int NV = 6;  // Jansen–Rit state variables
 
 struct AdjArgs {
     int B, N, T, R, K, CK, n_ck;
+    int store_all;        // 1: the forward keeps x(s), g(s) of every step (CK == T), no re-computation
     int cfk;              // HBC_SIGMOIDAL or HBC_LINEAR
     int gain_idx;         // index of the gain in the resolved coupling row (Sigmoidal 3, Linear 0)
     float dt, dt_half;
@@ -124,18 +126,112 @@ __device__ __forceinline__ void jr_vjp(const float* p, const float* y, float c0,
     u_a = u[3] * (A * sv[0] - 2.0f * y[3] - 2.0f * a * y[0]) + u[4] * (A * Mv - 2.0f * y[4] - 2.0f * a * y[1]);
 }
 
-// coupling sum of target i at step s from the delay ring [R][N] (runtime.rs:162-204 reads)
-__device__ __forceinline__ float gather_ring(const float* ring, const AdjArgs& A, int i, int s) {
+// The lambda-independent part of one reverse step at state x(s) with coupling sum g(s): the nonzero
+// Jacobian factors of the Jansen-Rit arm at x and at the Heun predictor p = x + h f(x), the parameter
+// derivative factors there, and the coupling slopes. With them the step's adjoint is a short chain of
+// multiply-adds in lambda (jr_lin_step), so the transcendental work of step s - 1 can be done while
+// step s is still in flight.
+struct JrCoef {
+    float q1x, q2x, p0x, q1p, q2p, p0p;     // J factors: d f4/d y0, d f5/d y0, d f3/d y1 at x and at p
+    float aAx, aAp, aMx, aMp;               // d f3/dA = a sv0, d f4/dA = a M at x and p
+    float bBx, bBp;                         // d f5/dB at x and p
+    float a3x, a4x, a3p, a4p;               // d f3/da, d f4/da at x and p
+    float dcdg, dcdgain;                    // coupling output slopes
+};
+
+__device__ __forceinline__ JrCoef jr_coef(const float* prm, const float* cp, int cfk, const float* xs, float g, float h) {
+    const float A = prm[0], B = prm[1], a = prm[2], b = prm[3], J = prm[7];
+    const float a1 = prm[8], a2 = prm[9], a3 = prm[10], a4 = prm[11], mu = prm[12];
+    JrCoef k;
+    const float c = coupling_post(cfk, cp, g);
+    coupling_post_grad(cfk, cp, g, k.dcdg, k.dcdgain);
+    float sv[3], dsv[3];
+    jr_sigmoids(prm, xs, sv, dsv);
+    // k1 = f(x, c) from the same sigmoid values, in the operation order of dfun.rs's Jansen-Rit arm
+    float k1[NV], p[NV];
+    {
+        k1[0] = xs[3];
+        k1[1] = xs[4];
+        k1[2] = xs[5];
+        float d3 = sv[0] * (A * a);
+        d3 = d3 - xs[3] * (2.0f * a);
+        d3 = d3 - xs[0] * (a * a);
+        k1[3] = d3;
+        float mt = sv[1] * (a2 * J);
+        mt = mt + mu;
+        mt = mt + c;
+        float d4 = mt * (A * a);
+        d4 = d4 - xs[4] * (2.0f * a);
+        d4 = d4 - xs[1] * (a * a);
+        k1[4] = d4;
+        float d5 = sv[2] * (a4 * J);
+        d5 = d5 * (B * b);
+        d5 = d5 - xs[5] * (2.0f * b);
+        d5 = d5 - xs[2] * (b * b);
+        k1[5] = d5;
+    }
+#pragma unroll
+    for (int v = 0; v < NV; v++) p[v] = xs[v] + k1[v] * h;
+    const float Aa = A * a, Bb = B * b;
+    k.q1x = Aa * (a2 * J) * dsv[1] * (a1 * J);
+    k.q2x = Bb * (a4 * J) * dsv[2] * (a3 * J);
+    k.p0x = Aa * dsv[0];
+    float Mx = (sv[1] * (a2 * J) + mu) + c;
+    k.aAx = a * sv[0];
+    k.aMx = a * Mx;
+    k.bBx = b * (sv[2] * (a4 * J));
+    k.a3x = A * sv[0] - 2.0f * xs[3] - 2.0f * a * xs[0];
+    k.a4x = A * Mx - 2.0f * xs[4] - 2.0f * a * xs[1];
+    jr_sigmoids(prm, p, sv, dsv);
+    k.q1p = Aa * (a2 * J) * dsv[1] * (a1 * J);
+    k.q2p = Bb * (a4 * J) * dsv[2] * (a3 * J);
+    k.p0p = Aa * dsv[0];
+    float Mp = (sv[1] * (a2 * J) + mu) + c;
+    k.aAp = a * sv[0];
+    k.aMp = a * Mp;
+    k.bBp = b * (sv[2] * (a4 * J));
+    k.a3p = A * sv[0] - 2.0f * p[3] - 2.0f * a * p[0];
+    k.a4p = A * Mp - 2.0f * p[4] - 2.0f * a * p[1];
+    return k;
+}
+
+// adjoint of one Heun step (engine.rs:710-720) given the coefficients: lambda(s+1) -> lambda(s)
+// (without the delayed-coupling and loss terms), mu_c = dL/dc(s), and the parameter terms
+__device__ __forceinline__ void jr_lin_step(const JrCoef& k, const float* prm, float h, float hh, float* lam,
+                                            float& mu_c, float& tA, float& tB, float& ta) {
+    const float A = prm[0], a = prm[2], b = prm[3];
+    const float na2 = -(a * a), nb2 = -(b * b), m2a = -2.0f * a, m2b = -2.0f * b;
+    float u2[NV], vp[NV], u1[NV], vx[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) u2[v] = hh * lam[v];
+    vp[0] = u2[3] * na2 + u2[4] * k.q1p + u2[5] * k.q2p;
+    vp[1] = u2[3] * k.p0p + u2[4] * na2;
+    vp[2] = -u2[3] * k.p0p + u2[5] * nb2;
+    vp[3] = u2[0] + u2[3] * m2a;
+    vp[4] = u2[1] + u2[4] * m2a;
+    vp[5] = u2[2] + u2[5] * m2b;
+#pragma unroll
+    for (int v = 0; v < NV; v++) u1[v] = hh * lam[v] + h * vp[v];
+    vx[0] = u1[3] * na2 + u1[4] * k.q1x + u1[5] * k.q2x;
+    vx[1] = u1[3] * k.p0x + u1[4] * na2;
+    vx[2] = -u1[3] * k.p0x + u1[5] * nb2;
+    vx[3] = u1[0] + u1[3] * m2a;
+    vx[4] = u1[1] + u1[4] * m2a;
+    vx[5] = u1[2] + u1[5] * m2b;
+#pragma unroll
+    for (int v = 0; v < NV; v++) lam[v] = lam[v] + (vp[v] + vx[v]);
+    mu_c = (u1[4] + u2[4]) * (A * a);
+    tA = (u1[3] * k.aAx + u1[4] * k.aMx) + (u2[3] * k.aAp + u2[4] * k.aMp);
+    tB = u1[5] * k.bBx + u2[5] * k.bBp;
+    ta = (u1[3] * k.a3x + u1[4] * k.a4x) + (u2[3] * k.a3p + u2[4] * k.a4p);
+}
+
+// coupling sum of target i at step 0: every edge reads the current state (runtime.rs:166-170)
+__device__ __forceinline__ float gather_step0(const float* ring, const AdjArgs& A, int i, int lane, int L) {
     float g = 0.0f;
-    const int R = A.R;
-    for (int e = A.rowptr[i]; e < A.rowptr[i + 1]; e++) {
+    for (int e = A.rowptr[i] + lane; e < A.rowptr[i + 1]; e += L) {
         const uint32_t m = A.edges[e];
-        const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
-        int t;
-        if (s == 0) t = 0;
-        else if (d > s) continue;
-        else t = s - d;
-        g += A.ew[e] * ring[(t % R) * A.N + src];
+        g += A.ew[e] * ring[(int)(m & 0xffffu)];
     }
     return g;
 }
@@ -161,111 +257,235 @@ __device__ __forceinline__ void load_params(const DevNet& net, int b, float* prm
     for (int i = 0; i < 8; i++) cp[i] = c[i];
 }
 
-// forward steps [s_begin, s_end) of node i from the ring in shared memory; K-step barrier blocks.
-// mode 0: write y(t) (and checkpoints at multiples of CK); mode 1: keep x(s), g(s) in the scratch.
-__device__ void forward_steps(float* ring, const AdjArgs& A, int b, int i, bool act, float* x, const float* prm,
-                              const float* cp, int s_begin, int s_end, int mode) {
-    const int N = A.N, R = A.R;
-    for (int s = s_begin; s < s_end; s++) {
-        if ((s - s_begin) % A.K == 0) {
-            __syncthreads();
-            if (mode == 0 && s % A.CK == 0) {
-                const int k = s / A.CK;
-                float* cr = A.ck_ring + ((size_t)k * A.B + b) * (size_t)R * N;
-                for (int q = threadIdx.x; q < R * N; q += blockDim.x) cr[q] = ring[q];
-                if (act) {
-                    float* cs = A.ck_state + ((size_t)k * A.B + b) * N * NV + (size_t)i * NV;
+__device__ __forceinline__ float lane_sum(float v, int L) {
+    for (int o = L >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// shared-memory tables: CSR rows of the targets (ring offsets src - d*N) and, for the reverse
+// sweep, the out-edges of the sources (ring offsets d*N + tgt)
+struct AdjTables {
+    const int* rowptr;
+    const int* eoff;
+    const float* ew;
+    const int* cptr;
+    const int* coff;
+    const float* cw;
+};
+
+__device__ AdjTables stage_tables(const AdjArgs& A, unsigned char* smem, size_t off, bool reverse) {
+    const int N = A.N, nnz = A.rowptr[N];
+    int* rp = reinterpret_cast<int*>(smem + off);
+    int* eo = rp + (N + 1);
+    float* w = reinterpret_cast<float*>(eo + nnz);
+    for (int q = threadIdx.x; q <= N; q += blockDim.x) rp[q] = A.rowptr[q];
+    for (int q = threadIdx.x; q < nnz; q += blockDim.x) {
+        const uint32_t m = A.edges[q];
+        eo[q] = (int)(m & 0xffffu) - (int)(m >> 16) * N;
+        w[q] = A.ew[q];
+    }
+    AdjTables t{rp, eo, w, nullptr, nullptr, nullptr};
+    if (reverse) {
+        int* cp = reinterpret_cast<int*>(w + nnz);
+        int* co = cp + (N + 1);
+        float* cw = reinterpret_cast<float*>(co + nnz);
+        for (int q = threadIdx.x; q <= N; q += blockDim.x) cp[q] = A.cptr[q];
+        for (int q = threadIdx.x; q < nnz; q += blockDim.x) { co[q] = A.cdel[q] * N + A.ctgt[q]; cw[q] = A.cw[q]; }
+        t.cptr = cp; t.coff = co; t.cw = cw;
+    }
+    return t;
+}
+
+// forward steps [s_begin, s_end) in blocks of K steps, from the ring in shared memory. The ring starts
+// zeroed, so a time before 0 reads 0 (runtime.rs:171-176), and every step after 0 reads time s - d at
+// ring offset (s mod R) * N + src - d * N, wrapped once. Every delay is >= K, so the K coupling sums
+// of a block read only times published before it:
+//   phase A (all threads, L lanes per node): the block's coupling sums into gbuf[K][N];
+//   phase B (thread t = node t): the K serial Heun steps, publishing x0 into the ring.
+// mode 0: write y(t) (and checkpoints at multiples of CK, or every step's x, g when store_all);
+// mode 1: keep x(s), g(s) in the scratch. x holds the state of node threadIdx.x.
+__device__ void forward_steps(float* ring, float* gbuf, const AdjArgs& A, const AdjTables& tb, int b, int L, float* x,
+                              const float* prm, const float* cp, int s_begin, int s_end, int mode) {
+    const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K;
+    const int t = threadIdx.x;
+    const int gi = t / L, gl = t - (t / L) * L;
+    const bool gact = gi < N, uact = t < N;
+    const int e0 = gact ? tb.rowptr[gi] : 0, e1 = gact ? tb.rowptr[gi + 1] : 0;
+    for (int s0 = s_begin; s0 < s_end; s0 += K) {
+        const int nb = (s_end - s0) < K ? (s_end - s0) : K;
+        __syncthreads();
+        if (mode == 0 && !A.store_all && s0 % A.CK == 0) {
+            const int k = s0 / A.CK;
+            float* cr = A.ck_ring + ((size_t)k * A.B + b) * (size_t)RN;
+            for (int q = t; q < RN; q += blockDim.x) cr[q] = ring[q];
+            if (uact) {
+                float* cs = A.ck_state + ((size_t)k * A.B + b) * N * NV + (size_t)t * NV;
 #pragma unroll
-                    for (int v = 0; v < NV; v++) cs[v] = x[v];
-                }
-                __syncthreads();
+                for (int v = 0; v < NV; v++) cs[v] = x[v];
             }
         }
-        if (!act) continue;
-        const float g = gather_ring(ring, A, i, s);
-        if (mode == 1) {
-            float* sc = A.scratch + (((size_t)b * A.CK + (s - s_begin)) * N + i) * 8;
-#pragma unroll
-            for (int v = 0; v < NV; v++) sc[v] = x[v];
-            sc[6] = g;
+        // phase A
+        int slot = s0 % R;
+        for (int j = 0; j < nb; j++) {
+            float part = 0.0f;
+            if (gact) {
+                if (s0 + j == 0) part = gather_step0(ring, A, gi, gl, L);
+                else {
+                    const int base = slot * N;
+                    for (int e = e0 + gl; e < e1; e += L) {
+                        int a = base + tb.eoff[e];
+                        a += (a < 0) ? RN : 0;
+                        part += tb.ew[e] * ring[a];
+                    }
+                }
+            }
+            part = lane_sum(part, L);
+            if (gact && gl == 0) gbuf[j * N + gi] = part;
+            slot = (slot + 1 == R) ? 0 : slot + 1;
         }
-        heun_step(prm, x, coupling_post(A.cfk, cp, g), A.dt, A.dt_half);
-        ring[((s + 1) % R) * N + i] = x[0];
-        if (mode == 0) A.Y[((size_t)s * A.B + b) * N + i] = x[1] - x[2];
+        __syncthreads();
+        // phase B
+        if (uact) {
+            slot = s0 % R;
+            for (int j = 0; j < nb; j++) {
+                const int s = s0 + j;
+                const float g = gbuf[j * N + t];
+                if (mode == 1 || A.store_all) {
+                    float* sc = A.scratch + (((size_t)b * A.CK + (s - s_begin)) * N + t) * 8;
+#pragma unroll
+                    for (int v = 0; v < NV; v++) sc[v] = x[v];
+                    sc[6] = g;
+                }
+                heun_step(prm, x, coupling_post(A.cfk, cp, g), A.dt, A.dt_half);
+                const int next = (slot + 1 == R) ? 0 : slot + 1;
+                ring[next * N + t] = x[0];
+                if (mode == 0) A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
+                slot = next;
+            }
+        }
     }
 }
 
-__global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A) {
-    extern __shared__ __align__(16) float ring[];
-    const int b = blockIdx.x, i = threadIdx.x, N = A.N;
+__device__ __forceinline__ size_t tables_size(int N, int nnz) { return (size_t)(N + 1) * 4 + (size_t)nnz * 8; }
+
+__global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* ring = reinterpret_cast<float*>(smem);
+    const int b = blockIdx.x, N = A.N, RN = A.R * A.N;
     const DevNet& net = *gnet;
-    const bool act = i < N;
     float prm[13], cp[8], x[NV];
     load_params(net, b, prm, cp);
-    for (int q = threadIdx.x; q < A.R * N; q += blockDim.x) ring[q] = 0.0f;
+    for (int q = threadIdx.x; q < RN; q += blockDim.x) ring[q] = 0.0f;
+    const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, false);
+    float* gbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + tables_size(N, A.rowptr[N]) + 15) & ~(size_t)15));
     __syncthreads();
+    const bool uact = (int)threadIdx.x < N;
 #pragma unroll
-    for (int v = 0; v < NV; v++) x[v] = act ? A.x0[(size_t)b * N * NV + i * NV + v] : 0.0f;
-    if (act) ring[i] = x[0];
-    forward_steps(ring, A, b, i, act, x, prm, cp, 0, A.T, 0);
+    for (int v = 0; v < NV; v++) x[v] = uact ? A.x0[(size_t)b * N * NV + threadIdx.x * NV + v] : 0.0f;
+    if (uact) ring[threadIdx.x] = x[0];
+    forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
 }
 
 // ---- statistics of y, FC, loss, and the coefficients of dL/dy ----
 __global__ void adj_stats_kernel(AdjArgs A) {
-    extern __shared__ __align__(16) float zs[];  // [32][N] chunk of z
+    extern __shared__ __align__(16) float zs[];  // [32][N rounded up to 4] chunk of y - shift
     const int b = blockIdx.x, N = A.N, T = A.T;
     const int tid = threadIdx.x, nth = blockDim.x;
-    for (int i = tid; i < N; i += nth) {
-        double s = 0.0;
-        for (int t = 0; t < T; t++) s += A.Y[((size_t)t * A.B + b) * N + i];
-        const double m = s / T;
-        double v = 0.0;
-        for (int t = 0; t < T; t++) { double d = A.Y[((size_t)t * A.B + b) * N + i] - m; v += d * d; }
-        A.mean[(size_t)b * N + i] = (float)m;
-        A.sdev[(size_t)b * N + i] = (float)sqrt(v / T);
-    }
-    __syncthreads();
-    const int n_pairs = N * (N + 1) / 2;
-    constexpr int PPT = 8;  // pairs per thread per pass over y
-    float* fc = A.fc + (size_t)b * N * N;
-    for (int base = 0; base < n_pairs; base += PPT * nth) {
-        int pi[PPT], pj[PPT];
-        double acc[PPT];
-#pragma unroll
-        for (int q = 0; q < PPT; q++) {
-            int p = base + tid + q * nth;
-            pi[q] = -1; pj[q] = -1; acc[q] = 0.0;
-            if (p < n_pairs) {  // p -> (i, j), i <= j, row-major upper triangle
-                int ii = 0, rem = p;
-                while (rem >= N - ii) { rem -= N - ii; ii++; }
-                pi[q] = ii; pj[q] = ii + rem;
-            }
+    const int N4 = (N + 3) / 4, W = N4 * 4;
+    // One pass over y: moments of y - c_i with the shift c_i = mean of the first 64 steps, summed in
+    // FP32 over chunks of 32 steps and in FP64 across chunks; FC_ij = cov_ij / (sd_i sd_j).
+    float* shift = zs + 32 * W;          // [W]
+    double* dsum = reinterpret_cast<double*>(shift + W);   // [W] sums of y - c
+    double* dsq = dsum + W;               // [W] sums of (y - c)^2 (diagonal of the tile products)
+    for (int k = tid; k < W; k += nth) {
+        float c = 0.0f;
+        if (k < N) {
+            const int n0 = T < 64 ? T : 64;
+            for (int t = 0; t < n0; t++) c += A.Y[((size_t)t * A.B + b) * N + k];
+            c /= (float)n0;
         }
+        shift[k] = c;
+        dsum[k] = 0.0;
+        dsq[k] = 0.0;
+    }
+    const int n_tiles = N4 * (N4 + 1) / 2;
+    float* fc = A.fc + (size_t)b * N * N;
+    for (int base = 0; base < n_tiles; base += nth) {
+        const int tile = base + tid;
+        int bi = -1, bj = -1;
+        if (tile < n_tiles) {
+            int rem = tile;
+            bi = 0;
+            while (rem >= N4 - bi) { rem -= N4 - bi; bi++; }
+            bj = bi + rem;
+        }
+        double acc[4][4];
+        float part[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] = 0.0;
         for (int t0 = 0; t0 < T; t0 += 32) {
             const int nt = (T - t0) < 32 ? (T - t0) : 32;
             __syncthreads();
-            for (int q = tid; q < nt * N; q += nth) {
-                const int tt = q / N, k = q - tt * N;
-                const float sd = A.sdev[(size_t)b * N + k];
-                zs[q] = sd > 0.0f ? (A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - A.mean[(size_t)b * N + k]) / sd : 0.0f;
+            for (int q = tid; q < 32 * W; q += nth) {
+                const int tt = q / W, k = q - tt * W;
+                float z = 0.0f;
+                if (tt < nt && k < N) z = A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - shift[k];
+                zs[q] = z;
             }
             __syncthreads();
-#pragma unroll
-            for (int q = 0; q < PPT; q++) {
-                if (pi[q] < 0) continue;
-                float part = 0.0f;
-                for (int tt = 0; tt < nt; tt++) part += zs[tt * N + pi[q]] * zs[tt * N + pj[q]];
-                acc[q] += part;
+            if (base == 0 && tid < N) {
+                float ssum = 0.0f;
+                for (int tt = 0; tt < nt; tt++) ssum += zs[tt * W + tid];
+                dsum[tid] += ssum;
             }
-        }
+            if (bi < 0) continue;
 #pragma unroll
-        for (int q = 0; q < PPT; q++) {
-            if (pi[q] < 0) continue;
-            float v = (float)(acc[q] / T);
-            if (pi[q] == pj[q]) v = 1.0f;
-            fc[pi[q] * N + pj[q]] = v;
-            fc[pj[q] * N + pi[q]] = v;
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) part[u][v] = 0.0f;
+            for (int tt = 0; tt < nt; tt++) {
+                const float4 zi = *reinterpret_cast<const float4*>(zs + tt * W + bi * 4);
+                const float4 zj = *reinterpret_cast<const float4*>(zs + tt * W + bj * 4);
+                const float ai[4] = {zi.x, zi.y, zi.z, zi.w}, aj[4] = {zj.x, zj.y, zj.z, zj.w};
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) part[u][v] = __fmaf_rn(ai[u], aj[v], part[u][v]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] += part[u][v];
         }
+        if (bi >= 0 && bi == bj) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) dsq[bi * 4 + u] = acc[u][u];
+        }
+        __syncthreads();
+        if (bi >= 0) {
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int ii = bi * 4 + u, jj = bj * 4 + v;
+                    if (ii >= N || jj >= N) continue;
+                    const double mi = dsum[ii] / T, mj = dsum[jj] / T;
+                    const double vi = dsq[ii] / T - mi * mi, vj = dsq[jj] / T - mj * mj;
+                    const double cov = acc[u][v] / T - mi * mj;
+                    const double den = sqrt(vi > 0.0 ? vi : 0.0) * sqrt(vj > 0.0 ? vj : 0.0);
+                    const float val = (ii == jj) ? 1.0f : (float)(den > 0.0 ? cov / den : 0.0);
+                    fc[ii * N + jj] = val;
+                    fc[jj * N + ii] = val;
+                }
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < N; k += nth) {
+        const double m = dsum[k] / T, v = dsq[k] / T - m * m;
+        A.mean[(size_t)b * N + k] = (float)(shift[k] + m);
+        A.sdev[(size_t)b * N + k] = (float)sqrt(v > 0.0 ? v : 0.0);
     }
     __syncthreads();
     // loss, M (off-diagonal dL/dFC), r_k, coef_k
@@ -317,103 +537,130 @@ __global__ void adj_source_kernel(AdjArgs A) {
     const float ck = A.coef[(size_t)b * N + k], rk = A.rk[(size_t)b * N + k];
     for (int tt = w; tt < nt; tt += TW) {
         float acc = 0.0f;
-        for (int j = 0; j < N; j++) acc += Ms[j * N + k] * zs[tt * N + j];
+        for (int j = 0; j < N; j++) acc = __fmaf_rn(Ms[j * N + k], zs[tt * N + j], acc);
         A.S[((size_t)(t0 + tt) * A.B + b) * N + k] = ck * (acc - rk * zs[tt * N + k]);
     }
 }
 
-__global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A) {
-    extern __shared__ __align__(16) float ring[];  // forward ring during recompute, mu ring during reversal
-    const int b = blockIdx.x, i = threadIdx.x, N = A.N, R = A.R, T = A.T;
+__device__ __forceinline__ JrCoef shfl_coef(const JrCoef& k, int src_lane, int L) {
+    JrCoef o;
+    const float* in = reinterpret_cast<const float*>(&k);
+    float* out = reinterpret_cast<float*>(&o);
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(JrCoef) / 4); q++) out[q] = __shfl_sync(0xffffffffu, in[q], src_lane, L);
+    return o;
+}
+
+__global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* ring = reinterpret_cast<float*>(smem);  // forward ring during recompute, mu ring during reversal
+    const int b = blockIdx.x, N = A.N, R = A.R, T = A.T, RN = A.R * A.N;
+    const int i = threadIdx.x / L, lane = threadIdx.x - (threadIdx.x / L) * L;
     const DevNet& net = *gnet;
     const bool act = i < N;
     float prm[13], cp[8];
     load_params(net, b, prm, cp);
+    const int nnz = A.rowptr[N];
+    const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, true);
+    float* gbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + 2 * tables_size(N, nnz) + 15) & ~(size_t)15));
+    __syncthreads();  // the tables are staged by other threads than the ones reading a node's range
     const float h = A.dt, hh = A.dt_half;
-    double lam[NV];  // adjoint state, carried in FP64 across the reverse sweep
+    float lam[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) lam[v] = 0.0;
+    for (int v = 0; v < NV; v++) lam[v] = 0.0f;
     if (act) {
         const float sT = A.S[((size_t)(T - 1) * A.B + b) * N + i];
         lam[1] = sT;
-        lam[2] = -(double)sT;
+        lam[2] = -sT;
     }
+    // gradients: FP32 sums over one checkpoint segment, added into FP64 totals once per segment
     double gA = 0.0, gB = 0.0, ga = 0.0, gG = 0.0;
-    float* mu_g = A.mu_ring + (size_t)b * R * N;
-    for (int q = threadIdx.x; q < R * N; q += blockDim.x) mu_g[q] = 0.0f;
+    float* mu_g = A.mu_ring + (size_t)b * RN;
+    for (int q = threadIdx.x; q < RN; q += blockDim.x) mu_g[q] = 0.0f;
+    const int c0 = act ? tb.cptr[i] : 0, c1 = act ? tb.cptr[i + 1] : 0;
     for (int seg = A.n_ck - 1; seg >= 0; seg--) {
         const int s_begin = seg * A.CK, s_end = (s_begin + A.CK) < T ? (s_begin + A.CK) : T;
-        // (a) recompute the segment forward from its checkpoint
+        // (a) recompute the segment forward from its checkpoint (unless the forward kept every step)
         __syncthreads();
-        {
-            const float* cr = A.ck_ring + ((size_t)seg * A.B + b) * (size_t)R * N;
-            for (int q = threadIdx.x; q < R * N; q += blockDim.x) ring[q] = cr[q];
-        }
-        float x[NV];
+        if (!A.store_all) {
+            const float* cr = A.ck_ring + ((size_t)seg * A.B + b) * (size_t)RN;
+            for (int q = threadIdx.x; q < RN; q += blockDim.x) ring[q] = cr[q];
+            float x[NV];
+            const bool uact = (int)threadIdx.x < N;
 #pragma unroll
-        for (int v = 0; v < NV; v++) x[v] = act ? A.ck_state[((size_t)seg * A.B + b) * N * NV + (size_t)i * NV + v] : 0.0f;
-        forward_steps(ring, A, b, i, act, x, prm, cp, s_begin, s_end, 1);
+            for (int v = 0; v < NV; v++)
+                x[v] = uact ? A.ck_state[((size_t)seg * A.B + b) * N * NV + (size_t)threadIdx.x * NV + v] : 0.0f;
+            forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, s_begin, s_end, 1);
+        }
         // (b) the mu ring of the later segments into shared memory
         __syncthreads();
-        for (int q = threadIdx.x; q < R * N; q += blockDim.x) ring[q] = mu_g[q];
-        // (c) reverse sweep
-        for (int s = s_end - 1; s >= s_begin; s--) {
-            if ((s_end - 1 - s) % A.K == 0) __syncthreads();
-            if (!act) continue;
-            const float* sc = A.scratch + (((size_t)b * A.CK + (s - s_begin)) * N + i) * 8;
-            float xs[NV];
+        for (int q = threadIdx.x; q < RN; q += blockDim.x) ring[q] = mu_g[q];
+        // (c) reverse sweep in groups of L steps: lane l of a node computes the coefficients of step
+        // s_hi - l, then the L steps run in order with the coefficients shuffled from their lane.
+        // mu(t) of a time never reached (t > T - 1) reads as the ring's initial 0.
+        float sA = 0.0f, sB = 0.0f, sa = 0.0f, sG = 0.0f;
+        int slot = (s_end - 1) % R;
+        for (int s_hi = s_end - 1; s_hi >= s_begin; s_hi -= L) {
+            JrCoef mine;
+            float src_mine = 0.0f;
+            const int sl = s_hi - lane;
+            if (act && sl >= s_begin) {
+                const float* sc = A.scratch + (((size_t)b * A.CK + (sl - s_begin)) * N + i) * 8;
+                float xs[NV];
 #pragma unroll
-            for (int v = 0; v < NV; v++) xs[v] = sc[v];
-            const float g = sc[6];
-            const float c = coupling_post(A.cfk, cp, g);
-            float cc[2] = {c, 0.0f}, k1[NV], p[NV];
-            hb::dfun(HBM_JR, prm, 0, xs, cc, k1);
-#pragma unroll
-            for (int v = 0; v < NV; v++) p[v] = xs[v] + k1[v] * h;
-            // adjoint of k2 = f(p): u2 = h/2 lam
-            float u2[NV], vp[NV], u1[NV], vx[NV];
-#pragma unroll
-            for (int v = 0; v < NV; v++) u2[v] = (float)(hh * lam[v]);
-            float uc2, uA2, uB2, ua2, uc1, uA1, uB1, ua1;
-            jr_vjp(prm, p, c, u2, vp, uc2, uA2, uB2, ua2);
-#pragma unroll
-            for (int v = 0; v < NV; v++) u1[v] = (float)(hh * lam[v] + (double)(h * vp[v]));
-            jr_vjp(prm, xs, c, u1, vx, uc1, uA1, uB1, ua1);
-#pragma unroll
-            for (int v = 0; v < NV; v++) lam[v] = lam[v] + ((double)vp[v] + (double)vx[v]);
-            const float mu_c = uc1 + uc2;
-            float dc_dg, dc_dgain;
-            coupling_post_grad(A.cfk, cp, g, dc_dg, dc_dgain);
-            gA += (double)uA1 + (double)uA2;
-            gB += (double)uB1 + (double)uB2;
-            ga += (double)ua1 + (double)ua2;
-            gG += (double)mu_c * (double)dc_dgain;
-            ring[(s % R) * N + i] = mu_c * dc_dg;
-            // lambda(s) for s >= 1: delayed-coupling terms pulled from later steps, then dL/dx(s)
-            if (s >= 1) {
+                for (int v = 0; v < NV; v++) xs[v] = sc[v];
+                mine = jr_coef(prm, cp, A.cfk, xs, sc[6], h);
+                if (sl >= 1) src_mine = A.S[((size_t)(sl - 1) * A.B + b) * N + i];
+            } else {
+                mine = JrCoef{};
+            }
+            for (int j = 0; j < L; j++) {
+                const int s = s_hi - j;
+                if (s < s_begin) break;
+                if ((s_end - 1 - s) % A.K == 0) __syncthreads();
                 float pull = 0.0f;
-                for (int e = A.cptr[i]; e < A.cptr[i + 1]; e++) {
-                    const int tt = s + A.cdel[e];
-                    if (tt <= T - 1) pull += A.cw[e] * ring[(tt % R) * N + A.ctgt[e]];
+                if (act && s >= 1) {
+                    const int base = slot * N;
+                    for (int e = c0 + lane; e < c1; e += L) {
+                        int a = base + tb.coff[e];
+                        a -= (a >= RN) ? RN : 0;
+                        pull += tb.cw[e] * ring[a];
+                    }
                 }
-                lam[0] += pull;
-                const float src = A.S[((size_t)(s - 1) * A.B + b) * N + i];
-                lam[1] += src;
-                lam[2] -= src;
+                pull = lane_sum(pull, L);
+                const JrCoef kc = shfl_coef(mine, j, L);
+                const float src = __shfl_sync(0xffffffffu, src_mine, j, L);
+                if (act) {
+                    float mu_c, tA, tB, ta;
+                    jr_lin_step(kc, prm, h, hh, lam, mu_c, tA, tB, ta);
+                    sA += tA;
+                    sB += tB;
+                    sa += ta;
+                    sG += mu_c * kc.dcdgain;
+                    if (lane == 0) ring[slot * N + i] = mu_c * kc.dcdg;
+                    // lambda(s) for s >= 1: delayed-coupling terms pulled from later steps, then dL/dx(s)
+                    if (s >= 1) {
+                        lam[0] += pull;
+                        lam[1] += src;
+                        lam[2] -= src;
+                    }
+                }
+                slot = (slot == 0) ? R - 1 : slot - 1;
             }
         }
+        gA += sA; gB += sB; ga += sa; gG += sG;
         __syncthreads();
-        for (int q = threadIdx.x; q < R * N; q += blockDim.x) mu_g[q] = ring[q];
+        for (int q = threadIdx.x; q < RN; q += blockDim.x) mu_g[q] = ring[q];
     }
-    if (act) {
+    if (act && lane == 0) {
         A.gA[(size_t)b * N + i] = gA;
         A.gB[(size_t)b * N + i] = gB;
         A.ga[(size_t)b * N + i] = ga;
     }
     // gain gradient: sum over nodes
     __syncthreads();
-    double* red = reinterpret_cast<double*>(ring);
-    red[threadIdx.x] = act ? gG : 0.0;
+    double* red = reinterpret_cast<double*>(smem);
+    red[threadIdx.x] = (act && lane == 0) ? gG : 0.0;
     __syncthreads();
     for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
         if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
@@ -426,7 +673,7 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A) 
 
 // ---- launch interface used by the engine (hb_engine.cu) ----
 struct HbAdjointLaunch {
-    int B, N, T, R, K, CK, n_ck, cfk, gain_idx;
+    int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
     float dt, dt_half;
     const float* x0;
     const int* rowptr; const uint32_t* edges; const float* ew;
@@ -439,21 +686,31 @@ struct HbAdjointLaunch {
 
 cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st) {
     AdjArgs A;
-    A.B = L.B; A.N = L.N; A.T = L.T; A.R = L.R; A.K = L.K; A.CK = L.CK; A.n_ck = L.n_ck;
+    A.B = L.B; A.N = L.N; A.T = L.T; A.R = L.R; A.K = L.K; A.CK = L.CK; A.n_ck = L.n_ck; A.store_all = L.store_all;
     A.cfk = L.cfk; A.gain_idx = L.gain_idx; A.dt = L.dt; A.dt_half = L.dt_half;
     A.x0 = L.x0; A.rowptr = L.rowptr; A.edges = L.edges; A.ew = L.ew;
     A.cptr = L.cptr; A.ctgt = L.ctgt; A.cdel = L.cdel; A.cw = L.cw;
     A.Y = L.Y; A.S = L.S; A.ck_state = L.ck_state; A.ck_ring = L.ck_ring; A.scratch = L.scratch; A.mu_ring = L.mu_ring;
     A.target = L.target; A.mean = L.mean; A.sdev = L.sdev; A.coef = L.coef; A.rk = L.rk; A.M = L.M; A.fc = L.fc;
     A.loss = L.loss; A.gG = L.gG; A.gA = L.gA; A.gB = L.gB; A.ga = L.ga;
-    const int threads = (L.N + 31) / 32 * 32;
+    // lanes per node: a power of two up to 4 within 1024 threads; the block a power of two for the
+    // final reduction
+    int lanes = 1;
+    while (lanes < 4 && L.N * lanes * 2 <= 1024) lanes *= 2;
+    int threads = 32;
+    while (threads < L.N * lanes) threads *= 2;
+    const int nnz = L.nnz;
     const size_t ring_bytes = (size_t)L.R * L.N * sizeof(float);
+    const size_t tab1 = (size_t)(L.N + 1) * 4 + (size_t)nnz * 8;
+    const size_t gbuf_bytes = (size_t)L.K * L.N * sizeof(float) + 16;
     if (phase == 0) {
-        if (cudaFuncSetAttribute(adj_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_bytes) != cudaSuccess)
+        const size_t sm = ring_bytes + tab1 + gbuf_bytes;
+        if (cudaFuncSetAttribute(adj_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
             return cudaGetLastError();
-        adj_forward_kernel<<<L.B, threads, ring_bytes, st>>>(d_net, A);
+        adj_forward_kernel<<<L.B, threads, sm, st>>>(d_net, A, lanes);
     } else if (phase == 1) {
-        const size_t sm = std::max((size_t)32 * L.N * sizeof(float), (size_t)512 * sizeof(double));
+        const size_t W = (size_t)(L.N + 3) / 4 * 4;
+        const size_t sm = std::max(33 * W * sizeof(float) + 2 * W * sizeof(double) + 16, (size_t)512 * sizeof(double));
         adj_stats_kernel<<<L.B, 512, sm, st>>>(A);
         const size_t sm2 = ((size_t)L.N * L.N + 64 * (size_t)L.N) * sizeof(float);
         if (cudaFuncSetAttribute(adj_source_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2) != cudaSuccess)
@@ -463,10 +720,13 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         dim3 grid(L.B, (L.T + 63) / 64);
         adj_source_kernel<<<grid, kpad * tw, sm2, st>>>(A);
     } else {
-        const size_t sm = std::max(ring_bytes, (size_t)threads * sizeof(double));
+        const int rl = lanes;
+        int rthreads = 32;
+        while (rthreads < L.N * rl) rthreads *= 2;
+        const size_t sm = std::max(ring_bytes + 2 * tab1 + gbuf_bytes, (size_t)rthreads * sizeof(double));
         if (cudaFuncSetAttribute(adj_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
             return cudaGetLastError();
-        adj_backward_kernel<<<L.B, threads, sm, st>>>(d_net, A);
+        adj_backward_kernel<<<L.B, rthreads, sm, st>>>(d_net, A, rl);
     }
     return cudaGetLastError();
 }

@@ -39,7 +39,7 @@ int hb_stream_group_budget_1(int model, int pre);
 int hb_stream_group_budget_2(int model, int pre);
 int hb_stream_group_budget_4(int model, int pre);
 struct HbAdjointLaunch {
-    int B, N, T, R, K, CK, n_ck, cfk, gain_idx;
+    int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
     float dt, dt_half;
     const float* x0;
     const int* rowptr; const uint32_t* edges; const float* ew;
@@ -1677,7 +1677,7 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     if (hp.ncv != 1 || !hp.direct) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs the coupling from and into the first coupling variable");
     if (eff_integrator(e, HBM_JR) != HBI_HEUN_DET) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint differentiates deterministic Heun");
     const int N = e->subs[0].nm, B = e->B;
-    if (N > 200) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports up to 200 nodes");
+    if (N > 120) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports up to 120 nodes");
     int dmin = 1 << 30;
     for (uint32_t m : hp.edges) dmin = std::min(dmin, (int)(m >> 16));
     if (hp.edges.empty()) dmin = 8;
@@ -1687,9 +1687,20 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     int dev = 0, optin = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if ((size_t)R * N * 4 + 1024 > (size_t)optin) return fail(HB_ERR_UNSUPPORTED, "the delay ring of one point does not fit shared memory");
+    if ((size_t)R * N * 4 + 2 * ((size_t)(N + 1) * 4 + hp.edges.size() * 8) + (size_t)K * N * 4 + 1024 > (size_t)optin)
+        return fail(HB_ERR_UNSUPPORTED, "the delay ring and edge tables of one point do not fit shared memory");
     int CK = std::max(K, (checkpoint_every + K - 1) / K * K);
     const int T = (int)n_steps;
+    // checkpoint_every <= 0: keep x(s), g(s) of every step when that takes at most a quarter of the
+    // free device memory (no re-computation in the reverse sweep); else checkpoint every 500 steps
+    int store_all = 0;
+    if (checkpoint_every <= 0) {
+        size_t free_b = 0, total_b = 0;
+        CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+        const double need = (double)T * B * N * 8 * 4 + 2.0 * T * B * N * 4;
+        if (need <= 0.25 * (double)free_b) { store_all = 1; CK = ((T + K - 1) / K) * K; }
+        else CK = (500 + K - 1) / K * K;
+    }
     const int n_ck = (T + CK - 1) / CK;
     // tables of the gain sweep (Sigmoidal a = parameter 3, Linear a = parameter 0)
     const int gain_param = hp.cf.kind == HBC_SIGMOIDAL ? 3 : 0;
@@ -1724,8 +1735,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     }
     const size_t TBN = (size_t)T * B * N;
     CUDA_TRY(W->Y.ensure(TBN)); CUDA_TRY(W->S.ensure(TBN));
-    CUDA_TRY(W->ck_state.ensure((size_t)n_ck * B * N * 6));
-    CUDA_TRY(W->ck_ring.ensure((size_t)n_ck * B * R * N));
+    CUDA_TRY(W->ck_state.ensure(store_all ? 1 : (size_t)n_ck * B * N * 6));
+    CUDA_TRY(W->ck_ring.ensure(store_all ? 1 : (size_t)n_ck * B * R * N));
     CUDA_TRY(W->scratch.ensure((size_t)B * CK * N * 8));
     CUDA_TRY(W->mu_ring.ensure((size_t)B * R * N));
     CUDA_TRY(W->target.ensure((size_t)N * N));
@@ -1735,7 +1746,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     CUDA_TRY(W->loss.ensure(B)); CUDA_TRY(W->gG.ensure(B));
     CUDA_TRY(W->gA.ensure((size_t)B * N)); CUDA_TRY(W->gB.ensure((size_t)B * N)); CUDA_TRY(W->ga.ensure((size_t)B * N));
     HbAdjointLaunch L;
-    L.B = B; L.N = N; L.T = T; L.R = R; L.K = K; L.CK = CK; L.n_ck = n_ck;
+    L.B = B; L.N = N; L.T = T; L.R = R; L.K = K; L.CK = CK; L.n_ck = n_ck; L.nnz = (int)hp.edges.size();
+    L.store_all = store_all;
     L.cfk = hp.cf.kind; L.gain_idx = gain_param;
     L.dt = e->net.dt; L.dt_half = e->net.dt_half;
     L.x0 = e->x0.p; L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;

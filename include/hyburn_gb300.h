@@ -289,8 +289,11 @@ void      hb_group_destroy(hb_group* group);
  * symmetric target_fc [nnodes][nnodes]. Outputs (any pointer may be NULL): loss [n_sweep],
  * d_gain [n_sweep], d_A / d_B / d_a [n_sweep][nnodes] (the JansenRit A, B, a taken per node),
  * fc [n_sweep][nnodes][nnodes], y [n_steps][n_sweep][nnodes]. The gradients are those of the
- * discrete FP32 step (discrete adjoint), accumulated in FP64, with the forward run re-computed
- * from checkpoints taken every checkpoint_every steps. The engine's state is left reset. */
+ * discrete FP32 step (discrete adjoint), summed in FP32 within a checkpoint segment and in FP64
+ * across segments. checkpoint_every > 0: the reverse sweep re-computes the forward run from
+ * checkpoints taken every checkpoint_every steps; <= 0: the forward keeps every step (32 B per
+ * node-step) when that takes at most a quarter of the free device memory, else checkpoints every
+ * 500 steps. The engine's state is left reset. */
 typedef struct hb_adjoint_out {
     double* loss;
     double* d_gain;

@@ -92,10 +92,16 @@ def test_adjoint_gradients_match_central_differences():
         assert errs["a"] <= 5e-4, (b, errs)
 
 
-def test_adjoint_checkpoint_interval_does_not_change_the_result():
+def test_adjoint_checkpoint_interval_changes_only_summation_rounding():
     cfg, sub, x0, net, target = ref_setup()
     eng = BatchHybridEngine.from_config(cfg, len(GAINS), semantics=HB_SEM_DELAY_RING)
     r1 = eng.adjoint_fc(GAINS, T, target, checkpoint_every=64)
     r2 = eng.adjoint_fc(GAINS, T, target, checkpoint_every=T)
+    r3 = eng.adjoint_fc(GAINS, T, target, checkpoint_every=0)  # every step kept, no re-computation
     for f in ("loss", "d_gain", "d_A", "d_B", "d_a"):
-        assert np.array_equal(getattr(r1, f), getattr(r2, f)), f
+        assert np.array_equal(getattr(r2, f), getattr(r3, f)), f
+    # the re-computed trajectory is bitwise the same; the gradient sums regroup per segment (FP32
+    # within a segment, FP64 across segments), so they agree to summation rounding
+    assert np.array_equal(r1.loss, r2.loss)
+    for f in ("d_gain", "d_A", "d_B", "d_a"):
+        np.testing.assert_allclose(getattr(r1, f), getattr(r2, f), rtol=1e-5, atol=1e-9 * np.abs(getattr(r2, f)).max())
