@@ -180,6 +180,113 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def _time_prepared(eng, steps, warmup):
+    """CUDA-event time per execute_prepared() of an engine, L2 flushed before each timed run."""
+    import torch
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(warmup):
+        eng.execute_prepared()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        eng.execute_prepared()
+        ms.append(eng.last_kernel_time()[0])
+    return statistics.median(ms), eng.last_kernel_time()[2]
+
+
+def run_other_workload(args):
+    """The other measured configurations (synthetic inputs with the stated shapes), one JSON line."""
+    import torch
+    from hyburn_gb300 import BatchHybridEngine, GroupedSweep, SweepParam, inputs
+    from hyburn_gb300._abi import HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING
+    torch.cuda.set_device(0)
+    peak, peak_kind = peaks()
+    line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "l2": "flushed (512 MiB write) before each timed run"}
+    with ClockSampler(0) as clk:
+        if args.workload == "single":
+            # one simulation: G2DO, 74 nodes, Heun dt 0.1, 10 000 steps, w = 0.01 mean-field Linear coupling
+            T = 10_000
+            cfg, meta = inputs.plain_single_sim(T)
+            eng = BatchHybridEngine.from_config(cfg, 1)
+            eng.prepare(SweepParam(0, 1), [cfg.network.subnetworks[0].params[1]], T)
+            ms, kind = _time_prepared(eng, args.steps, args.warmup)
+            line.update(metric="node-steps/s", value=74 * T / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+                        config={"workload": "g2do-74n-1pt-meanfield-heun-10000steps", "kernel_kind": kind},
+                        roofline={"bound": "latency", "note": "one point on one SM; no roofline fraction",
+                                  "us_per_integration_step": ms * 1e3 / T})
+        elif args.workload == "kuramoto":
+            # Kuramoto, 1000 nodes, 5 % CSR, delays U[10,250] mm at 5 mm/ms, 256 points over G, BOLD on
+            T = 10_000
+            cfg, meta = inputs.kuramoto_scale(n=1000, n_points=256, n_steps=T, bold=True)
+            eng = BatchHybridEngine.from_config(cfg, 256, semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT)
+            eng.prepare(SweepParam(-1, 0), meta["values"], T)
+            ms, kind = _time_prepared(eng, args.steps, args.warmup)
+            nnz = sum(len(p.weights["data"]) for p in cfg.network.projections)
+            bpns = 4.0 * nnz / 1000 + 4.0
+            ns = 256 * 1000 * T
+            line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+                        config={"workload": f"kuramoto-1000n-256pt-csr5pct-delays-{meta['min_delay']}-{meta['max_delay']}"
+                                            f"-heun-bold-{T}steps (of 100000)", "kernel_kind": kind},
+                        roofline={"bound": "hbm", "achieved": bpns * ns / (ms / 1e3) / 1e9, "peak": peak,
+                                  "unit": "GB/s", "frac": bpns * ns / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                                  "algorithmic_bytes_per_node_step": bpns, "traffic": None})
+        elif args.workload == "uneven":
+            # MPR, {68, 84, 164, 400} nodes x 128 points, (G, eta) grid, RK4 dt 0.05, BOLD TR 2 s, one launch
+            T = 20_000
+            members, ns, bytes_ = [], 0, 0.0
+            for n in (68, 84, 164, 400):
+                cfg, meta = inputs.mpr_grid(n, 128, T, seed=3, bold=True)
+                eng = BatchHybridEngine.from_config(cfg, 128, semantics=HB_SEM_DELAY_RING)
+                members.append((eng, SweepParam(-1, 0), list(np.linspace(0.0, 1.0, 128)), T, None))
+                nnz = len(cfg.network.projections[0].weights["data"])
+                ns += 128 * n * T
+                bytes_ += 128 * T * (8.0 * nnz + 8.0 * n)
+            g = GroupedSweep(members)
+            for _ in range(args.warmup):
+                g.execute()
+            times = []
+            for _ in range(args.steps):
+                g.execute()
+                times.append(g.last_kernel_time())
+            ms = statistics.median(times)
+            line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+                        config={"workload": f"mpr-68/84/164/400n-x128pt-csr20pct-per-edge-delays-rk4-dt0.05-bold-"
+                                            f"{T}steps (of 1200000), one grouped launch", "kernel_kind": 5},
+                        roofline={"bound": "hbm", "achieved": bytes_ / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                  "frac": bytes_ / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                                  "algorithmic_bytes_per_node_step": bytes_ / ns, "traffic": None})
+        else:
+            # adjoint: JR 74 nodes x 64 points, Sigmoidal delayed CSR coupling, Heun dt 0.1, 20 000 steps,
+            # FC loss of y1 - y2; gradients w.r.t. the coupling gain and per-node A, B, a
+            T, n, B = 20_000, 74, 64
+            cfg, meta = inputs.jr_fc_adjoint(T, B, n)
+            gains = meta["gains"]
+            eng = BatchHybridEngine.from_config(cfg, B, semantics=HB_SEM_DELAY_RING)
+            eng.prepare(SweepParam(-1, 3), gains, T)
+            fwd_ms, _ = _time_prepared(eng, args.steps, args.warmup)
+            eng.reset()
+            target = np.eye(n, dtype=np.float32)
+            for _ in range(max(1, args.warmup)):
+                eng.adjoint_fc(gains, T, target, checkpoint_every=0)
+            tot, parts = [], None
+            for _ in range(args.steps):
+                r = eng.adjoint_fc(gains, T, target, checkpoint_every=0)
+                tot.append(r.forward_ms + r.statistics_ms + r.reverse_ms)
+                parts = (r.forward_ms, r.statistics_ms, r.reverse_ms)
+            ms = statistics.median(tot)
+            line.update(metric="gradient evaluations/s", value=B / (ms / 1e3), unit="points/s", ms_per_step=ms,
+                        higher_is_better=True,
+                        config={"workload": "jr-74n-64pt-sigmoidal-csr-delays-heun-20000steps-fc-loss",
+                                "gradients": "coupling gain, per-node A, B, a", "trajectory": "kept in HBM"},
+                        adjoint={"forward_ms": parts[0], "statistics_ms": parts[1], "reverse_ms": parts[2],
+                                 "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
+    line["clocks"] = clk.summary()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,9 +301,15 @@ def main():
     ap.add_argument("--two-phase", action="store_true", help="batch each block's gathers before its updates")
     ap.add_argument("--no-pipe", action="store_true", help="do not use the warp-specialised pipeline")
     ap.add_argument("--pipe-lanes", type=int, default=0, help="pipeline producer threads per node (0: engine's choice)")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto"],
+                    help="sweep: the 128-point batched sweep (default); the others are the remaining "
+                         "measured configurations, one JSON line each")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.workload != "sweep":
+        run_other_workload(args)
         return
 
     import torch

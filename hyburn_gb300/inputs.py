@@ -159,3 +159,24 @@ def kuramoto_scale(n: int = 1000, n_points: int = 256, n_steps: int = 100_000, s
     values = np.linspace(0.0, 2.0, n_points).astype(np.float32).tolist()
     return cfg, {"n_sweep": n_points, "values": values, "n_steps": n_steps, "omega": omega,
                  "max_delay": int(max(delays)), "min_delay": int(min(delays))}
+
+
+def jr_fc_adjoint(n_steps: int = 20_000, n_points: int = 64, n: int = 74, seed: int = 4) -> Tuple[SimConfig, dict]:
+    """The FC-adjoint workload: JansenRit, n nodes on the batched-sweep connectome recipe (20 %
+    density, tract lengths U[10, 200] mm at 3 mm/ms, dt 0.1 ms), Sigmoidal coupling
+    (cmin 0, cmax 0.1, midpoint 0, gain, sigma 0.05) with per-edge delays, Heun, nsig 0, and
+    n_points coupling gains in [0.5, 1.5]. Initial state uniform per variable from `seed`."""
+    c = connectome(n, 0.2, seed)
+    delays = tract_lengths_to_delays(c.lengths, 3.0, 0.1)
+    rng = np.random.default_rng(seed)
+    ranges = [(-0.5, 0.5), (0.0, 20.0), (0.0, 20.0), (-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0)]
+    x0 = np.stack([rng.uniform(lo, hi, n) for lo, hi in ranges], 1).astype(np.float32).ravel().tolist()
+    cfg = SimConfig(
+        sim_length=n_steps * 0.1, dt=0.1, integrator="heun", nsig=0.0,
+        network=NetworkConfig(
+            subnetworks=[SubnetworkConfig("JansenRit", n, x0, list(DEFAULT_PARAMS["JansenRit"]))],
+            projections=[ProjectionConfig(0, 0, c.csr_weights(), conn_type="csr", delays=delays,
+                                          coupling_fn="Sigmoidal", coupling_params=[0.0, 0.1, 0.0, 1.0, 0.05])]))
+    gains = np.linspace(0.5, 1.5, n_points).astype(np.float32)
+    return cfg, {"gains": gains, "connectome": c, "min_delay": int(min(delays)), "max_delay": int(max(delays))}
+
