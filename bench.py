@@ -208,18 +208,18 @@ def run_other_workload(args):
     with ClockSampler(0) as clk:
         if args.workload == "single":
             # one simulation: G2DO, 74 nodes, Heun dt 0.1, 10 000 steps, w = 0.01 mean-field Linear coupling
-            T = 10_000
+            T = args.run_steps or 10_000
             cfg, meta = inputs.plain_single_sim(T)
             eng = BatchHybridEngine.from_config(cfg, 1)
             eng.prepare(SweepParam(0, 1), [cfg.network.subnetworks[0].params[1]], T)
             ms, kind = _time_prepared(eng, args.steps, args.warmup)
             line.update(metric="node-steps/s", value=74 * T / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
-                        config={"workload": "g2do-74n-1pt-meanfield-heun-10000steps", "kernel_kind": kind},
+                        config={"workload": f"g2do-74n-1pt-meanfield-heun-{T}steps", "kernel_kind": kind},
                         roofline={"bound": "latency", "note": "one point on one SM; no roofline fraction",
                                   "us_per_integration_step": ms * 1e3 / T})
         elif args.workload == "kuramoto":
             # Kuramoto, 1000 nodes, 5 % CSR, delays U[10,250] mm at 5 mm/ms, 256 points over G, BOLD on
-            T = 10_000
+            T = args.run_steps or 10_000
             cfg, meta = inputs.kuramoto_scale(n=1000, n_points=256, n_steps=T, bold=True)
             eng = BatchHybridEngine.from_config(cfg, 256, semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT)
             eng.prepare(SweepParam(-1, 0), meta["values"], T)
@@ -235,7 +235,7 @@ def run_other_workload(args):
                                   "algorithmic_bytes_per_node_step": bpns, "traffic": None})
         elif args.workload == "uneven":
             # MPR, {68, 84, 164, 400} nodes x 128 points, (G, eta) grid, RK4 dt 0.05, BOLD TR 2 s, one launch
-            T = 20_000
+            T = args.run_steps or 20_000
             members, ns, bytes_ = [], 0, 0.0
             for n in (68, 84, 164, 400):
                 cfg, meta = inputs.mpr_grid(n, 128, T, seed=3, bold=True)
@@ -261,7 +261,7 @@ def run_other_workload(args):
         else:
             # adjoint: JR 74 nodes x 64 points, Sigmoidal delayed CSR coupling, Heun dt 0.1, 20 000 steps,
             # FC loss of y1 - y2; gradients w.r.t. the coupling gain and per-node A, B, a
-            T, n, B = 20_000, 74, 64
+            T, n, B = args.run_steps or 20_000, 74, 64
             cfg, meta = inputs.jr_fc_adjoint(T, B, n)
             gains = meta["gains"]
             eng = BatchHybridEngine.from_config(cfg, B, semantics=HB_SEM_DELAY_RING)
@@ -279,7 +279,7 @@ def run_other_workload(args):
             ms = statistics.median(tot)
             line.update(metric="gradient evaluations/s", value=B / (ms / 1e3), unit="points/s", ms_per_step=ms,
                         higher_is_better=True,
-                        config={"workload": "jr-74n-64pt-sigmoidal-csr-delays-heun-20000steps-fc-loss",
+                        config={"workload": f"jr-74n-64pt-sigmoidal-csr-delays-heun-{T}steps-fc-loss",
                                 "gradients": "coupling gain, per-node A, B, a", "trajectory": "kept in HBM"},
                         adjoint={"forward_ms": parts[0], "statistics_ms": parts[1], "reverse_ms": parts[2],
                                  "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
@@ -294,7 +294,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--run-steps", type=int, default=N_STEPS,
+    ap.add_argument("--run-steps", type=int, default=None,
                     help="integration steps per run (smaller values only for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="threads per node (0: the engine's choice)")
@@ -311,6 +311,8 @@ def main():
     if args.workload != "sweep":
         run_other_workload(args)
         return
+    if args.run_steps is None:
+        args.run_steps = N_STEPS
 
     import torch
 
