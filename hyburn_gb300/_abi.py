@@ -56,6 +56,7 @@ def HB_RUN_STREAM_NPT(n: int) -> int:
 
 
 HB_RUN_STREAM_PREFETCH = 1 << 27
+HB_RUN_PIPE_WIDE = 1 << 28
 
 
 def HB_RUN_LANES(n: int) -> int:

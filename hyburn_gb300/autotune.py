@@ -67,6 +67,9 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
         if dmin >= 15:
             for pl in (1, 2, 4, 8):
                 out.append((f"pipeline producer lanes {pl}", _abi.HB_RUN_NO_STREAM | _abi.HB_RUN_PIPE_LANES(pl)))
+            for pl in (2, 4):
+                out.append((f"pipeline (1024-thread form) producer lanes {pl}",
+                            _abi.HB_RUN_NO_STREAM | _abi.HB_RUN_PIPE_WIDE | _abi.HB_RUN_PIPE_LANES(pl)))
             for npt in (1, 2, 4):
                 out.append((f"streamed history {npt} node(s) per thread", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_NPT(npt)))
     else:

@@ -23,6 +23,7 @@ UNITS = [
     ("hb_stream_2.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_4.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_pipe.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_pipe_1024.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_1024.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_fast_512.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_resident_generic.cu", ["--fmad=false", "-lineinfo"]),

@@ -24,8 +24,10 @@ cudaError_t hb_launch_resident(int model, int fast, const DevNet* d_net, const R
                                cudaStream_t st);
 cudaError_t hb_launch_bold_batch_mean(const DevBold& bold, int m, int n_windows, int B, float* means, cudaStream_t st);
 int hb_resident_smem_budget(int model, int fast, int threads);
-cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
-int hb_pipe_budget(int model, int pre);
+cudaError_t hb_launch_pipe_512(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_pipe_1024(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_pipe_budget_512(int model, int pre);
+int hb_pipe_budget_1024(int model, int pre);
 cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
@@ -500,7 +502,7 @@ struct RunPlan {
     const float* noise_dev = nullptr;
     bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false;
     int64_t noise_rows_per_step = 0, chunk = 0;
-    int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1;
+    int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1, pipe_maxt = 512;
     size_t smem = 0, stream_smem = 0;
     RunArgs a;
     std::vector<std::vector<double>> new_times;
@@ -557,32 +559,37 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         else if (k == HBC_KURAMOTO && e->projs[0].ncv == 1) fast = 1;                                     // PRE_KURA
     }
     e->last_kind = fast >= 0 ? 2 : 1;
-    // warp-specialised pipeline: one thread per node for the updates plus 8 producer warps
-    int pipe = -1;
+    // warp-specialised pipeline: one thread per node for the updates plus producer warps, in a
+    // 512-thread form or (for more producer lanes or nodes) a 1024-thread form with fewer registers
+    int pipe = -1, pipe_maxt = 512;
     if (fast >= 0 && e->dmin >= 15 && e->R >= std::max(e->H, 1) + 16 && !(run_flags & HB_RUN_NO_PIPE) &&
-        ((e->subs[0].nm + 31) / 32 * 32 + 256) <= 512 && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE))
+        ((e->subs[0].nm + 31) / 32 * 32 + 64) <= 1024 && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE))
         pipe = fast;
     int pipe_lanes = 1;
     if (pipe >= 0) {
-        // producer threads: PL lanes per node (a power of two), every node covered, and consumer
-        // plus producer threads within the kernel's 512-thread bound
+        // producer threads: PL lanes per node (a power of two), every node covered, consumers plus
+        // producers within the form's thread bound
         const int nm0 = e->subs[0].nm;
         const int n_cons = (nm0 + 31) / 32 * 32;
-        const int max_prod = 512 - n_cons;
-        int forced_pl = (int)((run_flags >> 20) & 0xf);
+        auto prod_of = [&](int pl) { return std::max(64, (nm0 * pl + 31) / 32 * 32); };
+        const int forced_pl = (int)((run_flags >> 20) & 0xf);
+        if (forced_pl && ((forced_pl & (forced_pl - 1)) != 0 || forced_pl > 8))
+            return fail(HB_ERR_INVALID_STATE, "pipeline producer lanes must be 1, 2, 4 or 8");
+        const bool wide = (run_flags & HB_RUN_PIPE_WIDE) || n_cons + 256 > 512 ||
+                          (forced_pl && n_cons + prod_of(forced_pl) > 512);
+        pipe_maxt = wide ? 1024 : 512;
+        const int max_prod = pipe_maxt - n_cons;
         pipe_lanes = forced_pl ? forced_pl : 1;
         if (!forced_pl)
             while (pipe_lanes < 8 && nm0 * pipe_lanes * 2 <= max_prod) pipe_lanes *= 2;
-        if ((pipe_lanes & (pipe_lanes - 1)) != 0 || pipe_lanes > 8)
-            return fail(HB_ERR_INVALID_STATE, "pipeline producer lanes must be 1, 2, 4 or 8");
-        const int prod = std::max(64, (nm0 * pipe_lanes + 31) / 32 * 32);
-        if (prod > max_prod)
+        if (prod_of(pipe_lanes) > max_prod)
             return fail(HB_ERR_UNSUPPORTED, "pipeline: %d nodes x %d producer lanes exceed the thread budget", nm0, pipe_lanes);
-        e->threads = n_cons + prod;
+        e->threads = n_cons + prod_of(pipe_lanes);
         e->last_kind = 3;
     }
     // ---- placement of the ring and the CSR rows (shared memory when they fit) ----
-    const int budget = pipe >= 0 ? hb_pipe_budget(e->kernel_model, pipe) : hb_resident_smem_budget(e->kernel_model, fast, e->threads);
+    const int budget = pipe >= 0 ? (pipe_maxt == 1024 ? hb_pipe_budget_1024(e->kernel_model, pipe) : hb_pipe_budget_512(e->kernel_model, pipe))
+                                 : hb_resident_smem_budget(e->kernel_model, fast, e->threads);
     if (budget < 0) return fail(HB_ERR_CUDA, "cannot query the shared-memory limit of the resident kernel");
     const size_t smem_cap = (size_t)budget - 64;
     size_t part_bytes = (size_t)2 * std::max(e->n_mean, 1) * 32 * 4 * 4;
@@ -752,6 +759,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     P.stream_npt = stream_npt;
     P.fast = fast;
     P.pipe = pipe;
+    P.pipe_maxt = pipe_maxt;
     P.smem = smem;
     P.stream_smem = stream_smem;
     P.a = a;
@@ -792,7 +800,8 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 2) CUDA_TRY(hb_launch_stream_2(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 4) CUDA_TRY(hb_launch_stream_4(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
-        else if (pipe >= 0) CUDA_TRY(hb_launch_pipe(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
+        else if (pipe >= 0 && P.pipe_maxt == 1024) CUDA_TRY(hb_launch_pipe_1024(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
+        else if (pipe >= 0) CUDA_TRY(hb_launch_pipe_512(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
         else CUDA_TRY(hb_launch_resident(e->kernel_model, fast, e->d_net, a, B, e->threads, smem, st));
         CUDA_TRY(cudaEventRecord(e->ev1, st));
         e->last_launches++;

@@ -1,4 +1,4 @@
-// Warp-specialised pipeline kernel instantiations (see hb_resident.cuh).
+// Warp-specialised pipeline kernel instantiations, 512-thread bound (see hb_resident.cuh).
 #include "hb_resident.cuh"
 
-HB_PIPE_UNIT
+HB_PIPE_UNIT(512)

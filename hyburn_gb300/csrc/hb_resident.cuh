@@ -924,8 +924,67 @@ cudaError_t launch_fast(const DevNet* d_net, const RunArgs& a, int B, int thread
 __device__ __forceinline__ void named_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
 __device__ __forceinline__ void named_arrive(int id, int count) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory"); }
 
-template <int MODEL, int PRE>
-__global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
+// Consumer steps of the pipeline for the common case — Heun (deterministic or stochastic), Linear
+// coupling delivered to the first coupling variables, no trajectory, no BOLD — as one straight-line
+// loop: the per-step branches of the general consumer (integrator, coupling function, channel map,
+// monitors) are resolved by the template arguments, with the same operations in the same order.
+template <int MODEL, int NVAR, int NCV, bool STOCH, bool SWEEP_FORM>
+__device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, const float* prm, const float* cp,
+                                                         const float* nscale, float dt, float dt_half,
+                                                         const float* gxbuf, const float* nzbuf, float* ring,
+                                                         int n, bool active, int nm, int cols, int R, int slot,
+                                                         int n_steps, int n_blocks, int nthreads) {
+    constexpr int PK = HB_PIPE_K;
+    const float ca = cp[0], cb = cp[1];
+    float ns[NVAR];
+#pragma unroll
+    for (int v = 0; v < NVAR; v++) ns[v] = nscale[v];
+    for (int blk = 0; blk < n_blocks; blk++) {
+        const int buf = blk & 1;
+        named_sync(HB_BAR_FULL0 + buf, nthreads);
+        const int nb = (n_steps - blk * PK) < PK ? (n_steps - blk * PK) : PK;
+        const float* gb = gxbuf + (size_t)buf * PK * nm * NCV + (size_t)n * NCV;
+        const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR + (size_t)n * NVAR;
+#pragma unroll 1
+        for (int j = 0; j < nb; j++) {
+            slot = (slot + 1 == R) ? 0 : slot + 1;
+            if (!active) continue;  // threads past the last node only take part in the barriers
+            float cc[2] = {0.0f, 0.0f};
+            cc[0] = gb[(size_t)j * nm * NCV] * ca + cb;
+            if (NCV > 1) cc[1] = gb[(size_t)j * nm * NCV + 1] * ca + cb;
+            float nz[NVAR];
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) nz[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
+            float k1[NVAR], k2[NVAR], tmp[NVAR];
+            dfun(MODEL, prm, SWEEP_FORM ? 1 : 0, x, cc, k1);
+            if (STOCH) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = (x[v] + k1[v] * dt) + nz[v];
+            } else {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) tmp[v] = x[v] + k1[v] * dt;
+            }
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, SWEEP_FORM ? 1 : 0, tmp, cc, k2);
+            if (STOCH) {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v];
+            } else {
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+            }
+            clamp(MODEL, x);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
+            ring[slot * cols + n * NCV] = x[0];
+            if (NCV > 1) ring[slot * cols + n * NCV + 1] = x[1];
+        }
+        named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+    }
+}
+
+template <int MODEL, int PRE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ DevNet net;
     {
@@ -1159,7 +1218,21 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
             }
         }
         int64_t s = a.s0;
-        for (int blk = 0; blk < n_blocks; blk++) {
+        const bool straight = PRE == PRE_ID && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) && cfk == HBC_LINEAR &&
+                              direct && pc == NCV && !has_rowsums && a.traj == nullptr && a.bold.n == 0;
+        if (straight) {
+            float nscale[8];
+#pragma unroll
+            for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
+            if (integ == HBI_HEUN_STOCH) {
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+            } else {
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+            }
+        }
+        for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
             const int buf = blk & 1;
             named_sync(HB_BAR_FULL0 + buf, nthreads);
             const int it0 = blk * PK;
@@ -1318,7 +1391,7 @@ __global__ void __launch_bounds__(512, 1) resident_pipe_kernel(const DevNet* __r
     }
 }
 
-template <int MODEL, int PRE>
+template <int MODEL, int PRE, int MAXT>
 int pipe_max_dynamic_smem() {
     static int cached = -1;
     if (cached >= 0) return cached;
@@ -1326,20 +1399,20 @@ int pipe_max_dynamic_smem() {
     cudaFuncAttributes fa;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
-    if (cudaFuncGetAttributes(&fa, resident_pipe_kernel<MODEL, PRE>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, resident_pipe_kernel<MODEL, PRE, MAXT>) != cudaSuccess) return -1;
     int maxdyn = optin - (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(resident_pipe_kernel<MODEL, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+    if (cudaFuncSetAttribute(resident_pipe_kernel<MODEL, PRE, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
         return -1;
     cached = maxdyn;
     return cached;
 }
 
-template <int MODEL, int PRE>
+template <int MODEL, int PRE, int MAXT>
 cudaError_t launch_pipe(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
-    int maxdyn = pipe_max_dynamic_smem<MODEL, PRE>();
+    int maxdyn = pipe_max_dynamic_smem<MODEL, PRE, MAXT>();
     if (maxdyn < 0) return cudaErrorInvalidConfiguration;
-    if ((long long)smem > maxdyn) return cudaErrorInvalidValue;
-    resident_pipe_kernel<MODEL, PRE><<<B, threads, smem, st>>>(d_net, a);
+    if ((long long)smem > maxdyn || threads > MAXT) return cudaErrorInvalidValue;
+    resident_pipe_kernel<MODEL, PRE, MAXT><<<B, threads, smem, st>>>(d_net, a);
     return cudaGetLastError();
 }
 
@@ -1437,32 +1510,36 @@ int hb_fast_budget_1024(int model, int pre);
         }                                                                                                            \
     }
 
-cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
-int hb_pipe_budget(int model, int pre);
+cudaError_t hb_launch_pipe_512(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+cudaError_t hb_launch_pipe_1024(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
+int hb_pipe_budget_512(int model, int pre);
+int hb_pipe_budget_1024(int model, int pre);
 
-#define HB_PIPE_UNIT                                                                                                \
-    cudaError_t hb_launch_pipe(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads,       \
-                               size_t smem, cudaStream_t st) {                                                       \
-        using F = cudaError_t (*)(const DevNet*, const RunArgs&, int, int, size_t, cudaStream_t);                   \
-        static const F table[12] = {                                                                                 \
-            hb::launch_pipe<0, hb::PRE_ID>, hb::launch_pipe<0, hb::PRE_KURA>, hb::launch_pipe<1, hb::PRE_ID>,        \
-            hb::launch_pipe<1, hb::PRE_KURA>, hb::launch_pipe<2, hb::PRE_ID>, hb::launch_pipe<2, hb::PRE_KURA>,      \
-            hb::launch_pipe<3, hb::PRE_ID>, hb::launch_pipe<3, hb::PRE_KURA>, hb::launch_pipe<4, hb::PRE_ID>,        \
-            hb::launch_pipe<4, hb::PRE_KURA>, hb::launch_pipe<5, hb::PRE_ID>, hb::launch_pipe<5, hb::PRE_KURA>};     \
+#define HB_PIPE_UNIT(MAXT_)                                                                                         \
+    cudaError_t hb_launch_pipe_##MAXT_(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, \
+                                       size_t smem, cudaStream_t st) {                                               \
+        using F = cudaError_t (*)(const DevNet*, const RunArgs&, int, int, size_t, cudaStream_t);                    \
+        static const F tab[12] = {                                                                                   \
+            hb::launch_pipe<0, hb::PRE_ID, MAXT_>, hb::launch_pipe<0, hb::PRE_KURA, MAXT_>,                          \
+            hb::launch_pipe<1, hb::PRE_ID, MAXT_>, hb::launch_pipe<1, hb::PRE_KURA, MAXT_>,                          \
+            hb::launch_pipe<2, hb::PRE_ID, MAXT_>, hb::launch_pipe<2, hb::PRE_KURA, MAXT_>,                          \
+            hb::launch_pipe<3, hb::PRE_ID, MAXT_>, hb::launch_pipe<3, hb::PRE_KURA, MAXT_>,                          \
+            hb::launch_pipe<4, hb::PRE_ID, MAXT_>, hb::launch_pipe<4, hb::PRE_KURA, MAXT_>,                          \
+            hb::launch_pipe<5, hb::PRE_ID, MAXT_>, hb::launch_pipe<5, hb::PRE_KURA, MAXT_>};                         \
         int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
         if (model < 0 || i >= 12) return cudaErrorInvalidValue;                                                      \
-        return table[i](d_net, a, B, threads, smem, st);                                                             \
+        return tab[i](d_net, a, B, threads, smem, st);                                                               \
     }                                                                                                                \
-    int hb_pipe_budget(int model, int pre) {                                                                         \
+    int hb_pipe_budget_##MAXT_(int model, int pre) {                                                                 \
         using G = int (*)();                                                                                         \
-        static const G table[12] = {                                                                                 \
-            hb::pipe_max_dynamic_smem<0, hb::PRE_ID>, hb::pipe_max_dynamic_smem<0, hb::PRE_KURA>,                    \
-            hb::pipe_max_dynamic_smem<1, hb::PRE_ID>, hb::pipe_max_dynamic_smem<1, hb::PRE_KURA>,                    \
-            hb::pipe_max_dynamic_smem<2, hb::PRE_ID>, hb::pipe_max_dynamic_smem<2, hb::PRE_KURA>,                    \
-            hb::pipe_max_dynamic_smem<3, hb::PRE_ID>, hb::pipe_max_dynamic_smem<3, hb::PRE_KURA>,                    \
-            hb::pipe_max_dynamic_smem<4, hb::PRE_ID>, hb::pipe_max_dynamic_smem<4, hb::PRE_KURA>,                    \
-            hb::pipe_max_dynamic_smem<5, hb::PRE_ID>, hb::pipe_max_dynamic_smem<5, hb::PRE_KURA>};                   \
+        static const G tab[12] = {                                                                                   \
+            hb::pipe_max_dynamic_smem<0, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<0, hb::PRE_KURA, MAXT_>,      \
+            hb::pipe_max_dynamic_smem<1, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<1, hb::PRE_KURA, MAXT_>,      \
+            hb::pipe_max_dynamic_smem<2, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<2, hb::PRE_KURA, MAXT_>,      \
+            hb::pipe_max_dynamic_smem<3, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<3, hb::PRE_KURA, MAXT_>,      \
+            hb::pipe_max_dynamic_smem<4, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<4, hb::PRE_KURA, MAXT_>,      \
+            hb::pipe_max_dynamic_smem<5, hb::PRE_ID, MAXT_>, hb::pipe_max_dynamic_smem<5, hb::PRE_KURA, MAXT_>};     \
         int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
         if (model < 0 || i >= 12) return -1;                                                                         \
-        return table[i]();                                                                                           \
+        return tab[i]();                                                                                             \
     }

@@ -85,6 +85,8 @@ typedef int32_t hb_status;
 #define HB_RUN_STREAM_NPT(n)  ((uint32_t)((n) & 0x7) << 24)
 /* streamed-history kernel: prefetch the history runs of upcoming edges into L2 */
 #define HB_RUN_STREAM_PREFETCH (1u << 27)
+/* warp-specialised pipeline: use its 1024-thread form (room for eight producer threads per node) */
+#define HB_RUN_PIPE_WIDE      (1u << 28)
 /* resident kernel: threads per node sharing its edge list (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_LANES(n) ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : 0) << 12)
 
