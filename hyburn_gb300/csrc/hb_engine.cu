@@ -276,6 +276,7 @@ struct hb_engine {
     // a run leaves behind (0: time-major ring, 1: streamed) must match the next run's kernel
     DBuf<float> sring;
     int hist_layout = 0, hist_rp = 0;
+    int hist_R = 0;           // ring length (slots) of the time-major history the last run left
     std::vector<DBuf<float>> d_params;
     DBuf<int> flags_buf;
     std::vector<BoldHost> bold;
@@ -562,7 +563,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     // warp-specialised pipeline: one thread per node for the updates plus producer warps, in a
     // 512-thread form or (for more producer lanes or nodes) a 1024-thread form with fewer registers
     int pipe = -1, pipe_maxt = 512;
-    if (fast >= 0 && e->dmin >= 15 && e->R >= std::max(e->H, 1) + 16 && !(run_flags & HB_RUN_NO_PIPE) &&
+    if (fast >= 0 && e->dmin >= 15 && !(run_flags & HB_RUN_NO_PIPE) &&
         ((e->subs[0].nm + 31) / 32 * 32 + 64) <= 1024 && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE))
         pipe = fast;
     int pipe_lanes = 1;
@@ -598,7 +599,12 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         const int pch = (pipe == 1) ? 2 : e->subs[0].ncvar;
         part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + e->subs[0].nvar) * 4 + (size_t)(e->subs[0].nm + 1) * 4 + 48;
     }
-    const size_t ring_bytes = (size_t)e->R * e->cols * 4;
+    // ring length of this run: the pipeline's producers run at most one block ahead of the consumers'
+    // writes, so slot reuse needs only more slots than the longest delay; the other kernels keep the
+    // engine's ring (longest delay + their barrier interval)
+    const int R_run = pipe >= 0 ? std::max(e->H, 1) + 1 : e->R;
+    e->net.R = R_run;
+    const size_t ring_bytes = (size_t)R_run * e->cols * 4;
     size_t edges = 0;
     for (auto& hp : e->projs) if (hp.kind == W_SPARSE) edges += hp.edges.size();
     const size_t edge_bytes = ((edges * 8) + 15) & ~(size_t)15;
@@ -652,10 +658,12 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     }
     {
         const int layout = stream_npt ? 1 : 0;
-        if (e->step > 0 && (layout != e->hist_layout || (layout == 1 && stream_rp != e->hist_rp)))
+        if (e->step > 0 && (layout != e->hist_layout || (layout == 1 && stream_rp != e->hist_rp) ||
+                            (layout == 0 && R_run != e->hist_R)))
             return fail(HB_ERR_UNSUPPORTED, "this run would change the history layout of a started simulation; reset the engine first");
         e->hist_layout = layout;
         e->hist_rp = stream_rp;
+        e->hist_R = R_run;
     }
     {
         size_t off = 0;
