@@ -28,6 +28,7 @@ UNITS = [
     ("hb_fast_512.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_resident_generic.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_kernels.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_single.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_adjoint.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_engine.cu", []),
     ("hb_noalloc.cu", ["--fmad=false"]),

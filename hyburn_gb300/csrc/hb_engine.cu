@@ -34,6 +34,7 @@ cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const Ru
 int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
+cudaError_t hb_launch_single(int model, int m, const DevNet* d_net, const RunArgs& a, int B, cudaStream_t st);
 cudaError_t hb_launch_stream_group_1(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_group_2(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
@@ -503,7 +504,7 @@ struct RunPlan {
     const float* noise_dev = nullptr;
     bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false;
     int64_t noise_rows_per_step = 0, chunk = 0;
-    int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1, pipe_maxt = 512;
+    int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1, pipe_maxt = 512, single_m = 0;
     size_t smem = 0, stream_smem = 0;
     RunArgs a;
     std::vector<std::vector<double>> new_times;
@@ -560,6 +561,19 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         else if (k == HBC_KURAMOTO && e->projs[0].ncv == 1) fast = 1;                                     // PRE_KURA
     }
     e->last_kind = fast >= 0 ? 2 : 1;
+    // one warp per point: one subnetwork, one Scalar projection onto itself without delay, no monitors
+    int single_m = 0;
+    {
+        const bool record_run = (run_flags & HB_RUN_TRAJECTORY) != 0;
+        const int n_bold_run = e->bold_removed ? 0 : (int)e->bold.size();
+        if (e->subs.size() == 1 && e->projs.size() == 1 && e->kernel_model >= 0 && !(run_flags & HB_RUN_GENERIC) &&
+            !record_run && n_bold_run == 0 && e->subs[0].nm <= 128) {
+            const HostProj& hp = e->projs[0];
+            if ((hp.kind == W_MEAN || hp.kind == W_DIAG) && hp.src == 0 && hp.tgt == 0 && hp.delay == 0)
+                single_m = (e->subs[0].nm + 31) / 32;
+        }
+        if (single_m) e->last_kind = 7;
+    }
     // warp-specialised pipeline: one thread per node for the updates plus producer warps, in a
     // 512-thread form or (for more producer lanes or nodes) a 1024-thread form with fewer registers
     int pipe = -1, pipe_maxt = 512;
@@ -768,6 +782,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     P.fast = fast;
     P.pipe = pipe;
     P.pipe_maxt = pipe_maxt;
+    P.single_m = single_m;
     P.smem = smem;
     P.stream_smem = stream_smem;
     P.a = a;
@@ -805,7 +820,8 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         }
         a.traj = record ? e->traj.p : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
+        if (P.single_m) CUDA_TRY(hb_launch_single(e->kernel_model, P.single_m, e->d_net, a, B, st));
+        else if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 2) CUDA_TRY(hb_launch_stream_2(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 4) CUDA_TRY(hb_launch_stream_4(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (pipe >= 0 && P.pipe_maxt == 1024) CUDA_TRY(hb_launch_pipe_1024(e->kernel_model, pipe, e->d_net, a, B, e->threads, smem, st));
