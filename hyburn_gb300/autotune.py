@@ -116,6 +116,9 @@ def tune(config: SimConfig, n_sweep: int, param: SweepParam, values: Sequence[fl
     """Measure every candidate on a probe of `probe_steps` steps; returns (best run flags, times in ms).
     Candidates the network cannot run (HB_ERR_UNSUPPORTED and the like) are skipped."""
     measure = measure or _measure
+    # the pipelines take a slower start-up path for the first longest-delay steps: probe well past it
+    longest = max((max(p.delays) for p in config.network.projections if p.delays), default=0)
+    probe_steps = max(probe_steps, 3 * longest)
     noise = None
     if config.integrator.endswith("stochastic"):
         noise = np.random.default_rng(0).standard_normal(noise_shape(config, probe_steps, n_sweep, semantics),

@@ -1184,7 +1184,12 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                     float4* d4 = reinterpret_cast<float4*>(nbuf);
                     for (int i = p; i < n4; i += n_prod) d4[i] = __ldcs(s4 + i);
                     for (int i = (n4 << 2) + p; i < total; i += n_prod) nbuf[i] = __ldcs(src + i);
-                    if (p == 0 && it0 + 4 * PK < a.n_steps) prefetch_l2(src + (size_t)4 * PK * nstride);
+                    // the noise rows of the block four blocks ahead into L2, one 128-byte line per thread
+                    if (it0 + 4 * PK < a.n_steps) {
+                        const int ahead = (a.n_steps - it0 - 4 * PK) < PK ? (a.n_steps - it0 - 4 * PK) : PK;
+                        const int lines = (ahead * row_len + 31) >> 5;
+                        for (int l = p; l < lines; l += n_prod) prefetch_l2(src + (size_t)4 * PK * nstride + (size_t)l * 32);
+                    }
                 } else {
                     for (int jj = 0; jj < nb; jj++)
                         for (int i = p; i < row_len; i += n_prod) nbuf[jj * row_len + i] = __ldcs(src + (size_t)jj * nstride + i);

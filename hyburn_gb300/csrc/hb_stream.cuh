@@ -192,6 +192,62 @@ __device__ __forceinline__ void stream_window(const float* q, float (&v)[HB_STRE
     }
 }
 
+// Consumer steps for Heun (deterministic or stochastic) with Linear coupling delivered directly, no
+// trajectory and no BOLD, one node per thread: one straight-line loop with the operations of
+// stream_node_step in the same order.
+template <int MODEL, bool STOCH, bool SF, bool NOISE_SMEM>
+__device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, const float* prm, const float* cp,
+                                                           const float* nscale, float dt, float dt_half,
+                                                           const float* gxbuf, const float* nzbuf, const float* noise_g,
+                                                           size_t nstride, float* ring, int n, bool active, int nm,
+                                                           int RPX, int RP, int wpos, int n_steps, int n_blocks,
+                                                           int nthreads) {
+    constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL), K = HB_STREAM_K;
+    const float ca = cp[0], cb = cp[1];
+    float ns[NVAR];
+#pragma unroll
+    for (int v = 0; v < NVAR; v++) ns[v] = nscale[v];
+    for (int blk = 0; blk < n_blocks; blk++) {
+        const int buf = blk & 1;
+        named_sync(HB_BAR_FULL0 + buf, nthreads);
+        const int it0 = blk * K;
+        const int nb = (n_steps - it0) < K ? (n_steps - it0) : K;
+        const float* gb = gxbuf + (size_t)buf * K * nm * NCV + (size_t)n * NCV;
+        const float* nbuf = nzbuf + (size_t)buf * K * nm * NVAR + (size_t)n * NVAR;
+#pragma unroll 1
+        for (int j = 0; j < nb; j++) {
+            const int pos = wpos;
+            wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
+            if (!active) continue;  // threads past the last node only take part in the barriers
+            float cc[2] = {0.0f, 0.0f};
+            cc[0] = gb[(size_t)j * nm * NCV] * ca + cb;
+            if (NCV > 1) cc[1] = gb[(size_t)j * nm * NCV + 1] * ca + cb;
+            float nz[NVAR];
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) {
+                if (!STOCH) nz[v] = 0.0f;
+                else if (NOISE_SMEM) nz[v] = nbuf[(size_t)j * nm * NVAR + v] * ns[v];
+                else nz[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * ns[v];
+            }
+            float k1[NVAR], k2[NVAR], tmp[NVAR];
+            dfun(MODEL, prm, SF ? 1 : 0, x, cc, k1);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tmp[v] = STOCH ? (x[v] + k1[v] * dt) + nz[v] : x[v] + k1[v] * dt;
+            clamp(MODEL, tmp);
+            dfun(MODEL, prm, SF ? 1 : 0, tmp, cc, k2);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++)
+                x[v] = STOCH ? (x[v] + (k1[v] + k2[v]) * dt_half) + nz[v] : x[v] + (k1[v] + k2[v]) * dt_half;
+            clamp(MODEL, x);
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
+            stream_publish<PRE_ID, NCV, NCV>(ring, n, RPX, RP, pos, x);
+        }
+        __threadfence_block();
+        named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+    }
+}
+
 // the whole run of sweep point b of one network (one CTA)
 template <int MODEL, int PRE, int NPT, int MAXT>
 __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, const RunArgs& a, const int b) {
@@ -358,6 +414,12 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                     float4* d4 = reinterpret_cast<float4*>(nbuf);
                     for (int i = p; i < n4; i += n_prod) d4[i] = __ldcs(s4 + i);
                     for (int i = (n4 << 2) + p; i < total; i += n_prod) nbuf[i] = __ldcs(src + i);
+                    // the rows of the block four blocks ahead into L2, one 128-byte line per thread
+                    if (it0 + 4 * K < a.n_steps) {
+                        const int ahead = (a.n_steps - it0 - 4 * K) < K ? (a.n_steps - it0 - 4 * K) : K;
+                        const int lines = (ahead * row_len + 31) >> 5;
+                        for (int l = p; l < lines; l += n_prod) prefetch_l2(src + (size_t)4 * K * nstride + (size_t)l * 32);
+                    }
                 } else {
                     for (int jj = 0; jj < nb; jj++)
                         for (int i = p; i < row_len; i += n_prod) nbuf[jj * row_len + i] = __ldcs(src + (size_t)jj * nstride + i);
@@ -394,7 +456,27 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
             }
         int64_t s = a.s0;
         int wpos = (int)((a.s0 + 1) % RP);
-        for (int blk = 0; blk < n_blocks; blk++) {
+        const bool straight = NPT == 1 && PRE == PRE_ID && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) &&
+                              P.cfk == HBC_LINEAR && P.direct && P.pc == NCV && !P.has_rowsums && a.traj == nullptr &&
+                              a.bold.n == 0;
+        if (straight) {
+            const int n = t;
+            float nscale[8];
+#pragma unroll
+            for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
+            const bool ns_smem = a.stream_noise_smem != 0;
+            float* x0 = x[0];
+            float* tv0 = tv[0];
+#define HB_SC(ST, SF, NS) stream_consume_heun_linear<MODEL, ST, SF, NS>(x0, tv0, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n, active[0], nm, RPX, RP, wpos, a.n_steps, n_blocks, nthreads)
+            if (integ == HBI_HEUN_STOCH) {
+                if (ns_smem) { if (sweep_form) HB_SC(true, true, true); else HB_SC(true, false, true); }
+                else { if (sweep_form) HB_SC(true, true, false); else HB_SC(true, false, false); }
+            } else {
+                if (sweep_form) HB_SC(false, true, true); else HB_SC(false, false, true);
+            }
+#undef HB_SC
+        }
+        for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
             const int buf = blk & 1;
             named_sync(HB_BAR_FULL0 + buf, nthreads);
             const int it0 = blk * K;
