@@ -894,6 +894,7 @@ hb_status run_finish(hb_engine* e, RunPlan& P, hb_result* res, bool device_part 
         }
         bh.n_out += n_new;
     }
+    if (flags_h[1] & 4) return fail(HB_ERR_TIMEOUT, "a bounded device-side wait on a bulk copy gave up");
     if (a.check_finite && flags_h[0]) return fail(HB_ERR_NONFINITE, "a state variable became NaN or Inf");
     return HB_OK;
 }

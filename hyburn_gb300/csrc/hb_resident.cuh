@@ -924,6 +924,31 @@ cudaError_t launch_fast(const DevNet* d_net, const RunArgs& a, int B, int thread
 __device__ __forceinline__ void named_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
 __device__ __forceinline__ void named_arrive(int id, int count) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory"); }
 
+// ---- bulk-copy engine (cp.async.bulk) with mbarrier completion, for contiguous 16-byte aligned runs ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// one thread: expect `bytes` on the barrier and start the copy global -> shared that delivers them
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+// wait for the phase of parity `parity` with an iteration limit; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // Consumer steps of the pipeline for the common case — Heun (deterministic or stochastic), Linear
 // coupling delivered to the first coupling variables, no trajectory, no BOLD — as one straight-line
 // loop: the per-step branches of the general consumer (integrator, coupling function, channel map,
@@ -933,7 +958,8 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
                                                          const float* nscale, float dt, float dt_half,
                                                          const float* gxbuf, const float* nzbuf, float* ring,
                                                          int n, bool active, int nm, int cols, int R, int slot,
-                                                         int n_steps, int n_blocks, int nthreads) {
+                                                         int n_steps, int n_blocks, int nthreads, uint64_t* nbar,
+                                                         int* err) {
     constexpr int PK = HB_PIPE_K;
     const float ca = cp[0], cb = cp[1];
     float ns[NVAR];
@@ -942,6 +968,7 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
     for (int blk = 0; blk < n_blocks; blk++) {
         const int buf = blk & 1;
         named_sync(HB_BAR_FULL0 + buf, nthreads);
+        if (STOCH && nbar && !mbar_wait(nbar + buf, (uint32_t)((blk >> 1) & 1))) atomicOr(err, 4);
         const int nb = (n_steps - blk * PK) < PK ? (n_steps - blk * PK) : PK;
         const float* gb = gxbuf + (size_t)buf * PK * nm * NCV + (size_t)n * NCV;
         const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR + (size_t)n * NVAR;
@@ -986,6 +1013,7 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
 template <int MODEL, int PRE, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ __align__(8) uint64_t noise_bar[2];  // bulk-copy completion of the two noise buffers
     __shared__ DevNet net;
     {
         const int* src = reinterpret_cast<const int*>(gnet);
@@ -1051,6 +1079,15 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
     const size_t nstride = (size_t)(a.noise_per_point ? B : 1) * net.noise_row;
     const int n_blocks = (a.n_steps + PK - 1) / PK;
     const bool is_consumer = t < n_cons;
+    // noise shared by all points, rows a multiple of 16 bytes: each block's rows are one contiguous
+    // aligned run, copied by the bulk-copy engine (one elected producer thread per block)
+    const bool use_bulk = stoch && !a.noise_per_point && (net.noise_row % 4) == 0 &&
+                          ((reinterpret_cast<uintptr_t>(noise_base) & 15) == 0) && ((reinterpret_cast<uintptr_t>(nzbuf) & 15) == 0);
+    if (use_bulk && t == 0) {
+        mbar_init(&noise_bar[0], 1);
+        mbar_init(&noise_bar[1], 1);
+        mbar_init_fence();
+    }
 
     // consumers publish x_{s0} before the first barrier
     const int n = t;
@@ -1178,7 +1215,14 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                 // raw draws of the block's rows; consumers apply the per-variable scale
                 float* nbuf = nzbuf + (size_t)buf * PK * row_len;
                 const float* src = noise_base + (size_t)it0 * nstride;
-                if (!a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                if (use_bulk) {
+                    if (p == 0) bulk_copy_g2s(nbuf, src, (uint32_t)(nb * row_len * 4), &noise_bar[buf]);
+                    if (it0 + 4 * PK < a.n_steps) {
+                        const int ahead = (a.n_steps - it0 - 4 * PK) < PK ? (a.n_steps - it0 - 4 * PK) : PK;
+                        const int lines = (ahead * row_len + 31) >> 5;
+                        for (int l = p; l < lines; l += n_prod) prefetch_l2(src + (size_t)4 * PK * nstride + (size_t)l * 32);
+                    }
+                } else if (!a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
                     const int total = nb * row_len, n4 = total >> 2;
                     const float4* s4 = reinterpret_cast<const float4*>(src);
                     float4* d4 = reinterpret_cast<float4*>(nbuf);
@@ -1230,16 +1274,17 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
 #pragma unroll
             for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
             if (integ == HBI_HEUN_STOCH) {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
             } else {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads);
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
             }
         }
         for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
             const int buf = blk & 1;
             named_sync(HB_BAR_FULL0 + buf, nthreads);
+            if (use_bulk && !mbar_wait(&noise_bar[buf], (uint32_t)((blk >> 1) & 1))) atomicOr(a.flags + 1, 4);
             const int it0 = blk * PK;
             const int nb = (a.n_steps - it0) < PK ? (a.n_steps - it0) : PK;
             const float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
