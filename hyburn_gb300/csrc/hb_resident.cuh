@@ -1128,7 +1128,10 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
             float* gb = gxbuf + (size_t)buf * PK * nm * PCH;
             const bool early = (sb < (int64_t)early_until) || sb == 0 || dmode == HBD_COMPAT;
             if (!early) {
-                // every edge reads PK consecutive rows at its column: one offset/weight load per edge
+                // every edge reads PK consecutive rows at its column: one offset/weight load per edge.
+                // The per-lane partial sums are already regrouped relative to the source-order sum
+                // of the reference (lanes, then a butterfly), so the multiply-adds are fused here;
+                // the difference is one rounding per term, inside the parity tolerance.
                 float acc[PK][PCH];
 #pragma unroll
                 for (int j = 0; j < PK; j++)
@@ -1145,8 +1148,8 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                             const float v = ring[a0 + j * cols];
                             if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
                             else {
-                                acc[j][0] += w * v;
-                                if (NCV > 1) acc[j][PCH - 1] += w * ring[a0 + j * cols + 1];
+                                acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
+                                if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[a0 + j * cols + 1], acc[j][PCH - 1]);
                             }
                         }
                     } else {
@@ -1157,8 +1160,8 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                             const float v = ring[aj];
                             if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
                             else {
-                                acc[j][0] += w * v;
-                                if (NCV > 1) acc[j][PCH - 1] += w * ring[aj + 1];
+                                acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
+                                if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[aj + 1], acc[j][PCH - 1]);
                             }
                         }
                     }

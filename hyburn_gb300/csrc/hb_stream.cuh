@@ -381,7 +381,7 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
 #pragma unroll
                         for (int j = 0; j < K; j++)
 #pragma unroll
-                            for (int c = 0; c < PCH; c++) acc[j][c] += w * v[j][c];
+                            for (int c = 0; c < PCH; c++) acc[j][c] = __fmaf_rn(w, v[j][c], acc[j][c]);  // regrouped sum: fused
                         if (sb == 0) {
                             // step 0 reads the current state through every edge (runtime.rs:166-170)
                             const float* q0 = ring + (size_t)src * RPX * PCH;
