@@ -180,6 +180,130 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+class PlainTorchSweep:
+    """The batched sweep step as plain per-operation GPU work (the comparator of the fused kernel):
+    per step, a gather of the delayed coupling variable of every edge from a [R, B, N] history,
+    a scatter-add over targets, the Linear coupling, the G2DO derivatives and the stochastic Heun
+    stages as element-wise tensor operations, and the history write — about twenty kernels,
+    replayed from a CUDA graph of `graph_steps` steps so that launch overhead does not dominate.
+    Ring semantics of runtime.rs:162-204 (current state at step 0, zero before time 0)."""
+
+    def __init__(self, cfg, values, noise, graph_steps=50):
+        import torch
+        dev = torch.device("cuda")
+        sub, proj = cfg.network.subnetworks[0], cfg.network.projections[0]
+        n = sub.nnodes
+        w = proj.weights
+        indptr = np.asarray(w["indptr"])
+        self.tgt = torch.tensor(np.repeat(np.arange(n), np.diff(indptr)), device=dev)
+        self.src = torch.tensor(np.asarray(w["indices"]), device=dev)
+        self.w = torch.tensor(np.asarray(w["data"], np.float32), device=dev)
+        self.d = torch.tensor(np.asarray(proj.delays, np.int64), device=dev)
+        self.R = int(max(proj.delays)) + 1
+        self.B, self.n, self.dt = len(values), n, cfg.dt
+        self.a = torch.tensor(np.asarray(values, np.float32), device=dev)[:, None]
+        self.b = float(proj.coupling_params[1]) if len(proj.coupling_params) > 1 else 0.0
+        self.p = [float(v) for v in sub.params]
+        self.scale = float(np.sqrt(2.0 * cfg.nsig) * np.sqrt(cfg.dt))
+        self.noise = torch.tensor(np.asarray(noise, np.float32), device=dev).reshape(-1, n, 2)
+        x0 = torch.tensor(np.asarray(sub.initial_state, np.float32), device=dev).reshape(n, 2)
+        self.x0 = x0[None].expand(self.B, n, 2).contiguous()
+        self.graph_steps = graph_steps
+        self.x = self.x0.clone()
+        self.ring = torch.zeros(self.R, self.B, n, device=dev)
+        self.s = torch.zeros((), dtype=torch.int64, device=dev)
+        self.graph = None
+
+    def _dfun(self, v, w, c):
+        p = self.p
+        tau, a_, b_, c_, d_, e_, f_, g_ = max(p[0], 1.1920929e-07), p[2], p[3], p[4], p[5], p[6], p[7], p[8]
+        alpha, beta, gamma = p[9], p[10], p[11]
+        iext = c * gamma + gamma * p[1]
+        v2 = v * v
+        dv = (w * alpha + iext - v * v2 * f_ + v2 * e_ + v * g_) * (d_ * tau)
+        dw = (v * b_ + v2 * c_ - w * beta + a_) * (d_ / tau)
+        return dv, dw
+
+    def _step(self):
+        import torch
+        s = self.s
+        t = s - self.d
+        idx = torch.remainder(t, self.R)
+        vals = self.ring[idx, :, self.src]                                    # [nnz, B]
+        cur = self.x[:, :, 0].t()[self.src]                                   # step 0 reads the current state
+        vals = torch.where((s == 0), cur, torch.where((t >= 0)[:, None], vals, torch.zeros_like(vals)))
+        g = torch.zeros(self.n, self.B, device=vals.device).index_add_(0, self.tgt, vals * self.w[:, None]).t()
+        c = g * self.a + self.b
+        nz = self.noise.index_select(0, s.view(1))[0] * self.scale           # [n, 2], shared by all points
+        v, w = self.x[..., 0], self.x[..., 1]
+        k1v, k1w = self._dfun(v, w, c)
+        pv, pw = v + k1v * self.dt + nz[:, 0], w + k1w * self.dt + nz[:, 1]
+        k2v, k2w = self._dfun(pv, pw, c)
+        v = v + (k1v + k2v) * (0.5 * self.dt) + nz[:, 0]
+        w = w + (k1w + k2w) * (0.5 * self.dt) + nz[:, 1]
+        self.x.copy_(torch.stack([v, w], -1))
+        self.ring.index_copy_(0, torch.remainder(s + 1, self.R).view(1), v[None])
+        self.s.add_(1)
+
+    def run(self, n_steps):
+        """n_steps steps from the initial state (a multiple of graph_steps)."""
+        import torch
+        self.x.copy_(self.x0)
+        self.ring.zero_()
+        self.s.zero_()
+        self.ring[0] = self.x0[:, :, 0]
+        if self.graph is None:
+            st = torch.cuda.Stream()
+            st.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(st):
+                for _ in range(3):
+                    self._step()
+            torch.cuda.current_stream().wait_stream(st)
+            self.x.copy_(self.x0)
+            self.ring.zero_()
+            self.s.zero_()
+            self.ring[0] = self.x0[:, :, 0]
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                for _ in range(self.graph_steps):
+                    self._step()
+            self.x.copy_(self.x0)
+            self.ring.zero_()
+            self.s.zero_()
+            self.ring[0] = self.x0[:, :, 0]
+        for _ in range(n_steps // self.graph_steps):
+            self.graph.replay()
+        return self.x
+
+
+def run_plain_arm(args):
+    """The same workload and metric as the default line, computed by PlainTorchSweep on a bounded
+    number of steps of the run (the per-step cost is constant)."""
+    import torch
+    torch.cuda.set_device(0)
+    n_run = 2000
+    cfg, meta, noise = workload(n_run)
+    plain = PlainTorchSweep(cfg, meta["values"], noise)
+    plain.run(plain.graph_steps)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(1, args.steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plain.run(n_run)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    node_steps = N_POINTS * N_NODES * n_run
+    print(json.dumps({"impl": "plain", "metric": METRIC, "value": node_steps / (ms / 1e3), "unit": "node-steps/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": ms * N_STEPS / n_run,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                      "data": "synthetic",
+                      "config": {"workload": WORKLOAD, "sample": f"{n_run} of {N_STEPS} steps",
+                                 "form": "per-operation tensor kernels, 50-step CUDA graphs"}}), flush=True)
+
+
 def _time_prepared(eng, steps, warmup):
     """CUDA-event time per execute_prepared() of an engine, L2 flushed before each timed run."""
     import torch
@@ -292,7 +416,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--run-steps", type=int, default=None,
                     help="integration steps per run (smaller values only for profiler captures)")
@@ -307,6 +431,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.impl == "plain":
+        run_plain_arm(args)
         return
     if args.workload != "sweep":
         run_other_workload(args)
