@@ -10,8 +10,9 @@
 // Kernels (one CTA per sweep point unless stated):
 //   adj_forward_kernel  the forward run as the engine computes it (same dfun, same op order), writing
 //                       y(t) and, every CK steps, a checkpoint of the state and the delay ring
-//   adj_stats_kernel    means, deviations, FC, the loss, and the coefficients of dL/dy(t)
-//   adj_source_kernel   dL/dy_k(t) = coef_k * (sum_j M_kj z_j(t) - r_k z_k(t))   (grid: points x time tiles)
+//   adj_moments_kernel  moments of y over one time slice (grid: points x up to 16 slices)
+//   adj_fc_kernel       adds the slices: means, deviations, FC, the loss, the coefficients of dL/dy(t)
+//   adj_source_kernel   dL/dy_k(t) = coef_k * (sum_j M_kj z_j(t) - r_k z_k(t))   (grid: points x 128-step tiles)
 //   adj_backward_kernel per checkpoint segment, last to first: recompute the segment forward from its
 //                       checkpoint (keeping x(s) and the coupling sum g(s)), then the reverse sweep
 //                       lambda(s) = lambda(s+1) * dx(s+1)/dx(s) + delayed-coupling terms + dL/dx(s).
@@ -75,55 +76,37 @@ __device__ __forceinline__ float coupling_post(int cfk, const float* cp, float g
     return out[0];
 }
 
-// dc/dg and dc/dgain of the coupling output at the weighted sum g
-__device__ __forceinline__ void coupling_post_grad(int cfk, const float* cp, float g, float& dc_dg, float& dc_dgain) {
-    if (cfk == HBC_SIGMOIDAL) {
-        const float cmin = cp[0], cmax = cp[1], mid = cp[2], a = cp[3], sigma = cp[4];
-        float sh = (g + (-mid)) / sigma;
-        float q = 1.0f / (expf(-(sh * a)) + 1.0f);
-        float dq = q * (1.0f - q);
-        dc_dg = (cmax - cmin) * dq * a / sigma;
-        dc_dgain = (cmax - cmin) * dq * sh;
-    } else {  // Linear: a * g + b
-        dc_dg = cp[0];
-        dc_dgain = g;
-    }
-}
-
-// Jansen–Rit sigmoid values and their derivatives with respect to their arguments at state y
-__device__ __forceinline__ void jr_sigmoids(const float* p, const float* y, float* sv, float* dsv) {
+// Jansen–Rit sigmoid values and their derivatives with respect to their arguments at state y, with
+// the hardware exponential and division (a few ulp): for the reverse coefficients, where the
+// linearisation point, not bit-exactness with the forward, is what matters
+__device__ __forceinline__ void jr_sigmoids_fast(const float* p, const float* y, float* sv, float* dsv) {
     const float J = p[7], v0 = p[4], nu_max = p[5], r = p[6], a1 = p[8], a3 = p[10];
     const float two_nu_max = 2.0f * nu_max;
     float args[3] = {y[1] - y[2], y[0] * (a1 * J), y[0] * (a3 * J)};
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        float arg = ((-args[q]) + v0) * r;
-        const float E = expf(arg);
-        float denom = E + 1.0f;
-        sv[q] = (1.0f * two_nu_max) / denom;
-        dsv[q] = sv[q] * r / (1.0f + 1.0f / E);  // E / (1 + E) without cancellation; 0 when E underflows
+        const float arg = ((-args[q]) + v0) * r;
+        const float E = __expf(arg);
+        const float inv = __fdividef(1.0f, E + 1.0f);
+        sv[q] = two_nu_max * inv;
+        dsv[q] = sv[q] * r * (1.0f - inv);  // E / (1 + E) = 1 - 1 / (1 + E)
     }
 }
 
-// u^T (df/dy) at state y (dfun.rs Jansen–Rit arm), and u . df/dc0, u . df/dA, u . df/dB, u . df/da
-__device__ __forceinline__ void jr_vjp(const float* p, const float* y, float c0, const float* u, float* out,
-                                       float& u_c, float& u_A, float& u_B, float& u_a) {
-    const float A = p[0], B = p[1], a = p[2], b = p[3], J = p[7];
-    const float a1 = p[8], a2 = p[9], a3 = p[10], a4 = p[11], mu = p[12];
-    float sv[3], dsv[3];
-    jr_sigmoids(p, y, sv, dsv);
-    const float Aa = A * a;
-    out[0] = u[3] * (-(a * a)) + u[4] * (Aa * (a2 * J) * dsv[1] * (a1 * J)) + u[5] * ((B * b) * (a4 * J) * dsv[2] * (a3 * J));
-    out[1] = u[3] * (Aa * dsv[0]) + u[4] * (-(a * a));
-    out[2] = -u[3] * (Aa * dsv[0]) + u[5] * (-(b * b));
-    out[3] = u[0] + u[3] * (-2.0f * a);
-    out[4] = u[1] + u[4] * (-2.0f * a);
-    out[5] = u[2] + u[5] * (-2.0f * b);
-    const float Mv = (sv[1] * (a2 * J) + mu) + c0;
-    u_c = u[4] * Aa;
-    u_A = u[3] * (a * sv[0]) + u[4] * (a * Mv);
-    u_B = u[5] * (b * (sv[2] * (a4 * J)));
-    u_a = u[3] * (A * sv[0] - 2.0f * y[3] - 2.0f * a * y[0]) + u[4] * (A * Mv - 2.0f * y[4] - 2.0f * a * y[1]);
+// coupling output c(g) and its slopes dc/dg, dc/dgain from one exponential
+__device__ __forceinline__ float coupling_post_and_grad(int cfk, const float* cp, float g, float& dc_dg, float& dc_dgain) {
+    if (cfk == HBC_SIGMOIDAL) {
+        const float cmin = cp[0], cmax = cp[1], mid = cp[2], a = cp[3], sigma = cp[4];
+        const float sh = (g + (-mid)) / sigma;
+        const float q = 1.0f / (expf(-(sh * a)) + 1.0f);
+        const float dq = (cmax - cmin) * (q * (1.0f - q));
+        dc_dg = dq * a / sigma;
+        dc_dgain = dq * sh;
+        return q * (cmax - cmin) + cmin;
+    }
+    dc_dg = cp[0];
+    dc_dgain = g;
+    return g * cp[0] + cp[1];
 }
 
 // The lambda-independent part of one reverse step at state x(s) with coupling sum g(s): the nonzero
@@ -143,10 +126,9 @@ __device__ __forceinline__ JrCoef jr_coef(const float* prm, const float* cp, int
     const float A = prm[0], B = prm[1], a = prm[2], b = prm[3], J = prm[7];
     const float a1 = prm[8], a2 = prm[9], a3 = prm[10], a4 = prm[11], mu = prm[12];
     JrCoef k;
-    const float c = coupling_post(cfk, cp, g);
-    coupling_post_grad(cfk, cp, g, k.dcdg, k.dcdgain);
+    const float c = coupling_post_and_grad(cfk, cp, g, k.dcdg, k.dcdgain);
     float sv[3], dsv[3];
-    jr_sigmoids(prm, xs, sv, dsv);
+    jr_sigmoids_fast(prm, xs, sv, dsv);
     // k1 = f(x, c) from the same sigmoid values, in the operation order of dfun.rs's Jansen-Rit arm
     float k1[NV], p[NV];
     {
@@ -182,7 +164,7 @@ __device__ __forceinline__ JrCoef jr_coef(const float* prm, const float* cp, int
     k.bBx = b * (sv[2] * (a4 * J));
     k.a3x = A * sv[0] - 2.0f * xs[3] - 2.0f * a * xs[0];
     k.a4x = A * Mx - 2.0f * xs[4] - 2.0f * a * xs[1];
-    jr_sigmoids(prm, p, sv, dsv);
+    jr_sigmoids_fast(prm, p, sv, dsv);
     k.q1p = Aa * (a2 * J) * dsv[1] * (a1 * J);
     k.q2p = Bb * (a4 * J) * dsv[2] * (a3 * J);
     k.p0p = Aa * dsv[0];
@@ -387,29 +369,31 @@ __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, i
 }
 
 // ---- statistics of y, FC, loss, and the coefficients of dL/dy ----
-__global__ void adj_stats_kernel(AdjArgs A) {
-    extern __shared__ __align__(16) float zs[];  // [32][N rounded up to 4] chunk of y - shift
-    const int b = blockIdx.x, N = A.N, T = A.T;
+// One pass over y in S time slices per point (grid: points x slices): moments of y - c_i with the
+// shift c_i = mean of the first 64 steps, summed in FP32 over chunks of 64 steps and in FP64 across
+// chunks, written per slice; adj_fc_kernel adds the slices and forms FC, the loss and the
+// coefficients of dL/dy. Each thread owns a 4 x 4 tile of the upper triangle of the product matrix.
+constexpr int MOM_CHUNK = 64;
+
+__device__ __forceinline__ float moment_shift(const AdjArgs& A, int b, int k) {
+    const int n0 = A.T < 64 ? A.T : 64;
+    float c = 0.0f;
+    for (int t = 0; t < n0; t++) c += A.Y[((size_t)t * A.B + b) * A.N + k];
+    return c / (float)n0;
+}
+
+__global__ void adj_moments_kernel(AdjArgs A, double* part, int slices) {
+    extern __shared__ __align__(16) float zs[];  // [MOM_CHUNK][W] chunk of y - shift, then shift[W]
+    const int b = blockIdx.x, sl = blockIdx.y, N = A.N, T = A.T;
     const int tid = threadIdx.x, nth = blockDim.x;
     const int N4 = (N + 3) / 4, W = N4 * 4;
-    // One pass over y: moments of y - c_i with the shift c_i = mean of the first 64 steps, summed in
-    // FP32 over chunks of 32 steps and in FP64 across chunks; FC_ij = cov_ij / (sd_i sd_j).
-    float* shift = zs + 32 * W;          // [W]
-    double* dsum = reinterpret_cast<double*>(shift + W);   // [W] sums of y - c
-    double* dsq = dsum + W;               // [W] sums of (y - c)^2 (diagonal of the tile products)
-    for (int k = tid; k < W; k += nth) {
-        float c = 0.0f;
-        if (k < N) {
-            const int n0 = T < 64 ? T : 64;
-            for (int t = 0; t < n0; t++) c += A.Y[((size_t)t * A.B + b) * N + k];
-            c /= (float)n0;
-        }
-        shift[k] = c;
-        dsum[k] = 0.0;
-        dsq[k] = 0.0;
-    }
+    const int Tc = ((T + slices - 1) / slices + MOM_CHUNK - 1) / MOM_CHUNK * MOM_CHUNK;
+    const int t_lo = sl * Tc, t_hi = (t_lo + Tc) < T ? (t_lo + Tc) : T;
+    float* shift = zs + MOM_CHUNK * W;
+    double* P = part + ((size_t)b * slices + sl) * ((size_t)W * W + W);  // Q [W][W], then S [W]
+    for (int k = tid; k < W; k += nth) shift[k] = k < N ? moment_shift(A, b, k) : 0.0f;
+    double ssum = 0.0;
     const int n_tiles = N4 * (N4 + 1) / 2;
-    float* fc = A.fc + (size_t)b * N * N;
     for (int base = 0; base < n_tiles; base += nth) {
         const int tile = base + tid;
         int bi = -1, bj = -1;
@@ -420,15 +404,15 @@ __global__ void adj_stats_kernel(AdjArgs A) {
             bj = bi + rem;
         }
         double acc[4][4];
-        float part[4][4];
+        float part4[4][4];
 #pragma unroll
         for (int u = 0; u < 4; u++)
 #pragma unroll
             for (int v = 0; v < 4; v++) acc[u][v] = 0.0;
-        for (int t0 = 0; t0 < T; t0 += 32) {
-            const int nt = (T - t0) < 32 ? (T - t0) : 32;
+        for (int t0 = t_lo; t0 < t_hi; t0 += MOM_CHUNK) {
+            const int nt = (t_hi - t0) < MOM_CHUNK ? (t_hi - t0) : MOM_CHUNK;
             __syncthreads();
-            for (int q = tid; q < 32 * W; q += nth) {
+            for (int q = tid; q < MOM_CHUNK * W; q += nth) {
                 const int tt = q / W, k = q - tt * W;
                 float z = 0.0f;
                 if (tt < nt && k < N) z = A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - shift[k];
@@ -436,15 +420,15 @@ __global__ void adj_stats_kernel(AdjArgs A) {
             }
             __syncthreads();
             if (base == 0 && tid < N) {
-                float ssum = 0.0f;
-                for (int tt = 0; tt < nt; tt++) ssum += zs[tt * W + tid];
-                dsum[tid] += ssum;
+                float s1 = 0.0f;
+                for (int tt = 0; tt < nt; tt++) s1 += zs[tt * W + tid];
+                ssum += s1;
             }
             if (bi < 0) continue;
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 4; v++) part[u][v] = 0.0f;
+                for (int v = 0; v < 4; v++) part4[u][v] = 0.0f;
             for (int tt = 0; tt < nt; tt++) {
                 const float4 zi = *reinterpret_cast<const float4*>(zs + tt * W + bi * 4);
                 const float4 zj = *reinterpret_cast<const float4*>(zs + tt * W + bj * 4);
@@ -452,54 +436,71 @@ __global__ void adj_stats_kernel(AdjArgs A) {
 #pragma unroll
                 for (int u = 0; u < 4; u++)
 #pragma unroll
-                    for (int v = 0; v < 4; v++) part[u][v] = __fmaf_rn(ai[u], aj[v], part[u][v]);
+                    for (int v = 0; v < 4; v++) part4[u][v] = __fmaf_rn(ai[u], aj[v], part4[u][v]);
             }
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 4; v++) acc[u][v] += part[u][v];
+                for (int v = 0; v < 4; v++) acc[u][v] += part4[u][v];
         }
-        if (bi >= 0 && bi == bj) {
-#pragma unroll
-            for (int u = 0; u < 4; u++) dsq[bi * 4 + u] = acc[u][u];
-        }
-        __syncthreads();
         if (bi >= 0) {
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
-                    const int ii = bi * 4 + u, jj = bj * 4 + v;
-                    if (ii >= N || jj >= N) continue;
-                    const double mi = dsum[ii] / T, mj = dsum[jj] / T;
-                    const double vi = dsq[ii] / T - mi * mi, vj = dsq[jj] / T - mj * mj;
-                    const double cov = acc[u][v] / T - mi * mj;
-                    const double den = sqrt(vi > 0.0 ? vi : 0.0) * sqrt(vj > 0.0 ? vj : 0.0);
-                    const float val = (ii == jj) ? 1.0f : (float)(den > 0.0 ? cov / den : 0.0);
-                    fc[ii * N + jj] = val;
-                    fc[jj * N + ii] = val;
+                    P[(size_t)(bi * 4 + u) * W + bj * 4 + v] = acc[u][v];
+                    P[(size_t)(bj * 4 + v) * W + bi * 4 + u] = acc[u][v];
                 }
         }
     }
-    __syncthreads();
+    if (tid < W) P[(size_t)W * W + tid] = tid < N ? ssum : 0.0;
+}
+
+__global__ void adj_fc_kernel(AdjArgs A, const double* part, int slices) {
+    extern __shared__ __align__(16) double red[];  // [nth], then dsum [W], dsq [W]
+    const int b = blockIdx.x, N = A.N, T = A.T;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int W = (N + 3) / 4 * 4;
+    double* dsum = red + nth;
+    double* dsq = dsum + W;
+    const double* P0 = part + (size_t)b * slices * ((size_t)W * W + W);
     for (int k = tid; k < N; k += nth) {
-        const double m = dsum[k] / T, v = dsq[k] / T - m * m;
-        A.mean[(size_t)b * N + k] = (float)(shift[k] + m);
+        double s1 = 0.0, s2 = 0.0;
+        for (int sl = 0; sl < slices; sl++) {
+            const double* P = P0 + (size_t)sl * ((size_t)W * W + W);
+            s1 += P[(size_t)W * W + k];
+            s2 += P[(size_t)k * W + k];
+        }
+        dsum[k] = s1;
+        dsq[k] = s2;
+        const double m = s1 / T, v = s2 / T - m * m;
+        A.mean[(size_t)b * N + k] = (float)(moment_shift(A, b, k) + m);
         A.sdev[(size_t)b * N + k] = (float)sqrt(v > 0.0 ? v : 0.0);
     }
     __syncthreads();
+    float* fc = A.fc + (size_t)b * N * N;
+    for (int q = tid; q < N * N; q += nth) {
+        const int ii = q / N, jj = q - ii * N;
+        double qs = 0.0;
+        for (int sl = 0; sl < slices; sl++) qs += P0[(size_t)sl * ((size_t)W * W + W) + (size_t)ii * W + jj];
+        const double mi = dsum[ii] / T, mj = dsum[jj] / T;
+        const double vi = dsq[ii] / T - mi * mi, vj = dsq[jj] / T - mj * mj;
+        const double cov = qs / T - mi * mj;
+        const double den = sqrt(vi > 0.0 ? vi : 0.0) * sqrt(vj > 0.0 ? vj : 0.0);
+        fc[q] = (ii == jj) ? 1.0f : (float)(den > 0.0 ? cov / den : 0.0);
+    }
+    __syncthreads();
     // loss, M (off-diagonal dL/dFC), r_k, coef_k
-    double* red = reinterpret_cast<double*>(zs);
-    double part = 0.0;
+    double part_l = 0.0;
     const double inv_n2 = 1.0 / ((double)N * N);
     float* Mb = A.M + (size_t)b * N * N;
     for (int q = tid; q < N * N; q += nth) {
         const int k = q / N, j = q - k * N;
         const double d = (double)fc[q] - (double)A.target[q];
-        part += d * d;
+        part_l += d * d;
         Mb[(size_t)j * N + k] = (k == j) ? 0.0f : (float)(2.0 * d * inv_n2);
     }
-    red[tid] = part;
+    red[tid] = part_l;
     __syncthreads();
     for (int o = nth >> 1; o > 0; o >>= 1) {
         if (tid < o) red[tid] += red[tid + o];
@@ -516,30 +517,53 @@ __global__ void adj_stats_kernel(AdjArgs A) {
 }
 
 // dL/dy_k(t) for a tile of 64 time steps of one point: block (threads k = 0..N-1) x (TW rows)
+// Time steps per source tile, time steps per thread, and the padded row length of the transposed
+// tile (a multiple of 4 for float4 reads; 132 spreads the transposing writes over 8 banks).
+constexpr int SRC_TS = 128, SRC_TT = 16, SRC_ROW = 132;
+
 __global__ void adj_source_kernel(AdjArgs A) {
     extern __shared__ __align__(16) float sm[];
     const int b = blockIdx.x, N = A.N;
-    const int t0 = blockIdx.y * 64;
-    const int nt = (A.T - t0) < 64 ? (A.T - t0) : 64;
-    float* Ms = sm;               // [N][N], M[j][k]
-    float* zs = sm + N * N;       // [64][N]
+    const int t0 = blockIdx.y * SRC_TS;
+    const int nt = (A.T - t0) < SRC_TS ? (A.T - t0) : SRC_TS;
+    float* Ms = sm;                                  // [N][N], M[j][k]
+    float* zt = sm + ((N * N + 3) & ~3);             // [N][SRC_ROW], z_j(t0 + tt) normalised
     const float* Mb = A.M + (size_t)b * N * N;
     for (int q = threadIdx.x; q < N * N; q += blockDim.x) Ms[q] = Mb[q];
-    for (int q = threadIdx.x; q < nt * N; q += blockDim.x) {
+    for (int q = threadIdx.x; q < SRC_TS * N; q += blockDim.x) {
         const int tt = q / N, k = q - tt * N;
-        const float sd = A.sdev[(size_t)b * N + k];
-        zs[q] = sd > 0.0f ? (A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - A.mean[(size_t)b * N + k]) / sd : 0.0f;
+        float z = 0.0f;
+        if (tt < nt) {
+            const float sd = A.sdev[(size_t)b * N + k];
+            z = sd > 0.0f ? (A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - A.mean[(size_t)b * N + k]) / sd : 0.0f;
+        }
+        zt[k * SRC_ROW + tt] = z;
     }
     __syncthreads();
     const int kpad = (N + 31) / 32 * 32;
-    const int k = threadIdx.x % kpad, w = threadIdx.x / kpad, TW = blockDim.x / kpad;
-    if (k >= N) return;
-    const float ck = A.coef[(size_t)b * N + k], rk = A.rk[(size_t)b * N + k];
-    for (int tt = w; tt < nt; tt += TW) {
-        float acc = 0.0f;
-        for (int j = 0; j < N; j++) acc = __fmaf_rn(Ms[j * N + k], zs[tt * N + j], acc);
-        A.S[((size_t)(t0 + tt) * A.B + b) * N + k] = ck * (acc - rk * zs[tt * N + k]);
+    const int k = threadIdx.x % kpad, w = threadIdx.x / kpad;
+    const int tt0 = w * SRC_TT;
+    if (k >= N || tt0 >= nt) return;
+    float acc[SRC_TT];
+#pragma unroll
+    for (int q = 0; q < SRC_TT; q++) acc[q] = 0.0f;
+    for (int j = 0; j < N; j++) {
+        const float m = Ms[j * N + k];
+        const float4* zj = reinterpret_cast<const float4*>(zt + j * SRC_ROW + tt0);
+#pragma unroll
+        for (int q = 0; q < SRC_TT / 4; q++) {
+            const float4 z = zj[q];
+            acc[4 * q + 0] = __fmaf_rn(m, z.x, acc[4 * q + 0]);
+            acc[4 * q + 1] = __fmaf_rn(m, z.y, acc[4 * q + 1]);
+            acc[4 * q + 2] = __fmaf_rn(m, z.z, acc[4 * q + 2]);
+            acc[4 * q + 3] = __fmaf_rn(m, z.w, acc[4 * q + 3]);
+        }
     }
+    const float ck = A.coef[(size_t)b * N + k], rk = A.rk[(size_t)b * N + k];
+    const float* zk = zt + k * SRC_ROW + tt0;
+#pragma unroll
+    for (int q = 0; q < SRC_TT; q++)
+        if (tt0 + q < nt) A.S[((size_t)(t0 + tt0 + q) * A.B + b) * N + k] = ck * (acc[q] - rk * zk[q]);
 }
 
 __device__ __forceinline__ JrCoef shfl_coef(const JrCoef& k, int src_lane, int L) {
@@ -672,17 +696,6 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
 }  // namespace
 
 // ---- launch interface used by the engine (hb_engine.cu) ----
-struct HbAdjointLaunch {
-    int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
-    float dt, dt_half;
-    const float* x0;
-    const int* rowptr; const uint32_t* edges; const float* ew;
-    const int* cptr; const int* ctgt; const int* cdel; const float* cw;
-    float *Y, *S, *ck_state, *ck_ring, *scratch, *mu_ring;
-    const float* target;
-    float *mean, *sdev, *coef, *rk, *M, *fc;
-    double *loss, *gG, *gA, *gB, *ga;
-};
 
 cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st) {
     AdjArgs A;
@@ -710,15 +723,16 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         adj_forward_kernel<<<L.B, threads, sm, st>>>(d_net, A, lanes);
     } else if (phase == 1) {
         const size_t W = (size_t)(L.N + 3) / 4 * 4;
-        const size_t sm = std::max(33 * W * sizeof(float) + 2 * W * sizeof(double) + 16, (size_t)512 * sizeof(double));
-        adj_stats_kernel<<<L.B, 512, sm, st>>>(A);
-        const size_t sm2 = ((size_t)L.N * L.N + 64 * (size_t)L.N) * sizeof(float);
+        const size_t sm = (MOM_CHUNK + 1) * W * sizeof(float) + 16;
+        const int n_tiles = (int)(W / 4 * (W / 4 + 1) / 2);
+        adj_moments_kernel<<<dim3(L.B, L.slices), n_tiles <= 256 ? 256 : 512, sm, st>>>(A, L.moments, L.slices);
+        adj_fc_kernel<<<L.B, 512, (512 + 2 * W) * sizeof(double), st>>>(A, L.moments, L.slices);
+        const size_t sm2 = ((((size_t)L.N * L.N + 3) & ~(size_t)3) + (size_t)SRC_ROW * L.N) * sizeof(float);
         if (cudaFuncSetAttribute(adj_source_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2) != cudaSuccess)
             return cudaGetLastError();
         const int kpad = (L.N + 31) / 32 * 32;
-        const int tw = std::max(1, 512 / kpad);
-        dim3 grid(L.B, (L.T + 63) / 64);
-        adj_source_kernel<<<grid, kpad * tw, sm2, st>>>(A);
+        dim3 grid(L.B, (L.T + SRC_TS - 1) / SRC_TS);
+        adj_source_kernel<<<grid, kpad * (SRC_TS / SRC_TT), sm2, st>>>(A);
     } else {
         const int rl = lanes;
         int rthreads = 32;

@@ -147,3 +147,27 @@ struct StreamJob {
     int first_block;   // first block of this job in the grouped grid
     int n_points;      // its sweep points (one block each)
 };
+
+// the FC-loss adjoint's buffers and sizes (hb_adjoint.cu); device pointers
+struct HbAdjointLaunch {
+    int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
+    int slices;        // time slices of the moment pass (hb_adjoint_moment_slices)
+    float dt, dt_half;
+    const float* x0;
+    const int* rowptr; const uint32_t* edges; const float* ew;
+    const int* cptr; const int* ctgt; const int* cdel; const float* cw;
+    float *Y, *S, *ck_state, *ck_ring, *scratch, *mu_ring;
+    const float* target;
+    float *mean, *sdev, *coef, *rk, *M, *fc;
+    double *loss, *gG, *gA, *gB, *ga;
+    double* moments;   // [B][slices][W * W + W] partial moments of y, W = N rounded up to 4
+};
+
+// time slices of the moment pass for B points of T steps: enough blocks to fill the SMs three times
+// over, at most 16, each slice at least 64 steps
+inline int hb_adjoint_moment_slices(int B, int T) {
+    int s = (456 + B - 1) / B;
+    if (s > 16) s = 16;
+    if (s > T / 64) s = T / 64;
+    return s < 1 ? 1 : s;
+}

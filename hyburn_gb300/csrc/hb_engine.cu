@@ -41,17 +41,6 @@ cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs
 int hb_stream_group_budget_1(int model, int pre);
 int hb_stream_group_budget_2(int model, int pre);
 int hb_stream_group_budget_4(int model, int pre);
-struct HbAdjointLaunch {
-    int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
-    float dt, dt_half;
-    const float* x0;
-    const int* rowptr; const uint32_t* edges; const float* ew;
-    const int* cptr; const int* ctgt; const int* cdel; const float* cw;
-    float *Y, *S, *ck_state, *ck_ring, *scratch, *mu_ring;
-    const float* target;
-    float *mean, *sdev, *coef, *rk, *M, *fc;
-    double *loss, *gG, *gA, *gB, *ga;
-};
 cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st);
 
 namespace {
@@ -611,7 +600,8 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     if (pipe >= 0) {
         // gx and noise double buffers: [2][8][nm][channels] + [2][8][nm*nvar]
         const int pch = (pipe == 1) ? 2 : e->subs[0].ncvar;
-        part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + e->subs[0].nvar) * 4 + (size_t)(e->subs[0].nm + 1) * 4 + 48;
+        part_bytes = (size_t)2 * 8 * e->subs[0].nm * (pch + (any_stoch ? e->subs[0].nvar : 0)) * 4 +
+                     (size_t)(e->subs[0].nm + 1) * 4 + 48;
     }
     // ring length of this run: the pipeline's producers run at most one block ahead of the consumers'
     // writes, so slot reuse needs only more slots than the longest delay; the other kernels keep the
@@ -1693,7 +1683,7 @@ void hb_group_destroy(hb_group* g) { delete g; }
 struct AdjWorkspace {
     DBuf<int> cptr, ctgt, cdel;
     DBuf<float> cw, Y, S, ck_state, ck_ring, scratch, mu_ring, target, mean, sdev, coef, rk, M, fc;
-    DBuf<double> loss, gG, gA, gB, ga;
+    DBuf<double> loss, gG, gA, gB, ga, moments;
 };
 
 hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n_values, int64_t n_steps,
@@ -1779,6 +1769,10 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     CUDA_TRY(W->rk.ensure((size_t)B * N)); CUDA_TRY(W->M.ensure((size_t)B * N * N)); CUDA_TRY(W->fc.ensure((size_t)B * N * N));
     CUDA_TRY(W->loss.ensure(B)); CUDA_TRY(W->gG.ensure(B));
     CUDA_TRY(W->gA.ensure((size_t)B * N)); CUDA_TRY(W->gB.ensure((size_t)B * N)); CUDA_TRY(W->ga.ensure((size_t)B * N));
+    {
+        const size_t Wn = (size_t)(N + 3) / 4 * 4;
+        CUDA_TRY(W->moments.ensure((size_t)B * hb_adjoint_moment_slices(B, T) * (Wn * Wn + Wn)));
+    }
     HbAdjointLaunch L;
     L.B = B; L.N = N; L.T = T; L.R = R; L.K = K; L.CK = CK; L.n_ck = n_ck; L.nnz = (int)hp.edges.size();
     L.store_all = store_all;
@@ -1790,6 +1784,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     L.mu_ring = W->mu_ring.p; L.target = W->target.p; L.mean = W->mean.p; L.sdev = W->sdev.p; L.coef = W->coef.p;
     L.rk = W->rk.p; L.M = W->M.p; L.fc = W->fc.p; L.loss = W->loss.p; L.gG = W->gG.p; L.gA = W->gA.p; L.gB = W->gB.p;
     L.ga = W->ga.p;
+    L.moments = W->moments.p;
+    L.slices = hb_adjoint_moment_slices(B, T);
     cudaEvent_t ev[4];
     for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
     cudaError_t ce = cudaEventRecord(ev[0], st);
@@ -1821,6 +1817,6 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
                     &W->coef, &W->rk, &W->M, &W->fc, &W->cw})
         b->release();
     W->cptr.release(); W->ctgt.release(); W->cdel.release();
-    W->loss.release(); W->gG.release(); W->gA.release(); W->gB.release(); W->ga.release();
+    W->loss.release(); W->gG.release(); W->gA.release(); W->gB.release(); W->ga.release(); W->moments.release();
     return HB_OK;
 }

@@ -1042,7 +1042,10 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
     float* gxbuf = reinterpret_cast<float*>(smem + off);
     off += (size_t)2 * PK * nm * PCH * sizeof(float);
     float* nzbuf = reinterpret_cast<float*>(smem + off);
-    off += (size_t)2 * PK * nm * NVAR * sizeof(float);
+    {
+        const int ig = net.sub[0].integ;  // noise buffers only for stochastic integrators
+        if (ig == HBI_EULER_STOCH || ig == HBI_HEUN_STOCH || ig == HBI_RK4_STOCH) off += (size_t)2 * PK * nm * NVAR * sizeof(float);
+    }
     off = (off + 15) & ~(size_t)15;
     int* s_rowptr = reinterpret_cast<int*>(smem + off);
     off += (size_t)(nm + 1) * 4;
