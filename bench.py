@@ -49,38 +49,57 @@ def peaks():
 
 
 class ClockSampler:
-    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+    """Samples SM clocks and throttle reasons while the timed region runs: one `nvidia-smi -lms 20`
+    process started (and seen answering) before the region, stopped after it; only the samples that
+    arrive inside the region are kept."""
 
-    def __init__(self, index: int):
-        self.index = index
-        self.samples = []
-        self._stop = threading.Event()
-        self._thr = None
-
-    def _run(self):
-        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                parts = [x.strip() for x in out.stdout.strip().split(",")]
-                if len(parts) >= 7:
-                    self.samples.append(parts)
-            except Exception:
-                pass
-            self._stop.wait(0.05)
+
+    def __init__(self, index: int, period_ms: int = 20):
+        self.index = index
+        self.period_ms = period_ms
+        self.samples = []
+        self._all = []
+        self._proc = None
+        self._thr = None
+        self._first = threading.Event()
+        self._t0 = self._t1 = None
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.strip().split(",")]
+            if len(parts) >= 7:
+                self._all.append((time.perf_counter(), parts))
+                self._first.set()
 
     def __enter__(self):
-        self._thr = threading.Thread(target=self._run, daemon=True)
-        self._thr.start()
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                           "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._thr = threading.Thread(target=self._read, daemon=True)
+            self._thr.start()
+            self._first.wait(5.0)
+        except OSError:
+            self._proc = None
+        self._t0 = time.perf_counter()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        if self._thr:
-            self._thr.join(timeout=10)
+        self._t1 = time.perf_counter()
+        if self._proc is not None:
+            time.sleep(2 * self.period_ms / 1e3)
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+            if self._thr:
+                self._thr.join(timeout=5)
+        inside = [p for t, p in self._all if self._t0 <= t <= self._t1 + self.period_ms / 1e3]
+        self.samples = inside or [p for _, p in self._all[-1:]]
 
     def summary(self):
         if not self.samples:

@@ -627,12 +627,12 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         const int nm0 = e->subs[0].nm, nvar0 = e->subs[0].nvar;
         const int pch = (fast == 1) ? 2 : e->subs[0].ncvar;
         // nodes per consumer thread: one (512 threads) for up to 96 nodes, else two (1024 threads, at
-        // least 256 producers); four on request
+        // least 256 producers); four (768 threads, two edge windows in flight per producer) on request
         auto fits = [&](int k, int nt) { return ((nm0 + k - 1) / k + 31) / 32 * 32 + (nt == 512 ? 128 : 256) <= nt; };
         const int want = (int)((run_flags >> 24) & 0x7);
         int npt = 0, threads = 0;
         if (want == 1 || (want == 0 && nm0 <= 96)) { if (fits(1, 512)) { npt = 1; threads = 512; } }
-        else if (want == 4) { if (fits(4, 1024)) { npt = 4; threads = 1024; } }
+        else if (want == 4) { if (fits(4, 768)) { npt = 4; threads = 768; } }
         else if (fits(2, 1024)) { npt = 2; threads = 1024; }
         const int sbudget = npt == 1 ? hb_stream_budget_1(e->kernel_model, fast)
                           : npt == 2 ? hb_stream_budget_2(e->kernel_model, fast)
@@ -1521,7 +1521,10 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     // one kernel instantiation for all: nodes per consumer thread from the largest member
     int max_nm = 0;
     for (int i = 0; i < n; i++) max_nm = std::max(max_nm, members[i].engine->subs[0].nm);
-    const int npt = max_nm <= 96 ? 1 : 2;
+    // four nodes per consumer thread (768 threads) when every member asks for it
+    bool want4 = true;
+    for (int i = 0; i < n; i++) want4 = want4 && ((members[i].run_flags >> 24) & 0x7) == 4;
+    const int npt = want4 && max_nm <= 2048 ? 4 : max_nm <= 96 ? 1 : 2;
     std::unique_ptr<hb_group> g(new hb_group());
     if (cuda_stream) g->user = (cudaStream_t)cuda_stream;
     else CUDA_TRY(cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking));
@@ -1575,7 +1578,8 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
         }
         CUDA_TRY(cudaStreamSynchronize(e->stream()));
     }
-    const int budget = npt == 1 ? hb_stream_group_budget_1(model, fast) : hb_stream_group_budget_2(model, fast);
+    const int budget = npt == 1 ? hb_stream_group_budget_1(model, fast)
+                     : npt == 2 ? hb_stream_group_budget_2(model, fast) : hb_stream_group_budget_4(model, fast);
     if (budget < 0 || smem + 64 > (size_t)budget) return fail(HB_ERR_UNSUPPORTED, "grouped launch: shared memory budget exceeded");
     // jobs, longest points first
     std::vector<int> order(n);
@@ -1595,7 +1599,7 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     }
     CUDA_TRY(g->jobs.ensure(n));
     CUDA_TRY(cudaMemcpy(g->jobs.p, jobs.data(), n * sizeof(StreamJob), cudaMemcpyHostToDevice));
-    const int threads = npt == 1 ? 512 : 1024;
+    const int threads = npt == 1 ? 512 : npt == 2 ? 1024 : 768;
     // the whole run as one graph: member resets, the grouped launch, batch-mean BOLD reductions
     cudaStream_t st = g->stream();
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1611,7 +1615,8 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev0, st, cudaEventRecordExternal);
     if (ce == cudaSuccess)
         ce = npt == 1 ? hb_launch_stream_group_1(model, fast, g->jobs.p, n, blocks, threads, smem, st)
-                      : hb_launch_stream_group_2(model, fast, g->jobs.p, n, blocks, threads, smem, st);
+           : npt == 2 ? hb_launch_stream_group_2(model, fast, g->jobs.p, n, blocks, threads, smem, st)
+                      : hb_launch_stream_group_4(model, fast, g->jobs.p, n, blocks, threads, smem, st);
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev1, st, cudaEventRecordExternal);
     for (auto& gm : g->m) {
         for (int mo = 0; mo < gm.P.n_bold_active && !gm.P.bold_pp && ce == cudaSuccess; mo++) {

@@ -192,6 +192,42 @@ __device__ __forceinline__ void stream_window(const float* q, float (&v)[HB_STRE
     }
 }
 
+// One edge's contribution to the K coupling sums of a block: the window of its source's history
+// starting `delay` steps before the block's first step, times the weight, added to acc (fused
+// multiply-adds: the regrouped sum). At step 0 the edge also reads the current state
+// (runtime.rs:166-170).
+template <int PCH>
+__device__ __forceinline__ void stream_edge_acc(const float* ring, uint32_t m, float w, int sbm, int RP, int RPX,
+                                                bool first_step, float (&acc)[HB_STREAM_K][PCH]) {
+    const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
+    int pos = sbm - d;
+    pos += (pos < 0) ? RP : 0;
+    float v[HB_STREAM_K][PCH];
+    stream_window<PCH>(ring + ((size_t)src * RPX + pos) * PCH, v);
+#pragma unroll
+    for (int j = 0; j < HB_STREAM_K; j++)
+#pragma unroll
+        for (int c = 0; c < PCH; c++) acc[j][c] = __fmaf_rn(w, v[j][c], acc[j][c]);
+    if (first_step) {
+        const float* q0 = ring + (size_t)src * RPX * PCH;
+#pragma unroll
+        for (int c = 0; c < PCH; c++) acc[0][c] += w * q0[c];
+    }
+}
+
+// L2 prefetch of the window of edge ep (when it is below e1)
+template <int PCH>
+__device__ __forceinline__ void stream_edge_prefetch(const float* ring, const uint32_t* ed, int ep, int e1, int sbm, int RP,
+                                                     int RPX) {
+    if (ep >= e1) return;
+    const uint32_t mp = ed[ep];
+    int pp = sbm - (int)(mp >> 16);
+    pp += (pp < 0) ? RP : 0;
+    const float* qp = ring + ((size_t)(mp & 0xffffu) * RPX + pp) * PCH;
+    prefetch_l2(qp);
+    prefetch_l2(qp + (HB_STREAM_K * PCH - 1));
+}
+
 // Consumer steps for Heun (deterministic or stochastic) with Linear coupling delivered directly, no
 // trajectory and no BOLD, one node per thread: one straight-line loop with the operations of
 // stream_node_step in the same order.
@@ -261,7 +297,8 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
     constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
     constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
     constexpr int K = HB_STREAM_K;
-    constexpr int UNR = (MAXT > 512) ? 1 : 2;  // edges in flight per producer thread (register budget)
+    constexpr int UNR = (MAXT > 768) ? 1 : 2;  // edges in flight per producer thread (register budget)
+    constexpr int DB = (MAXT > 768) ? 1 : 8;   // edge descriptors loaded per batch (register budget)
     const int t = threadIdx.x, nthreads = blockDim.x;
     const int nm = gnet->sub[0].nm;
     const int RP = a.stream_rp, RPX = RP + 2 * K;
@@ -358,35 +395,35 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                     for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
                 if (node < nm) {
                     const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
+                    if constexpr (DB == 1) {
 #pragma unroll UNR
-                    for (int e = e0 + lane; e < e1; e += PL) {
-                        if (pf) {
-                            const int ep = e + pf * PL;
-                            if (ep < e1) {
-                                const uint32_t mp = ed[ep];
-                                int pp = sbm - (int)(mp >> 16);
-                                pp += (pp < 0) ? RP : 0;
-                                const float* qp = ring + ((size_t)(mp & 0xffffu) * RPX + pp) * PCH;
-                                prefetch_l2(qp);
-                                prefetch_l2(qp + (K * PCH - 1));
-                            }
+                        for (int e = e0 + lane; e < e1; e += PL) {
+                            if (pf) stream_edge_prefetch<PCH>(ring, ed, e + pf * PL, e1, sbm, RP, RPX);
+                            stream_edge_acc<PCH>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
                         }
-                        const uint32_t m = ed[e];
-                        const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
-                        const float w = ew[e];
-                        int pos = sbm - d;
-                        pos += (pos < 0) ? RP : 0;
-                        float v[K][PCH];
-                        stream_window<PCH>(ring + ((size_t)src * RPX + pos) * PCH, v);
+                    } else {
+                        // the edge descriptors DB at a time, loaded together, so that their latency is
+                        // paid once per batch instead of before every window read; the batch is
+                        // consumed in order by rotating it through registers
+                        for (int eb = e0 + lane; eb < e1; eb += DB * PL) {
+                            uint32_t mb[DB];
+                            float wb[DB];
 #pragma unroll
-                        for (int j = 0; j < K; j++)
+                            for (int u = 0; u < DB; u++) {
+                                const int e = eb + u * PL;
+                                mb[u] = (e < e1) ? ed[e] : 0u;
+                                wb[u] = (e < e1) ? ew[e] : 0.0f;
+                            }
+                            const int cnt = (e1 - eb + PL - 1) / PL < DB ? (e1 - eb + PL - 1) / PL : DB;
+#pragma unroll UNR
+                            for (int u = 0; u < cnt; u++) {
+                                const uint32_t m = mb[0];
+                                const float w = wb[0];
 #pragma unroll
-                            for (int c = 0; c < PCH; c++) acc[j][c] = __fmaf_rn(w, v[j][c], acc[j][c]);  // regrouped sum: fused
-                        if (sb == 0) {
-                            // step 0 reads the current state through every edge (runtime.rs:166-170)
-                            const float* q0 = ring + (size_t)src * RPX * PCH;
-#pragma unroll
-                            for (int c = 0; c < PCH; c++) acc[0][c] += w * q0[c];
+                                for (int q = 0; q + 1 < DB; q++) { mb[q] = mb[q + 1]; wb[q] = wb[q + 1]; }
+                                if (pf) stream_edge_prefetch<PCH>(ring, ed, eb + (u + pf) * PL, e1, sbm, RP, RPX);
+                                stream_edge_acc<PCH>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                            }
                         }
                     }
                 }

@@ -1,3 +1,4 @@
-// streamed-history pipeline kernels: 4 nodes per consumer thread, 1024 threads
+// streamed-history pipeline kernels: 4 nodes per consumer thread, up to 768 threads (two edge
+// windows in flight per producer thread)
 #include "hb_stream.cuh"
-HB_STREAM_UNIT(4, 1024)
+HB_STREAM_UNIT(4, 768)

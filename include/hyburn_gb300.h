@@ -81,7 +81,9 @@ typedef int32_t hb_status;
 #define HB_RUN_NO_STREAM      (1u << 19) /* never use the streamed-history pipeline */
 /* pipeline kernel: producer threads per node (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_PIPE_LANES(n)  ((uint32_t)((n) & 0xf) << 20)
-/* streamed-history kernel: nodes per consumer thread (1, 2 or 4; 0 lets the engine choose) */
+/* streamed-history kernel: nodes per consumer thread (1: 512 threads, 2: 1024 threads, 4: 768 threads
+   with two edge windows in flight per producer; 0 lets the engine choose). A grouped launch uses 4 when
+   every member asks for it. */
 #define HB_RUN_STREAM_NPT(n)  ((uint32_t)((n) & 0x7) << 24)
 /* streamed-history kernel: prefetch the history runs of upcoming edges into L2 */
 #define HB_RUN_STREAM_PREFETCH (1u << 27)

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, GroupedSweep, SweepParam
-from hyburn_gb300._abi import HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING
+from hyburn_gb300._abi import HB_RUN_STREAM_NPT, HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING
 from hyburn_gb300.config import MonitorConfig, Unsupported
 from oracle.hb_oracle import OracleEngine
 
@@ -26,8 +26,10 @@ def _check(members, sem, results):
                 close(r.bold[m], o.bold[m], atol=BOLD_ATOL, what="bold")
 
 
-@pytest.mark.parametrize("sem", [HB_SEM_DELAY_RING, HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT])
-def test_group_uneven_sizes_steps_and_bold(sem):
+@pytest.mark.parametrize("sem,run_flags", [(HB_SEM_DELAY_RING, 0), (HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT, 0),
+                                           (HB_SEM_DELAY_RING, HB_RUN_STREAM_NPT(4))])
+def test_group_uneven_sizes_steps_and_bold(sem, run_flags):
+    """run_flags HB_RUN_STREAM_NPT(4): the 768-thread form, four nodes per consumer thread."""
     mons = [MonitorConfig("Bold", tr=0.004, bold_period=10)]
     spec = [(20, 3, 260, "rk4"), (45, 2, 180, "rk4"), (70, 4, 330, "heun"), (33, 1, 90, "rk4")]
     members, cfgs = [], []
@@ -37,7 +39,7 @@ def test_group_uneven_sizes_steps_and_bold(sem):
         vals = np.linspace(-1.0, 0.5, pts).astype(np.float32).tolist()
         members.append((cfg, pts, SweepParam(0, 4), vals, steps, None))
     engines = [BatchHybridEngine.from_config(c, p, semantics=sem) for c, p, *_ in members]
-    g = GroupedSweep([(e, m[2], m[3], m[4], m[5]) for e, m in zip(engines, members)])
+    g = GroupedSweep([(e, m[2], m[3], m[4], m[5]) for e, m in zip(engines, members)], run_flags=run_flags)
     for _ in range(2):
         g.execute()
         _check(members, sem, g.results())
