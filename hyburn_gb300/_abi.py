@@ -325,6 +325,9 @@ def load_library():
         "hb_result_trajectory": (FP, [P, I32, C.POINTER(I64)]),
         "hb_result_bold": (FP, [P, I32, C.POINTER(I64)]),
         "hb_result_free": (None, [P]),
+        "hb_npy_write_f32": (I32, [C.c_char_p, FP, C.POINTER(I64), I32]),
+        "hb_npy_read_f32": (I32, [C.c_char_p, FP, I64, C.POINTER(I64), I32, C.POINTER(I32), C.POINTER(I64)]),
+        "hb_engine_write_tavg": (I32, [P, P, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -32,6 +32,7 @@ UNITS = [
     ("hb_adjoint.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_engine.cu", []),
     ("hb_noalloc.cu", ["--fmad=false"]),
+    ("hb_io.cu", []),
 ]
 
 

@@ -42,6 +42,9 @@ int hb_stream_group_budget_1(int model, int pre);
 int hb_stream_group_budget_2(int model, int pre);
 int hb_stream_group_budget_4(int model, int pre);
 cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st);
+// hb_io.cu
+hb_status hb_io_make_dirs(const std::string& dir);
+hb_status hb_io_write_npy(const std::string& path, const float* data, const std::vector<int64_t>& shape);
 
 namespace {
 
@@ -1470,6 +1473,23 @@ const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
     if (len) *len = (int64_t)r->traj[i].size();
     return r->traj[i].data();
 }
+hb_status hb_engine_write_tavg(const hb_engine* e, const hb_result* r, const char* output_dir) {
+    if (!e || !r || !output_dir) return fail(HB_ERR_INVALID_STATE, "hb_engine_write_tavg: null argument");
+    if (r->tavg.size() > e->subs.size()) return fail(HB_ERR_INVALID_STATE, "result has more subnetworks than the engine");
+    hb_status s = hb_io_make_dirs(output_dir);
+    if (s) return s;
+    for (size_t i = 0; i < r->tavg.size(); i++) {
+        // the shape label [n_sweep, nvar, nnodes*nmodes] of cli.rs:961-970 over data laid out
+        // [n_sweep, nnodes*nmodes, nvar]
+        const std::vector<int64_t> shape = {r->n_sweep, e->subs[i].nvar, e->subs[i].nm};
+        if ((int64_t)r->tavg[i].size() != shape[0] * shape[1] * shape[2])
+            return fail(HB_ERR_INVALID_STATE, "tavg of subnetwork %zu does not match the engine's shape", i);
+        s = hb_io_write_npy(std::string(output_dir) + "/tavg_sub" + std::to_string(i) + ".npy", r->tavg[i].data(), shape);
+        if (s) return s;
+    }
+    return HB_OK;
+}
+
 void hb_result_free(hb_result* r) { delete r; }
 
 }  // extern "C"

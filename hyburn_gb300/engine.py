@@ -13,6 +13,7 @@ fallback: if the library or a GPU is missing, construction raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from itertools import product
 from typing import List, Optional, Sequence, Tuple
@@ -180,14 +181,21 @@ class BatchHybridEngine:
             lib.hb_result_free(r)
 
     def run_sweep(self, param: SweepParam, param_values: Sequence[float], n_steps: int,
-                  noise=None, run_flags: int = 0) -> BatchSweepResult:
-        """BatchHybridEngine::run_sweep (engine.rs:477-484)."""
+                  noise=None, run_flags: int = 0, output_dir: Optional[str] = None) -> BatchSweepResult:
+        """BatchHybridEngine::run_sweep (engine.rs:477-484). With `output_dir`, the library also
+        writes the run's tavg_sub{i}.npy files there (cli.rs:961-970, hb_engine_write_tavg)."""
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
         r = C.c_void_p()
         st = self._lib.hb_engine_run_sweep(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals),
                                            vals.size, int(n_steps), int(run_flags), nptr, nlen, C.byref(r))
         raise_for(st, self._lib.hb_last_error().decode())
+        if output_dir is not None:
+            st = self._lib.hb_engine_write_tavg(self._h, r, os.fsencode(output_dir))
+            if st != _abi.HB_OK:
+                msg = self._lib.hb_last_error().decode()
+                self._lib.hb_result_free(r)
+                raise_for(st, msg)
         return self._result(r, bool(run_flags & _abi.HB_RUN_TRAJECTORY))
 
     def run_sweep_with_trajectory(self, param: SweepParam, param_values, n_steps: int, noise=None,

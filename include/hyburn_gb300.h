@@ -325,6 +325,29 @@ const float* hb_result_trajectory(const hb_result* r, int32_t sub_idx, int64_t* 
 const float* hb_result_bold(const hb_result* r, int32_t monitor_idx, int64_t* len);
 void         hb_result_free(hb_result* r);
 
+/* ---- NPY files (io.rs:19-125) ---- */
+
+/* write_npy_f32 (io.rs:88-125): `ndim` dimensions in `shape`, their product of values from `data`;
+ * version 1.0 header "{'descr': '<f4', 'fortran_order': False, 'shape': (...) }" padded with spaces
+ * to a 64-byte multiple, little-endian f32 values. HB_ERR_IO when the file cannot be written. */
+hb_status hb_npy_write_f32(const char* path, const float* data, const int64_t* shape, int32_t ndim);
+
+/* read_npy_f32 (io.rs:25-83): with out == NULL, a size query (n_values, ndim and up to max_ndim
+ * entries of shape); otherwise also the values into out[capacity]. Descriptors '<f4', '|f4', 'f4'
+ * and '<f8' (rounded to f32); 'fortran_order' is ignored; every whole value after the header is
+ * returned, so n_values can exceed the shape's product when the file has trailing bytes.
+ * HB_ERR_IO when the file cannot be read, HB_ERR_INVALID_STATE for the format errors of the
+ * reference ("Not a valid .npy file", "No 'shape' key in NPY header", "Failed to parse NPY shape",
+ * "Unsupported NPY dtype descriptor", "NPY data truncated (f32|f64)") and for files shorter than
+ * the fixed 10-byte prefix. */
+hb_status hb_npy_read_f32(const char* path, float* out, int64_t capacity, int64_t* shape, int32_t max_ndim,
+                          int32_t* ndim, int64_t* n_values);
+
+/* The batch sweep's output files (cli.rs:947-970): `output_dir` and its parents are created, then
+ * tavg_sub{i}.npy per subnetwork i of the result, labelled [n_sweep, nvar, nnodes*nmodes] over data
+ * laid out [n_sweep, nnodes*nmodes, nvar], as the reference writes them. */
+hb_status hb_engine_write_tavg(const hb_engine* engine, const hb_result* result, const char* output_dir);
+
 #ifdef __cplusplus
 }
 #endif
