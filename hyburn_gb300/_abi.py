@@ -57,6 +57,7 @@ def HB_RUN_STREAM_NPT(n: int) -> int:
 
 HB_RUN_STREAM_PREFETCH = 1 << 27
 HB_RUN_PIPE_WIDE = 1 << 28
+HB_RUN_DEVICE_TRAJECTORY = 1 << 29
 
 
 def HB_RUN_LANES(n: int) -> int:
@@ -282,6 +283,12 @@ class hb_adjoint_out(C.Structure):
                 ("reverse_ms", C.c_float)]
 
 
+class hb_fc_features(C.Structure):
+    _fields_ = [("fc", C.POINTER(C.c_float)), ("features", C.POINTER(C.c_float)), ("fcd", C.POINTER(C.c_float)),
+                ("fcd_stats", C.POINTER(C.c_float)), ("n_windows", C.c_int32), ("nnodes", C.c_int32),
+                ("nvar", C.c_int32), ("ms", C.c_float)]
+
+
 def load_library():
     """Load the in-tree engine library; raises if it has not been built."""
     global _LIB
@@ -328,6 +335,7 @@ def load_library():
         "hb_npy_write_f32": (I32, [C.c_char_p, FP, C.POINTER(I64), I32]),
         "hb_npy_read_f32": (I32, [C.c_char_p, FP, I64, C.POINTER(I64), I32, C.POINTER(I32), C.POINTER(I64)]),
         "hb_engine_write_tavg": (I32, [P, P, C.c_char_p]),
+        "hb_engine_fc_features": (I32, [P, I32, I32, I32, C.POINTER(hb_fc_features)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -33,6 +33,7 @@ UNITS = [
     ("hb_engine.cu", []),
     ("hb_noalloc.cu", ["--fmad=false"]),
     ("hb_io.cu", []),
+    ("hb_features.cu", ["--fmad=false", "-lineinfo"]),
 ]
 
 

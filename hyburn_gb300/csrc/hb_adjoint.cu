@@ -29,6 +29,7 @@
 
 #include "hb_device.h"
 #include "hb_models.cuh"
+#include "hb_moments.cuh"
 
 namespace {
 
@@ -373,7 +374,7 @@ __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, i
 // shift c_i = mean of the first 64 steps, summed in FP32 over chunks of 64 steps and in FP64 across
 // chunks, written per slice; adj_fc_kernel adds the slices and forms FC, the loss and the
 // coefficients of dL/dy. Each thread owns a 4 x 4 tile of the upper triangle of the product matrix.
-constexpr int MOM_CHUNK = 64;
+using hb::MOM_CHUNK;
 
 __device__ __forceinline__ float moment_shift(const AdjArgs& A, int b, int k) {
     const int n0 = A.T < 64 ? A.T : 64;
@@ -385,75 +386,15 @@ __device__ __forceinline__ float moment_shift(const AdjArgs& A, int b, int k) {
 __global__ void adj_moments_kernel(AdjArgs A, double* part, int slices) {
     extern __shared__ __align__(16) float zs[];  // [MOM_CHUNK][W] chunk of y - shift, then shift[W]
     const int b = blockIdx.x, sl = blockIdx.y, N = A.N, T = A.T;
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const int N4 = (N + 3) / 4, W = N4 * 4;
+    const int W = (N + 3) / 4 * 4;
     const int Tc = ((T + slices - 1) / slices + MOM_CHUNK - 1) / MOM_CHUNK * MOM_CHUNK;
     const int t_lo = sl * Tc, t_hi = (t_lo + Tc) < T ? (t_lo + Tc) : T;
     float* shift = zs + MOM_CHUNK * W;
     double* P = part + ((size_t)b * slices + sl) * ((size_t)W * W + W);  // Q [W][W], then S [W]
-    for (int k = tid; k < W; k += nth) shift[k] = k < N ? moment_shift(A, b, k) : 0.0f;
-    double ssum = 0.0;
-    const int n_tiles = N4 * (N4 + 1) / 2;
-    for (int base = 0; base < n_tiles; base += nth) {
-        const int tile = base + tid;
-        int bi = -1, bj = -1;
-        if (tile < n_tiles) {
-            int rem = tile;
-            bi = 0;
-            while (rem >= N4 - bi) { rem -= N4 - bi; bi++; }
-            bj = bi + rem;
-        }
-        double acc[4][4];
-        float part4[4][4];
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-#pragma unroll
-            for (int v = 0; v < 4; v++) acc[u][v] = 0.0;
-        for (int t0 = t_lo; t0 < t_hi; t0 += MOM_CHUNK) {
-            const int nt = (t_hi - t0) < MOM_CHUNK ? (t_hi - t0) : MOM_CHUNK;
-            __syncthreads();
-            for (int q = tid; q < MOM_CHUNK * W; q += nth) {
-                const int tt = q / W, k = q - tt * W;
-                float z = 0.0f;
-                if (tt < nt && k < N) z = A.Y[((size_t)(t0 + tt) * A.B + b) * N + k] - shift[k];
-                zs[q] = z;
-            }
-            __syncthreads();
-            if (base == 0 && tid < N) {
-                float s1 = 0.0f;
-                for (int tt = 0; tt < nt; tt++) s1 += zs[tt * W + tid];
-                ssum += s1;
-            }
-            if (bi < 0) continue;
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) part4[u][v] = 0.0f;
-            for (int tt = 0; tt < nt; tt++) {
-                const float4 zi = *reinterpret_cast<const float4*>(zs + tt * W + bi * 4);
-                const float4 zj = *reinterpret_cast<const float4*>(zs + tt * W + bj * 4);
-                const float ai[4] = {zi.x, zi.y, zi.z, zi.w}, aj[4] = {zj.x, zj.y, zj.z, zj.w};
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) part4[u][v] = __fmaf_rn(ai[u], aj[v], part4[u][v]);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) acc[u][v] += part4[u][v];
-        }
-        if (bi >= 0) {
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) {
-                    P[(size_t)(bi * 4 + u) * W + bj * 4 + v] = acc[u][v];
-                    P[(size_t)(bj * 4 + v) * W + bi * 4 + u] = acc[u][v];
-                }
-        }
-    }
-    if (tid < W) P[(size_t)W * W + tid] = tid < N ? ssum : 0.0;
+    for (int k = threadIdx.x; k < W; k += blockDim.x) shift[k] = k < N ? moment_shift(A, b, k) : 0.0f;
+    const float* Y = A.Y;
+    const int B = A.B;
+    hb::series_moments([=](int t, int k) { return Y[((size_t)t * B + b) * N + k]; }, N, t_lo, t_hi, shift, zs, P);
 }
 
 __global__ void adj_fc_kernel(AdjArgs A, const double* part, int slices) {

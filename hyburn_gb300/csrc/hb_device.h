@@ -163,6 +163,23 @@ struct HbAdjointLaunch {
     double* moments;   // [B][slices][W * W + W] partial moments of y, W = N rounded up to 4
 };
 
+// FC / FCD features of a device trajectory (hb_features.cu); device pointers
+struct HbFeatLaunch {
+    const float* traj;   // [T][B][state_len]
+    int T, B, state_len, off, nnodes, nmodes, nvar;
+    int window, stride, n_windows;  // FCD windows (n_windows >= 2), else n_windows = 0
+    int b0, nb;          // this batch: points b0 .. b0 + nb - 1
+    int fc_slices, win_slices;
+    float* fc;           // [B][nvar][nnodes][nnodes]
+    float* feat;         // [B][nvar][7]: mean, std, min, max, median of FC's upper triangle; homotopic mean, std
+    float* fcd;          // [B][nvar][n_windows][n_windows]
+    float* fcd_stats;    // [B][nvar][5]
+    double* part;        // moments workspace: nb * nvar * max(fc_slices, n_windows * win_slices) * (W * W + W)
+    float* ut;           // nb * nvar * n_windows * nnodes (nnodes - 1) / 2 window-FC upper triangles
+    double* ut_mv;       // nb * nvar * n_windows * 2: mean and centred sum of squares of each
+};
+cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st);
+
 // time slices of the moment pass for B points of T steps: enough blocks to fill the SMs three times
 // over, at most 16, each slice at least 64 steps
 inline int hb_adjoint_moment_slices(int B, int T) {

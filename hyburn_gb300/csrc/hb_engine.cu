@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -265,6 +266,10 @@ struct hb_engine {
     DevNet net;
     DevNet* d_net = nullptr;
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
+    DBuf<float> dtraj;          // HB_RUN_DEVICE_TRAJECTORY: [dtraj_steps][B][state_len] of the last run
+    int64_t dtraj_steps = 0;    // 0: the last run kept no device trajectory
+    DBuf<float> fe_fc, fe_feat, fe_fcd, fe_fcds, fe_ut;  // hb_engine_fc_features outputs and workspace
+    DBuf<double> fe_part, fe_mv;
     // streamed-history kernel: its own ring [B][nm][rp + K][channels]; the layout of the history
     // a run leaves behind (0: time-major ring, 1: streamed) must match the next run's kernel
     DBuf<float> sring;
@@ -494,7 +499,7 @@ struct RunPlan {
     uint32_t run_flags = 0;
     const float* noise_host = nullptr;
     const float* noise_dev = nullptr;
-    bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false;
+    bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false, dev_traj = false;
     int64_t noise_rows_per_step = 0, chunk = 0;
     int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1, pipe_maxt = 512, single_m = 0;
     size_t smem = 0, stream_smem = 0;
@@ -556,7 +561,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     // one warp per point: one subnetwork, one Scalar projection onto itself without delay, no monitors
     int single_m = 0;
     {
-        const bool record_run = (run_flags & HB_RUN_TRAJECTORY) != 0;
+        const bool record_run = (run_flags & (HB_RUN_TRAJECTORY | HB_RUN_DEVICE_TRAJECTORY)) != 0;
         const int n_bold_run = e->bold_removed ? 0 : (int)e->bold.size();
         if (e->subs.size() == 1 && e->projs.size() == 1 && e->kernel_model >= 0 && !(run_flags & HB_RUN_GENERIC) &&
             !record_run && n_bold_run == 0 && e->subs[0].nm <= 128) {
@@ -722,14 +727,28 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     const bool record = (run_flags & HB_RUN_TRAJECTORY) != 0;
     int64_t chunk = n_steps;
     const size_t traj_step_bytes = (size_t)B * e->state_len * 4;
-    if (record) chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, (int64_t)((512ull << 20) / std::max<size_t>(traj_step_bytes, 1))));
+    if (record && !(run_flags & HB_RUN_DEVICE_TRAJECTORY))
+        chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, (int64_t)((512ull << 20) / std::max<size_t>(traj_step_bytes, 1))));
     if (any_stoch && !noise_on_device) {
         const size_t nb = (size_t)noise_rows_per_step * 4;
         chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, (int64_t)((2048ull << 20) / std::max<size_t>(nb, 1))));
     }
     chunk = std::min<int64_t>(chunk, (int64_t)1 << 30);
+    const bool dev_traj = (run_flags & HB_RUN_DEVICE_TRAJECTORY) != 0;
+    if (dev_traj) {
+        const size_t need = (size_t)n_steps * traj_step_bytes;
+        if (e->dtraj.n * 4 < need) {
+            e->dtraj.release();
+            size_t free_b = 0, total_b = 0;
+            CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+            if (need + (256ull << 20) > free_b)
+                return fail(HB_ERR_UNSUPPORTED, "device trajectory needs %.2f GB, %.2f GB free", need / 1e9, free_b / 1e9);
+            CUDA_TRY(e->dtraj.ensure(need / 4));
+        }
+    }
+    e->dtraj_steps = 0;
     if (record && res) {
-        CUDA_TRY(e->traj.ensure((size_t)chunk * B * e->state_len));
+        if (!dev_traj) CUDA_TRY(e->traj.ensure((size_t)chunk * B * e->state_len));
         res->traj.assign(e->subs.size(), std::vector<float>());
         for (size_t i = 0; i < e->subs.size(); i++) res->traj[i].resize((size_t)n_steps * B * e->subs[i].nm * e->subs[i].nvar);
     }
@@ -765,6 +784,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     P.noise_on_device = noise_on_device;
     P.any_stoch = any_stoch;
     P.record = record;
+    P.dev_traj = dev_traj;
     P.bold_pp = bold_pp;
     P.noise_rows_per_step = noise_rows_per_step;
     P.chunk = chunk;
@@ -788,7 +808,7 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
     cudaStream_t st = e->stream();
     const int B = P.B;
     const int64_t n_steps = P.n_steps, chunk = P.chunk, noise_rows_per_step = P.noise_rows_per_step;
-    const bool any_stoch = P.any_stoch, noise_on_device = P.noise_on_device, record = P.record;
+    const bool any_stoch = P.any_stoch, noise_on_device = P.noise_on_device, record = P.record, dev_traj = P.dev_traj;
     const float* noise_dev = P.noise_dev;
     const float* noise_host = P.noise_host;
     const int stream_npt = P.stream_npt, fast = P.fast, pipe = P.pipe;
@@ -811,7 +831,8 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
                 a.noise = e->noise.p;
             }
         }
-        a.traj = record ? e->traj.p : nullptr;
+        float* traj_dst = dev_traj ? e->dtraj.p + (size_t)c0 * B * e->state_len : e->traj.p;
+        a.traj = (record || dev_traj) ? traj_dst : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
         if (P.single_m) CUDA_TRY(hb_launch_single(e->kernel_model, P.single_m, e->d_net, a, B, st));
         else if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
@@ -824,7 +845,7 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         e->last_launches++;
         if (record) {
             traj_host.resize((size_t)n * B * e->state_len);
-            CUDA_TRY(cudaMemcpyAsync(traj_host.data(), e->traj.p, traj_host.size() * 4, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaMemcpyAsync(traj_host.data(), traj_dst, traj_host.size() * 4, cudaMemcpyDeviceToHost, st));
         }
         CUDA_TRY(cudaEventSynchronize(e->ev1));
         float ms = 0;
@@ -844,6 +865,7 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         }
     }
     e->last_ms = kernel_ms_total;
+    e->dtraj_steps = dev_traj ? n_steps : 0;
     return HB_OK;
 }
 
@@ -1315,7 +1337,9 @@ void hb_engine_destroy(hb_engine* e) {
     for (auto& b : e->d_params) b.release();
     for (auto& bh : e->bold) { bh.bw.release(); bh.acc.release(); bh.win.release(); bh.out_run.release(); bh.emit.release(); }
     e->state.release(); e->x0.release(); e->tavg.release(); e->ring.release(); e->noise.release(); e->prep_noise.release();
-    e->traj.release();
+    e->traj.release(); e->dtraj.release();
+    e->fe_fc.release(); e->fe_feat.release(); e->fe_fcd.release(); e->fe_fcds.release(); e->fe_ut.release();
+    e->fe_part.release(); e->fe_mv.release();
     e->means.release(); e->flags_buf.release();
     if (e->d_net) cudaFree(e->d_net);
     if (e->ev0) cudaEventDestroy(e->ev0);
@@ -1473,6 +1497,81 @@ const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
     if (len) *len = (int64_t)r->traj[i].size();
     return r->traj[i].data();
 }
+hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_len, int32_t stride, hb_fc_features* out) {
+    if (!e || !out) return fail(HB_ERR_INVALID_STATE, "hb_engine_fc_features: null argument");
+    if (sub_idx < 0 || sub_idx >= (int32_t)e->subs.size()) return fail(HB_ERR_INVALID_STATE, "subnetwork index %d out of range", sub_idx);
+    const int64_t T64 = e->dtraj_steps;
+    if (T64 < 1) return fail(HB_ERR_INVALID_STATE, "the last run kept no device trajectory (run with HB_RUN_DEVICE_TRAJECTORY)");
+    if (T64 > INT32_MAX / 2) return fail(HB_ERR_UNSUPPORTED, "device trajectory of %lld steps is too long for the features", (long long)T64);
+    const int T = (int)T64;
+    const HostSub& sb = e->subs[sub_idx];
+    const int N = sb.nnodes, nvar = sb.nvar, B = e->B;
+    if (N > 1024) return fail(HB_ERR_UNSUPPORTED, "FC features support up to 1024 nodes, got %d", N);
+    int nw = 0;
+    if (window_len != 0) {
+        if (window_len < 2 || window_len > T) return fail(HB_ERR_INVALID_STATE, "window_len must be in [2, n_steps]");
+        if (stride < 1) return fail(HB_ERR_INVALID_STATE, "stride must be > 0");
+        nw = (T - window_len) / stride + 1;
+        if (nw <= 1) nw = 0;
+        if (nw > 32768) return fail(HB_ERR_UNSUPPORTED, "%d FCD windows; at most 32768 are supported", nw);
+    }
+    if (!out->fc && !out->features && !out->fcd && !out->fcd_stats) {  // size query
+        out->n_windows = nw; out->nnodes = N; out->nvar = nvar; out->ms = 0.0f;
+        return HB_OK;
+    }
+    const size_t W = (size_t)(N + 3) / 4 * 4, pl = W * W + W, n_ut = (size_t)N * (N - 1) / 2;
+    // points per batch: moments and window workspaces within 1 GiB
+    const int fc_sl_full = hb_adjoint_moment_slices(B * nvar, T);
+    const size_t per_point = (size_t)nvar * (std::max<size_t>(16, (size_t)std::max(nw, 1) * 8) * pl * 8 + (size_t)nw * (n_ut * 4 + 16));
+    const int nb = (int)std::max<size_t>(1, std::min<size_t>((size_t)B, (1ull << 30) / std::max<size_t>(per_point, 1)));
+    CUDA_TRY(e->fe_fc.ensure((size_t)B * nvar * N * N));
+    CUDA_TRY(e->fe_feat.ensure((size_t)B * nvar * 7));
+    CUDA_TRY(e->fe_fcd.ensure((size_t)B * nvar * std::max(nw, 1) * std::max(nw, 1)));
+    CUDA_TRY(e->fe_fcds.ensure((size_t)B * nvar * 5));
+    HbFeatLaunch L;
+    memset(&L, 0, sizeof L);
+    L.traj = e->dtraj.p; L.T = T; L.B = B; L.state_len = e->state_len; L.off = e->net.sub[sub_idx].state_off;
+    L.nnodes = N; L.nmodes = sb.nmodes; L.nvar = nvar;
+    L.window = window_len; L.stride = stride; L.n_windows = nw;
+    L.fc = e->fe_fc.p; L.feat = e->fe_feat.p; L.fcd = e->fe_fcd.p; L.fcd_stats = e->fe_fcds.p;
+    // slices: enough blocks to fill the SMs, each slice at least 64 steps
+    L.fc_slices = std::max(1, std::min(fc_sl_full, std::max(1, T / 64)));
+    L.win_slices = nw ? std::max(1, std::min({8, (456 + nb * nvar * nw - 1) / (nb * nvar * nw), std::max(1, window_len / 64),
+                                              65535 / nw})) : 1;
+    const size_t part_n = (size_t)nb * nvar * std::max<size_t>((size_t)L.fc_slices, (size_t)nw * L.win_slices) * pl;
+    CUDA_TRY(e->fe_part.ensure(part_n));
+    L.part = e->fe_part.p;
+    if (nw) {
+        CUDA_TRY(e->fe_ut.ensure((size_t)nb * nvar * nw * std::max<size_t>(n_ut, 1)));
+        CUDA_TRY(e->fe_mv.ensure((size_t)nb * nvar * nw * 2));
+        L.ut = e->fe_ut.p;
+        L.ut_mv = e->fe_mv.p;
+    }
+    cudaStream_t st = e->stream();
+    CUDA_TRY(cudaEventRecord(e->ev0, st));
+    for (int b0 = 0; b0 < B; b0 += nb) {
+        L.b0 = b0;
+        L.nb = std::min(nb, B - b0);
+        CUDA_TRY(hb_launch_fc_features(L, st));
+    }
+    CUDA_TRY(cudaEventRecord(e->ev1, st));
+    const size_t nbv = (size_t)B * nvar;
+    if (out->fc) CUDA_TRY(cudaMemcpyAsync(out->fc, e->fe_fc.p, nbv * N * N * 4, cudaMemcpyDeviceToHost, st));
+    if (out->features) CUDA_TRY(cudaMemcpyAsync(out->features, e->fe_feat.p, nbv * 7 * 4, cudaMemcpyDeviceToHost, st));
+    if (out->fcd && nw) CUDA_TRY(cudaMemcpyAsync(out->fcd, e->fe_fcd.p, nbv * nw * nw * 4, cudaMemcpyDeviceToHost, st));
+    if (out->fcd_stats && nw) CUDA_TRY(cudaMemcpyAsync(out->fcd_stats, e->fe_fcds.p, nbv * 5 * 4, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (out->fcd_stats && !nw)
+        for (size_t i = 0; i < nbv * 5; i++) out->fcd_stats[i] = std::numeric_limits<float>::quiet_NaN();
+    float ms = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    out->ms = ms;
+    out->n_windows = nw;
+    out->nnodes = N;
+    out->nvar = nvar;
+    return HB_OK;
+}
+
 hb_status hb_engine_write_tavg(const hb_engine* e, const hb_result* r, const char* output_dir) {
     if (!e || !r || !output_dir) return fail(HB_ERR_INVALID_STATE, "hb_engine_write_tavg: null argument");
     if (r->tavg.size() > e->subs.size()) return fail(HB_ERR_INVALID_STATE, "result has more subnetworks than the engine");

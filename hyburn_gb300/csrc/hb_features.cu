@@ -1,0 +1,277 @@
+// hb_features.cu — functional-connectivity features of a trajectory kept in device memory
+// (HB_RUN_DEVICE_TRAJECTORY), so that no step's state crosses to the host: the FeatureSet::Fc arm
+// of sbi/features/mod.rs:257-280 and sbi/features/fc.rs:11-186.
+//
+// For every sweep point b and state variable v, the node series is the mean over modes,
+//     y_n(t) = (sum_m x[t][b][n * nmodes + m][v]) / nmodes   (f32, modes in order, mod.rs:262-271),
+// and
+//   FC       Pearson correlation over all steps (fc.rs:11-58): means and deviations over T (not
+//            T - 1), a deviation below 1e-12 replaced by 1, every entry (the diagonal included)
+//            cov / (sd_i sd_j) clamped to [-1, 1];
+//   features fc_stats of FC's upper triangle (mean, std, min, max, median; fc.rs:62-83) and the
+//            homotopic mean and std of FC[i][N-1-i] (fc.rs:189-203): 7 values per (b, v);
+//   FCD      FC of each window [w * stride, w * stride + window) (fc.rs:87-141), then the Pearson
+//            correlation of every pair of window FCs' upper triangles (fc.rs:144-179), diagonal 1;
+//            and fc_stats of that matrix (fc.rs:182-187).
+// Moments use hb::series_moments (FP32 sums over chunks of steps, FP64 across chunks) on the series
+// shifted by the FP64 mean of the range's first 64 steps rounded to f32, so that a constant series
+// gives exactly zero deviation, as in the reference. The statistics use the reference's f32
+// summation order (one thread); the median is the k-th smallest value, found by bisection on the
+// values' ordered bit patterns.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "hb_device.h"
+#include "hb_moments.cuh"
+
+namespace {
+
+__device__ __forceinline__ float series_value(const HbFeatLaunch& L, int t, int b, int v, int n) {
+    const float* x = L.traj + ((size_t)t * L.B + b) * L.state_len + L.off + (size_t)n * L.nmodes * L.nvar + v;
+    float s = 0.0f;
+    for (int m = 0; m < L.nmodes; m++) s += x[(size_t)m * L.nvar];
+    return s / (float)L.nmodes;
+}
+
+// moments of range r = blockIdx.y / slices ([r * stride, r * stride + len)), slice blockIdx.y % slices,
+// of point-variable blockIdx.x of the batch
+template <int CHUNK, int MAXT>
+__global__ void __launch_bounds__(MAXT) feat_moments_kernel(HbFeatLaunch L, int n_ranges, int stride, int len,
+                                                            int slices) {
+    extern __shared__ __align__(16) float zs[];  // [CHUNK][W] chunk of y - shift, then shift[W]
+    const int bv = blockIdx.x, b = L.b0 + bv / L.nvar, v = bv - (bv / L.nvar) * L.nvar;
+    const int r = blockIdx.y / slices, sl = blockIdx.y - r * slices;
+    const int N = L.nnodes, W = (N + 3) / 4 * 4;
+    const int start = r * stride;
+    const int Tc = ((len + slices - 1) / slices + CHUNK - 1) / CHUNK * CHUNK;
+    const int t_lo = start + sl * Tc, t_end = start + len;
+    const int t_hi = (t_lo + Tc) < t_end ? (t_lo + Tc) : t_end;
+    float* shift = zs + CHUNK * W;
+    const int n0 = len < 64 ? len : 64;
+    for (int k = threadIdx.x; k < W; k += blockDim.x) {
+        double c = 0.0;
+        if (k < N) {
+            for (int t = 0; t < n0; t++) c += (double)series_value(L, start + t, b, v, k);
+            c /= n0;
+        }
+        shift[k] = (float)c;
+    }
+    double* P = L.part + (((size_t)bv * n_ranges + r) * slices + sl) * ((size_t)W * W + W);
+    hb::series_moments<CHUNK>([&](int t, int k) { return series_value(L, t, b, v, k); }, N, t_lo, t_hi, shift, zs, P);
+}
+
+// FC of range blockIdx.y from its slices' moments: the full matrix into `full` and / or the upper
+// triangle (row-major, i < j) into `ut`
+__global__ void feat_corr_kernel(HbFeatLaunch L, int n_ranges, int len, int slices, float* full, float* ut) {
+    extern __shared__ __align__(16) double ms[];  // mean [W], sd [W]
+    const int bv = blockIdx.x, r = blockIdx.y;
+    const int N = L.nnodes, W = (N + 3) / 4 * 4;
+    const size_t pl = (size_t)W * W + W;
+    const double* P0 = L.part + ((size_t)bv * n_ranges + r) * slices * pl;
+    double* mean = ms;
+    double* sd = ms + W;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int q = 0; q < slices; q++) {
+            s1 += P0[q * pl + (size_t)W * W + k];
+            s2 += P0[q * pl + (size_t)k * W + k];
+        }
+        const double m = s1 / len, var = s2 / len - m * m;
+        double d = sqrt(var > 0.0 ? var : 0.0);
+        if (d < 1e-12) d = 1.0;  // constant series (fc.rs:35-37)
+        mean[k] = m;
+        sd[k] = d;
+    }
+    __syncthreads();
+    const size_t rr = (size_t)bv * n_ranges + r;
+    const size_t n_ut = (size_t)N * (N - 1) / 2;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int i = q / N, j = q - (q / N) * N;
+        double qs = 0.0;
+        for (int s = 0; s < slices; s++) qs += P0[s * pl + (size_t)i * W + j];
+        const double cov = qs / len - mean[i] * mean[j];
+        double c = cov / (sd[i] * sd[j]);
+        c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+        const float f = (float)c;
+        if (full) full[rr * N * N + q] = f;
+        if (ut && i < j) ut[rr * n_ut + (size_t)i * N - (size_t)i * (i + 1) / 2 + (j - i - 1)] = f;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T block_sum(T x, T* red) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[w] = x;
+    __syncthreads();
+    T s = 0;
+    for (int i = 0; i < nw; i++) s += red[i];
+    return s;
+}
+
+// mean and centred sum of squares of each window FC's upper triangle (FP64)
+__global__ void feat_ut_moments_kernel(HbFeatLaunch L) {
+    __shared__ double red[32];
+    const size_t n_ut = (size_t)L.nnodes * (L.nnodes - 1) / 2;
+    const size_t w = (size_t)blockIdx.x * L.n_windows + blockIdx.y;
+    const float* a = L.ut + w * n_ut;
+    double s = 0.0;
+    for (size_t k = threadIdx.x; k < n_ut; k += blockDim.x) s += (double)a[k];
+    const double m = block_sum(s, red) / (double)n_ut;
+    double q = 0.0;
+    for (size_t k = threadIdx.x; k < n_ut; k += blockDim.x) {
+        const double d = (double)a[k] - m;
+        q += d * d;
+    }
+    const double qq = block_sum(q, red);
+    if (threadIdx.x == 0) { L.ut_mv[2 * w] = m; L.ut_mv[2 * w + 1] = qq; }
+}
+
+// row i = blockIdx.y of the FCD matrix of point-variable blockIdx.x (fc.rs:130-139, 144-179)
+__global__ void feat_fcd_kernel(HbFeatLaunch L) {
+    __shared__ double red[32];
+    const int nw = L.n_windows, i = blockIdx.y, bv = blockIdx.x;
+    const size_t n_ut = (size_t)L.nnodes * (L.nnodes - 1) / 2;
+    const float* ai = L.ut + ((size_t)bv * nw + i) * n_ut;
+    const double mi = L.ut_mv[2 * ((size_t)bv * nw + i)], vi = L.ut_mv[2 * ((size_t)bv * nw + i) + 1];
+    float* F = L.fcd + ((size_t)L.b0 * L.nvar + bv) * nw * nw;
+    if (threadIdx.x == 0) F[(size_t)i * nw + i] = 1.0f;
+    for (int j = i + 1; j < nw; j++) {
+        const float* aj = L.ut + ((size_t)bv * nw + j) * n_ut;
+        const double mj = L.ut_mv[2 * ((size_t)bv * nw + j)], vj = L.ut_mv[2 * ((size_t)bv * nw + j) + 1];
+        double c = 0.0;
+        for (size_t k = threadIdx.x; k < n_ut; k += blockDim.x) c += ((double)ai[k] - mi) * ((double)aj[k] - mj);
+        c = block_sum(c, red);
+        if (threadIdx.x == 0) {
+            double r = 0.0;
+            if (vi > 0.0 && vj > 0.0) {
+                r = c / (sqrt(vi) * sqrt(vj));
+                r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+            }
+            F[(size_t)i * nw + j] = (float)r;
+            F[(size_t)j * nw + i] = (float)r;
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t order_key(float x) {
+    const uint32_t u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float key_value(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// fc_stats (fc.rs:62-83) of the upper triangle of the n x n matrix blockIdx.x of `mats` into
+// stats[blockIdx.x * sstride .. + 5], and, when homo is set, homotopic_fc (fc.rs:189-203) into
+// homo[blockIdx.x * sstride .. + 2]
+__global__ void feat_stats_kernel(const float* mats, int n, float* stats, int sstride, float* homo) {
+    __shared__ int cnt_red[32];
+    const float* M = mats + (size_t)blockIdx.x * n * n;
+    float* S = stats + (size_t)blockIdx.x * sstride;
+    const long long nut = (long long)n * (n - 1) / 2;
+    const float qnan = __int_as_float(0x7fc00000);
+    if (nut == 0) {
+        if (threadIdx.x < 5) S[threadIdx.x] = qnan;
+    } else {
+        if (threadIdx.x == 0) {
+            float sum = 0.0f, mn = __int_as_float(0x7f800000), mx = -__int_as_float(0x7f800000);
+            for (int i = 0; i < n; i++)
+                for (int j = i + 1; j < n; j++) {
+                    const float x = M[(size_t)i * n + j];
+                    sum += x;
+                    mn = fminf(mn, x);
+                    mx = fmaxf(mx, x);
+                }
+            const float mean = sum / (float)nut;
+            float var = 0.0f;
+            for (int i = 0; i < n; i++)
+                for (int j = i + 1; j < n; j++) {
+                    const float d = M[(size_t)i * n + j] - mean;
+                    var += d * d;
+                }
+            var = var / (float)nut;
+            S[0] = mean;
+            S[1] = sqrtf(var);
+            S[2] = mn;
+            S[3] = mx;
+        }
+        __syncthreads();
+        // median: sorted[nut / 2], the smallest key whose count of keys <= it exceeds nut / 2
+        const long long k = nut / 2;
+        uint32_t lo = 0u, hi = 0xffffffffu;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            int c = 0;
+            for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
+                const int i = (int)(q / n), j = (int)(q - (q / n) * n);
+                if (i < j && order_key(M[q]) <= mid) c++;
+            }
+            const long long total = block_sum<int>(c, cnt_red);
+            if (total > k) hi = mid;
+            else lo = mid + 1;
+        }
+        if (threadIdx.x == 0) S[4] = key_value(lo);
+    }
+    if (homo && threadIdx.x == 0) {
+        float* H = homo + (size_t)blockIdx.x * sstride;
+        const int np = n / 2;
+        if (np == 0) { H[0] = qnan; H[1] = qnan; }
+        else {
+            float sum = 0.0f;
+            for (int i = 0; i < np; i++) sum += M[(size_t)i * n + (n - 1 - i)];
+            const float mean = sum / (float)np;
+            float var = 0.0f;
+            for (int i = 0; i < np; i++) {
+                const float d = M[(size_t)i * n + (n - 1 - i)] - mean;
+                var += d * d;
+            }
+            H[0] = mean;
+            H[1] = sqrtf(var / (float)np);
+        }
+    }
+}
+
+template <int CHUNK, int MAXT>
+cudaError_t launch_moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, int slices, cudaStream_t st) {
+    const int W = (L.nnodes + 3) / 4 * 4;
+    const size_t sm = ((size_t)CHUNK + 1) * W * sizeof(float) + 16;
+    cudaError_t e = cudaFuncSetAttribute(feat_moments_kernel<CHUNK, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const int n4 = W / 4, tiles = n4 * (n4 + 1) / 2;
+    int threads = MAXT;
+    if (MAXT == 512 && tiles <= 256 && L.nnodes <= 256) threads = 256;
+    feat_moments_kernel<CHUNK, MAXT><<<dim3(L.nb * L.nvar, n_ranges * slices), threads, sm, st>>>(L, n_ranges, stride, len, slices);
+    return cudaGetLastError();
+}
+
+cudaError_t moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, int slices, cudaStream_t st) {
+    if (L.nnodes <= 512) return launch_moments<64, 512>(L, n_ranges, stride, len, slices, st);
+    return launch_moments<32, 1024>(L, n_ranges, stride, len, slices, st);
+}
+
+}  // namespace
+
+cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st) {
+    const int N = L.nnodes, W = (N + 3) / 4 * 4, nbv = L.nb * L.nvar;
+    if (N < 1 || N > 1024) return cudaErrorInvalidValue;
+    cudaError_t e;
+    // static FC over all steps, its statistics and homotopic values
+    if ((e = moments(L, 1, 0, L.T, L.fc_slices, st)) != cudaSuccess) return e;
+    float* fc_b = L.fc + (size_t)L.b0 * L.nvar * N * N;
+    feat_corr_kernel<<<dim3(nbv, 1), 256, 2 * W * sizeof(double), st>>>(L, 1, L.T, L.fc_slices, fc_b, nullptr);
+    feat_stats_kernel<<<nbv, 256, 0, st>>>(fc_b, N, L.feat + (size_t)L.b0 * L.nvar * 7, 7, L.feat + (size_t)L.b0 * L.nvar * 7 + 5);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (L.n_windows < 2) return cudaSuccess;
+    // FCD: window FCs, their pairwise correlations, statistics
+    const int nw = L.n_windows;
+    if ((e = moments(L, nw, L.stride, L.window, L.win_slices, st)) != cudaSuccess) return e;
+    feat_corr_kernel<<<dim3(nbv, nw), 256, 2 * W * sizeof(double), st>>>(L, nw, L.window, L.win_slices, nullptr, L.ut);
+    feat_ut_moments_kernel<<<dim3(nbv, nw), 256, 0, st>>>(L);
+    feat_fcd_kernel<<<dim3(nbv, nw), 256, 0, st>>>(L);
+    feat_stats_kernel<<<nbv, 256, 0, st>>>(L.fcd + (size_t)L.b0 * L.nvar * nw * nw, nw,
+                                            L.fcd_stats + (size_t)L.b0 * L.nvar * 5, 5, nullptr);
+    return cudaGetLastError();
+}

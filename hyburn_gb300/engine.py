@@ -104,6 +104,18 @@ def noise_shape(config: SimConfig, n_steps: int, n_sweep: int, semantics: int = 
 
 
 @dataclass
+class FcFeatures:
+    """Functional-connectivity features of a device-resident trajectory (hb_engine_fc_features;
+    sbi/features/fc.rs, mod.rs:257-280)."""
+    fc: np.ndarray                   # [n_sweep, nvar, nnodes, nnodes]
+    features: np.ndarray             # [n_sweep, nvar, 7]: mean, std, min, max, median, homotopic mean, std
+    fcd: Optional[np.ndarray]        # [n_sweep, nvar, n_windows, n_windows] or None
+    fcd_stats: Optional[np.ndarray]  # [n_sweep, nvar, 5] (NaN when there is no FCD) or None
+    n_windows: int
+    ms: float
+
+
+@dataclass
 class AdjointResult:
     """Loss and gradients of a functional-connectivity fit (hb_engine_adjoint_fc)."""
     loss: np.ndarray          # [n_sweep]
@@ -238,6 +250,25 @@ class BatchHybridEngine:
     def set_stream(self, stream_handle: Optional[int]) -> None:
         raise_for(self._lib.hb_engine_set_stream(self._h, C.c_void_p(stream_handle or 0)),
                   self._lib.hb_last_error().decode())
+
+    def fc_features(self, sub_idx: int = 0, window_len: int = 0, stride: int = 1) -> FcFeatures:
+        """FC, FC statistics and, with window_len > 0, FCD of the last run's trajectory, which must
+        have been kept on the device (run_flags HB_RUN_DEVICE_TRAJECTORY); computed on the GPU."""
+        q = _abi.hb_fc_features()
+        st = self._lib.hb_engine_fc_features(self._h, int(sub_idx), int(window_len), int(stride), C.byref(q))
+        raise_for(st, self._lib.hb_last_error().decode())
+        B, N, nvar, nw = self.n_sweep, q.nnodes, q.nvar, q.n_windows
+        fc = np.empty((B, nvar, N, N), np.float32)
+        feat = np.empty((B, nvar, 7), np.float32)
+        fcd = np.empty((B, nvar, max(nw, 1), max(nw, 1)), np.float32)
+        fcds = np.empty((B, nvar, 5), np.float32)
+        out = _abi.hb_fc_features()
+        out.fc, out.features = _abi.f32p(fc), _abi.f32p(feat)
+        out.fcd, out.fcd_stats = _abi.f32p(fcd), _abi.f32p(fcds)
+        st = self._lib.hb_engine_fc_features(self._h, int(sub_idx), int(window_len), int(stride), C.byref(out))
+        raise_for(st, self._lib.hb_last_error().decode())
+        return FcFeatures(fc=fc, features=feat, fcd=fcd if nw else None, fcd_stats=fcds if window_len else None,
+                          n_windows=int(nw), ms=float(out.ms))
 
     def adjoint_fc(self, gain_values, n_steps: int, target_fc, checkpoint_every: int = 500,
                    return_y: bool = False) -> AdjointResult:

@@ -89,6 +89,10 @@ typedef int32_t hb_status;
 #define HB_RUN_STREAM_PREFETCH (1u << 27)
 /* warp-specialised pipeline: use its 1024-thread form (room for eight producer threads per node) */
 #define HB_RUN_PIPE_WIDE      (1u << 28)
+/* keep every step's state of the run in device memory ([n_steps][n_sweep][state]) for
+ * hb_engine_fc_features, with no host copy (the reference copies each step to the host,
+ * engine.rs:779-782); HB_ERR_UNSUPPORTED when it does not fit the device's free memory */
+#define HB_RUN_DEVICE_TRAJECTORY (1u << 29)
 /* resident kernel: threads per node sharing its edge list (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_LANES(n) ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : 0) << 12)
 
@@ -312,6 +316,29 @@ typedef struct hb_adjoint_out {
 } hb_adjoint_out;
 hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,
                                const float* target_fc, int32_t checkpoint_every, hb_adjoint_out* out);
+
+/* ---- functional-connectivity features on the device (sbi/features/fc.rs, mod.rs:257-280) ----
+ * From the trajectory of the engine's last run, which must have used HB_RUN_DEVICE_TRAJECTORY, for
+ * every sweep point and state variable of subnetwork sub_idx: the node series (mean over modes)
+ * over all the run's steps, its FC matrix (fc_matrix, fc.rs:11-58), the FeatureSet::Fc values
+ * (fc_stats of FC's upper triangle: mean, std, min, max, median; homotopic mean and std), and, with
+ * window_len > 0, the FCD matrix of windows [w * stride, w * stride + window_len) (fcd_matrix,
+ * fc.rs:87-141) and its fc_stats. n_windows = (n_steps - window_len) / stride + 1, reported as 0
+ * (FCD empty, fcd_stats NaN) when it is 1. window_len outside [2, n_steps] or stride < 1 (assertion
+ * failures in the reference) return HB_ERR_INVALID_STATE. Any output pointer may be NULL; with all
+ * four NULL the call only validates and reports n_windows, nnodes and nvar (a size query). */
+typedef struct hb_fc_features {
+    float*  fc;          /* [n_sweep][nvar][nnodes][nnodes] */
+    float*  features;    /* [n_sweep][nvar][7] */
+    float*  fcd;         /* [n_sweep][nvar][n_windows][n_windows] */
+    float*  fcd_stats;   /* [n_sweep][nvar][5] */
+    int32_t n_windows;   /* out */
+    int32_t nnodes;      /* out */
+    int32_t nvar;        /* out */
+    float   ms;          /* out: device time of the feature kernels */
+} hb_fc_features;
+hb_status hb_engine_fc_features(hb_engine* engine, int32_t sub_idx, int32_t window_len, int32_t stride,
+                                hb_fc_features* out);
 
 /* ---- results: BatchSweepResult (engine.rs:15-31) ---- */
 int32_t      hb_result_n_sweep(const hb_result* r);
