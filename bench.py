@@ -401,6 +401,48 @@ def run_other_workload(args):
                         roofline={"bound": "hbm", "achieved": bytes_ / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": bytes_ / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bytes_ / ns, "traffic": None})
+        elif args.workload == "fc":
+            # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
+            # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
+            # 500), against the same run streaming its trajectory to the host (the reference's per-step copy)
+            from hyburn_gb300._abi import HB_RUN_DEVICE_TRAJECTORY, HB_RUN_TRAJECTORY
+            T = args.run_steps or 20_000
+            W, S = min(2000, T // 2), max(1, min(500, T // 8))
+            cfg, meta, noise = workload(T)
+            eng = BatchHybridEngine.from_config(cfg, N_POINTS, semantics=HB_SEM_DELAY_RING)
+            eng.prepare(SweepParam(-1, 0), meta["values"], T, noise=noise, run_flags=HB_RUN_DEVICE_TRAJECTORY)
+            flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+            for _ in range(args.warmup):
+                eng.execute_prepared()
+                eng.fc_features(0, W, S)
+            run_ms, feat_ms, wall = [], [], []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                eng.execute_prepared()
+                f = eng.fc_features(0, W, S)
+                wall.append((time.perf_counter() - t0) * 1e3)
+                run_ms.append(eng.last_kernel_time()[0])
+                feat_ms.append(f.ms)
+            eng2 = BatchHybridEngine.from_config(cfg, N_POINTS, semantics=HB_SEM_DELAY_RING)
+            eng2.run_sweep(SweepParam(-1, 0), meta["values"], min(T, 2000), noise=noise[:min(T, 2000)],
+                           run_flags=HB_RUN_TRAJECTORY)
+            eng2.reset()
+            t0 = time.perf_counter()
+            eng2.run_sweep(SweepParam(-1, 0), meta["values"], T, noise=noise, run_flags=HB_RUN_TRAJECTORY)
+            host_traj_ms = (time.perf_counter() - t0) * 1e3
+            ms = statistics.median(run_ms) + statistics.median(feat_ms)
+            ns = N_POINTS * N_NODES * T
+            line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+                        config={"workload": f"g2do-74n-128pt-csr20pct-per-edge-delays-heun-stochastic-{T}steps"
+                                            f"-device-trajectory-fc-fcd-w{W}-s{S}", "n_windows": f.n_windows},
+                        fc={"run_ms": statistics.median(run_ms), "features_ms": statistics.median(feat_ms),
+                            "wall_ms_run_plus_features_with_d2h_of_features": statistics.median(wall),
+                            "host_trajectory_run_ms": host_traj_ms,
+                            "trajectory_bytes": T * N_POINTS * N_NODES * 2 * 4})
+            eng.close()
+            eng2.close()
         else:
             # adjoint: JR 74 nodes x 64 points, Sigmoidal delayed CSR coupling, Heun dt 0.1, 20 000 steps,
             # FC loss of y1 - y2; gradients w.r.t. the coupling gain and per-node A, B, a
@@ -444,7 +486,7 @@ def main():
     ap.add_argument("--two-phase", action="store_true", help="batch each block's gathers before its updates")
     ap.add_argument("--no-pipe", action="store_true", help="do not use the warp-specialised pipeline")
     ap.add_argument("--pipe-lanes", type=int, default=0, help="pipeline producer threads per node (0: engine's choice)")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto"],
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "fc"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()

@@ -1520,10 +1520,14 @@ hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_le
         return HB_OK;
     }
     const size_t W = (size_t)(N + 3) / 4 * 4, pl = W * W + W, n_ut = (size_t)N * (N - 1) / 2;
-    // points per batch: moments and window workspaces within 1 GiB
-    const int fc_sl_full = hb_adjoint_moment_slices(B * nvar, T);
-    const size_t per_point = (size_t)nvar * (std::max<size_t>(16, (size_t)std::max(nw, 1) * 8) * pl * 8 + (size_t)nw * (n_ut * 4 + 16));
-    const int nb = (int)std::max<size_t>(1, std::min<size_t>((size_t)B, (1ull << 30) / std::max<size_t>(per_point, 1)));
+    // slices of the moment passes: enough blocks to fill the SMs, each slice at least 64 steps
+    const int fc_slices = std::max(1, std::min(hb_adjoint_moment_slices(B * nvar, T), std::max(1, T / 64)));
+    const int win_slices = nw ? std::max(1, std::min({8, (456 + B * nvar * nw - 1) / (B * nvar * nw),
+                                                      std::max(1, window_len / 64), 65535 / nw})) : 1;
+    // points per batch: moments and window workspaces within 4 GiB
+    const size_t per_point = (size_t)nvar * (std::max<size_t>((size_t)fc_slices, (size_t)nw * win_slices) * pl * 8 +
+                                             (size_t)nw * (n_ut * 4 + 16));
+    const int nb = (int)std::max<size_t>(1, std::min<size_t>((size_t)B, (4ull << 30) / std::max<size_t>(per_point, 1)));
     CUDA_TRY(e->fe_fc.ensure((size_t)B * nvar * N * N));
     CUDA_TRY(e->fe_feat.ensure((size_t)B * nvar * 7));
     CUDA_TRY(e->fe_fcd.ensure((size_t)B * nvar * std::max(nw, 1) * std::max(nw, 1)));
@@ -1534,10 +1538,8 @@ hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_le
     L.nnodes = N; L.nmodes = sb.nmodes; L.nvar = nvar;
     L.window = window_len; L.stride = stride; L.n_windows = nw;
     L.fc = e->fe_fc.p; L.feat = e->fe_feat.p; L.fcd = e->fe_fcd.p; L.fcd_stats = e->fe_fcds.p;
-    // slices: enough blocks to fill the SMs, each slice at least 64 steps
-    L.fc_slices = std::max(1, std::min(fc_sl_full, std::max(1, T / 64)));
-    L.win_slices = nw ? std::max(1, std::min({8, (456 + nb * nvar * nw - 1) / (nb * nvar * nw), std::max(1, window_len / 64),
-                                              65535 / nw})) : 1;
+    L.fc_slices = fc_slices;
+    L.win_slices = win_slices;
     const size_t part_n = (size_t)nb * nvar * std::max<size_t>((size_t)L.fc_slices, (size_t)nw * L.win_slices) * pl;
     CUDA_TRY(e->fe_part.ensure(part_n));
     L.part = e->fe_part.p;

@@ -11,7 +11,8 @@
 //   features fc_stats of FC's upper triangle (mean, std, min, max, median; fc.rs:62-83) and the
 //            homotopic mean and std of FC[i][N-1-i] (fc.rs:189-203): 7 values per (b, v);
 //   FCD      FC of each window [w * stride, w * stride + window) (fc.rs:87-141), then the Pearson
-//            correlation of every pair of window FCs' upper triangles (fc.rs:144-179), diagonal 1;
+//            correlation of every pair of window FCs' upper triangles (fc.rs:144-179; FP32
+//            products of the centred values, summed in FP64), diagonal 1;
 //            and fc_stats of that matrix (fc.rs:182-187).
 // Moments use hb::series_moments (FP32 sums over chunks of steps, FP64 across chunks) on the series
 // shifted by the FP64 mean of the range's first 64 steps rounded to f32, so that a constant series
@@ -26,17 +27,10 @@
 
 namespace {
 
-__device__ __forceinline__ float series_value(const HbFeatLaunch& L, int t, int b, int v, int n) {
-    const float* x = L.traj + ((size_t)t * L.B + b) * L.state_len + L.off + (size_t)n * L.nmodes * L.nvar + v;
-    float s = 0.0f;
-    for (int m = 0; m < L.nmodes; m++) s += x[(size_t)m * L.nvar];
-    return s / (float)L.nmodes;
-}
-
 // moments of range r = blockIdx.y / slices ([r * stride, r * stride + len)), slice blockIdx.y % slices,
 // of point-variable blockIdx.x of the batch
 template <int CHUNK, int MAXT>
-__global__ void __launch_bounds__(MAXT) feat_moments_kernel(HbFeatLaunch L, int n_ranges, int stride, int len,
+__global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) feat_moments_kernel(HbFeatLaunch L, int n_ranges, int stride, int len,
                                                             int slices) {
     extern __shared__ __align__(16) float zs[];  // [CHUNK][W] chunk of y - shift, then shift[W]
     const int bv = blockIdx.x, b = L.b0 + bv / L.nvar, v = bv - (bv / L.nvar) * L.nvar;
@@ -47,29 +41,41 @@ __global__ void __launch_bounds__(MAXT) feat_moments_kernel(HbFeatLaunch L, int 
     const int t_lo = start + sl * Tc, t_end = start + len;
     const int t_hi = (t_lo + Tc) < t_end ? (t_lo + Tc) : t_end;
     float* shift = zs + CHUNK * W;
+    // the series of point b, variable v: x[t * tstride + n * nstride + m * nvar]
+    const float* x0 = L.traj + (size_t)b * L.state_len + L.off + v;
+    const size_t tstride = (size_t)L.B * L.state_len;
+    const int nvar = L.nvar, nmodes = L.nmodes, nstride = L.nmodes * L.nvar;
+    const float fm = (float)nmodes;
+    auto load = [=](int t, int n) {
+        const float* x = x0 + (size_t)t * tstride + (size_t)n * nstride;
+        if (nmodes == 1) return x[0];  // (0 + x) / 1 == x up to the sign of zero
+        float s = 0.0f;
+        for (int m = 0; m < nmodes; m++) s += x[(size_t)m * nvar];
+        return s / fm;
+    };
     const int n0 = len < 64 ? len : 64;
     for (int k = threadIdx.x; k < W; k += blockDim.x) {
         double c = 0.0;
         if (k < N) {
-            for (int t = 0; t < n0; t++) c += (double)series_value(L, start + t, b, v, k);
+            for (int t = 0; t < n0; t++) c += (double)load(start + t, k);
             c /= n0;
         }
         shift[k] = (float)c;
     }
     double* P = L.part + (((size_t)bv * n_ranges + r) * slices + sl) * ((size_t)W * W + W);
-    hb::series_moments<CHUNK>([&](int t, int k) { return series_value(L, t, b, v, k); }, N, t_lo, t_hi, shift, zs, P);
+    hb::series_moments<CHUNK>(load, N, t_lo, t_hi, shift, zs, P);
 }
 
 // FC of range blockIdx.y from its slices' moments: the full matrix into `full` and / or the upper
 // triangle (row-major, i < j) into `ut`
 __global__ void feat_corr_kernel(HbFeatLaunch L, int n_ranges, int len, int slices, float* full, float* ut) {
-    extern __shared__ __align__(16) double ms[];  // mean [W], sd [W]
+    extern __shared__ __align__(16) double ms[];  // mean [W], 1 / sd [W]
     const int bv = blockIdx.x, r = blockIdx.y;
     const int N = L.nnodes, W = (N + 3) / 4 * 4;
     const size_t pl = (size_t)W * W + W;
     const double* P0 = L.part + ((size_t)bv * n_ranges + r) * slices * pl;
     double* mean = ms;
-    double* sd = ms + W;
+    double* rsd = ms + W;
     for (int k = threadIdx.x; k < N; k += blockDim.x) {
         double s1 = 0.0, s2 = 0.0;
         for (int q = 0; q < slices; q++) {
@@ -80,21 +86,35 @@ __global__ void feat_corr_kernel(HbFeatLaunch L, int n_ranges, int len, int slic
         double d = sqrt(var > 0.0 ? var : 0.0);
         if (d < 1e-12) d = 1.0;  // constant series (fc.rs:35-37)
         mean[k] = m;
-        sd[k] = d;
+        rsd[k] = 1.0 / d;
     }
     __syncthreads();
     const size_t rr = (size_t)bv * n_ranges + r;
     const size_t n_ut = (size_t)N * (N - 1) / 2;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        const int i = q / N, j = q - (q / N) * N;
-        double qs = 0.0;
-        for (int s = 0; s < slices; s++) qs += P0[s * pl + (size_t)i * W + j];
-        const double cov = qs / len - mean[i] * mean[j];
-        double c = cov / (sd[i] * sd[j]);
-        c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
-        const float f = (float)c;
-        if (full) full[rr * N * N + q] = f;
-        if (ut && i < j) ut[rr * n_ut + (size_t)i * N - (size_t)i * (i + 1) / 2 + (j - i - 1)] = f;
+    const double rlen = 1.0 / len;
+    if (full) {
+        for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+            const int i = q / N, j = q - (q / N) * N;
+            double qs = 0.0;
+            for (int s = 0; s < slices; s++) qs += P0[s * pl + (size_t)i * W + j];
+            double c = (qs * rlen - mean[i] * mean[j]) * rsd[i] * rsd[j];
+            c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+            full[rr * N * N + q] = (float)c;
+        }
+    } else {
+        // upper triangle only, in its row-major order
+        for (size_t u = threadIdx.x; u < n_ut; u += blockDim.x) {
+            // row i holds N - 1 - i entries; invert the running count
+            int i = (int)((2.0 * N - 1.0 - sqrt((2.0 * N - 1.0) * (2.0 * N - 1.0) - 8.0 * (double)u)) * 0.5);
+            while (i > 0 && (size_t)i * N - (size_t)i * (i + 1) / 2 > u) i--;
+            while ((size_t)(i + 1) * N - (size_t)(i + 1) * (i + 2) / 2 <= u) i++;
+            const int j = (int)(u - ((size_t)i * N - (size_t)i * (i + 1) / 2)) + i + 1;
+            double qs = 0.0;
+            for (int s = 0; s < slices; s++) qs += P0[s * pl + (size_t)i * W + j];
+            double c = (qs * rlen - mean[i] * mean[j]) * rsd[i] * rsd[j];
+            c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+            ut[rr * n_ut + u] = (float)c;
+        }
     }
 }
 
@@ -126,6 +146,9 @@ __global__ void feat_ut_moments_kernel(HbFeatLaunch L) {
     }
     const double qq = block_sum(q, red);
     if (threadIdx.x == 0) { L.ut_mv[2 * w] = m; L.ut_mv[2 * w + 1] = qq; }
+    // the centred values, rounded to f32, for the pair products of feat_fcd_kernel
+    float* ac = L.ut + w * n_ut;
+    for (size_t k = threadIdx.x; k < n_ut; k += blockDim.x) ac[k] = (float)((double)ac[k] - m);
 }
 
 // row i = blockIdx.y of the FCD matrix of point-variable blockIdx.x (fc.rs:130-139, 144-179)
@@ -133,15 +156,20 @@ __global__ void feat_fcd_kernel(HbFeatLaunch L) {
     __shared__ double red[32];
     const int nw = L.n_windows, i = blockIdx.y, bv = blockIdx.x;
     const size_t n_ut = (size_t)L.nnodes * (L.nnodes - 1) / 2;
-    const float* ai = L.ut + ((size_t)bv * nw + i) * n_ut;
-    const double mi = L.ut_mv[2 * ((size_t)bv * nw + i)], vi = L.ut_mv[2 * ((size_t)bv * nw + i) + 1];
+    const float* ai = L.ut + ((size_t)bv * nw + i) * n_ut;  // centred
+    const double vi = L.ut_mv[2 * ((size_t)bv * nw + i) + 1];
     float* F = L.fcd + ((size_t)L.b0 * L.nvar + bv) * nw * nw;
     if (threadIdx.x == 0) F[(size_t)i * nw + i] = 1.0f;
     for (int j = i + 1; j < nw; j++) {
         const float* aj = L.ut + ((size_t)bv * nw + j) * n_ut;
-        const double mj = L.ut_mv[2 * ((size_t)bv * nw + j)], vj = L.ut_mv[2 * ((size_t)bv * nw + j) + 1];
+        const double vj = L.ut_mv[2 * ((size_t)bv * nw + j) + 1];
+        // FP32 products summed per thread in runs of 64, FP64 across runs and threads
         double c = 0.0;
-        for (size_t k = threadIdx.x; k < n_ut; k += blockDim.x) c += ((double)ai[k] - mi) * ((double)aj[k] - mj);
+        for (size_t k0 = threadIdx.x; k0 < n_ut; k0 += 64 * (size_t)blockDim.x) {
+            float part = 0.0f;
+            for (size_t k = k0; k < n_ut && k < k0 + 64 * (size_t)blockDim.x; k += blockDim.x) part = __fmaf_rn(ai[k], aj[k], part);
+            c += part;
+        }
         c = block_sum(c, red);
         if (threadIdx.x == 0) {
             double r = 0.0;
@@ -240,14 +268,14 @@ cudaError_t launch_moments(const HbFeatLaunch& L, int n_ranges, int stride, int 
     const size_t sm = ((size_t)CHUNK + 1) * W * sizeof(float) + 16;
     cudaError_t e = cudaFuncSetAttribute(feat_moments_kernel<CHUNK, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const int n4 = W / 4, tiles = n4 * (n4 + 1) / 2;
-    int threads = MAXT;
-    if (MAXT == 512 && tiles <= 256 && L.nnodes <= 256) threads = 256;
-    feat_moments_kernel<CHUNK, MAXT><<<dim3(L.nb * L.nvar, n_ranges * slices), threads, sm, st>>>(L, n_ranges, stride, len, slices);
+    feat_moments_kernel<CHUNK, MAXT><<<dim3(L.nb * L.nvar, n_ranges * slices), MAXT, sm, st>>>(L, n_ranges, stride, len, slices);
     return cudaGetLastError();
 }
 
+// 256 threads (three blocks per SM) while the 4 x 4 tiles fit one pass, else one thread per node
 cudaError_t moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, int slices, cudaStream_t st) {
+    const int n4 = (L.nnodes + 3) / 4;
+    if (n4 * (n4 + 1) / 2 <= 256) return launch_moments<64, 256>(L, n_ranges, stride, len, slices, st);
     if (L.nnodes <= 512) return launch_moments<64, 512>(L, n_ranges, stride, len, slices, st);
     return launch_moments<32, 1024>(L, n_ranges, stride, len, slices, st);
 }

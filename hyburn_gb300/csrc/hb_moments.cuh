@@ -13,8 +13,8 @@ constexpr int MOM_CHUNK = 64;  // steps summed in FP32 before an FP64 accumulati
 // Products are summed in FP32 over chunks of CHUNK steps and in FP64 across chunks; each thread
 // owns a 4 x 4 tile of Q's upper triangle (several passes over the range when the tiles outnumber
 // the threads). zs: CHUNK * W floats of 16-byte aligned shared memory; shift: W floats of shared
-// memory, written before the call (the first barrier inside orders it). Needs N <= blockDim.x;
-// every thread of the block calls it.
+// memory, written before the call (the first barrier inside orders it). Needs N <= blockDim.x and
+// blockDim.x a multiple of 32; every thread of the block calls it.
 template <int CHUNK = MOM_CHUNK, class Load>
 __device__ __forceinline__ void series_moments(const Load& load, int N, int t_lo, int t_hi, const float* shift,
                                                float* zs, double* P) {
@@ -40,12 +40,13 @@ __device__ __forceinline__ void series_moments(const Load& load, int N, int t_lo
         for (int t0 = t_lo; t0 < t_hi; t0 += CHUNK) {
             const int nt = (t_hi - t0) < CHUNK ? (t_hi - t0) : CHUNK;
             __syncthreads();
-            for (int q = tid; q < CHUNK * W; q += nth) {
-                const int tt = q / W, k = q - tt * W;
-                float z = 0.0f;
-                if (tt < nt && k < N) z = load(t0 + tt, k) - shift[k];
-                zs[q] = z;
-            }
+            // one step per warp at a time, its lanes along the series (no index division)
+            for (int tt = tid >> 5; tt < CHUNK; tt += nth >> 5)
+                for (int k = tid & 31; k < W; k += 32) {
+                    float z = 0.0f;
+                    if (tt < nt && k < N) z = load(t0 + tt, k) - shift[k];
+                    zs[tt * W + k] = z;
+                }
             __syncthreads();
             if (base == 0 && tid < N) {
                 float s1 = 0.0f;
