@@ -170,15 +170,17 @@ struct HbFeatLaunch {
     int window, stride, n_windows;  // FCD windows (n_windows >= 2), else n_windows = 0
     int b0, nb;          // this batch: points b0 .. b0 + nb - 1
     int fc_slices, win_slices;
+    int block_len;       // > 0: FCD window moments from blocks of this many steps (divides window and stride)
     float* fc;           // [B][nvar][nnodes][nnodes]
     float* feat;         // [B][nvar][7]: mean, std, min, max, median of FC's upper triangle; homotopic mean, std
     float* fcd;          // [B][nvar][n_windows][n_windows]
     float* fcd_stats;    // [B][nvar][5]
-    double* part;        // moments workspace: nb * nvar * max(fc_slices, n_windows * win_slices) * (W * W + W)
+    double* part;        // moments workspace: nb * nvar * (ranges of the largest pass) * hb_fc_part_len(nnodes)
     float* ut;           // nb * nvar * n_windows * nnodes (nnodes - 1) / 2 window-FC upper triangles
     double* ut_mv;       // nb * nvar * n_windows * 2: mean and centred sum of squares of each
 };
 cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st);
+size_t hb_fc_part_len(int nnodes);  // doubles of one range's moments in HbFeatLaunch::part
 
 // time slices of the moment pass for B points of T steps: enough blocks to fill the SMs three times
 // over, at most 16, each slice at least 64 steps

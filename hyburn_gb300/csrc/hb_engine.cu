@@ -1519,13 +1519,24 @@ hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_le
         out->n_windows = nw; out->nnodes = N; out->nvar = nvar; out->ms = 0.0f;
         return HB_OK;
     }
-    const size_t W = (size_t)(N + 3) / 4 * 4, pl = W * W + W, n_ut = (size_t)N * (N - 1) / 2;
+    const size_t pl = hb_fc_part_len(N), n_ut = (size_t)N * (N - 1) / 2;
     // slices of the moment passes: enough blocks to fill the SMs, each slice at least 64 steps
-    const int fc_slices = std::max(1, std::min(hb_adjoint_moment_slices(B * nvar, T), std::max(1, T / 64)));
+    const int fc_slices = std::max(1, std::min({16, (4 * 456 + B * nvar - 1) / (B * nvar), std::max(1, T / 64)}));
     const int win_slices = nw ? std::max(1, std::min({8, (456 + B * nvar * nw - 1) / (B * nvar * nw),
                                                       std::max(1, window_len / 64), 65535 / nw})) : 1;
+    // FCD from blocks of G = gcd(window, stride) steps when G >= 64 and a window spans at most 12
+    int block_len = 0, n_blocks = 0;
+    if (nw) {
+        int g = window_len, h = stride;
+        while (h) { const int t = g % h; g = h; h = t; }
+        if (g >= 64 && window_len / g <= 12 && N <= 512) {
+            block_len = g;
+            n_blocks = (nw - 1) * (stride / g) + window_len / g;
+        }
+    }
+    const size_t win_ranges = block_len ? (size_t)n_blocks : (size_t)nw * win_slices;
     // points per batch: moments and window workspaces within 4 GiB
-    const size_t per_point = (size_t)nvar * (std::max<size_t>((size_t)fc_slices, (size_t)nw * win_slices) * pl * 8 +
+    const size_t per_point = (size_t)nvar * (std::max<size_t>((size_t)fc_slices, win_ranges) * pl * 8 +
                                              (size_t)nw * (n_ut * 4 + 16));
     const int nb = (int)std::max<size_t>(1, std::min<size_t>((size_t)B, (4ull << 30) / std::max<size_t>(per_point, 1)));
     CUDA_TRY(e->fe_fc.ensure((size_t)B * nvar * N * N));
@@ -1540,7 +1551,8 @@ hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_le
     L.fc = e->fe_fc.p; L.feat = e->fe_feat.p; L.fcd = e->fe_fcd.p; L.fcd_stats = e->fe_fcds.p;
     L.fc_slices = fc_slices;
     L.win_slices = win_slices;
-    const size_t part_n = (size_t)nb * nvar * std::max<size_t>((size_t)L.fc_slices, (size_t)nw * L.win_slices) * pl;
+    L.block_len = block_len;
+    const size_t part_n = (size_t)nb * nvar * std::max<size_t>((size_t)L.fc_slices, win_ranges) * pl;
     CUDA_TRY(e->fe_part.ensure(part_n));
     L.part = e->fe_part.p;
     if (nw) {

@@ -10,7 +10,9 @@
 //            cov / (sd_i sd_j) clamped to [-1, 1];
 //   features fc_stats of FC's upper triangle (mean, std, min, max, median; fc.rs:62-83) and the
 //            homotopic mean and std of FC[i][N-1-i] (fc.rs:189-203): 7 values per (b, v);
-//   FCD      FC of each window [w * stride, w * stride + window) (fc.rs:87-141), then the Pearson
+//   FCD      FC of each window [w * stride, w * stride + window) (fc.rs:87-141; when window and
+//            stride share a divisor G >= 64, from moments of G-step blocks computed once and
+//            combined per window by the parallel-axis formula), then the Pearson
 //            correlation of every pair of window FCs' upper triangles (fc.rs:144-179; FP32
 //            products of the centred values, summed in FP64), diagonal 1;
 //            and fc_stats of that matrix (fc.rs:182-187).
@@ -26,6 +28,20 @@
 #include "hb_moments.cuh"
 
 namespace {
+
+// one range's moments in the workspace: Q [W][W], S [W] (sums of y - shift), the shift [W]
+__host__ __device__ __forceinline__ size_t part_len(int N) {
+    const size_t W = (size_t)(N + 3) / 4 * 4;
+    return W * W + 2 * W;
+}
+
+// the upper-triangle entry u (row-major, i < j) of an N x N matrix as (i, j)
+__device__ __forceinline__ void ut_index(size_t u, int N, int& i, int& j) {
+    i = (int)((2.0 * N - 1.0 - sqrt((2.0 * N - 1.0) * (2.0 * N - 1.0) - 8.0 * (double)u)) * 0.5);
+    while (i > 0 && (size_t)i * N - (size_t)i * (i + 1) / 2 > u) i--;
+    while ((size_t)(i + 1) * N - (size_t)(i + 1) * (i + 2) / 2 <= u) i++;
+    j = (int)(u - ((size_t)i * N - (size_t)i * (i + 1) / 2)) + i + 1;
+}
 
 // moments of range r = blockIdx.y / slices ([r * stride, r * stride + len)), slice blockIdx.y % slices,
 // of point-variable blockIdx.x of the batch
@@ -62,8 +78,9 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) feat_moments_kernel
         }
         shift[k] = (float)c;
     }
-    double* P = L.part + (((size_t)bv * n_ranges + r) * slices + sl) * ((size_t)W * W + W);
+    double* P = L.part + (((size_t)bv * n_ranges + r) * slices + sl) * part_len(N);
     hb::series_moments<CHUNK>(load, N, t_lo, t_hi, shift, zs, P);
+    for (int k = threadIdx.x; k < W; k += blockDim.x) P[(size_t)W * W + W + k] = (double)shift[k];
 }
 
 // FC of range blockIdx.y from its slices' moments: the full matrix into `full` and / or the upper
@@ -72,7 +89,7 @@ __global__ void feat_corr_kernel(HbFeatLaunch L, int n_ranges, int len, int slic
     extern __shared__ __align__(16) double ms[];  // mean [W], 1 / sd [W]
     const int bv = blockIdx.x, r = blockIdx.y;
     const int N = L.nnodes, W = (N + 3) / 4 * 4;
-    const size_t pl = (size_t)W * W + W;
+    const size_t pl = part_len(N);
     const double* P0 = L.part + ((size_t)bv * n_ranges + r) * slices * pl;
     double* mean = ms;
     double* rsd = ms + W;
@@ -104,17 +121,66 @@ __global__ void feat_corr_kernel(HbFeatLaunch L, int n_ranges, int len, int slic
     } else {
         // upper triangle only, in its row-major order
         for (size_t u = threadIdx.x; u < n_ut; u += blockDim.x) {
-            // row i holds N - 1 - i entries; invert the running count
-            int i = (int)((2.0 * N - 1.0 - sqrt((2.0 * N - 1.0) * (2.0 * N - 1.0) - 8.0 * (double)u)) * 0.5);
-            while (i > 0 && (size_t)i * N - (size_t)i * (i + 1) / 2 > u) i--;
-            while ((size_t)(i + 1) * N - (size_t)(i + 1) * (i + 2) / 2 <= u) i++;
-            const int j = (int)(u - ((size_t)i * N - (size_t)i * (i + 1) / 2)) + i + 1;
+            int i, j;
+            ut_index(u, N, i, j);
             double qs = 0.0;
             for (int s = 0; s < slices; s++) qs += P0[s * pl + (size_t)i * W + j];
             double c = (qs * rlen - mean[i] * mean[j]) * rsd[i] * rsd[j];
             c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
             ut[rr * n_ut + u] = (float)c;
         }
+    }
+}
+
+// FC upper triangle of window w = blockIdx.y from the moments of its K consecutive blocks of G
+// steps (blocks w * (stride / G) ...), combined exactly by the parallel-axis formula: with block
+// means mu_q = shift_q + S_q / G and the window mean mu,
+//   M_ij = sum_q (Q_q,ij - S_q,i S_q,j / G) + G sum_q (mu_q,i - mu_i)(mu_q,j - mu_j),  cov = M / (K G).
+// A series constant over the window has M = 0 exactly (each block's shift is its value).
+__global__ void feat_corr_blocks_kernel(HbFeatLaunch L, int n_blocks, int G, int K, int step) {
+    extern __shared__ __align__(16) double sb[];  // S [K][W], S / G [K][W], mu_q - mu [K][W], 1/sd [W]
+    const int bv = blockIdx.x, w = blockIdx.y;
+    const int N = L.nnodes, W = (N + 3) / 4 * 4;
+    const size_t pl = part_len(N);
+    const double* P0 = L.part + ((size_t)bv * n_blocks + (size_t)w * step) * pl;
+    double* S = sb;
+    double* Sg = sb + (size_t)K * W;
+    double* dq = Sg + (size_t)K * W;
+    double* rsd = dq + (size_t)K * W;
+    const double g = (double)G, rg = 1.0 / g, rlen = 1.0 / ((double)K * G);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        double m = 0.0;
+        for (int q = 0; q < K; q++) {
+            const double sq = P0[q * pl + (size_t)W * W + k];
+            S[q * W + k] = sq;
+            Sg[q * W + k] = sq * rg;
+            const double mb = P0[q * pl + (size_t)W * W + W + k] + sq * rg;
+            dq[q * W + k] = mb;
+            m += mb;
+        }
+        m /= K;
+        double M = 0.0;
+        for (int q = 0; q < K; q++) {
+            const double d = dq[q * W + k] - m;
+            dq[q * W + k] = d;
+            M += P0[q * pl + (size_t)k * W + k] - S[q * W + k] * Sg[q * W + k] + g * d * d;
+        }
+        double sd = sqrt(M > 0.0 ? M * rlen : 0.0);
+        if (sd < 1e-12) sd = 1.0;
+        rsd[k] = 1.0 / sd;
+    }
+    __syncthreads();
+    const size_t n_ut = (size_t)N * (N - 1) / 2;
+    float* out = L.ut + ((size_t)bv * L.n_windows + w) * n_ut;
+    for (size_t u = threadIdx.x; u < n_ut; u += blockDim.x) {
+        int i, j;
+        ut_index(u, N, i, j);
+        double M = 0.0;
+        for (int q = 0; q < K; q++)
+            M += P0[q * pl + (size_t)i * W + j] - S[q * W + i] * Sg[q * W + j] + g * dq[q * W + i] * dq[q * W + j];
+        double c = M * rlen * rsd[i] * rsd[j];
+        c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+        out[u] = (float)c;
     }
 }
 
@@ -282,6 +348,8 @@ cudaError_t moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, in
 
 }  // namespace
 
+size_t hb_fc_part_len(int nnodes) { return part_len(nnodes); }
+
 cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st) {
     const int N = L.nnodes, W = (N + 3) / 4 * 4, nbv = L.nb * L.nvar;
     if (N < 1 || N > 1024) return cudaErrorInvalidValue;
@@ -295,8 +363,19 @@ cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st) {
     if (L.n_windows < 2) return cudaSuccess;
     // FCD: window FCs, their pairwise correlations, statistics
     const int nw = L.n_windows;
-    if ((e = moments(L, nw, L.stride, L.window, L.win_slices, st)) != cudaSuccess) return e;
-    feat_corr_kernel<<<dim3(nbv, nw), 256, 2 * W * sizeof(double), st>>>(L, nw, L.window, L.win_slices, nullptr, L.ut);
+    if (L.block_len > 0) {
+        // moments of blocks of block_len steps, each window the sum of window / block_len of them
+        const int G = L.block_len, K = L.window / G, step = L.stride / G;
+        const int n_blocks = (nw - 1) * step + K;
+        if ((e = moments(L, n_blocks, G, G, 1, st)) != cudaSuccess) return e;
+        const size_t sm = ((size_t)3 * K + 1) * W * sizeof(double);
+        if ((e = cudaFuncSetAttribute(feat_corr_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+            return e;
+        feat_corr_blocks_kernel<<<dim3(nbv, nw), 256, sm, st>>>(L, n_blocks, G, K, step);
+    } else {
+        if ((e = moments(L, nw, L.stride, L.window, L.win_slices, st)) != cudaSuccess) return e;
+        feat_corr_kernel<<<dim3(nbv, nw), 256, 2 * W * sizeof(double), st>>>(L, nw, L.window, L.win_slices, nullptr, L.ut);
+    }
     feat_ut_moments_kernel<<<dim3(nbv, nw), 256, 0, st>>>(L);
     feat_fcd_kernel<<<dim3(nbv, nw), 256, 0, st>>>(L);
     feat_stats_kernel<<<nbv, 256, 0, st>>>(L.fcd + (size_t)L.b0 * L.nvar * nw * nw, nw,

@@ -114,7 +114,9 @@ def test_device_fc_features_stochastic_long_and_windows():
                        delays="per_edge_long", nsig=1e-3, seed=4)
     T = 3000
     eng, r = _run(cfg, 2, T, SweepParam(-1, 0), [0.0, 0.1], noise_for(cfg, T, 2, False, 9))
-    _check(eng, r, cfg, 2, 1000, 333)
+    _check(eng, r, cfg, 2, 1000, 333)   # windows summed directly (gcd 1)
+    _check(eng, r, cfg, 2, 1000, 250)   # windows combined from 250-step blocks (four per window)
+    _check(eng, r, cfg, 2, 768, 128)    # six 128-step blocks per window
     _check(eng, r, cfg, 2, 0, 1)
     eng.close()
 
