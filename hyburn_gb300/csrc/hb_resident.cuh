@@ -950,16 +950,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Consumer steps of the pipeline for the common case — Heun (deterministic or stochastic), Linear
-// coupling delivered to the first coupling variables, no trajectory, no BOLD — as one straight-line
-// loop: the per-step branches of the general consumer (integrator, coupling function, channel map,
-// monitors) are resolved by the template arguments, with the same operations in the same order.
+// coupling delivered to the first coupling variables, no BOLD — as one straight-line loop: the
+// per-step branches of the general consumer (integrator, coupling function, channel map, monitors)
+// are resolved by the template arguments, with the same operations in the same order. With traj
+// set, each step's state of node n goes to traj + step * traj_stride.
 template <int MODEL, int NVAR, int NCV, bool STOCH, bool SWEEP_FORM>
 __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, const float* prm, const float* cp,
                                                          const float* nscale, float dt, float dt_half,
                                                          const float* gxbuf, const float* nzbuf, float* ring,
                                                          int n, bool active, int nm, int cols, int R, int slot,
                                                          int n_steps, int n_blocks, int nthreads, uint64_t* nbar,
-                                                         int* err) {
+                                                         int* err, float* traj, size_t traj_stride) {
     constexpr int PK = HB_PIPE_K;
     const float ca = cp[0], cb = cp[1];
     float ns[NVAR];
@@ -1005,6 +1006,11 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
             for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
             ring[slot * cols + n * NCV] = x[0];
             if (NCV > 1) ring[slot * cols + n * NCV + 1] = x[1];
+            if (traj) {
+                float* tr = traj + (size_t)(blk * PK + j) * traj_stride;
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) __stcs(tr + v, x[v]);
+            }
         }
         named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
     }
@@ -1274,17 +1280,19 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
         }
         int64_t s = a.s0;
         const bool straight = PRE == PRE_ID && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) && cfk == HBC_LINEAR &&
-                              direct && pc == NCV && !has_rowsums && a.traj == nullptr && a.bold.n == 0;
+                              direct && pc == NCV && !has_rowsums && a.bold.n == 0;
         if (straight) {
+            float* trj = a.traj ? a.traj + (size_t)b * net.state_len + (size_t)n * NVAR : nullptr;
+            const size_t trs = (size_t)B * net.state_len;
             float nscale[8];
 #pragma unroll
             for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
             if (integ == HBI_HEUN_STOCH) {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
             } else {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1);
+                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
+                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
             }
         }
         for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
