@@ -384,17 +384,15 @@ __device__ __forceinline__ float moment_shift(const AdjArgs& A, int b, int k) {
 }
 
 __global__ void adj_moments_kernel(AdjArgs A, double* part, int slices) {
-    extern __shared__ __align__(16) float zs[];  // [MOM_CHUNK][W] chunk of y - shift, then shift[W]
+    extern __shared__ __align__(16) float zs[];  // [2][MOM_CHUNK][W] chunks of y - shift, then shift[W]
     const int b = blockIdx.x, sl = blockIdx.y, N = A.N, T = A.T;
     const int W = (N + 3) / 4 * 4;
     const int Tc = ((T + slices - 1) / slices + MOM_CHUNK - 1) / MOM_CHUNK * MOM_CHUNK;
     const int t_lo = sl * Tc, t_hi = (t_lo + Tc) < T ? (t_lo + Tc) : T;
-    float* shift = zs + MOM_CHUNK * W;
+    float* shift = zs + 2 * MOM_CHUNK * W;
     double* P = part + ((size_t)b * slices + sl) * ((size_t)W * W + W);  // Q [W][W], then S [W]
     for (int k = threadIdx.x; k < W; k += blockDim.x) shift[k] = k < N ? moment_shift(A, b, k) : 0.0f;
-    const float* Y = A.Y;
-    const int B = A.B;
-    hb::series_moments([=](int t, int k) { return Y[((size_t)t * B + b) * N + k]; }, N, t_lo, t_hi, shift, zs, P);
+    hb::series_moments_strided(A.Y + (size_t)b * N, (size_t)A.B * N, 1, N, t_lo, t_hi, shift, zs, P);
 }
 
 __global__ void adj_fc_kernel(AdjArgs A, const double* part, int slices) {
@@ -664,7 +662,9 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         adj_forward_kernel<<<L.B, threads, sm, st>>>(d_net, A, lanes);
     } else if (phase == 1) {
         const size_t W = (size_t)(L.N + 3) / 4 * 4;
-        const size_t sm = (MOM_CHUNK + 1) * W * sizeof(float) + 16;
+        const size_t sm = (2 * MOM_CHUNK + 1) * W * sizeof(float) + 16;
+        if (cudaFuncSetAttribute(adj_moments_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return cudaGetLastError();
         const int n_tiles = (int)(W / 4 * (W / 4 + 1) / 2);
         adj_moments_kernel<<<dim3(L.B, L.slices), n_tiles <= 256 ? 256 : 512, sm, st>>>(A, L.moments, L.slices);
         adj_fc_kernel<<<L.B, 512, (512 + 2 * W) * sizeof(double), st>>>(A, L.moments, L.slices);

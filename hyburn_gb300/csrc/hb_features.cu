@@ -48,7 +48,7 @@ __device__ __forceinline__ void ut_index(size_t u, int N, int& i, int& j) {
 template <int CHUNK, int MAXT>
 __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) feat_moments_kernel(HbFeatLaunch L, int n_ranges, int stride, int len,
                                                             int slices) {
-    extern __shared__ __align__(16) float zs[];  // [CHUNK][W] chunk of y - shift, then shift[W]
+    extern __shared__ __align__(16) float zs[];  // [2][CHUNK][W] chunks of y - shift, then shift[W]
     const int bv = blockIdx.x, b = L.b0 + bv / L.nvar, v = bv - (bv / L.nvar) * L.nvar;
     const int r = blockIdx.y / slices, sl = blockIdx.y - r * slices;
     const int N = L.nnodes, W = (N + 3) / 4 * 4;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) feat_moments_kernel
     const int Tc = ((len + slices - 1) / slices + CHUNK - 1) / CHUNK * CHUNK;
     const int t_lo = start + sl * Tc, t_end = start + len;
     const int t_hi = (t_lo + Tc) < t_end ? (t_lo + Tc) : t_end;
-    float* shift = zs + CHUNK * W;
+    float* shift = zs + 2 * CHUNK * W;
     // the series of point b, variable v: x[t * tstride + n * nstride + m * nvar]
     const float* x0 = L.traj + (size_t)b * L.state_len + L.off + v;
     const size_t tstride = (size_t)L.B * L.state_len;
@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 256 ? 3 : 1) feat_moments_kernel
         shift[k] = (float)c;
     }
     double* P = L.part + (((size_t)bv * n_ranges + r) * slices + sl) * part_len(N);
-    hb::series_moments<CHUNK>(load, N, t_lo, t_hi, shift, zs, P);
+    if (nmodes == 1) hb::series_moments_strided<CHUNK>(x0, tstride, nvar, N, t_lo, t_hi, shift, zs, P);
+    else hb::series_moments<CHUNK>(load, N, t_lo, t_hi, shift, zs, P);
     for (int k = threadIdx.x; k < W; k += blockDim.x) P[(size_t)W * W + W + k] = (double)shift[k];
 }
 
@@ -331,7 +332,7 @@ __global__ void feat_stats_kernel(const float* mats, int n, float* stats, int ss
 template <int CHUNK, int MAXT>
 cudaError_t launch_moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, int slices, cudaStream_t st) {
     const int W = (L.nnodes + 3) / 4 * 4;
-    const size_t sm = ((size_t)CHUNK + 1) * W * sizeof(float) + 16;
+    const size_t sm = ((size_t)2 * CHUNK + 1) * W * sizeof(float) + 16;
     cudaError_t e = cudaFuncSetAttribute(feat_moments_kernel<CHUNK, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     feat_moments_kernel<CHUNK, MAXT><<<dim3(L.nb * L.nvar, n_ranges * slices), MAXT, sm, st>>>(L, n_ranges, stride, len, slices);
@@ -342,8 +343,8 @@ cudaError_t launch_moments(const HbFeatLaunch& L, int n_ranges, int stride, int 
 cudaError_t moments(const HbFeatLaunch& L, int n_ranges, int stride, int len, int slices, cudaStream_t st) {
     const int n4 = (L.nnodes + 3) / 4;
     if (n4 * (n4 + 1) / 2 <= 256) return launch_moments<64, 256>(L, n_ranges, stride, len, slices, st);
-    if (L.nnodes <= 512) return launch_moments<64, 512>(L, n_ranges, stride, len, slices, st);
-    return launch_moments<32, 1024>(L, n_ranges, stride, len, slices, st);
+    if (L.nnodes <= 512) return launch_moments<32, 512>(L, n_ranges, stride, len, slices, st);
+    return launch_moments<16, 1024>(L, n_ranges, stride, len, slices, st);
 }
 
 }  // namespace
