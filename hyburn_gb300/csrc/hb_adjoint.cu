@@ -351,7 +351,82 @@ __device__ void forward_steps(float* ring, float* gbuf, const AdjArgs& A, const 
 
 __device__ __forceinline__ size_t tables_size(int N, int nnz) { return (size_t)(N + 1) * 4 + (size_t)nnz * 8; }
 
-__global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L) {
+constexpr int ADJ_BAR_FULL0 = 1, ADJ_BAR_EMPTY0 = 3;  // named barriers 1-2 and 3-4 (0 is __syncthreads)
+
+__device__ __forceinline__ void bar_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+__device__ __forceinline__ void bar_arrive(int id, int count) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+
+// The forward with every step's state kept (store_all) as a producer / consumer pipeline, when every
+// delay is at least 2K - 1 steps: the first n_cons threads are consumers (thread t integrates node t),
+// the others producers (L lanes per node) that gather block k + 1's coupling sums into one of two
+// buffers while the consumers integrate block k from the other; named barriers hand the buffers
+// over. The values read for block k + 1 are at least K steps old when block k starts, so the
+// consumers of block k never write them. Per step the same operations in the same order as
+// forward_steps (mode 0).
+__device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, const AdjTables& tb, int b, int L,
+                                  float* x, const float* prm, const float* cp, int n_cons) {
+    const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K, T = A.T;
+    const int t = threadIdx.x, nthreads = blockDim.x;
+    const int n_blocks = (T + K - 1) / K;
+    if (t >= n_cons) {
+        const int p = t - n_cons;
+        const int gi = p / L, gl = p - (p / L) * L;
+        const bool gact = gi < N;
+        const int e0 = gact ? tb.rowptr[gi] : 0, e1 = gact ? tb.rowptr[gi + 1] : 0;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            if (blk >= 2) bar_sync(ADJ_BAR_EMPTY0 + buf, nthreads);
+            const int s0 = blk * K, nb = (T - s0) < K ? (T - s0) : K;
+            float* gb = gbuf2 + (size_t)buf * K * N;
+            int slot = s0 % R;
+            for (int j = 0; j < nb; j++) {
+                float part = 0.0f;
+                if (gact) {
+                    if (s0 + j == 0) part = gather_step0(ring, A, gi, gl, L);
+                    else {
+                        const int base = slot * N;
+                        for (int e = e0 + gl; e < e1; e += L) {
+                            int a = base + tb.eoff[e];
+                            a += (a < 0) ? RN : 0;
+                            part += tb.ew[e] * ring[a];
+                        }
+                    }
+                }
+                part = lane_sum(part, L);
+                if (gact && gl == 0) gb[j * N + gi] = part;
+                slot = (slot + 1 == R) ? 0 : slot + 1;
+            }
+            bar_arrive(ADJ_BAR_FULL0 + buf, nthreads);
+        }
+    } else {
+        const bool uact = t < N;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            bar_sync(ADJ_BAR_FULL0 + buf, nthreads);
+            const int s0 = blk * K, nb = (T - s0) < K ? (T - s0) : K;
+            const float* gb = gbuf2 + (size_t)buf * K * N;
+            if (uact) {
+                int slot = s0 % R;
+                for (int j = 0; j < nb; j++) {
+                    const int s = s0 + j;
+                    const float g = gb[j * N + t];
+                    float* sc = A.scratch + (((size_t)b * A.CK + s) * N + t) * 8;
+#pragma unroll
+                    for (int v = 0; v < NV; v++) sc[v] = x[v];
+                    sc[6] = g;
+                    heun_step(prm, x, coupling_post(A.cfk, cp, g), A.dt, A.dt_half);
+                    const int next = (slot + 1 == R) ? 0 : slot + 1;
+                    ring[next * N + t] = x[0];
+                    A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
+                    slot = next;
+                }
+            }
+            bar_arrive(ADJ_BAR_EMPTY0 + buf, nthreads);
+        }
+    }
+}
+
+__global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L, int n_cons) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* ring = reinterpret_cast<float*>(smem);
     const int b = blockIdx.x, N = A.N, RN = A.R * A.N;
@@ -366,7 +441,12 @@ __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, i
 #pragma unroll
     for (int v = 0; v < NV; v++) x[v] = uact ? A.x0[(size_t)b * N * NV + threadIdx.x * NV + v] : 0.0f;
     if (uact) ring[threadIdx.x] = x[0];
-    forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
+    if (n_cons > 0) {
+        __syncthreads();
+        forward_pipelined(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons);
+    } else {
+        forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
+    }
 }
 
 // ---- statistics of y, FC, loss, and the coefficients of dL/dy ----
@@ -656,10 +736,13 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
     const size_t tab1 = (size_t)(L.N + 1) * 4 + (size_t)nnz * 8;
     const size_t gbuf_bytes = (size_t)L.K * L.N * sizeof(float) + 16;
     if (phase == 0) {
-        const size_t sm = ring_bytes + tab1 + gbuf_bytes;
+        // pipelined: one consumer thread per node (warp aligned), then lanes producer threads per node
+        const int n_cons = L.pipelined ? (L.N + 31) / 32 * 32 : 0;
+        const int fthreads = L.pipelined ? n_cons + (L.N * lanes + 31) / 32 * 32 : threads;
+        const size_t sm = ring_bytes + tab1 + (L.pipelined ? 2 * gbuf_bytes : gbuf_bytes);
         if (cudaFuncSetAttribute(adj_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
             return cudaGetLastError();
-        adj_forward_kernel<<<L.B, threads, sm, st>>>(d_net, A, lanes);
+        adj_forward_kernel<<<L.B, fthreads, sm, st>>>(d_net, A, lanes, n_cons);
     } else if (phase == 1) {
         const size_t W = (size_t)(L.N + 3) / 4 * 4;
         const size_t sm = (2 * MOM_CHUNK + 1) * W * sizeof(float) + 16;
