@@ -949,12 +949,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-// Consumer steps of the pipeline for the common case — Heun (deterministic or stochastic), Linear
-// coupling delivered to the first coupling variables, no BOLD — as one straight-line loop: the
-// per-step branches of the general consumer (integrator, coupling function, channel map, monitors)
-// are resolved by the template arguments, with the same operations in the same order. With traj
-// set, each step's state of node n goes to traj + step * traj_stride.
-template <int MODEL, int NVAR, int NCV, bool STOCH, bool SWEEP_FORM>
+// Consumer steps of the pipeline for the common case — Heun (deterministic or stochastic), Linear or
+// Sigmoidal coupling (CFK) delivered to the first coupling variables, no BOLD — as one straight-line
+// loop: the per-step branches of the general consumer (integrator, coupling function, channel map,
+// monitors) are resolved by the template arguments, with the same operations in the same order
+// (post() for the coupling). With traj set, each step's state of node n goes to
+// traj + step * traj_stride.
+template <int MODEL, int NVAR, int NCV, bool STOCH, bool SWEEP_FORM, int CFK>
 __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, const float* prm, const float* cp,
                                                          const float* nscale, float dt, float dt_half,
                                                          const float* gxbuf, const float* nzbuf, float* ring,
@@ -962,7 +963,7 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
                                                          int n_steps, int n_blocks, int nthreads, uint64_t* nbar,
                                                          int* err, float* traj, size_t traj_stride) {
     constexpr int PK = HB_PIPE_K;
-    const float ca = cp[0], cb = cp[1];
+    const float ca = cp[0], cb = cp[1], c2 = cp[2], c3 = cp[3], c4 = cp[4];
     float ns[NVAR];
 #pragma unroll
     for (int v = 0; v < NVAR; v++) ns[v] = nscale[v];
@@ -978,8 +979,18 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
             slot = (slot + 1 == R) ? 0 : slot + 1;
             if (!active) continue;  // threads past the last node only take part in the barriers
             float cc[2] = {0.0f, 0.0f};
-            cc[0] = gb[(size_t)j * nm * NCV] * ca + cb;
-            if (NCV > 1) cc[1] = gb[(size_t)j * nm * NCV + 1] * ca + cb;
+#pragma unroll
+            for (int c = 0; c < NCV; c++) {
+                const float g = gb[(size_t)j * nm * NCV + c];
+                if (CFK == HBC_SIGMOIDAL) {
+                    const float sh = (g + (-c2)) / c4;
+                    const float ex = -(sh * c3);
+                    const float den = expf(ex) + 1.0f;
+                    cc[c] = (1.0f / den) * (cb - ca) + ca;
+                } else {
+                    cc[c] = g * ca + cb;
+                }
+            }
             float nz[NVAR];
 #pragma unroll
             for (int v = 0; v < NVAR; v++) nz[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
@@ -1279,21 +1290,25 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
             }
         }
         int64_t s = a.s0;
-        const bool straight = PRE == PRE_ID && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) && cfk == HBC_LINEAR &&
-                              direct && pc == NCV && !has_rowsums && a.bold.n == 0;
+        const bool straight = PRE == PRE_ID && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) &&
+                              (cfk == HBC_LINEAR || cfk == HBC_SIGMOIDAL) && direct && pc == NCV && !has_rowsums &&
+                              a.bold.n == 0;
         if (straight) {
             float* trj = a.traj ? a.traj + (size_t)b * net.state_len + (size_t)n * NVAR : nullptr;
             const size_t trs = (size_t)B * net.state_len;
             float nscale[8];
 #pragma unroll
             for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
-            if (integ == HBI_HEUN_STOCH) {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, true, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, true, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
+            uint64_t* nb_ = use_bulk ? noise_bar : nullptr;
+#define HB_STRAIGHT(ST, SF, CF) pipe_consume_heun_linear<MODEL, NVAR, NCV, ST, SF, CF>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, nb_, a.flags + 1, trj, trs)
+            if (cfk == HBC_SIGMOIDAL) {
+                if (integ == HBI_HEUN_STOCH) { if (sweep_form) HB_STRAIGHT(true, true, HBC_SIGMOIDAL); else HB_STRAIGHT(true, false, HBC_SIGMOIDAL); }
+                else { if (sweep_form) HB_STRAIGHT(false, true, HBC_SIGMOIDAL); else HB_STRAIGHT(false, false, HBC_SIGMOIDAL); }
             } else {
-                if (sweep_form) pipe_consume_heun_linear<MODEL, NVAR, NCV, false, true>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
-                else pipe_consume_heun_linear<MODEL, NVAR, NCV, false, false>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, use_bulk ? noise_bar : nullptr, a.flags + 1, trj, trs);
+                if (integ == HBI_HEUN_STOCH) { if (sweep_form) HB_STRAIGHT(true, true, HBC_LINEAR); else HB_STRAIGHT(true, false, HBC_LINEAR); }
+                else { if (sweep_form) HB_STRAIGHT(false, true, HBC_LINEAR); else HB_STRAIGHT(false, false, HBC_LINEAR); }
             }
+#undef HB_STRAIGHT
         }
         for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
             const int buf = blk & 1;

@@ -39,3 +39,20 @@ def test_straight_consumer_two_coupling_variables(integrator):
     eng, _, _, _ = compare(cfg, 3, SweepParam(0, NATIVE_SWEEP["MontbrioPazoRoxin"]),
                            sweep_values("MontbrioPazoRoxin", 3), 400, semantics=HB_SEM_DELAY_RING, noise=nz, traj=False)
     assert eng.last_kernel_time()[2] == PIPE_KIND
+
+
+@pytest.mark.parametrize("model,integrator,n_cv", [("JansenRit", "heun", 1), ("JansenRit", "heun_stochastic", 1),
+                                                   ("MontbrioPazoRoxin", "heun", 2)])
+def test_straight_consumer_sigmoidal(model, integrator, n_cv):
+    """Sigmoidal coupling through the straight-line consumer, with and without a trajectory, and a
+    coupling-parameter sweep (per-point coupling rows)."""
+    dt = 0.05 if model == "MontbrioPazoRoxin" else 0.1
+    cfg = single_model(model, 24, integrator, "Sigmoidal", (0.0, 0.1, 0.0, 1.0, 0.05), weights="csr",
+                       delays="per_edge_long", nsig=1e-4, dt=dt, seed=6)
+    nz = noise_for(cfg, 300, 3, False, 3) if "stochastic" in integrator else None
+    for traj in (False, True):
+        eng, _, _, _ = compare(cfg, 3, SweepParam(0, NATIVE_SWEEP[model]), sweep_values(model, 3), 300,
+                               semantics=HB_SEM_DELAY_RING, noise=nz, traj=traj)
+        assert eng.last_kernel_time()[2] == PIPE_KIND
+    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 3), [0.5, 1.0, 1.5], 300, semantics=HB_SEM_DELAY_RING, noise=nz)
+    assert eng.last_kernel_time()[2] == PIPE_KIND
