@@ -712,6 +712,139 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
     if (threadIdx.x == 0) A.gG[b] = red[0];
 }
 
+// The reverse sweep when the forward kept every step (one segment) and every delay is at least 2K
+// steps, as a producer / consumer pipeline: the first n_cons threads are consumers (L lanes per node:
+// coefficients lane-parallel, the lambda chain, the mu ring writes), the others producers (L lanes
+// per node) that pull the delayed-coupling sums sum_e w_e mu_tgt(e)(s + d_e) of block k + 1 into
+// one of two buffers while the consumers run block k. The mu values a producer pulls for block
+// k + 1 belong to steps the consumers finished before block k began. Per step the same operations,
+// lanes and summation order as adj_backward_kernel, so the gradients are bitwise the same.
+constexpr int ADJ_PIPE_MAXT = 640;  // register budget: 102 per thread
+
+__global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(const DevNet* __restrict__ gnet, AdjArgs A,
+                                                                            int L, int n_cons) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* ring = reinterpret_cast<float*>(smem);  // mu ring
+    const int b = blockIdx.x, N = A.N, R = A.R, T = A.T, RN = A.R * A.N, K = A.K;
+    const int nthreads = blockDim.x;
+    const DevNet& net = *gnet;
+    float prm[13], cp[8];
+    load_params(net, b, prm, cp);
+    const int nnz = A.rowptr[N];
+    const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, true);
+    float* pbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + 2 * tables_size(N, nnz) + 15) & ~(size_t)15));
+    for (int q = threadIdx.x; q < RN; q += nthreads) ring[q] = 0.0f;  // mu of steps past the end reads 0
+    __syncthreads();
+    const int n_blocks = (T + K - 1) / K;
+    double gG = 0.0;
+    bool owner = false;
+    if ((int)threadIdx.x >= n_cons) {
+        const int p = threadIdx.x - n_cons;
+        const int i = p / L, lane = p - (p / L) * L;
+        const bool act = i < N;
+        const int c0 = act ? tb.cptr[i] : 0, c1 = act ? tb.cptr[i + 1] : 0;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            if (blk >= 2) bar_sync(ADJ_BAR_EMPTY0 + buf, nthreads);
+            const int s_top = T - 1 - blk * K, nb = (s_top + 1) < K ? (s_top + 1) : K;
+            float* pb = pbuf + (size_t)buf * K * N;
+            for (int j = 0; j < nb; j++) {
+                const int s = s_top - j;
+                float pull = 0.0f;
+                if (act && s >= 1) {
+                    const int base = (s % R) * N;
+                    for (int e = c0 + lane; e < c1; e += L) {
+                        int a = base + tb.coff[e];
+                        a -= (a >= RN) ? RN : 0;
+                        pull += tb.cw[e] * ring[a];
+                    }
+                }
+                pull = lane_sum(pull, L);
+                if (act && lane == 0) pb[j * N + i] = pull;
+            }
+            bar_arrive(ADJ_BAR_FULL0 + buf, nthreads);
+        }
+    } else {
+        const int i = threadIdx.x / L, lane = threadIdx.x - (threadIdx.x / L) * L;
+        const bool act = i < N;
+        owner = act && lane == 0;
+        const float h = A.dt, hh = A.dt_half;
+        float lam[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) lam[v] = 0.0f;
+        if (act) {
+            const float sT = A.S[((size_t)(T - 1) * A.B + b) * N + i];
+            lam[1] = sT;
+            lam[2] = -sT;
+        }
+        float sA = 0.0f, sB = 0.0f, sa = 0.0f, sG = 0.0f;
+        for (int blk = 0; blk < n_blocks; blk++) {
+            const int buf = blk & 1;
+            bar_sync(ADJ_BAR_FULL0 + buf, nthreads);
+            const int s_top = T - 1 - blk * K, nb = (s_top + 1) < K ? (s_top + 1) : K;
+            const float* pb = pbuf + (size_t)buf * K * N;
+            for (int g = 0; g < nb; g += L) {
+                const int s_hi = s_top - g;
+                JrCoef mine;
+                float src_mine = 0.0f;
+                const int sl = s_hi - lane;
+                if (act && g + lane < nb) {
+                    const float* sc = A.scratch + (((size_t)b * A.CK + sl) * N + i) * 8;
+                    float xs[NV];
+#pragma unroll
+                    for (int v = 0; v < NV; v++) xs[v] = sc[v];
+                    mine = jr_coef(prm, cp, A.cfk, xs, sc[6], h);
+                    if (sl >= 1) src_mine = A.S[((size_t)(sl - 1) * A.B + b) * N + i];
+                } else {
+                    mine = JrCoef{};
+                }
+                for (int j = 0; j < L; j++) {
+                    const int jj = g + j;
+                    if (jj >= nb) break;
+                    const int s = s_top - jj;
+                    const JrCoef kc = shfl_coef(mine, j, L);
+                    const float src = __shfl_sync(0xffffffffu, src_mine, j, L);
+                    if (act) {
+                        float mu_c, tA, tB, ta;
+                        jr_lin_step(kc, prm, h, hh, lam, mu_c, tA, tB, ta);
+                        sA += tA;
+                        sB += tB;
+                        sa += ta;
+                        sG += mu_c * kc.dcdgain;
+                        if (lane == 0) ring[(s % R) * N + i] = mu_c * kc.dcdg;
+                        if (s >= 1) {
+                            lam[0] += pb[jj * N + i];
+                            lam[1] += src;
+                            lam[2] -= src;
+                        }
+                    }
+                }
+            }
+            bar_arrive(ADJ_BAR_EMPTY0 + buf, nthreads);
+        }
+        if (owner) {
+            A.gA[(size_t)b * N + i] = (double)sA;
+            A.gB[(size_t)b * N + i] = (double)sB;
+            A.ga[(size_t)b * N + i] = (double)sa;
+            gG = (double)sG;
+        }
+    }
+    // gain gradient: sum over nodes, a tree over the next power of two of the block (zeros past it)
+    __syncthreads();
+    int p2 = 1;
+    while (p2 < nthreads) p2 <<= 1;
+    double* red = reinterpret_cast<double*>(smem);
+    for (int q = threadIdx.x; q < p2; q += nthreads) red[q] = 0.0;
+    __syncthreads();
+    if (owner) red[threadIdx.x] = gG;
+    __syncthreads();
+    for (int o = p2 >> 1; o > 0; o >>= 1) {
+        for (int q = threadIdx.x; q < o; q += nthreads) red[q] += red[q + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.gG[b] = red[0];
+}
+
 }  // namespace
 
 // ---- launch interface used by the engine (hb_engine.cu) ----
@@ -759,6 +892,20 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         adj_source_kernel<<<grid, kpad * (SRC_TS / SRC_TT), sm2, st>>>(A);
     } else {
         const int rl = lanes;
+        // pipelined reverse: one segment, every delay >= 2K, coefficient groups inside a block
+        const int pc = (L.N * rl + 31) / 32 * 32, pthreads = 2 * pc;
+        const size_t psm = std::max(((ring_bytes + 2 * tab1 + 15) & ~(size_t)15) + 2 * (size_t)L.K * L.N * sizeof(float),
+                                    (size_t)1024 * sizeof(double));
+        int max_sm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (L.store_all && L.n_ck == 1 && L.dmin >= 2 * L.K && L.K % rl == 0 && pthreads <= ADJ_PIPE_MAXT &&
+            psm <= (size_t)max_sm) {
+            if (cudaFuncSetAttribute(adj_backward_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm) != cudaSuccess)
+                return cudaGetLastError();
+            adj_backward_pipe_kernel<<<L.B, pthreads, psm, st>>>(d_net, A, rl, pc);
+            return cudaGetLastError();
+        }
         int rthreads = 32;
         while (rthreads < L.N * rl) rthreads *= 2;
         const size_t sm = std::max(ring_bytes + 2 * tab1 + gbuf_bytes, (size_t)rthreads * sizeof(double));

@@ -153,6 +153,7 @@ struct HbAdjointLaunch {
     int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
     int slices;        // time slices of the moment pass (hb_adjoint_moment_slices)
     int pipelined;     // forward as a producer / consumer pipeline (store_all and every delay >= 2K - 1)
+    int dmin;          // smallest edge delay (steps)
     float dt, dt_half;
     const float* x0;
     const int* rowptr; const uint32_t* edges; const float* ew;

@@ -1925,6 +1925,7 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     L.moments = W->moments.p;
     L.slices = hb_adjoint_moment_slices(B, T);
     L.pipelined = (store_all && dmin >= 2 * K - 1) ? 1 : 0;
+    L.dmin = dmin;
     cudaEvent_t ev[4];
     for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
     cudaError_t ce = cudaEventRecord(ev[0], st);
