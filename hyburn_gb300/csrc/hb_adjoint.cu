@@ -2,7 +2,8 @@
 //
 // Scope: one Jansen–Rit subnetwork coupled to itself through one CSR projection with per-edge
 // delays (ring semantics of runtime.rs:125-211), Sigmoidal or Linear coupling, deterministic Heun
-// (engine.rs:710-720). The loss of sweep point b is
+// (engine.rs:710-720) or RK4 (the engine's stage order, coupling held over the step). The loss of
+// sweep point b is
 //     L_b = mean_{i,j} (FC_ij - FCt_ij)^2,   FC = Pearson correlation over t = 1..T of y = y1 - y2,
 // and the gradients are dL_b/dG (the coupling function's gain: Sigmoidal `a`, Linear `a`) and
 // dL_b/dA_i, dL_b/dB_i, dL_b/da_i for every node i (the Jansen–Rit parameters taken per node).
@@ -41,6 +42,8 @@ struct AdjArgs {
     int cfk;              // HBC_SIGMOIDAL or HBC_LINEAR
     int gain_idx;         // index of the gain in the resolved coupling row (Sigmoidal 3, Linear 0)
     float dt, dt_half;
+    int rk4;              // 1: deterministic RK4, 0: deterministic Heun
+    float dt_h2, dt_sixth;// dt / 2 and dt / 6 as the engine's RK4 uses them
     const float* x0;      // [B][N*6] initial states
     const int* rowptr;    // CSR by target [N+1]
     const uint32_t* edges;// (delay << 16) | src
@@ -209,6 +212,112 @@ __device__ __forceinline__ void jr_lin_step(const JrCoef& k, const float* prm, f
     ta = (u1[3] * k.a3x + u1[4] * k.a4x) + (u2[3] * k.a3p + u2[4] * k.a4p);
 }
 
+// The lambda-independent part of one reverse RK4 step: the Jacobian and parameter factors of the
+// Jansen-Rit arm at the four stage states x1 = x, x2 = x + h/2 k1, x3 = x + h/2 k2, x4 = x + h k3
+// (k_i = f(x_i, c), with the hardware exponential like jr_coef), and the coupling slopes.
+struct JrCoef4 {
+    float q1[4], q2[4], p0[4];          // J factors: d f4/d y0, d f5/d y0, d f3/d y1
+    float aA[4], aM[4], bB[4];          // d f3/dA = a sv0, d f4/dA = a M, d f5/dB
+    float a3[4], a4[4];                 // d f3/da, d f4/da
+    float dcdg, dcdgain;
+};
+
+// factors of one stage state y, and f(y, c) into k
+__device__ __forceinline__ void jr_stage(const float* prm, const float* y, float c, JrCoef4& k, int i, float* f) {
+    const float A = prm[0], B = prm[1], a = prm[2], b = prm[3], J = prm[7];
+    const float a1 = prm[8], a2 = prm[9], a3 = prm[10], a4 = prm[11], mu = prm[12];
+    float sv[3], dsv[3];
+    jr_sigmoids_fast(prm, y, sv, dsv);
+    const float Aa = A * a, Bb = B * b;
+    k.q1[i] = Aa * (a2 * J) * dsv[1] * (a1 * J);
+    k.q2[i] = Bb * (a4 * J) * dsv[2] * (a3 * J);
+    k.p0[i] = Aa * dsv[0];
+    const float M = (sv[1] * (a2 * J) + mu) + c;
+    k.aA[i] = a * sv[0];
+    k.aM[i] = a * M;
+    k.bB[i] = b * (sv[2] * (a4 * J));
+    k.a3[i] = A * sv[0] - 2.0f * y[3] - 2.0f * a * y[0];
+    k.a4[i] = A * M - 2.0f * y[4] - 2.0f * a * y[1];
+    if (f) {
+        f[0] = y[3];
+        f[1] = y[4];
+        f[2] = y[5];
+        f[3] = (sv[0] * Aa - y[3] * (2.0f * a)) - y[0] * (a * a);
+        f[4] = (M * Aa - y[4] * (2.0f * a)) - y[1] * (a * a);
+        f[5] = ((sv[2] * (a4 * J)) * Bb - y[5] * (2.0f * b)) - y[2] * (b * b);
+    }
+}
+
+__device__ __forceinline__ JrCoef4 jr_coef_rk4(const float* prm, const float* cp, int cfk, const float* xs, float g,
+                                               float h, float h2) {
+    JrCoef4 k;
+    const float c = coupling_post_and_grad(cfk, cp, g, k.dcdg, k.dcdgain);
+    float f[NV], y[NV];
+    jr_stage(prm, xs, c, k, 0, f);
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v] = xs[v] + f[v] * h2;
+    jr_stage(prm, y, c, k, 1, f);
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v] = xs[v] + f[v] * h2;
+    jr_stage(prm, y, c, k, 2, f);
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v] = xs[v] + f[v] * h;
+    jr_stage(prm, y, c, k, 3, nullptr);
+    return k;
+}
+
+// u^T J at stage i
+__device__ __forceinline__ void jr_vjp4(const JrCoef4& k, int i, const float* u, float na2, float nb2, float m2a,
+                                        float m2b, float* v) {
+    v[0] = u[3] * na2 + u[4] * k.q1[i] + u[5] * k.q2[i];
+    v[1] = u[3] * k.p0[i] + u[4] * na2;
+    v[2] = -u[3] * k.p0[i] + u[5] * nb2;
+    v[3] = u[0] + u[3] * m2a;
+    v[4] = u[1] + u[4] * m2a;
+    v[5] = u[2] + u[5] * m2b;
+}
+
+// adjoint of one RK4 step given the coefficients: lambda(s+1) -> lambda(s) (without the
+// delayed-coupling and loss terms), mu_c = dL/dc(s), and the parameter terms. With a_i the adjoint
+// of k_i and g_i = a_i^T J(x_i): a4 = h/6 lam, a3 = h/3 lam + h g4, a2 = h/3 lam + h/2 g3,
+// a1 = h/6 lam + h/2 g2, lambda(s) = lam + g1 + g2 + g3 + g4.
+__device__ __forceinline__ void jr_lin_step_rk4(const JrCoef4& k, const float* prm, float h, float h2, float h6,
+                                                float* lam, float& mu_c, float& tA, float& tB, float& ta) {
+    const float A = prm[0], a = prm[2], b = prm[3];
+    const float na2 = -(a * a), nb2 = -(b * b), m2a = -2.0f * a, m2b = -2.0f * b;
+    const float h3 = 2.0f * h6;
+    float ai[NV], gi[NV], gsum[NV];
+    float c4 = 0.0f;
+    tA = 0.0f;
+    tB = 0.0f;
+    ta = 0.0f;
+#pragma unroll
+    for (int v = 0; v < NV; v++) ai[v] = h6 * lam[v];                 // a4
+#pragma unroll
+    for (int st = 3; st >= 0; st--) {
+        jr_vjp4(k, st, ai, na2, nb2, m2a, m2b, gi);
+        c4 += ai[4];
+        tA += ai[3] * k.aA[st] + ai[4] * k.aM[st];
+        tB += ai[5] * k.bB[st];
+        ta += ai[3] * k.a3[st] + ai[4] * k.a4[st];
+#pragma unroll
+        for (int v = 0; v < NV; v++) gsum[v] = (st == 3) ? gi[v] : gsum[v] + gi[v];
+        if (st == 3) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) ai[v] = h3 * lam[v] + h * gi[v];   // a3
+        } else if (st == 2) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) ai[v] = h3 * lam[v] + h2 * gi[v];  // a2
+        } else if (st == 1) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) ai[v] = h6 * lam[v] + h2 * gi[v];  // a1
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; v++) lam[v] = lam[v] + gsum[v];
+    mu_c = c4 * (A * a);
+}
+
 // coupling sum of target i at step 0: every edge reads the current state (runtime.rs:166-170)
 __device__ __forceinline__ float gather_step0(const float* ring, const AdjArgs& A, int i, int lane, int L) {
     float g = 0.0f;
@@ -228,6 +337,35 @@ __device__ __forceinline__ void heun_step(const float* p, float* x, float c, flo
     hb::dfun(HBM_JR, p, 0, tmp, cc, k2);
 #pragma unroll
     for (int v = 0; v < NV; v++) x[v] = x[v] + (k1[v] + k2[v]) * dt_half;
+}
+
+// one deterministic RK4 step (the engine's stage order: x + k h/2, x + k h/2, x + k h, then
+// x + (k1 + 2 k2 + 2 k3 + k4) h/6 summed left to right; no clamp for JR)
+__device__ __forceinline__ void rk4_step(const float* p, float* x, float c, float dt, float h2, float h6) {
+    float cc[2] = {c, 0.0f}, k1[NV], k2[NV], k3[NV], k4[NV], tmp[NV];
+    hb::dfun(HBM_JR, p, 0, x, cc, k1);
+#pragma unroll
+    for (int v = 0; v < NV; v++) tmp[v] = x[v] + k1[v] * h2;
+    hb::dfun(HBM_JR, p, 0, tmp, cc, k2);
+#pragma unroll
+    for (int v = 0; v < NV; v++) tmp[v] = x[v] + k2[v] * h2;
+    hb::dfun(HBM_JR, p, 0, tmp, cc, k3);
+#pragma unroll
+    for (int v = 0; v < NV; v++) tmp[v] = x[v] + k3[v] * dt;
+    hb::dfun(HBM_JR, p, 0, tmp, cc, k4);
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        float sacc = k1[v] + k2[v] * 2.0f;
+        sacc = sacc + k3[v] * 2.0f;
+        sacc = sacc + k4[v];
+        x[v] = x[v] + sacc * h6;
+    }
+}
+
+template <bool RK4>
+__device__ __forceinline__ void adj_step(const AdjArgs& A, const float* prm, float* x, float c) {
+    if constexpr (RK4) rk4_step(prm, x, c, A.dt, A.dt_h2, A.dt_sixth);
+    else heun_step(prm, x, c, A.dt, A.dt_half);
 }
 
 __device__ __forceinline__ void load_params(const DevNet& net, int b, float* prm, float* cp) {
@@ -287,6 +425,7 @@ __device__ AdjTables stage_tables(const AdjArgs& A, unsigned char* smem, size_t 
 //   phase B (thread t = node t): the K serial Heun steps, publishing x0 into the ring.
 // mode 0: write y(t) (and checkpoints at multiples of CK, or every step's x, g when store_all);
 // mode 1: keep x(s), g(s) in the scratch. x holds the state of node threadIdx.x.
+template <bool RK4>
 __device__ void forward_steps(float* ring, float* gbuf, const AdjArgs& A, const AdjTables& tb, int b, int L, float* x,
                               const float* prm, const float* cp, int s_begin, int s_end, int mode) {
     const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K;
@@ -339,7 +478,7 @@ __device__ void forward_steps(float* ring, float* gbuf, const AdjArgs& A, const 
                     for (int v = 0; v < NV; v++) sc[v] = x[v];
                     sc[6] = g;
                 }
-                heun_step(prm, x, coupling_post(A.cfk, cp, g), A.dt, A.dt_half);
+                adj_step<RK4>(A, prm, x, coupling_post(A.cfk, cp, g));
                 const int next = (slot + 1 == R) ? 0 : slot + 1;
                 ring[next * N + t] = x[0];
                 if (mode == 0) A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
@@ -363,6 +502,7 @@ __device__ __forceinline__ void bar_arrive(int id, int count) { asm volatile("ba
 // over. The values read for block k + 1 are at least K steps old when block k starts, so the
 // consumers of block k never write them. Per step the same operations in the same order as
 // forward_steps (mode 0).
+template <bool RK4>
 __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, const AdjTables& tb, int b, int L,
                                   float* x, const float* prm, const float* cp, int n_cons) {
     const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K, T = A.T;
@@ -414,7 +554,7 @@ __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, c
 #pragma unroll
                     for (int v = 0; v < NV; v++) sc[v] = x[v];
                     sc[6] = g;
-                    heun_step(prm, x, coupling_post(A.cfk, cp, g), A.dt, A.dt_half);
+                    adj_step<RK4>(A, prm, x, coupling_post(A.cfk, cp, g));
                     const int next = (slot + 1 == R) ? 0 : slot + 1;
                     ring[next * N + t] = x[0];
                     A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
@@ -426,6 +566,7 @@ __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, c
     }
 }
 
+template <bool RK4>
 __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L, int n_cons) {
     extern __shared__ __align__(16) unsigned char smem[];
     float* ring = reinterpret_cast<float*>(smem);
@@ -443,9 +584,9 @@ __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, i
     if (uact) ring[threadIdx.x] = x[0];
     if (n_cons > 0) {
         __syncthreads();
-        forward_pipelined(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons);
+        forward_pipelined<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons);
     } else {
-        forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
+        forward_steps<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
     }
 }
 
@@ -585,16 +726,45 @@ __global__ void adj_source_kernel(AdjArgs A) {
         if (tt0 + q < nt) A.S[((size_t)(t0 + tt0 + q) * A.B + b) * N + k] = ck * (acc[q] - rk * zk[q]);
 }
 
-__device__ __forceinline__ JrCoef shfl_coef(const JrCoef& k, int src_lane, int L) {
-    JrCoef o;
+template <class C>
+__device__ __forceinline__ C shfl_coef(const C& k, int src_lane, int L) {
+    C o;
     const float* in = reinterpret_cast<const float*>(&k);
     float* out = reinterpret_cast<float*>(&o);
 #pragma unroll
-    for (int q = 0; q < (int)(sizeof(JrCoef) / 4); q++) out[q] = __shfl_sync(0xffffffffu, in[q], src_lane, L);
+    for (int q = 0; q < (int)(sizeof(C) / 4); q++) out[q] = __shfl_sync(0xffffffffu, in[q], src_lane, L);
     return o;
 }
 
+// the reverse-step coefficients and their linear step for Heun (JrCoef) or RK4 (JrCoef4)
+template <bool RK4>
+struct RevStep;
+template <>
+struct RevStep<false> {
+    using Coef = JrCoef;
+    static __device__ __forceinline__ Coef coef(const AdjArgs& A, const float* prm, const float* cp, const float* xs, float g) {
+        return jr_coef(prm, cp, A.cfk, xs, g, A.dt);
+    }
+    static __device__ __forceinline__ void lin(const AdjArgs& A, const Coef& k, const float* prm, float* lam, float& mu_c,
+                                               float& tA, float& tB, float& ta) {
+        jr_lin_step(k, prm, A.dt, A.dt_half, lam, mu_c, tA, tB, ta);
+    }
+};
+template <>
+struct RevStep<true> {
+    using Coef = JrCoef4;
+    static __device__ __forceinline__ Coef coef(const AdjArgs& A, const float* prm, const float* cp, const float* xs, float g) {
+        return jr_coef_rk4(prm, cp, A.cfk, xs, g, A.dt, A.dt_h2);
+    }
+    static __device__ __forceinline__ void lin(const AdjArgs& A, const Coef& k, const float* prm, float* lam, float& mu_c,
+                                               float& tA, float& tB, float& ta) {
+        jr_lin_step_rk4(k, prm, A.dt, A.dt_h2, A.dt_sixth, lam, mu_c, tA, tB, ta);
+    }
+};
+
+template <bool RK4>
 __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L) {
+    using RS = RevStep<RK4>;
     extern __shared__ __align__(16) unsigned char smem[];
     float* ring = reinterpret_cast<float*>(smem);  // forward ring during recompute, mu ring during reversal
     const int b = blockIdx.x, N = A.N, R = A.R, T = A.T, RN = A.R * A.N;
@@ -607,7 +777,6 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
     const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, true);
     float* gbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + 2 * tables_size(N, nnz) + 15) & ~(size_t)15));
     __syncthreads();  // the tables are staged by other threads than the ones reading a node's range
-    const float h = A.dt, hh = A.dt_half;
     float lam[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) lam[v] = 0.0f;
@@ -633,7 +802,7 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
 #pragma unroll
             for (int v = 0; v < NV; v++)
                 x[v] = uact ? A.ck_state[((size_t)seg * A.B + b) * N * NV + (size_t)threadIdx.x * NV + v] : 0.0f;
-            forward_steps(ring, gbuf, A, tb, b, L, x, prm, cp, s_begin, s_end, 1);
+            forward_steps<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, s_begin, s_end, 1);
         }
         // (b) the mu ring of the later segments into shared memory
         __syncthreads();
@@ -644,7 +813,7 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
         float sA = 0.0f, sB = 0.0f, sa = 0.0f, sG = 0.0f;
         int slot = (s_end - 1) % R;
         for (int s_hi = s_end - 1; s_hi >= s_begin; s_hi -= L) {
-            JrCoef mine;
+            typename RS::Coef mine;
             float src_mine = 0.0f;
             const int sl = s_hi - lane;
             if (act && sl >= s_begin) {
@@ -652,10 +821,10 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
                 float xs[NV];
 #pragma unroll
                 for (int v = 0; v < NV; v++) xs[v] = sc[v];
-                mine = jr_coef(prm, cp, A.cfk, xs, sc[6], h);
+                mine = RS::coef(A, prm, cp, xs, sc[6]);
                 if (sl >= 1) src_mine = A.S[((size_t)(sl - 1) * A.B + b) * N + i];
             } else {
-                mine = JrCoef{};
+                mine = typename RS::Coef{};
             }
             for (int j = 0; j < L; j++) {
                 const int s = s_hi - j;
@@ -671,11 +840,11 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
                     }
                 }
                 pull = lane_sum(pull, L);
-                const JrCoef kc = shfl_coef(mine, j, L);
+                const typename RS::Coef kc = shfl_coef(mine, j, L);
                 const float src = __shfl_sync(0xffffffffu, src_mine, j, L);
                 if (act) {
                     float mu_c, tA, tB, ta;
-                    jr_lin_step(kc, prm, h, hh, lam, mu_c, tA, tB, ta);
+                    RS::lin(A, kc, prm, lam, mu_c, tA, tB, ta);
                     sA += tA;
                     sB += tB;
                     sa += ta;
@@ -721,8 +890,10 @@ __global__ void adj_backward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, 
 // lanes and summation order as adj_backward_kernel, so the gradients are bitwise the same.
 constexpr int ADJ_PIPE_MAXT = 640;  // register budget: 102 per thread
 
+template <bool RK4>
 __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(const DevNet* __restrict__ gnet, AdjArgs A,
                                                                             int L, int n_cons) {
+    using RS = RevStep<RK4>;
     extern __shared__ __align__(16) unsigned char smem[];
     float* ring = reinterpret_cast<float*>(smem);  // mu ring
     const int b = blockIdx.x, N = A.N, R = A.R, T = A.T, RN = A.R * A.N, K = A.K;
@@ -768,7 +939,6 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
         const int i = threadIdx.x / L, lane = threadIdx.x - (threadIdx.x / L) * L;
         const bool act = i < N;
         owner = act && lane == 0;
-        const float h = A.dt, hh = A.dt_half;
         float lam[NV];
 #pragma unroll
         for (int v = 0; v < NV; v++) lam[v] = 0.0f;
@@ -785,7 +955,7 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
             const float* pb = pbuf + (size_t)buf * K * N;
             for (int g = 0; g < nb; g += L) {
                 const int s_hi = s_top - g;
-                JrCoef mine;
+                typename RS::Coef mine;
                 float src_mine = 0.0f;
                 const int sl = s_hi - lane;
                 if (act && g + lane < nb) {
@@ -793,20 +963,20 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
                     float xs[NV];
 #pragma unroll
                     for (int v = 0; v < NV; v++) xs[v] = sc[v];
-                    mine = jr_coef(prm, cp, A.cfk, xs, sc[6], h);
+                    mine = RS::coef(A, prm, cp, xs, sc[6]);
                     if (sl >= 1) src_mine = A.S[((size_t)(sl - 1) * A.B + b) * N + i];
                 } else {
-                    mine = JrCoef{};
+                    mine = typename RS::Coef{};
                 }
                 for (int j = 0; j < L; j++) {
                     const int jj = g + j;
                     if (jj >= nb) break;
                     const int s = s_top - jj;
-                    const JrCoef kc = shfl_coef(mine, j, L);
+                    const typename RS::Coef kc = shfl_coef(mine, j, L);
                     const float src = __shfl_sync(0xffffffffu, src_mine, j, L);
                     if (act) {
                         float mu_c, tA, tB, ta;
-                        jr_lin_step(kc, prm, h, hh, lam, mu_c, tA, tB, ta);
+                        RS::lin(A, kc, prm, lam, mu_c, tA, tB, ta);
                         sA += tA;
                         sB += tB;
                         sa += ta;
@@ -853,6 +1023,7 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
     AdjArgs A;
     A.B = L.B; A.N = L.N; A.T = L.T; A.R = L.R; A.K = L.K; A.CK = L.CK; A.n_ck = L.n_ck; A.store_all = L.store_all;
     A.cfk = L.cfk; A.gain_idx = L.gain_idx; A.dt = L.dt; A.dt_half = L.dt_half;
+    A.rk4 = L.rk4; A.dt_h2 = L.dt_h2; A.dt_sixth = L.dt_sixth;
     A.x0 = L.x0; A.rowptr = L.rowptr; A.edges = L.edges; A.ew = L.ew;
     A.cptr = L.cptr; A.ctgt = L.ctgt; A.cdel = L.cdel; A.cw = L.cw;
     A.Y = L.Y; A.S = L.S; A.ck_state = L.ck_state; A.ck_ring = L.ck_ring; A.scratch = L.scratch; A.mu_ring = L.mu_ring;
@@ -873,9 +1044,10 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         const int n_cons = L.pipelined ? (L.N + 31) / 32 * 32 : 0;
         const int fthreads = L.pipelined ? n_cons + (L.N * lanes + 31) / 32 * 32 : threads;
         const size_t sm = ring_bytes + tab1 + (L.pipelined ? 2 * gbuf_bytes : gbuf_bytes);
-        if (cudaFuncSetAttribute(adj_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        auto kf = L.rk4 ? adj_forward_kernel<true> : adj_forward_kernel<false>;
+        if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
             return cudaGetLastError();
-        adj_forward_kernel<<<L.B, fthreads, sm, st>>>(d_net, A, lanes, n_cons);
+        kf<<<L.B, fthreads, sm, st>>>(d_net, A, lanes, n_cons);
     } else if (phase == 1) {
         const size_t W = (size_t)(L.N + 3) / 4 * 4;
         const size_t sm = (2 * MOM_CHUNK + 1) * W * sizeof(float) + 16;
@@ -901,17 +1073,19 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (L.store_all && L.n_ck == 1 && L.dmin >= 2 * L.K && L.K % rl == 0 && pthreads <= ADJ_PIPE_MAXT &&
             psm <= (size_t)max_sm) {
-            if (cudaFuncSetAttribute(adj_backward_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm) != cudaSuccess)
+            auto kp = L.rk4 ? adj_backward_pipe_kernel<true> : adj_backward_pipe_kernel<false>;
+            if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm) != cudaSuccess)
                 return cudaGetLastError();
-            adj_backward_pipe_kernel<<<L.B, pthreads, psm, st>>>(d_net, A, rl, pc);
+            kp<<<L.B, pthreads, psm, st>>>(d_net, A, rl, pc);
             return cudaGetLastError();
         }
         int rthreads = 32;
         while (rthreads < L.N * rl) rthreads *= 2;
         const size_t sm = std::max(ring_bytes + 2 * tab1 + gbuf_bytes, (size_t)rthreads * sizeof(double));
-        if (cudaFuncSetAttribute(adj_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        auto kb = L.rk4 ? adj_backward_kernel<true> : adj_backward_kernel<false>;
+        if (cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
             return cudaGetLastError();
-        adj_backward_kernel<<<L.B, rthreads, sm, st>>>(d_net, A, rl);
+        kb<<<L.B, rthreads, sm, st>>>(d_net, A, rl);
     }
     return cudaGetLastError();
 }

@@ -154,6 +154,8 @@ struct HbAdjointLaunch {
     int slices;        // time slices of the moment pass (hb_adjoint_moment_slices)
     int pipelined;     // forward as a producer / consumer pipeline (store_all and every delay >= 2K - 1)
     int dmin;          // smallest edge delay (steps)
+    int rk4;           // deterministic RK4 (else Heun)
+    float dt_h2, dt_sixth;
     float dt, dt_half;
     const float* x0;
     const int* rowptr; const uint32_t* edges; const float* ew;

@@ -1837,7 +1837,9 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     if (hp.cf.kind != HBC_SIGMOIDAL && hp.cf.kind != HBC_LINEAR)
         return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports Sigmoidal and Linear coupling");
     if (hp.ncv != 1 || !hp.direct) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs the coupling from and into the first coupling variable");
-    if (eff_integrator(e, HBM_JR) != HBI_HEUN_DET) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint differentiates deterministic Heun");
+    const int adj_integ = eff_integrator(e, HBM_JR);
+    if (adj_integ != HBI_HEUN_DET && adj_integ != HBI_RK4)
+        return fail(HB_ERR_UNSUPPORTED, "the FC adjoint differentiates deterministic Heun or RK4");
     const int N = e->subs[0].nm, B = e->B;
     if (N > 120) return fail(HB_ERR_UNSUPPORTED, "the FC adjoint supports up to 120 nodes");
     int dmin = 1 << 30;
@@ -1916,6 +1918,7 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     L.store_all = store_all;
     L.cfk = hp.cf.kind; L.gain_idx = gain_param;
     L.dt = e->net.dt; L.dt_half = e->net.dt_half;
+    L.rk4 = adj_integ == HBI_RK4 ? 1 : 0; L.dt_h2 = e->net.dt_h2; L.dt_sixth = e->net.dt_sixth;
     L.x0 = e->x0.p; L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
     L.cptr = W->cptr.p; L.ctgt = W->ctgt.p; L.cdel = W->cdel.p; L.cw = W->cw.p;
     L.Y = W->Y.p; L.S = W->S.p; L.ck_state = W->ck_state.p; L.ck_ring = W->ck_ring.p; L.scratch = W->scratch.p;

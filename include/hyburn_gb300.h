@@ -291,7 +291,7 @@ void      hb_group_destroy(hb_group* group);
 /* ---- adjoint of a functional-connectivity loss (no counterpart in the reference, which has no adjoint) ----
  * For an engine with one JansenRit subnetwork coupled to itself through one CSR projection with
  * per-edge delays (HB_SEM_DELAY_RING), Sigmoidal or Linear coupling and the deterministic Heun
- * integrator: sweep point b runs n_steps from the engine's initial state with the coupling gain
+ * or RK4 integrator: sweep point b runs n_steps from the engine's initial state with the coupling gain
  * gain_values[b] (Sigmoidal `a`, Linear `a`); y = y1 - y2; FC = Pearson correlation over the
  * post-step states t = 1..n_steps; loss_b = mean over i, j of (FC_ij - target_fc_ij)^2 with a
  * symmetric target_fc [nnodes][nnodes]. Outputs (any pointer may be NULL): loss [n_sweep],

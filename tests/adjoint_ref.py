@@ -2,7 +2,8 @@
 
 One JansenRit subnetwork, one CSR projection with per-edge delays read with the serial engine's
 ring rules (runtime.rs:162-204: current state at step 0, zero for d > s, else the state d steps
-back), Sigmoidal or Linear coupling on y0, deterministic Heun (engine.rs:710-720). The JansenRit
+back), Sigmoidal or Linear coupling on y0, deterministic Heun (engine.rs:710-720) or RK4
+(integrator.rs RK4 stages with the coupling held over the step). The JansenRit
 A, B and a may differ per node, which the batched engine does not support; central finite
 differences of the FC loss over these per-node parameters are the check of the GPU adjoint.
 Pinned against the FP64 oracle at uniform parameters in tests/test_adjoint_ref.py.
@@ -45,7 +46,19 @@ def params_dict(params13, n, A=None, B=None, a=None):
     return p
 
 
-def forward(p, x0, indptr, indices, weights, delays, kind, cp, dt, n_steps):
+def step(p, x, c, dt, integrator):
+    """One deterministic Heun or RK4 step of the node states x [N, 6] at coupling c."""
+    k1 = jr_dfun(p, x, c)
+    if integrator == "rk4":
+        k2 = jr_dfun(p, x + 0.5 * dt * k1, c)
+        k3 = jr_dfun(p, x + 0.5 * dt * k2, c)
+        k4 = jr_dfun(p, x + dt * k3, c)
+        return x + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4)
+    k2 = jr_dfun(p, x + dt * k1, c)
+    return x + 0.5 * dt * (k1 + k2)
+
+
+def forward(p, x0, indptr, indices, weights, delays, kind, cp, dt, n_steps, integrator="heun"):
     """y1 - y2 after every step: [n_steps, N]."""
     n = x0.shape[0]
     x = np.array(x0, np.float64)
@@ -61,9 +74,7 @@ def forward(p, x0, indptr, indices, weights, delays, kind, cp, dt, n_steps):
             vals = np.where(t >= 0, hist[np.maximum(t, 0), indices], 0.0)
         g = np.bincount(rows, weights=weights * vals, minlength=n)
         c = post(kind, cp, g)
-        k1 = jr_dfun(p, x, c)
-        k2 = jr_dfun(p, x + dt * k1, c)
-        x = x + 0.5 * dt * (k1 + k2)
+        x = step(p, x, c, dt, integrator)
         hist[s + 1] = x[:, 0]
         ys[s] = x[:, 1] - x[:, 2]
     return ys
@@ -102,10 +113,10 @@ def jr_vjp(p, y, c, u):
     return out, uc, uA, uB, ua
 
 
-def adjoint(p, x0, indptr, indices, weights, delays, cp, dt, n_steps, target, dtype=np.float64):
-    """Discrete adjoint of the Heun step for the FC loss (Sigmoidal coupling), the algorithm of the
-    GPU kernels restated in NumPy: forward in `dtype`, adjoint in FP64. Returns loss and gradients
-    (gain, A, B, a)."""
+def adjoint(p, x0, indptr, indices, weights, delays, cp, dt, n_steps, target, dtype=np.float64, integrator="heun"):
+    """Discrete adjoint of the Heun (or RK4) step for the FC loss (Sigmoidal coupling), the
+    algorithm of the GPU kernels restated in NumPy: forward in `dtype`, adjoint in FP64. Returns
+    loss and gradients (gain, A, B, a)."""
     n = x0.shape[0]
     rows = np.repeat(np.arange(n), np.diff(indptr))
     cmin, cmax, mid, gain, sigma = cp
@@ -121,9 +132,12 @@ def adjoint(p, x0, indptr, indices, weights, delays, cp, dt, n_steps, target, dt
         g = np.bincount(rows, weights=(w * vals).astype(np.float64), minlength=n).astype(dtype)
         c = (cmin + (cmax - cmin) / (1.0 + np.exp(-gain * (g - mid) / sigma))).astype(dtype)
         xs[s], gs[s] = x, g
-        k1 = jr_dfun(pd, x, c).astype(dtype)
-        k2 = jr_dfun(pd, (x + dtype(dt) * k1).astype(dtype), c).astype(dtype)
-        x = (x + dtype(0.5 * dt) * (k1 + k2)).astype(dtype)
+        if integrator == "rk4":
+            x = step(pd, x, c, dtype(dt), "rk4").astype(dtype)
+        else:
+            k1 = jr_dfun(pd, x, c).astype(dtype)
+            k2 = jr_dfun(pd, (x + dtype(dt) * k1).astype(dtype), c).astype(dtype)
+            x = (x + dtype(0.5 * dt) * (k1 + k2)).astype(dtype)
         hist[s + 1] = x[:, 0]
         ys[s] = x[:, 1] - x[:, 2]
     T = n_steps
@@ -148,17 +162,38 @@ def adjoint(p, x0, indptr, indices, weights, delays, cp, dt, n_steps, target, dt
         q = 1.0 / (1.0 + np.exp(-gain * (g - mid) / sigma))
         c = cmin + (cmax - cmin) * q
         k1 = jr_dfun(p, x_s, c)
-        pp = x_s + dt * k1
-        u2 = 0.5 * dt * lam
-        vp, uc2, uA2, uB2, ua2 = jr_vjp(p, pp, c, u2)
-        u1 = 0.5 * dt * lam + dt * vp
-        vx, uc1, uA1, uB1, ua1 = jr_vjp(p, x_s, c, u1)
-        lam = lam + vp + vx
-        mu_c = uc1 + uc2
+        if integrator == "rk4":
+            # x' = x + h/6 (k1 + 2 k2 + 2 k3 + k4), k_i = f(x_i): x2 = x + h/2 k1, x3 = x + h/2 k2, x4 = x + h k3
+            x2 = x_s + 0.5 * dt * k1
+            k2 = jr_dfun(p, x2, c)
+            x3 = x_s + 0.5 * dt * k2
+            k3 = jr_dfun(p, x3, c)
+            x4 = x_s + dt * k3
+            a4 = (dt / 6.0) * lam
+            g4, uc4, uA4, uB4, ua4 = jr_vjp(p, x4, c, a4)
+            a3 = (dt / 3.0) * lam + dt * g4
+            g3, uc3, uA3, uB3, ua3 = jr_vjp(p, x3, c, a3)
+            a2 = (dt / 3.0) * lam + 0.5 * dt * g3
+            g2, uc2, uA2, uB2, ua2 = jr_vjp(p, x2, c, a2)
+            a1 = (dt / 6.0) * lam + 0.5 * dt * g2
+            g1, uc1, uA1, uB1, ua1 = jr_vjp(p, x_s, c, a1)
+            lam = lam + g1 + g2 + g3 + g4
+            mu_c = uc1 + uc2 + uc3 + uc4
+            gA += uA1 + uA2 + uA3 + uA4
+            gB += uB1 + uB2 + uB3 + uB4
+            ga += ua1 + ua2 + ua3 + ua4
+        else:
+            pp = x_s + dt * k1
+            u2 = 0.5 * dt * lam
+            vp, uc2, uA2, uB2, ua2 = jr_vjp(p, pp, c, u2)
+            u1 = 0.5 * dt * lam + dt * vp
+            vx, uc1, uA1, uB1, ua1 = jr_vjp(p, x_s, c, u1)
+            lam = lam + vp + vx
+            mu_c = uc1 + uc2
+            gA += uA1 + uA2
+            gB += uB1 + uB2
+            ga += ua1 + ua2
         dq = (cmax - cmin) * q * (1.0 - q)
-        gA += uA1 + uA2
-        gB += uB1 + uB2
-        ga += ua1 + ua2
         gG += float(np.sum(mu_c * dq * (g - mid) / sigma))
         mug[s] = mu_c * dq * gain / sigma
         if s >= 1:

@@ -1,5 +1,5 @@
-"""FC-loss adjoint (hb_engine_adjoint_fc) against central finite differences of the FP64 NumPy
-forward, and against the engine's own forward run. Relative errors are 2-norms over each gradient
+"""FC-loss adjoint (hb_engine_adjoint_fc), for deterministic Heun and RK4, against central finite
+differences of the FP64 NumPy forward, and against the engine's own forward run. Relative errors are 2-norms over each gradient
 vector (the gain, and the per-node A, B, a of one sweep point); the bounds are given below.
 
 Step of the differences: h = 1e-6. With h = 1e-3 the central difference has not converged for the
@@ -30,20 +30,20 @@ GAINS = [0.8, 1.25]
 CP = lambda g: (0.0, 0.1, 0.0, g, 0.05)
 
 
-def ref_setup():
-    cfg = jr_case(N, 1.0)
+def ref_setup(integrator="heun"):
+    cfg = jr_case(N, 1.0, integrator=integrator)
     sub = cfg.network.subnetworks[0]
     x0 = np.asarray(sub.initial_state, np.float64).reshape(N, 6)
     indptr, indices, data, delays = arrays(cfg)
     tgt_ys = ar.forward(ar.params_dict(sub.params, N), x0, indptr, indices, data, delays, "Sigmoidal", CP(0.4),
-                        cfg.dt, T)
+                        cfg.dt, T, integrator)
     target = np.corrcoef(tgt_ys.T)
     return cfg, sub, x0, (indptr, indices, data, delays), target
 
 
 def loss_at(sub, x0, net, cfg, target, gain, A=None, B=None, a=None):
     p = ar.params_dict(sub.params, N, A, B, a)
-    ys = ar.forward(p, x0, *net, "Sigmoidal", CP(gain), cfg.dt, T)
+    ys = ar.forward(p, x0, *net, "Sigmoidal", CP(gain), cfg.dt, T, cfg.integrator)
     return ar.fc_loss(ys, target)[0]
 
 
@@ -51,8 +51,9 @@ def rel(g, fd):
     return float(np.linalg.norm(g - fd) / max(np.linalg.norm(fd), 1e-30))
 
 
-def test_adjoint_forward_and_loss_match_engine_and_fp64():
-    cfg, sub, x0, net, target = ref_setup()
+@pytest.mark.parametrize("integrator", ["heun", "rk4"])
+def test_adjoint_forward_and_loss_match_engine_and_fp64(integrator):
+    cfg, sub, x0, net, target = ref_setup(integrator)
     eng = BatchHybridEngine.from_config(cfg, len(GAINS), semantics=HB_SEM_DELAY_RING)
     r = eng.adjoint_fc(GAINS, T, target, checkpoint_every=64, return_y=True)
     g = eng.run_sweep_with_trajectory(SweepParam(-1, 3), GAINS, T)
@@ -64,10 +65,13 @@ def test_adjoint_forward_and_loss_match_engine_and_fp64():
         assert abs(r.loss[b] - l64) <= 1e-4 * abs(l64), (r.loss[b], l64)
 
 
-def test_adjoint_gradients_match_central_differences():
-    cfg, sub, x0, net, target = ref_setup()
+@pytest.mark.parametrize("integrator,checkpoint_every", [("heun", 64), ("heun", 0), ("rk4", 64), ("rk4", 0)])
+def test_adjoint_gradients_match_central_differences(integrator, checkpoint_every):
+    """checkpoint_every 64: segments re-computed from checkpoints (two-phase forward); 0: every
+    step kept (pipelined forward and reverse)."""
+    cfg, sub, x0, net, target = ref_setup(integrator)
     eng = BatchHybridEngine.from_config(cfg, len(GAINS), semantics=HB_SEM_DELAY_RING)
-    r = eng.adjoint_fc(GAINS, T, target, checkpoint_every=64)
+    r = eng.adjoint_fc(GAINS, T, target, checkpoint_every=checkpoint_every)
     A0, B0, a0 = (float(sub.params[k]) for k in range(3))
     for b, gain in enumerate(GAINS):
         fd_g = (loss_at(sub, x0, net, cfg, target, gain + H_FD) - loss_at(sub, x0, net, cfg, target, gain - H_FD)) / (2 * H_FD)
@@ -92,8 +96,9 @@ def test_adjoint_gradients_match_central_differences():
         assert errs["a"] <= 5e-4, (b, errs)
 
 
-def test_adjoint_checkpoint_interval_changes_only_summation_rounding():
-    cfg, sub, x0, net, target = ref_setup()
+@pytest.mark.parametrize("integrator", ["heun", "rk4"])
+def test_adjoint_checkpoint_interval_changes_only_summation_rounding(integrator):
+    cfg, sub, x0, net, target = ref_setup(integrator)
     eng = BatchHybridEngine.from_config(cfg, len(GAINS), semantics=HB_SEM_DELAY_RING)
     r1 = eng.adjoint_fc(GAINS, T, target, checkpoint_every=64)
     r2 = eng.adjoint_fc(GAINS, T, target, checkpoint_every=T)
