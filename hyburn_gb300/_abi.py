@@ -283,6 +283,11 @@ class hb_adjoint_out(C.Structure):
                 ("reverse_ms", C.c_float)]
 
 
+class hb_order_adjoint_out(C.Structure):
+    _fields_ = [("loss", C.POINTER(C.c_double)), ("d_gain", C.POINTER(C.c_double)), ("d_omega", C.POINTER(C.c_double)),
+                ("forward_ms", C.c_float), ("prepare_ms", C.c_float), ("reverse_ms", C.c_float)]
+
+
 class hb_fc_features(C.Structure):
     _fields_ = [("fc", C.POINTER(C.c_float)), ("features", C.POINTER(C.c_float)), ("fcd", C.POINTER(C.c_float)),
                 ("fcd_stats", C.POINTER(C.c_float)), ("n_windows", C.c_int32), ("nnodes", C.c_int32),
@@ -336,6 +341,7 @@ def load_library():
         "hb_npy_read_f32": (I32, [C.c_char_p, FP, I64, C.POINTER(I64), I32, C.POINTER(I32), C.POINTER(I64)]),
         "hb_engine_write_tavg": (I32, [P, P, C.c_char_p]),
         "hb_engine_fc_features": (I32, [P, I32, I32, I32, C.POINTER(hb_fc_features)]),
+        "hb_engine_adjoint_order": (I32, [P, FP, I32, I64, C.POINTER(hb_order_adjoint_out)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

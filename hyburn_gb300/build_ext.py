@@ -34,6 +34,7 @@ UNITS = [
     ("hb_noalloc.cu", ["--fmad=false"]),
     ("hb_io.cu", []),
     ("hb_features.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_kuradj.cu", ["--fmad=false", "-lineinfo"]),
 ]
 
 

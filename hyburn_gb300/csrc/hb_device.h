@@ -186,6 +186,22 @@ struct HbFeatLaunch {
 cudaError_t hb_launch_fc_features(const HbFeatLaunch& L, cudaStream_t st);
 size_t hb_fc_part_len(int nnodes);  // doubles of one range's moments in HbFeatLaunch::part
 
+// the Kuramoto order-parameter adjoint (hb_kuradj.cu); device pointers
+struct HbKuraAdjLaunch {
+    const float* traj;   // [T][B][N] phases after each step
+    const float* x0;     // [B][N] initial phases
+    int B, N, T, K;      // K: steps per reverse block (<= 8 and <= every delay)
+    float dt;
+    const float* k;      // [B] the coupling's a / N as the engine resolves it
+    const int* rowptr; const uint32_t* edges; const float* ew;          // CSR by target
+    const int* cptr; const int* ctgt; const int* cdel; const float* cw;  // CSC by source
+    float* sc;           // [B][N][T + 1][2] sin, cos of every phase
+    float* z;            // [B][T][2] mean cos, mean sin after each step
+    float* nu;           // [B][N][T][2] the pulled adjoint terms
+    double* loss; double* gA; double* gW;  // [B]
+};
+cudaError_t hb_launch_kura_adjoint(const HbKuraAdjLaunch& L, int phase, cudaStream_t st);
+
 // time slices of the moment pass for B points of T steps: enough blocks to fill the SMs three times
 // over, at most 16, each slice at least 64 steps
 inline int hb_adjoint_moment_slices(int B, int T) {

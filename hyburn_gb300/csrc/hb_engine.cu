@@ -1497,6 +1497,99 @@ const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
     if (len) *len = (int64_t)r->traj[i].size();
     return r->traj[i].data();
 }
+hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_t n_values, int64_t n_steps,
+                                  hb_order_adjoint_out* out) {
+    if (!e || !gain_values || !out) return fail(HB_ERR_INVALID_STATE, "NULL argument");
+    if (n_values != e->B) return fail(HB_ERR_INVALID_STATE, "expected %d gain values, got %d", e->B, n_values);
+    if (n_steps < 2 || n_steps > (1 << 28)) return fail(HB_ERR_INVALID_STATE, "n_steps must be in [2, 2^28]");
+    if (e->subs.size() != 1 || e->projs.size() != 1 || e->subs[0].model != HBM_KURAMOTO || e->subs[0].nmodes != 1)
+        return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint needs one Kuramoto subnetwork (one mode) and one projection");
+    HostProj& hp = e->projs[0];
+    if (hp.kind != W_SPARSE || hp.dmode != HBD_EDGE || hp.cf.kind != HBC_KURAMOTO || hp.ncv != 1)
+        return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint needs Kuramoto coupling through a CSR projection with "
+                    "per-edge delays (HB_SEM_DELAY_RING)");
+    if (eff_integrator(e, HBM_KURAMOTO) != HBI_HEUN_DET)
+        return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint differentiates deterministic Heun");
+    const int N = e->subs[0].nm, B = e->B, T = (int)n_steps;
+    if (N > 1024) return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint supports up to 1024 nodes");
+    int dmin = 1 << 30;
+    for (uint32_t m : hp.edges) dmin = std::min(dmin, (int)(m >> 16));
+    if (hp.edges.empty()) dmin = 8;
+    if (dmin < 1) return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint needs every edge delay >= 1");
+    const int K = std::min(dmin, 8);
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const double need = (double)B * N * ((double)(T + 1) * 8 + (double)T * 8 + (double)T * 4) + (double)B * T * 8;
+    if (need > 0.8 * (double)free_b)
+        return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint needs %.2f GB of device memory, %.2f GB free", need / 1e9,
+                    free_b / 1e9);
+    // forward: the engine's own run from its initial state, every step's phase kept on the device
+    hb_status s = hb_engine_reset(e);
+    if (s) return s;
+    hb_result* res = nullptr;
+    s = hb_engine_run_sweep(e, -1, 0, gain_values, n_values, n_steps, HB_RUN_DEVICE_TRAJECTORY, nullptr, 0, &res);
+    if (s) return s;
+    hb_result_free(res);
+    const float forward_ms = (float)e->last_ms;
+    // out-edges of every source node (transpose of the CSR rows)
+    std::vector<int> cptr(N + 1, 0), ctgt(hp.edges.size()), cdel(hp.edges.size());
+    std::vector<float> cw(hp.edges.size()), kh(B);
+    for (uint32_t m : hp.edges) cptr[(m & 0xffffu) + 1]++;
+    for (int j = 0; j < N; j++) cptr[j + 1] += cptr[j];
+    {
+        std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+        for (int i = 0; i < N; i++)
+            for (int q = hp.rowptr[i]; q < hp.rowptr[i + 1]; q++) {
+                const int src = (int)(hp.edges[q] & 0xffffu), c = fill[src]++;
+                ctgt[c] = i; cdel[c] = (int)(hp.edges[q] >> 16); cw[c] = hp.ew[q];
+            }
+    }
+    // the coupling's a / N as the engine resolves it for each point
+    for (int b = 0; b < B; b++) kh[b] = gain_values[b] / (float)hp.nsrc;
+    DBuf<int> d_cptr, d_ctgt, d_cdel;
+    DBuf<float> d_cw, d_k, d_sc, d_z, d_nu;
+    DBuf<double> d_loss, d_gA, d_gW;
+    cudaStream_t st = e->stream();
+    const size_t nnz = std::max<size_t>(hp.edges.size(), 1);
+    CUDA_TRY(d_cptr.ensure(N + 1)); CUDA_TRY(d_ctgt.ensure(nnz)); CUDA_TRY(d_cdel.ensure(nnz)); CUDA_TRY(d_cw.ensure(nnz));
+    CUDA_TRY(d_k.ensure(B));
+    CUDA_TRY(d_sc.ensure((size_t)B * N * (T + 1) * 2)); CUDA_TRY(d_z.ensure((size_t)B * T * 2));
+    CUDA_TRY(d_nu.ensure((size_t)B * N * T * 2));
+    CUDA_TRY(d_loss.ensure(B)); CUDA_TRY(d_gA.ensure(B)); CUDA_TRY(d_gW.ensure(B));
+    CUDA_TRY(cudaMemcpyAsync(d_cptr.p, cptr.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
+    if (!hp.edges.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(d_ctgt.p, ctgt.data(), ctgt.size() * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_cdel.p, cdel.data(), cdel.size() * 4, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(d_cw.p, cw.data(), cw.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_k.p, kh.data(), B * 4, cudaMemcpyHostToDevice, st));
+    HbKuraAdjLaunch L;
+    memset(&L, 0, sizeof L);
+    L.traj = e->dtraj.p; L.x0 = e->x0.p; L.B = B; L.N = N; L.T = T; L.K = K; L.dt = e->net.dt; L.k = d_k.p;
+    L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
+    L.cptr = d_cptr.p; L.ctgt = d_ctgt.p; L.cdel = d_cdel.p; L.cw = d_cw.p;
+    L.sc = d_sc.p; L.z = d_z.p; L.nu = d_nu.p; L.loss = d_loss.p; L.gA = d_gA.p; L.gW = d_gW.p;
+    cudaEvent_t ev[3];
+    for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
+    cudaError_t ce = cudaEventRecord(ev[0], st);
+    if (ce == cudaSuccess) ce = hb_launch_kura_adjoint(L, 0, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev[1], st);
+    if (ce == cudaSuccess) ce = hb_launch_kura_adjoint(L, 1, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ev[2], st);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(ev[2]);
+    float ms[2] = {0, 0};
+    for (int q = 0; q < 2 && ce == cudaSuccess; q++) ce = cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]);
+    for (auto& v : ev) cudaEventDestroy(v);
+    if (ce != cudaSuccess) return fail(HB_ERR_CUDA, "order-parameter adjoint: %s", cudaGetErrorString(ce));
+    if (out->loss) CUDA_TRY(cudaMemcpy(out->loss, d_loss.p, B * 8, cudaMemcpyDeviceToHost));
+    if (out->d_gain) CUDA_TRY(cudaMemcpy(out->d_gain, d_gA.p, B * 8, cudaMemcpyDeviceToHost));
+    if (out->d_omega) CUDA_TRY(cudaMemcpy(out->d_omega, d_gW.p, B * 8, cudaMemcpyDeviceToHost));
+    out->forward_ms = forward_ms;
+    out->prepare_ms = ms[0];
+    out->reverse_ms = ms[1];
+    return HB_OK;
+}
+
 hb_status hb_engine_fc_features(hb_engine* e, int32_t sub_idx, int32_t window_len, int32_t stride, hb_fc_features* out) {
     if (!e || !out) return fail(HB_ERR_INVALID_STATE, "hb_engine_fc_features: null argument");
     if (sub_idx < 0 || sub_idx >= (int32_t)e->subs.size()) return fail(HB_ERR_INVALID_STATE, "subnetwork index %d out of range", sub_idx);

@@ -116,6 +116,17 @@ class FcFeatures:
 
 
 @dataclass
+class OrderAdjointResult:
+    """Time-averaged Kuramoto order parameter and its gradients (hb_engine_adjoint_order)."""
+    loss: np.ndarray      # [n_sweep]
+    d_gain: np.ndarray    # [n_sweep] dL/da, the coupling scale
+    d_omega: np.ndarray   # [n_sweep] dL/domega
+    forward_ms: float = 0.0
+    prepare_ms: float = 0.0
+    reverse_ms: float = 0.0
+
+
+@dataclass
 class AdjointResult:
     """Loss and gradients of a functional-connectivity fit (hb_engine_adjoint_fc)."""
     loss: np.ndarray          # [n_sweep]
@@ -269,6 +280,20 @@ class BatchHybridEngine:
         raise_for(st, self._lib.hb_last_error().decode())
         return FcFeatures(fc=fc, features=feat, fcd=fcd if nw else None, fcd_stats=fcds if window_len else None,
                           n_windows=int(nw), ms=float(out.ms))
+
+    def adjoint_order(self, gain_values, n_steps: int) -> OrderAdjointResult:
+        """Kuramoto: loss = time average of the order parameter R over n_steps from the initial state
+        (the engine is reset), with the coupling scale a = gain_values[b] per point; gradients with
+        respect to a and omega by the discrete adjoint on the GPU."""
+        g = np.ascontiguousarray(np.asarray(gain_values, np.float32))
+        B = self.n_sweep
+        loss, dg, dw = (np.zeros(B, np.float64) for _ in range(3))
+        out = _abi.hb_order_adjoint_out()
+        dp = C.POINTER(C.c_double)
+        out.loss, out.d_gain, out.d_omega = (a.ctypes.data_as(dp) for a in (loss, dg, dw))
+        st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), C.byref(out))
+        raise_for(st, self._lib.hb_last_error().decode())
+        return OrderAdjointResult(loss, dg, dw, out.forward_ms, out.prepare_ms, out.reverse_ms)
 
     def adjoint_fc(self, gain_values, n_steps: int, target_fc, checkpoint_every: int = 500,
                    return_y: bool = False) -> AdjointResult:

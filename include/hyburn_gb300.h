@@ -317,6 +317,24 @@ typedef struct hb_adjoint_out {
 hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,
                                const float* target_fc, int32_t checkpoint_every, hb_adjoint_out* out);
 
+/* ---- adjoint of the time-averaged Kuramoto order parameter (no counterpart in the reference) ----
+ * For an engine with one Kuramoto subnetwork (one mode) coupled to itself through one CSR projection
+ * with per-edge delays (HB_SEM_DELAY_RING), Kuramoto coupling and deterministic Heun: the engine is
+ * reset and runs n_steps with the coupling scale a = gain_values[b] for sweep point b, keeping
+ * every step's phase on the device; loss_b = (1/n_steps) sum_{t=1..n_steps} R_b(t) with
+ * R = |mean_j exp(i theta_j)|. Outputs (any pointer may be NULL): loss, d_gain = dL/da and
+ * d_omega = dL/domega, [n_sweep] each, and the device times of the forward run, the preparation
+ * (sin / cos rows, order parameter) and the reverse sweep. The phase wrap to [0, 2 pi) is taken with
+ * derivative 1 (the loss depends on the phases only through sin and cos). */
+typedef struct hb_order_adjoint_out {
+    double* loss;
+    double* d_gain;
+    double* d_omega;
+    float   forward_ms, prepare_ms, reverse_ms;
+} hb_order_adjoint_out;
+hb_status hb_engine_adjoint_order(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,
+                                  hb_order_adjoint_out* out);
+
 /* ---- functional-connectivity features on the device (sbi/features/fc.rs, mod.rs:257-280) ----
  * From the trajectory of the engine's last run, which must have used HB_RUN_DEVICE_TRAJECTORY, for
  * every sweep point and state variable of subnetwork sub_idx: the node series (mean over modes)
