@@ -401,6 +401,29 @@ def run_other_workload(args):
                         roofline={"bound": "hbm", "achieved": bytes_ / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": bytes_ / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bytes_ / ns, "traffic": None})
+        elif args.workload == "kuramoto-adjoint":
+            # Kuramoto 1000 nodes x 256 points (the kuramoto workload's network): loss = time average of
+            # the order parameter over T steps, gradients w.r.t. the coupling scale and omega
+            T = args.run_steps or 2_000
+            cfg, meta = inputs.kuramoto_scale(n=1000, n_points=256, n_steps=T, bold=False)
+            eng = BatchHybridEngine.from_config(cfg, 256, semantics=HB_SEM_DELAY_RING)
+            eng.prepare(SweepParam(-1, 0), meta["values"], T)
+            fwd_ms, _ = _time_prepared(eng, args.steps, args.warmup)
+            for _ in range(max(1, args.warmup)):
+                eng.adjoint_order(meta["values"], T)
+            tot, parts = [], None
+            for _ in range(args.steps):
+                r = eng.adjoint_order(meta["values"], T)
+                tot.append(r.forward_ms + r.prepare_ms + r.reverse_ms)
+                parts = (r.forward_ms, r.prepare_ms, r.reverse_ms)
+            ms = statistics.median(tot)
+            eng.close()
+            line.update(metric="gradient evaluations/s", value=256 / (ms / 1e3), unit="points/s", ms_per_step=ms,
+                        config={"workload": f"kuramoto-1000n-256pt-csr5pct-delays-{meta['min_delay']}-{meta['max_delay']}"
+                                            f"-heun-{T}steps-order-parameter-loss",
+                                "gradients": "coupling scale, omega", "trajectory": "kept in HBM"},
+                        adjoint={"forward_ms": parts[0], "prepare_ms": parts[1], "reverse_ms": parts[2],
+                                 "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -486,7 +509,7 @@ def main():
     ap.add_argument("--two-phase", action="store_true", help="batch each block's gathers before its updates")
     ap.add_argument("--no-pipe", action="store_true", help="do not use the warp-specialised pipeline")
     ap.add_argument("--pipe-lanes", type=int, default=0, help="pipeline producer threads per node (0: engine's choice)")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "fc"],
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint", "fc"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()
