@@ -341,7 +341,7 @@ def load_library():
         "hb_npy_read_f32": (I32, [C.c_char_p, FP, I64, C.POINTER(I64), I32, C.POINTER(I32), C.POINTER(I64)]),
         "hb_engine_write_tavg": (I32, [P, P, C.c_char_p]),
         "hb_engine_fc_features": (I32, [P, I32, I32, I32, C.POINTER(hb_fc_features)]),
-        "hb_engine_adjoint_order": (I32, [P, FP, I32, I64, C.POINTER(hb_order_adjoint_out)]),
+        "hb_engine_adjoint_order": (I32, [P, FP, I32, I64, U32, C.POINTER(hb_order_adjoint_out)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -125,6 +125,7 @@ struct RunArgs {
     const float* noise;   // noise rows of this launch: [n_steps][row] or [n_steps][B][row]
     int noise_per_point;
     float* traj;          // [n_steps][B][state_len] or nullptr
+    float* gx_out;        // [n_steps][B][nm][2] the two coupling sums of every step (Kuramoto), or nullptr
     int ring_in_smem;     // resident kernel: ring cached in shared memory
     int smem_edges;       // resident kernel: edges cached in shared memory
     int sync_every;       // specialised kernel: steps between CTA barriers (<= smallest delay, R >= H + sync_every)
@@ -195,6 +196,7 @@ struct HbKuraAdjLaunch {
     const float* k;      // [B] the coupling's a / N as the engine resolves it
     const int* rowptr; const uint32_t* edges; const float* ew;          // CSR by target
     const int* cptr; const int* ctgt; const int* cdel; const float* cw;  // CSC by source
+    const float* cs;     // [T][B][N][2] the forward's coupling sums S, C of every step, or nullptr
     float* sc;           // [B][N][T + 1][2] sin, cos of every phase
     float* z;            // [B][T][2] mean cos, mean sin after each step
     float* nu;           // [B][N][T][2] the pulled adjoint terms

@@ -268,6 +268,7 @@ struct hb_engine {
     DBuf<float> state, x0, tavg, ring, noise, prep_noise, traj, means;
     DBuf<float> dtraj;          // HB_RUN_DEVICE_TRAJECTORY: [dtraj_steps][B][state_len] of the last run
     int64_t dtraj_steps = 0;    // 0: the last run kept no device trajectory
+    float* cs_out = nullptr;    // the order-parameter adjoint's request for the coupling sums of every step
     DBuf<float> fe_fc, fe_feat, fe_fcd, fe_fcds, fe_ut;  // hb_engine_fc_features outputs and workspace
     DBuf<double> fe_part, fe_mv;
     // streamed-history kernel: its own ring [B][nm][rp + K][channels]; the layout of the history
@@ -833,6 +834,7 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         }
         float* traj_dst = dev_traj ? e->dtraj.p + (size_t)c0 * B * e->state_len : e->traj.p;
         a.traj = (record || dev_traj) ? traj_dst : nullptr;
+        a.gx_out = e->cs_out ? e->cs_out + (size_t)c0 * B * e->subs[0].nm * 2 : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
         if (P.single_m) CUDA_TRY(hb_launch_single(e->kernel_model, P.single_m, e->d_net, a, B, st));
         else if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
@@ -1498,7 +1500,7 @@ const float* hb_result_trajectory(const hb_result* r, int32_t i, int64_t* len) {
     return r->traj[i].data();
 }
 hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_t n_values, int64_t n_steps,
-                                  hb_order_adjoint_out* out) {
+                                  uint32_t run_flags, hb_order_adjoint_out* out) {
     if (!e || !gain_values || !out) return fail(HB_ERR_INVALID_STATE, "NULL argument");
     if (n_values != e->B) return fail(HB_ERR_INVALID_STATE, "expected %d gain values, got %d", e->B, n_values);
     if (n_steps < 2 || n_steps > (1 << 28)) return fail(HB_ERR_INVALID_STATE, "n_steps must be in [2, 2^28]");
@@ -1519,18 +1521,26 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     const int K = std::min(dmin, 8);
     size_t free_b = 0, total_b = 0;
     CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    const double need = (double)B * N * ((double)(T + 1) * 8 + (double)T * 8 + (double)T * 4) + (double)B * T * 8;
+    const double need = (double)B * N * ((double)(T + 1) * 8 + (double)T * 8 + (double)T * 4 + (double)T * 8) +
+                        (double)B * T * 8;
     if (need > 0.8 * (double)free_b)
         return fail(HB_ERR_UNSUPPORTED, "the order-parameter adjoint needs %.2f GB of device memory, %.2f GB free", need / 1e9,
                     free_b / 1e9);
     // forward: the engine's own run from its initial state, every step's phase kept on the device
+    // (the pipeline and streamed-history kernels also write the coupling sums S, C of every step)
+    DBuf<float> d_cs;
+    CUDA_TRY(d_cs.ensure((size_t)T * B * N * 2));
     hb_status s = hb_engine_reset(e);
     if (s) return s;
     hb_result* res = nullptr;
-    s = hb_engine_run_sweep(e, -1, 0, gain_values, n_values, n_steps, HB_RUN_DEVICE_TRAJECTORY, nullptr, 0, &res);
+    e->cs_out = d_cs.p;
+    s = hb_engine_run_sweep(e, -1, 0, gain_values, n_values, n_steps,
+                            (run_flags & ~HB_RUN_TRAJECTORY) | HB_RUN_DEVICE_TRAJECTORY, nullptr, 0, &res);
+    e->cs_out = nullptr;
     if (s) return s;
     hb_result_free(res);
     const float forward_ms = (float)e->last_ms;
+    const bool have_cs = e->last_kind == 3 || e->last_kind == 4;
     // out-edges of every source node (transpose of the CSR rows)
     std::vector<int> cptr(N + 1, 0), ctgt(hp.edges.size()), cdel(hp.edges.size());
     std::vector<float> cw(hp.edges.size()), kh(B);
@@ -1569,6 +1579,7 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
     L.cptr = d_cptr.p; L.ctgt = d_ctgt.p; L.cdel = d_cdel.p; L.cw = d_cw.p;
     L.sc = d_sc.p; L.z = d_z.p; L.nu = d_nu.p; L.loss = d_loss.p; L.gA = d_gA.p; L.gW = d_gW.p;
+    L.cs = have_cs ? d_cs.p : nullptr;
     cudaEvent_t ev[3];
     for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
     cudaError_t ce = cudaEventRecord(ev[0], st);

@@ -14,7 +14,8 @@
 //                        sc [B][N][T + 1][2] (t = 0 is the initial phase)
 //   kura_order_kernel    the order parameter's components per step: z [B][T][2] (t = 1..T)
 //   kura_reverse_kernel  one CTA per point, one thread per node, in blocks of K steps from the end:
-//                        (A) each node gathers S, C of the block's steps over its in-edges and pulls
+//                        (A) each node reads S, C of the block's steps (written by the forward's
+//                        consumers, else gathered again over its in-edges) and pulls
 //                        sum_e w_e nu_tgt(s + d_e) over its out-edges; (B) each node runs the
 //                        block's steps of
 //                          lambda(s) = lambda(s+1) (1 + dt dc/dth) + cos th P_c + sin th P_s + dR/dth / T
@@ -122,7 +123,19 @@ __global__ void __launch_bounds__(1024) kura_reverse_kernel(HbKuraAdjLaunch L) {
             float sS[8], sC[8], pc[8], ps[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) { sS[j] = 0.0f; sC[j] = 0.0f; pc[j] = 0.0f; ps[j] = 0.0f; }
-            for (int e = r0; e < r1; e++) {
+            if (L.cs) {
+                // the sums the forward used, written by its consumers
+                const float2* cs = reinterpret_cast<const float2*>(L.cs);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (j < nb) {
+                        const float2 v = cs[((size_t)(s_top - j) * L.B + b) * N + i];
+                        sS[j] = v.x;
+                        sC[j] = v.y;
+                    }
+                }
+            }
+            for (int e = L.cs ? r1 : r0; e < r1; e++) {
                 const uint32_t m = L.edges[e];
                 const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
                 const float w = L.ew[e];

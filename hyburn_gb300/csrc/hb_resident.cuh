@@ -1324,6 +1324,9 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                     float gx[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                     for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
+                    if (PCH == 2 && a.gx_out)
+                        __stcs(reinterpret_cast<float2*>(a.gx_out) + ((size_t)(it0 + j) * B + b) * nm + n,
+                               make_float2(gx[0], gx[PCH - 1]));
                     float nz[NVAR];
 #pragma unroll
                     for (int v = 0; v < NVAR; v++) nz[v] = stoch ? nbuf[(size_t)j * nm * NVAR + n * NVAR + v] * net.noise_scale[v] : 0.0f;

@@ -529,6 +529,9 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                     float gx[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                     for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
+                    if (PCH == 2 && a.gx_out)
+                        __stcs(reinterpret_cast<float2*>(a.gx_out) + ((size_t)(it0 + j) * B + b) * nm + n,
+                               make_float2(gx[0], gx[PCH - 1]));
                     float nz[NVAR];
 #pragma unroll
                     for (int v = 0; v < NVAR; v++) {

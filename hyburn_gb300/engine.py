@@ -281,7 +281,7 @@ class BatchHybridEngine:
         return FcFeatures(fc=fc, features=feat, fcd=fcd if nw else None, fcd_stats=fcds if window_len else None,
                           n_windows=int(nw), ms=float(out.ms))
 
-    def adjoint_order(self, gain_values, n_steps: int) -> OrderAdjointResult:
+    def adjoint_order(self, gain_values, n_steps: int, run_flags: int = 0) -> OrderAdjointResult:
         """Kuramoto: loss = time average of the order parameter R over n_steps from the initial state
         (the engine is reset), with the coupling scale a = gain_values[b] per point; gradients with
         respect to a and omega by the discrete adjoint on the GPU."""
@@ -291,7 +291,7 @@ class BatchHybridEngine:
         out = _abi.hb_order_adjoint_out()
         dp = C.POINTER(C.c_double)
         out.loss, out.d_gain, out.d_omega = (a.ctypes.data_as(dp) for a in (loss, dg, dw))
-        st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), C.byref(out))
+        st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), int(run_flags), C.byref(out))
         raise_for(st, self._lib.hb_last_error().decode())
         return OrderAdjointResult(loss, dg, dw, out.forward_ms, out.prepare_ms, out.reverse_ms)
 

@@ -324,8 +324,11 @@ hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int3
  * every step's phase on the device; loss_b = (1/n_steps) sum_{t=1..n_steps} R_b(t) with
  * R = |mean_j exp(i theta_j)|. Outputs (any pointer may be NULL): loss, d_gain = dL/da and
  * d_omega = dL/domega, [n_sweep] each, and the device times of the forward run, the preparation
- * (sin / cos rows, order parameter) and the reverse sweep. The phase wrap to [0, 2 pi) is taken with
- * derivative 1 (the loss depends on the phases only through sin and cos). */
+ * (sin / cos rows, order parameter) and the reverse sweep. run_flags (HB_RUN_*) choose the forward's
+ * kernel form as for hb_engine_run_sweep; the pipeline and streamed-history forms also hand the
+ * coupling sums of every step to the reverse sweep, which otherwise gathers them again. The phase
+ * wrap to [0, 2 pi) is taken with derivative 1 (the loss depends on the phases only through sin
+ * and cos). */
 typedef struct hb_order_adjoint_out {
     double* loss;
     double* d_gain;
@@ -333,7 +336,7 @@ typedef struct hb_order_adjoint_out {
     float   forward_ms, prepare_ms, reverse_ms;
 } hb_order_adjoint_out;
 hb_status hb_engine_adjoint_order(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,
-                                  hb_order_adjoint_out* out);
+                                  uint32_t run_flags, hb_order_adjoint_out* out);
 
 /* ---- functional-connectivity features on the device (sbi/features/fc.rs, mod.rs:257-280) ----
  * From the trajectory of the engine's last run, which must have used HB_RUN_DEVICE_TRAJECTORY, for

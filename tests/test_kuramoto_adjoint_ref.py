@@ -57,8 +57,9 @@ def test_fp64_adjoint_matches_central_differences():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,T,dt", [(16, 300, 0.1), (40, 500, 0.05)])
-def test_gpu_order_adjoint_matches_central_differences(n, T, dt):
+@pytest.mark.parametrize("n,T,dt,form", [(16, 300, 0.1, "pipe"), (40, 500, 0.05, "pipe"), (16, 300, 0.1, "stream"),
+                                        (40, 500, 0.05, "stream"), (16, 300, 0.1, "generic")])
+def test_gpu_order_adjoint_matches_central_differences(n, T, dt, form):
     """hb_engine_adjoint_order against central differences (h = 1e-6) of the FP64 forward. The GPU
     differentiates its FP32 trajectory, whose phases drift from the FP64 ones by ~1e-6 over these
     runs: the loss agrees within 1e-4 (relative; measured 1e-5), each gradient within
@@ -72,8 +73,15 @@ def test_gpu_order_adjoint_matches_central_differences(n, T, dt):
     omega, h = float(sub.params[0]), 1e-6
     gains = [0.6, 1.9]
     eng = BatchHybridEngine.from_config(cfg, len(gains), semantics=HB_SEM_DELAY_RING)
-    r = eng.adjoint_order(gains, T)
+    from hyburn_gb300._abi import HB_RUN_GENERIC, HB_RUN_STREAM
+    flags = {"pipe": 0, "stream": HB_RUN_STREAM, "generic": HB_RUN_GENERIC}[form]
+    r = eng.adjoint_order(gains, T, run_flags=flags)
+    kind = eng.last_kernel_time()[2]
     eng.close()
+    print(f"forward kernel kind {kind}")
+    # pipeline (3) and streamed-history (4) forms hand their coupling sums to the reverse sweep; the
+    # generic resident form (1) does not, and the reverse gathers them again
+    assert kind == {"pipe": 3, "stream": 4, "generic": 1}[form]
 
     def L(om, aa):
         return kr.order_loss(kr.forward(th0, om, aa, *net, cfg.dt, T)[0])
