@@ -215,10 +215,20 @@ int parse_cvar_map(const char* s, int* ps, int* pt, int maxn) {
     return n;
 }
 
+// a device allocation owned by its holder (freed on destruction; move-only)
 template <typename T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
     cudaError_t ensure(size_t count) {
         if (count <= n && p) return cudaSuccess;
         if (p) cudaFree(p);
