@@ -142,3 +142,17 @@ def test_device_fc_features_errors_and_empty_fcd():
     f = _check(eng, r, cfg, 2, 100, 50)   # (120 - 100) / 50 + 1 = 1 window: no FCD, NaN stats
     assert f.n_windows == 0 and f.fcd is None and np.isnan(f.fcd_stats).all()
     eng.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [2, 3, 5])
+def test_device_fc_features_few_nodes(n):
+    """Two to five nodes: one to ten upper-triangle values, homotopic pairs n // 2, and the median
+    of very short value lists."""
+    from cases import single_model
+    from hyburn_gb300 import SweepParam
+    cfg = single_model("Generic2dOscillator", n, "heun", "Linear", (0.05,), weights="csr", delays="per_edge_long",
+                       density=1.0, seed=7)
+    eng, r = _run(cfg, 2, 400, SweepParam(-1, 0), [0.0, 0.1])
+    _check(eng, r, cfg, 2, 100, 50)
+    eng.close()

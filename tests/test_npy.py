@@ -193,3 +193,52 @@ def test_sweep_writes_tavg_files(tmp_path):
     r2 = npy.run_batch_sweep(cfg, 0, 4, vals, 40, str(tmp_path / "cli"))
     assert (tmp_path / "cli" / "tavg_sub0.npy").read_bytes() == npy_ref.write_bytes(r2.tavg[0], [3, 2, 6])
     assert np.array_equal(r.tavg[0], r2.tavg[0])
+
+
+def test_reader_matches_oracle_on_generated_headers(tmp_path):
+    """Seeded random headers built from the pieces the scanner cares about (keys inside and outside
+    string literals, either quote, spacing, tuples with odd entries, descriptors, trailing or
+    missing data): the library and the oracle agree on every one, value or error."""
+    rng = np.random.default_rng(11)
+    keys_descr = ["'<f4'", "'|f4'", "'f4'", "'<f8'", "'>f4'", "'<i4'", '"<f4"', "'<f4", "<f4"]
+    shapes = ["(3,)", "(1, 3)", "(3, 1, )", "( 3 )", "(+3,)", "(3,x)", "()", "(1, (3))", "3", "(0,)"]
+    noise = ["", " ", "'fortran_order': False, ", "'note': \"'shape': (9,)\", ", "'x': 'y', ", '"q": "\'", ']
+    checked = 0
+    for k in range(300):
+        parts = []
+        for _ in range(3):
+            if rng.random() < 0.5:
+                parts.append(noise[rng.integers(len(noise))])
+        q = "'" if rng.random() < 0.8 else '"'
+        items = [f"{q}descr{q}: {keys_descr[rng.integers(len(keys_descr))]}, ",
+                 f"{q}shape{q}:{' ' * int(rng.integers(0, 3))}{shapes[rng.integers(len(shapes))]}, "]
+        if rng.random() < 0.1:
+            items.pop(int(rng.integers(2)))
+        order = rng.permutation(len(items) + len(parts))
+        allp = items + parts
+        header = "{" + "".join(allp[i] for i in order) + "}\n"
+        h = header.encode()
+        n_vals = int(rng.integers(0, 6))
+        payload = np.arange(n_vals, dtype=np.float32).tobytes() if rng.random() < 0.7 else \
+            np.arange(n_vals, dtype=np.float64).tobytes()
+        if rng.random() < 0.1:
+            payload += b"\x00\x01"
+        b = b"\x93NUMPY" + bytes([1 if rng.random() < 0.7 else 2, 0])
+        b += struct.pack("<H", len(h)) if b[6] == 1 else struct.pack("<I", len(h))
+        b += h + payload
+        p = tmp_path / f"g{k}.npy"
+        p.write_bytes(b)
+        try:
+            want = npy_ref.read_bytes(b)
+        except npy_ref.NpyError as e:
+            with pytest.raises(InvalidState) as got:
+                npy.read_npy_f32(str(p))
+            if "unclosed" not in str(e):
+                assert str(e) == str(got.value), header
+            checked += 1
+            continue
+        vals, shape = npy.read_npy_f32(str(p))
+        assert shape == want[1], header
+        assert vals.tobytes() == np.asarray(want[0], np.float32).tobytes(), header
+        checked += 1
+    assert checked == 300
