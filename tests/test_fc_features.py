@@ -71,7 +71,7 @@ def _run(cfg, n_pts, n_steps, param, vals, noise=None):
     return eng, r
 
 
-def _check(eng, r, cfg, n_pts, window, stride):
+def _check(eng, r, cfg, n_pts, window, stride, fcd_atol=FCD_ATOL):
     sub = cfg.network.subnetworks[0]
     from hyburn_gb300.config import MODEL_REGISTRY
     nvar = MODEL_REGISTRY[sub.model][0]
@@ -82,8 +82,8 @@ def _check(eng, r, cfg, n_pts, window, stride):
     if window:
         assert f.n_windows == (fcd.shape[2] if fcd.ndim == 4 else 0)
         if f.n_windows:
-            np.testing.assert_allclose(f.fcd, fcd, atol=FCD_ATOL, rtol=0)
-        np.testing.assert_allclose(f.fcd_stats, fcds, atol=FCD_ATOL, rtol=0, equal_nan=True)
+            np.testing.assert_allclose(f.fcd, fcd, atol=fcd_atol, rtol=0)
+        np.testing.assert_allclose(f.fcd_stats, fcds, atol=fcd_atol, rtol=0, equal_nan=True)
     return f
 
 
@@ -148,11 +148,13 @@ def test_device_fc_features_errors_and_empty_fcd():
 @pytest.mark.parametrize("n", [2, 3, 5])
 def test_device_fc_features_few_nodes(n):
     """Two to five nodes: one to ten upper-triangle values, homotopic pairs n // 2, and the median
-    of very short value lists."""
+    of very short value lists. With three nodes each window FC has three upper-triangle values, and
+    the Pearson correlation of two such triples is ill conditioned: FP32 rounding of the FC entries
+    (~1e-7) moves it by up to ~5e-5 (measured 5.06e-5), so the FCD bound is 5e-4 there."""
     from cases import single_model
     from hyburn_gb300 import SweepParam
     cfg = single_model("Generic2dOscillator", n, "heun", "Linear", (0.05,), weights="csr", delays="per_edge_long",
                        density=1.0, seed=7)
     eng, r = _run(cfg, 2, 400, SweepParam(-1, 0), [0.0, 0.1])
-    _check(eng, r, cfg, 2, 100, 50)
+    _check(eng, r, cfg, 2, 100, 50, fcd_atol=5e-4 if n <= 3 else FCD_ATOL)
     eng.close()
