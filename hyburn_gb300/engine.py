@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from itertools import product
 from typing import List, Optional, Sequence, Tuple
 

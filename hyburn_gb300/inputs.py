@@ -8,12 +8,11 @@ max 1; uniform tract lengths converted to integer delays with ``ceil(L / speed /
 from __future__ import annotations
 
 from dataclasses import dataclass
-from typing import List, Optional, Tuple
+from typing import List, Tuple
 
 import numpy as np
 
-from .config import (DEFAULT_PARAMS, MODEL_REGISTRY, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig,
-                     SubnetworkConfig, tract_lengths_to_delays)
+from .config import (DEFAULT_PARAMS, MonitorConfig, NetworkConfig, ProjectionConfig, SimConfig, SubnetworkConfig, tract_lengths_to_delays)
 
 G2DO_BENCH_PARAMS = [1.0, 0.0, -2.0, -10.0, 0.0, 0.02, 3.0, 1.0, 0.0, 1.0, 1.0, 1.0]
 

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from hyburn_gb300.config import (DEFAULT_PARAMS, MODEL_REGISTRY, MonitorConfig, NetworkConfig, ProjectionConfig,
+from hyburn_gb300.config import (DEFAULT_PARAMS, MODEL_REGISTRY, NetworkConfig, ProjectionConfig,
                                  SimConfig, SubnetworkConfig)
 from hyburn_gb300.inputs import connectome, tract_lengths_to_delays
 

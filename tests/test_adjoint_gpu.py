@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, SweepParam
-from hyburn_gb300._abi import HB_SEM_DELAY_RING, HB_RUN_TRAJECTORY
+from hyburn_gb300._abi import HB_SEM_DELAY_RING
 
 import adjoint_ref as ar
 from test_adjoint_ref import arrays, jr_case

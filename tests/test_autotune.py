@@ -1,5 +1,4 @@
 """Autotuner host logic on CPU (fake timings) and on the GPU (the chosen form matches the oracle)."""
-import numpy as np
 import pytest
 
 from hyburn_gb300 import SweepParam, autotune

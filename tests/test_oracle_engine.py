@@ -2,14 +2,13 @@
 (src/engine/batch_engine/engine.rs:1431-3058) and the semantics the CUDA engine is checked
 against (history shift window, per-edge ring, multi-sweep rules)."""
 import numpy as np
-import pytest
 
 from hyburn_gb300 import SweepParam, SweepPoint, SweepSpec
 from hyburn_gb300._abi import HB_SEM_DELAY_RING, HB_SEM_NOISE_PER_POINT
 from hyburn_gb300.config import DEFAULT_PARAMS, NetworkConfig, ProjectionConfig, SimConfig, SubnetworkConfig
 from oracle.hb_oracle import OracleEngine
 
-from cases import noise_for, single_model, sub, three_subnet_ring
+from cases import noise_for, single_model, three_subnet_ring
 
 
 def g2do_cfg(n=4, integrator="heun", init=None, projections=()):

@@ -7,7 +7,6 @@ trusted as the checker of the CUDA engine.
 import math
 
 import numpy as np
-import pytest
 
 from oracle import hb_oracle as O
 

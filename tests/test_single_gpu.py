@@ -1,9 +1,8 @@
 """One-warp-per-point kernel (Scalar coupling onto itself without delay): parity with the oracle for
 the plain single simulation and for sweeps, in mean-field and diagonal form."""
-import numpy as np
 import pytest
 
-from hyburn_gb300 import BatchHybridEngine, SweepParam
+from hyburn_gb300 import SweepParam
 from hyburn_gb300._abi import HB_SEM_NOISE_PER_POINT, HB_SEM_SCALAR_DIAGONAL
 
 from cases import NATIVE_SWEEP, noise_for, single_model, sweep_values
