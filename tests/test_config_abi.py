@@ -162,3 +162,16 @@ def test_create_rejects_invalid_descriptors_before_touching_the_gpu():
     gt.network.projections[0].coupling_params = [1, 1, 1, 1, 0.5, 1, 1]
     with pytest.raises(Unsupported, match="global_t"):
         BatchHybridEngine.from_config(gt, 2)
+
+
+def test_new_entry_points_reject_null_arguments_without_a_gpu():
+    """NPY, tavg, feature and adjoint entry points validate their arguments before any CUDA call."""
+    lib = _abi.load_library()
+    assert lib.hb_npy_write_f32(None, None, None, 0) == _abi.HB_ERR_INVALID_STATE
+    assert lib.hb_npy_read_f32(None, None, 0, None, 0, None, None) == _abi.HB_ERR_INVALID_STATE
+    assert lib.hb_engine_write_tavg(None, None, b"x") == _abi.HB_ERR_INVALID_STATE
+    out = _abi.hb_fc_features()
+    assert lib.hb_engine_fc_features(None, 0, 0, 1, C.byref(out)) == _abi.HB_ERR_INVALID_STATE
+    oa = _abi.hb_order_adjoint_out()
+    assert lib.hb_engine_adjoint_order(None, None, 0, 10, 0, C.byref(oa)) == _abi.HB_ERR_INVALID_STATE
+    assert b"NULL" in lib.hb_last_error() or b"null" in lib.hb_last_error()
