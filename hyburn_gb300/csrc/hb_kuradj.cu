@@ -16,7 +16,8 @@
 //   kura_reverse_kernel  one CTA per point, one thread per node, in blocks of K steps from the end:
 //                        (A) each node reads S, C of the block's steps (written by the forward's
 //                        consumers, else gathered again over its in-edges) and pulls
-//                        sum_e w_e nu_tgt(s + d_e) over its out-edges; (B) each node runs the
+//                        sum_e w_e nu_tgt(s + d_e) over its out-edges, two windows in flight;
+//                        (B) each node runs the
 //                        block's steps of
 //                          lambda(s) = lambda(s+1) (1 + dt dc/dth) + cos th P_c + sin th P_s + dR/dth / T
 //                        writing nu(s) = lambda(s+1) dt k (cos th(s), sin th(s)) for the pulls of
@@ -118,54 +119,77 @@ __global__ void __launch_bounds__(1024) kura_reverse_kernel(HbKuraAdjLaunch L) {
     const int n_blocks = (T + K - 1) / K;
     for (int blk = 0; blk < n_blocks; blk++) {
         const int s_top = T - 1 - blk * K, nb = (s_top + 1) < K ? (s_top + 1) : K;
-        // (A) gathers over in-edges and pulls over out-edges for the block's steps
+        // (A) S, C of the block's steps (the forward's, else gathered again over the in-edges), and
+        // the pulls over the out-edges, two windows in flight per iteration
         if (act) {
-            float sS[8], sC[8], pc[8], ps[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) { sS[j] = 0.0f; sC[j] = 0.0f; pc[j] = 0.0f; ps[j] = 0.0f; }
             if (L.cs) {
-                // the sums the forward used, written by its consumers
                 const float2* cs = reinterpret_cast<const float2*>(L.cs);
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j < nb) {
-                        const float2 v = cs[((size_t)(s_top - j) * L.B + b) * N + i];
-                        sS[j] = v.x;
-                        sC[j] = v.y;
-                    }
+                for (int j = 0; j < nb; j++) {
+                    const float2 v = cs[((size_t)(s_top - j) * L.B + b) * N + i];
+                    Sb[j * N + i] = v.x;
+                    Cb[j * N + i] = v.y;
                 }
-            }
-            for (int e = L.cs ? r1 : r0; e < r1; e++) {
-                const uint32_t m = L.edges[e];
-                const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
-                const float w = L.ew[e];
-                const float2* rs = sc + (size_t)src * (T + 1);
+            } else {
+                float sS[8], sC[8];
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j < nb) {
-                        const int s = s_top - j;
-                        const int t = (s == 0) ? 0 : s - d;  // step 0 reads the current state
-                        if (t >= 0) {
-                            const float2 v = rs[t];
-                            sS[j] += w * v.x;
-                            sC[j] += w * v.y;
+                for (int j = 0; j < 8; j++) { sS[j] = 0.0f; sC[j] = 0.0f; }
+                for (int e = r0; e < r1; e++) {
+                    const uint32_t m = L.edges[e];
+                    const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
+                    const float w = L.ew[e];
+                    const float2* rs = sc + (size_t)src * (T + 1);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (j < nb) {
+                            const int s = s_top - j;
+                            const int t = (s == 0) ? 0 : s - d;  // step 0 reads the current state
+                            if (t >= 0) {
+                                const float2 v = rs[t];
+                                sS[j] += w * v.x;
+                                sC[j] += w * v.y;
+                            }
                         }
                     }
                 }
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (j < nb) { Sb[j * N + i] = sS[j]; Cb[j * N + i] = sC[j]; }
             }
-            for (int e = c0; e < c1; e++) {
+            float pc[8], ps[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) { pc[j] = 0.0f; ps[j] = 0.0f; }
+            int e = c0;
+            for (; e + 1 < c1; e += 2) {
+                const int tg0 = L.ctgt[e], d0 = L.cdel[e], tg1 = L.ctgt[e + 1], d1 = L.cdel[e + 1];
+                const float w0 = L.cw[e], w1 = L.cw[e + 1];
+                const float2* rn0 = nu + (size_t)tg0 * T;
+                const float2* rn1 = nu + (size_t)tg1 * T;
+                float2 v0[8], v1[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int t0 = s_top - j + d0, t1 = s_top - j + d1;
+                    v0[j] = (j < nb && t0 <= T - 1) ? rn0[t0] : make_float2(0.0f, 0.0f);
+                    v1[j] = (j < nb && t1 <= T - 1) ? rn1[t1] : make_float2(0.0f, 0.0f);
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    pc[j] += w0 * v0[j].x;
+                    ps[j] += w0 * v0[j].y;
+                    pc[j] += w1 * v1[j].x;
+                    ps[j] += w1 * v1[j].y;
+                }
+            }
+            if (e < c1) {
                 const int tg = L.ctgt[e], d = L.cdel[e];
                 const float w = L.cw[e];
                 const float2* rn = nu + (size_t)tg * T;
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
-                    if (j < nb) {
-                        const int t = s_top - j + d;
-                        if (t <= T - 1) {
-                            const float2 v = rn[t];
-                            pc[j] += w * v.x;
-                            ps[j] += w * v.y;
-                        }
+                    const int t = s_top - j + d;
+                    if (j < nb && t <= T - 1) {
+                        const float2 v = rn[t];
+                        pc[j] += w * v.x;
+                        ps[j] += w * v.y;
                     }
                 }
             }
@@ -173,8 +197,6 @@ __global__ void __launch_bounds__(1024) kura_reverse_kernel(HbKuraAdjLaunch L) {
             for (int j = 0; j < 8; j++) {
                 if (j < nb) {
                     const float2 th = sc[(size_t)i * (T + 1) + (s_top - j)];
-                    Sb[j * N + i] = sS[j];
-                    Cb[j * N + i] = sC[j];
                     Pb[j * N + i] = th.y * pc[j] + th.x * ps[j];
                 }
             }
