@@ -158,6 +158,21 @@ def calibrated_cpu_reference(n_threads, target_s=12.0):
     return rate, sample
 
 
+CPU_BASELINE_NOTE = ("the oracle: a C restatement (-O3, no fused multiply-add) of the reference's NdArray batch "
+                     "path, OpenMP over sweep points like rayon_batch_sweep (engine.rs:1363-1429); it is not the "
+                     "reference's NdArray code, which the reference publishes at 3.62e6 node-steps/s on 32 EPYC "
+                     "cores for a simpler undelayed 128 x 74 G2DO sweep (docs/BENCHMARK_EXAMPLES.md:32)")
+
+
+def cpu_baseline_line(target_s=12.0):
+    """The oracle timed on all host cores (value) and on one core, each on a bounded sample."""
+    n_threads = os.cpu_count() or 1
+    rate, sample = calibrated_cpu_reference(n_threads, target_s)
+    rate1, sample1 = calibrated_cpu_reference(1, target_s)
+    return {"value": rate, "unit": "node-steps/s", "cores": n_threads, "kind": "port", "sample": sample,
+            "single_thread": {"value": rate1, "cores": 1, "sample": sample1}, "note": CPU_BASELINE_NOTE}
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -194,7 +209,7 @@ def run_reference_arm(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "points": N_POINTS, "nodes": N_NODES, "steps_per_run": N_STEPS},
             "cpu_baseline": {"value": v, "unit": "node-steps/s", "cores": n_threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "note": CPU_BASELINE_NOTE},
             "e2e": {"value": v, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -372,7 +387,8 @@ def run_other_workload(args):
             ns = 256 * 1000 * T
             line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
                         config={"workload": f"kuramoto-1000n-256pt-csr5pct-delays-{meta['min_delay']}-{meta['max_delay']}"
-                                            f"-heun-bold-{T}steps (of 100000)", "kernel_kind": kind},
+                                            f"-heun-bold-{T}steps (of 100000)", "kernel_kind": kind,
+                                "omega": "per node, N(0, 1) (seed 5)"},
                         roofline={"bound": "hbm", "achieved": bpns * ns / (ms / 1e3) / 1e9, "peak": peak,
                                   "unit": "GB/s", "frac": bpns * ns / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bpns, "traffic": None})
@@ -381,9 +397,10 @@ def run_other_workload(args):
             T = args.run_steps or 20_000
             members, ns, bytes_ = [], 0, 0.0
             for n in (68, 84, 164, 400):
+                # 16 coupling scales G x 8 values of eta per size; eta through per-point parameter tables
                 cfg, meta = inputs.mpr_grid(n, 128, T, seed=3, bold=True)
                 eng = BatchHybridEngine.from_config(cfg, 128, semantics=HB_SEM_DELAY_RING)
-                members.append((eng, SweepParam(-1, 0), list(np.linspace(0.0, 1.0, 128)), T, None))
+                members.append((eng, SweepParam(-1, 0), meta["values"], T, None))
                 nnz = len(cfg.network.projections[0].weights["data"])
                 ns += 128 * n * T
                 bytes_ += 128 * T * (8.0 * nnz + 8.0 * n)
@@ -396,8 +413,9 @@ def run_other_workload(args):
                 times.append(g.last_kernel_time())
             ms = statistics.median(times)
             line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
-                        config={"workload": f"mpr-68/84/164/400n-x128pt-csr20pct-per-edge-delays-rk4-dt0.05-bold-"
-                                            f"{T}steps (of 1200000), one grouped launch", "kernel_kind": 5},
+                        config={"workload": f"mpr-68/84/164/400n-x128pt-(G16xeta8)-csr20pct-per-edge-delays-rk4-dt0.05-bold-"
+                                            f"{T}steps (of 1200000), one grouped launch", "kernel_kind": 5,
+                                "grid": "per size: G in linspace(0, 1, 16) x eta in linspace(-6, -3, 8)"},
                         roofline={"bound": "hbm", "achieved": bytes_ / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": bytes_ / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bytes_ / ns, "traffic": None})
@@ -421,7 +439,8 @@ def run_other_workload(args):
             line.update(metric="gradient evaluations/s", value=256 / (ms / 1e3), unit="points/s", ms_per_step=ms,
                         config={"workload": f"kuramoto-1000n-256pt-csr5pct-delays-{meta['min_delay']}-{meta['max_delay']}"
                                             f"-heun-{T}steps-order-parameter-loss",
-                                "gradients": "coupling scale, omega", "trajectory": "kept in HBM"},
+                                "omega": "per node, N(0, 1) (seed 5)",
+                                "gradients": "coupling scale, omega per node", "trajectory": "kept in HBM"},
                         adjoint={"forward_ms": parts[0], "prepare_ms": parts[1], "reverse_ms": parts[2],
                                  "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
         elif args.workload == "fc":
@@ -476,19 +495,21 @@ def run_other_workload(args):
             eng.prepare(SweepParam(-1, 3), gains, T)
             fwd_ms, _ = _time_prepared(eng, args.steps, args.warmup)
             eng.reset()
-            target = np.eye(n, dtype=np.float32)
+            target = inputs.jr_target_fc(cfg, T)
+            K = 500
             for _ in range(max(1, args.warmup)):
-                eng.adjoint_fc(gains, T, target, checkpoint_every=0)
+                eng.adjoint_fc(gains, T, target, checkpoint_every=K)
             tot, parts = [], None
             for _ in range(args.steps):
-                r = eng.adjoint_fc(gains, T, target, checkpoint_every=0)
+                r = eng.adjoint_fc(gains, T, target, checkpoint_every=K)
                 tot.append(r.forward_ms + r.statistics_ms + r.reverse_ms)
                 parts = (r.forward_ms, r.statistics_ms, r.reverse_ms)
             ms = statistics.median(tot)
             line.update(metric="gradient evaluations/s", value=B / (ms / 1e3), unit="points/s", ms_per_step=ms,
                         higher_is_better=True,
                         config={"workload": f"jr-74n-64pt-sigmoidal-csr-delays-heun-{T}steps-fc-loss",
-                                "gradients": "coupling gain, per-node A, B, a", "trajectory": "kept in HBM"},
+                                "gradients": "coupling gain, per-node A, B, a",
+                                "checkpoint_every": K, "target_fc": "FC of y1 - y2 of a seeded forward run (gain 1, initial state seed 40)"},
                         adjoint={"forward_ms": parts[0], "statistics_ms": parts[1], "reverse_ms": parts[2],
                                  "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
     line["clocks"] = clk.summary()
@@ -629,9 +650,7 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        rate, sample = calibrated_cpu_reference(os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": rate, "unit": "node-steps/s", "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": sample}
+        line["cpu_baseline"] = cpu_baseline_line()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if backend_ready:

@@ -4,7 +4,7 @@ The public surface mirrors the reference's engine API (src/engine/batch_engine/e
 TOML configuration (src/config.rs); the compute runs in hand-written sm_103a CUDA kernels loaded
 from the in-tree C-ABI library ``hyburn_gb300/_lib/libhyburn_gb300.so``.
 """
-from .config import (BackendError, InvalidConfig, InvalidState, IOError_, MonitorConfig, NetworkConfig,
+from .config import (BackendError, DeviceTimeout, InvalidConfig, InvalidState, IOError_, MonitorConfig, NetworkConfig,
                      NonFinite, ProjectionConfig, SimConfig, SimulationError, SubnetworkConfig, SweepConfig,
                      Unsupported, parse_sweep_param)
 from .engine import BatchHybridEngine, BatchSweepResult, GroupedSweep, SweepParam, SweepPoint, SweepSpec, noise_shape
@@ -13,5 +13,5 @@ __all__ = [
     "BatchHybridEngine", "BatchSweepResult", "GroupedSweep", "SweepParam", "SweepPoint", "SweepSpec", "SimConfig",
     "NetworkConfig", "SubnetworkConfig", "ProjectionConfig", "MonitorConfig", "SweepConfig",
     "parse_sweep_param", "noise_shape", "SimulationError", "InvalidConfig", "InvalidState", "BackendError",
-    "IOError_", "NonFinite", "Unsupported",
+    "IOError_", "NonFinite", "Unsupported", "DeviceTimeout",
 ]

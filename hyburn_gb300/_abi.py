@@ -12,7 +12,7 @@ from typing import Any, List, Optional, Sequence
 
 import numpy as np
 
-HB_ABI_VERSION = 1
+HB_ABI_VERSION = 2
 
 HB_OK = 0
 HB_ERR_INVALID_CONFIG = 1
@@ -58,6 +58,7 @@ def HB_RUN_STREAM_NPT(n: int) -> int:
 HB_RUN_STREAM_PREFETCH = 1 << 27
 HB_RUN_PIPE_WIDE = 1 << 28
 HB_RUN_DEVICE_TRAJECTORY = 1 << 29
+HB_RUN_TEST_UNSET_WAIT = 1 << 30
 
 
 def HB_RUN_LANES(n: int) -> int:
@@ -84,6 +85,8 @@ class hb_subnet_desc(C.Structure):
         ("n_params", C.c_int32),
         ("initial_state", C.POINTER(C.c_float)),
         ("n_initial_state", C.c_int64),
+        ("node_params", C.POINTER(C.c_float)),
+        ("n_node_params", C.c_int64),
     ]
 
 
@@ -186,6 +189,12 @@ def build_sim_desc(cfg, resolved_states: Sequence[np.ndarray], flags: int = 0) -
         sub_arr[i].n_params = params.size
         sub_arr[i].initial_state = f32p(x0)
         sub_arr[i].n_initial_state = x0.size
+        node_params = getattr(s, "node_params", None)
+        if node_params is not None:
+            npar = _arr(node_params, np.float32).ravel()
+            keep.append(npar)
+            sub_arr[i].node_params = f32p(npar)
+            sub_arr[i].n_node_params = npar.size
         nv = MODEL_INFO.get(s.model, (0, 0, 0))[0]
         nvars.append(nv)
         nodes.append(int(s.nnodes) * int(s.nmodes))
@@ -285,6 +294,7 @@ class hb_adjoint_out(C.Structure):
 
 class hb_order_adjoint_out(C.Structure):
     _fields_ = [("loss", C.POINTER(C.c_double)), ("d_gain", C.POINTER(C.c_double)), ("d_omega", C.POINTER(C.c_double)),
+                ("d_omega_node", C.POINTER(C.c_double)),
                 ("forward_ms", C.c_float), ("prepare_ms", C.c_float), ("reverse_ms", C.c_float)]
 
 

@@ -37,6 +37,10 @@ class NonFinite(SimulationError):
     pass
 
 
+class DeviceTimeout(BackendError):
+    """A bounded device-side wait gave up (HB_ERR_TIMEOUT)."""
+
+
 class Unsupported(SimulationError):
     pass
 
@@ -107,6 +111,10 @@ class SubnetworkConfig:
     initial_state: InitialState
     params: List[float]
     nmodes: int = 1
+    # Extension of this engine (not in the reference's SubnetworkConfig): parameter rows per node,
+    # [nnodes*nmodes, n_params] shared by all sweep points or [n_sweep, nnodes*nmodes, n_params];
+    # they replace `params` node by node, and a swept model parameter still takes its sweep value.
+    node_params: Optional[Any] = None
 
 
 @dataclass

@@ -52,7 +52,16 @@ struct DevSub {
     int n_mean_out;   // mean-field projections whose source is this subnetwork
     int mean_out[HB_MAX_PROJ];
     const float* params;   // [B][HB_PSTRIDE]
+    const float* node_params;  // [B or 1][nm][HB_PSTRIDE] per-node rows (extension), or nullptr
+    int node_pp;               // node_params holds one table per sweep point
 };
+
+// parameter row of node `n` of sweep point `b` of a subnetwork: its node row when the subnetwork has
+// per-node parameters, else the point's row
+__host__ __device__ inline const float* hb_param_row(const DevSub& s, int b, int n) {
+    return s.node_params ? s.node_params + ((size_t)(s.node_pp ? b : 0) * s.nm + n) * HB_PSTRIDE
+                         : s.params + (size_t)b * HB_PSTRIDE;
+}
 
 struct DevProj {
     int src, tgt, kind, dmode, delay, nsrc, ntgt;
@@ -138,6 +147,7 @@ struct RunArgs {
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error
     int check_finite;
+    int test_unset_wait;  // pipeline kernel: one bounded wait on a barrier nothing completes (timeout test)
     DevBold bold;
 };
 
@@ -201,6 +211,7 @@ struct HbKuraAdjLaunch {
     float* z;            // [B][T][2] mean cos, mean sin after each step
     float* nu;           // [B][N][T][2] the pulled adjoint terms
     double* loss; double* gA; double* gW;  // [B]
+    double* gWn;         // [B][N] dL/domega_i per node, or nullptr
 };
 cudaError_t hb_launch_kura_adjoint(const HbKuraAdjLaunch& L, int phase, cudaStream_t st);
 

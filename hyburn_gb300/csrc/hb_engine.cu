@@ -131,6 +131,8 @@ bool cfn_parse(const char* name, const float* cp, int n, Cfn& f) {
 struct HostSub {
     int model, nnodes, nmodes, nm, nvar, ncvar, nparams;
     std::vector<float> params, x0;
+    std::vector<float> node_params;  // [nm][nparams] or [B][nm][nparams] (extension), empty for none
+    bool node_pp = false;            // node_params holds one table per sweep point
 };
 
 enum { W_MEAN = 0, W_DIAG = 1, W_SPARSE = 2 };
@@ -252,6 +254,8 @@ struct BoldHost {
 
 struct RunTables {
     std::vector<std::vector<float>> params;  // per sub [B][PSTRIDE]
+    std::vector<std::vector<float>> node_params;  // per sub [Bn][nm][PSTRIDE] (Bn = 1 or B), empty without node rows
+    std::vector<int> node_pp;                // per sub: node table per point (Bn = B)
     std::vector<int> sweep_form;
     std::vector<std::vector<float>> cp_pp;   // per proj [B][NCP] or empty
     std::vector<float> param_values;
@@ -287,6 +291,7 @@ struct hb_engine {
     int hist_layout = 0, hist_rp = 0;
     int hist_R = 0;           // ring length (slots) of the time-major history the last run left
     std::vector<DBuf<float>> d_params;
+    std::vector<DBuf<float>> d_node_params;
     DBuf<int> flags_buf;
     std::vector<BoldHost> bold;
     cudaStream_t own_stream = nullptr, user_stream = nullptr;
@@ -328,6 +333,14 @@ int eff_integrator(const hb_engine* e, int model) {
     case HB_INT_RK4_STOCHASTIC: return HBI_RK4_STOCH;
     default: return HBI_EULER;  // `_ =>` arm: Heun under hybrid integration for non-oscillators
     }
+}
+
+// shared memory of the streamed-history kernel's parameter rows [nm][params used] (several nodes per
+// consumer thread only), with the alignment padding before them
+size_t stream_prm_bytes(int model, int nm, int npt) {
+    static const int used[6] = {12, 7, 8, 1, 13, 26};  // c_nparams_used of hb_models.cuh, by model id
+    if (npt <= 1 || model < 0 || model > 5) return 0;
+    return (size_t)nm * used[model] * 4 + 16;
 }
 
 bool is_stochastic(int integ) { return integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH; }
@@ -407,6 +420,30 @@ hb_status build_tables(hb_engine* e, const hb_sweep_point* dims, int n_dims, boo
     }
     for (int i = 0; i < ns; i++)
         for (int b = 0; b < B; b++) fill_derived(e->subs[i].model, &T.params[i][(size_t)b * HB_PSTRIDE]);
+    // node rows (extension): the node's row, then the swept values of point b as above
+    T.node_params.assign(ns, std::vector<float>());
+    T.node_pp.assign(ns, 0);
+    for (int i = 0; i < ns; i++) {
+        const HostSub& S = e->subs[i];
+        if (S.node_params.empty()) continue;
+        const int Bn = (S.node_pp || mode[i] != 0) ? B : 1;
+        T.node_pp[i] = Bn == B ? 1 : 0;
+        T.node_params[i].assign((size_t)Bn * S.nm * HB_PSTRIDE, 0.0f);
+        for (int b = 0; b < Bn; b++) {
+            const float* src_tab = S.node_params.data() + (S.node_pp ? (size_t)b * S.nm * S.nparams : 0);
+            for (int n = 0; n < S.nm; n++) {
+                float* row = &T.node_params[i][((size_t)b * S.nm + n) * HB_PSTRIDE];
+                for (int k = 0; k < S.nparams; k++) row[k] = src_tab[(size_t)n * S.nparams + k];
+                if (mode[i] != 0) {
+                    const float* pr = &T.params[i][(size_t)b * HB_PSTRIDE];
+                    for (int d = 0; d < n_dims; d++)
+                        if (dims[d].sub_idx == i && dims[d].param_idx >= 0 && dims[d].param_idx < S.nparams)
+                            row[dims[d].param_idx] = pr[dims[d].param_idx];
+                }
+                fill_derived(S.model, row);
+            }
+        }
+    }
     return HB_OK;
 }
 
@@ -468,6 +505,12 @@ hb_status upload_net(hb_engine* e, const RunTables& T) {
         CUDA_TRY(cudaMemcpyAsync(e->d_params[i].p, T.params[i].data(), T.params[i].size() * 4, cudaMemcpyHostToDevice, st));
         e->net.sub[i].params = e->d_params[i].p;
         e->net.sub[i].sweep_form = T.sweep_form[i];
+        if (T.node_params[i].empty()) { e->net.sub[i].node_params = nullptr; e->net.sub[i].node_pp = 0; continue; }
+        CUDA_TRY(e->d_node_params[i].ensure(T.node_params[i].size()));
+        CUDA_TRY(cudaMemcpyAsync(e->d_node_params[i].p, T.node_params[i].data(), T.node_params[i].size() * 4,
+                                 cudaMemcpyHostToDevice, st));
+        e->net.sub[i].node_params = e->d_node_params[i].p;
+        e->net.sub[i].node_pp = T.node_pp[i];
     }
     for (size_t p = 0; p < e->projs.size(); p++) {
         HostProj& hp = e->projs[p];
@@ -575,7 +618,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         const bool record_run = (run_flags & (HB_RUN_TRAJECTORY | HB_RUN_DEVICE_TRAJECTORY)) != 0;
         const int n_bold_run = e->bold_removed ? 0 : (int)e->bold.size();
         if (e->subs.size() == 1 && e->projs.size() == 1 && e->kernel_model >= 0 && !(run_flags & HB_RUN_GENERIC) &&
-            !record_run && n_bold_run == 0 && e->subs[0].nm <= 128) {
+            !record_run && n_bold_run == 0 && e->subs[0].nm <= 128 && e->subs[0].node_params.empty()) {
             const HostProj& hp = e->projs[0];
             if ((hp.kind == W_MEAN || hp.kind == W_DIAG) && hp.src == 0 && hp.tgt == 0 && hp.delay == 0)
                 single_m = (e->subs[0].nm + 31) / 32;
@@ -662,10 +705,11 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
             const size_t nz_b = any_stoch ? (size_t)2 * HB_STREAM_K * nm0 * nvar0 * 4 : 0;
             const size_t rp_b = ((size_t)(nm0 + 1) * 4 + 15) & ~(size_t)15;
             const size_t ed_b = e->projs[0].edges.size() * 8;
-            if (gx_b + rp_b + 16 <= cap) {
+            const size_t pr_b = stream_prm_bytes(e->kernel_model, nm0, npt);
+            if (gx_b + rp_b + pr_b + 16 <= cap) {
                 stream_npt = npt;
-                stream_noise_smem = (nz_b > 0 && gx_b + nz_b + rp_b + 16 <= cap) ? 1 : 0;
-                size_t used = gx_b + (stream_noise_smem ? nz_b : 0) + rp_b + 16;
+                stream_noise_smem = (nz_b > 0 && gx_b + nz_b + rp_b + pr_b + 16 <= cap) ? 1 : 0;
+                size_t used = gx_b + (stream_noise_smem ? nz_b : 0) + rp_b + pr_b + 16;
                 if (used + ed_b <= cap) { stream_edges = (int)e->projs[0].edges.size(); used += ed_b; }
                 stream_smem = used;
                 const int n_cons = ((nm0 + npt - 1) / npt + 31) / 32 * 32;
@@ -786,6 +830,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     if (stream_npt) { a.ring = e->sring.p; a.ring_in_smem = 0; }
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
+    a.test_unset_wait = (run_flags & HB_RUN_TEST_UNSET_WAIT) ? 1 : 0;
     a.bold = db;
 
     P.n_steps = n_steps;
@@ -1051,6 +1096,15 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
             return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: initial_state has %lld values, expected %d (nvar=%d * nnodes=%d * nmodes=%d)",
                              i, (long long)sd.n_initial_state, s.nm * s.nvar, s.nvar, s.nnodes, s.nmodes));
         s.x0.assign(sd.initial_state, sd.initial_state + s.nm * s.nvar);
+        if (sd.n_node_params > 0) {
+            const int64_t per = (int64_t)s.nm * sd.n_params;
+            if (!sd.node_params || (sd.n_node_params != per && sd.n_node_params != per * n_sweep))
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: node_params has %lld values, expected %lld "
+                                 "(nnodes*nmodes * n_params) or %lld (n_sweep * nnodes*nmodes * n_params)", i,
+                                 (long long)sd.n_node_params, (long long)per, (long long)(per * n_sweep)));
+            s.node_params.assign(sd.node_params, sd.node_params + sd.n_node_params);
+            s.node_pp = sd.n_node_params != per || n_sweep == 1;
+        }
         if (ring && s.nmodes != 1) return bail(fail(HB_ERR_UNSUPPORTED, "ring-buffer delay semantics need nmodes == 1"));
         if (s.nm > 65535) return bail(fail(HB_ERR_UNSUPPORTED, "subnetwork %d has %d nodes; at most 65535 are supported", i, s.nm));
         DevSub& ds = e->net.sub[i];
@@ -1307,6 +1361,7 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
         if ((s = cu(cudaMemcpy(e->state.p, x0.data(), stn * 4, cudaMemcpyHostToDevice), "upload state"))) return bail(s);
     }
     e->d_params.resize(e->subs.size());
+    e->d_node_params.resize(e->subs.size());
     for (size_t p = 0; p < e->projs.size(); p++) {
         HostProj& hp = e->projs[p];
         DevProj& dp = e->net.proj[p];
@@ -1347,6 +1402,7 @@ void hb_engine_destroy(hb_engine* e) {
         if (hp.d_cp_pp) cudaFree(hp.d_cp_pp);
     }
     for (auto& b : e->d_params) b.release();
+    for (auto& b : e->d_node_params) b.release();
     for (auto& bh : e->bold) { bh.bw.release(); bh.acc.release(); bh.win.release(); bh.out_run.release(); bh.emit.release(); }
     e->state.release(); e->x0.release(); e->tavg.release(); e->ring.release(); e->noise.release(); e->prep_noise.release();
     e->traj.release(); e->dtraj.release();
@@ -1568,14 +1624,14 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     for (int b = 0; b < B; b++) kh[b] = gain_values[b] / (float)hp.nsrc;
     DBuf<int> d_cptr, d_ctgt, d_cdel;
     DBuf<float> d_cw, d_k, d_sc, d_z, d_nu;
-    DBuf<double> d_loss, d_gA, d_gW;
+    DBuf<double> d_loss, d_gA, d_gW, d_gWn;
     cudaStream_t st = e->stream();
     const size_t nnz = std::max<size_t>(hp.edges.size(), 1);
     CUDA_TRY(d_cptr.ensure(N + 1)); CUDA_TRY(d_ctgt.ensure(nnz)); CUDA_TRY(d_cdel.ensure(nnz)); CUDA_TRY(d_cw.ensure(nnz));
     CUDA_TRY(d_k.ensure(B));
     CUDA_TRY(d_sc.ensure((size_t)B * N * (T + 1) * 2)); CUDA_TRY(d_z.ensure((size_t)B * T * 2));
     CUDA_TRY(d_nu.ensure((size_t)B * N * T * 2));
-    CUDA_TRY(d_loss.ensure(B)); CUDA_TRY(d_gA.ensure(B)); CUDA_TRY(d_gW.ensure(B));
+    CUDA_TRY(d_loss.ensure(B)); CUDA_TRY(d_gA.ensure(B)); CUDA_TRY(d_gW.ensure(B)); CUDA_TRY(d_gWn.ensure((size_t)B * N));
     CUDA_TRY(cudaMemcpyAsync(d_cptr.p, cptr.data(), (N + 1) * 4, cudaMemcpyHostToDevice, st));
     if (!hp.edges.empty()) {
         CUDA_TRY(cudaMemcpyAsync(d_ctgt.p, ctgt.data(), ctgt.size() * 4, cudaMemcpyHostToDevice, st));
@@ -1588,7 +1644,7 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     L.traj = e->dtraj.p; L.x0 = e->x0.p; L.B = B; L.N = N; L.T = T; L.K = K; L.dt = e->net.dt; L.k = d_k.p;
     L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
     L.cptr = d_cptr.p; L.ctgt = d_ctgt.p; L.cdel = d_cdel.p; L.cw = d_cw.p;
-    L.sc = d_sc.p; L.z = d_z.p; L.nu = d_nu.p; L.loss = d_loss.p; L.gA = d_gA.p; L.gW = d_gW.p;
+    L.sc = d_sc.p; L.z = d_z.p; L.nu = d_nu.p; L.loss = d_loss.p; L.gA = d_gA.p; L.gW = d_gW.p; L.gWn = d_gWn.p;
     L.cs = have_cs ? d_cs.p : nullptr;
     cudaEvent_t ev[3];
     for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
@@ -1605,6 +1661,7 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     if (out->loss) CUDA_TRY(cudaMemcpy(out->loss, d_loss.p, B * 8, cudaMemcpyDeviceToHost));
     if (out->d_gain) CUDA_TRY(cudaMemcpy(out->d_gain, d_gA.p, B * 8, cudaMemcpyDeviceToHost));
     if (out->d_omega) CUDA_TRY(cudaMemcpy(out->d_omega, d_gW.p, B * 8, cudaMemcpyDeviceToHost));
+    if (out->d_omega_node) CUDA_TRY(cudaMemcpy(out->d_omega_node, d_gWn.p, (size_t)B * N * 8, cudaMemcpyDeviceToHost));
     out->forward_ms = forward_ms;
     out->prepare_ms = ms[0];
     out->reverse_ms = ms[1];
@@ -1945,6 +2002,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     if (n_steps < 2 || n_steps > (1 << 30)) return fail(HB_ERR_INVALID_STATE, "n_steps must be in [2, 2^30]");
     if (e->subs.size() != 1 || e->projs.size() != 1 || e->subs[0].model != HBM_JR || e->subs[0].nmodes != 1)
         return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs one JansenRit subnetwork (one mode) and one projection");
+    if (!e->subs[0].node_params.empty())
+        return fail(HB_ERR_UNSUPPORTED, "the FC adjoint differentiates one JansenRit parameter row per point (no node_params)");
     HostProj& hp = e->projs[0];
     if (hp.kind != W_SPARSE || hp.dmode != HBD_EDGE)
         return fail(HB_ERR_UNSUPPORTED, "the FC adjoint needs a CSR projection with per-edge delays (HB_SEM_DELAY_RING)");

@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(1024) kura_reverse_kernel(HbKuraAdjLaunch L) {
         }
         __syncthreads();  // nu of this block before the pulls of the next
     }
+    if (act && L.gWn) L.gWn[(size_t)b * N + i] = gW;
     // block sums of the loss and the two gradients (FP64)
     __shared__ double red[3][32];
     double v[3] = {lsum, gA, gW};

@@ -1,20 +1,24 @@
 // hb_noalloc.cu — a sweep entry point that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: a host framework that owns every byte of device memory
-// through its own arena (so a foreign allocation would fail or fragment it), or a control loop
-// that must not pay cudaMalloc's implicit device synchronisation between steps. For them,
-// hb_noalloc_run_csr_sweep runs the hot-path network shape — one subnetwork coupled to itself
-// through one CSR projection with one delay per edge — on inputs and outputs the caller already
-// holds in device memory. Everything else the kernel needs (its network tables, per-point
-// parameter rows and the coupling-variable history ring) lives in one file-scope device array of
-// HB_NOALLOC_SCRATCH_BYTES bytes, which every GPU that loads this library keeps until exit.
+// Some callers cannot call cudaMalloc: a host framework whose own caching allocator or arena owns
+// every byte of device memory (a foreign allocation would fail once the arena has reserved the
+// device, or fragment it), or code that runs where allocation is not allowed, such as a callback
+// that may not synchronise the device. For them, hb_noalloc_run_csr_sweep runs the hot-path
+// network shape — one subnetwork coupled to itself through one CSR projection with one delay per
+// edge — on inputs and outputs the caller already holds in device memory. Everything else the
+// kernel needs (its network tables, per-point parameter rows and the coupling-variable history
+// ring) lives in one file-scope device array of HB_NOALLOC_SCRATCH_BYTES bytes, which every GPU
+// that loads this library keeps until exit.
 //
 // The array's address is resolved once per device with cudaGetSymbolAddress (host code may not
-// use the symbol itself as a device address); the first call on a device does that set-up, so it
-// should come before any stream capture. All calls share the array and it keeps the last call's
-// contents: this file clears the status flags each call; the ring needs no clearing because the
-// kernel never reads a time before the run's first step. Calls that overlap on the GPU race on
-// the array and must be serialised by the caller.
+// use the symbol itself as a device address); the first call on a device does that set-up. All
+// calls share the array and it keeps the last call's contents: this file clears the status flags
+// each call; the ring needs no clearing because the kernel never reads a time before the run's
+// first step. Calls that overlap on the GPU race on the array and must be serialised by the
+// caller. The call makes no explicit synchronisation: the CSR input is checked on the device, and a
+// malformed one turns the run into an edge-free one whose outputs are NaN. Its small parameter
+// tables go to the array by cudaMemcpyAsync from pageable host memory, which the CUDA driver
+// stages before the call returns (and for which it may wait on the stream).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -89,9 +93,26 @@ __global__ void replicate_kernel(const float* __restrict__ x0, int per, int B, f
     if (i < (int64_t)per * B) out[i] = x0[i % per];
 }
 
-__global__ void scale_kernel(float* __restrict__ v, int64_t n, float s) {
+// After pack_edges_kernel: when it flagged the CSR input as malformed, every target row of the
+// projection is pointed at an empty edge range, so the run that follows reads only in-bounds memory.
+__global__ void guard_kernel(DevNet* __restrict__ net, int* __restrict__ empty_rows, int nnodes,
+                             const int* __restrict__ flags) {
+    if (!flags[1]) return;
+    for (int i = threadIdx.x; i <= nnodes; i += blockDim.x) empty_rows[i] = 0;
+    if (threadIdx.x == 0) net->proj[0].rowptr = empty_rows;
+}
+
+// tavg = sum / n_steps; both outputs become NaN when the CSR input was malformed
+__global__ void finish_kernel(float* __restrict__ tavg, float* __restrict__ fin, int64_t n, float s,
+                              const int* __restrict__ flags) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = v[i] * s;
+    if (i >= n) return;
+    if (flags[1]) {
+        tavg[i] = __int_as_float(0x7fc00000);
+        fin[i] = __int_as_float(0x7fc00000);
+    } else {
+        tavg[i] = tavg[i] * s;
+    }
 }
 
 struct ModelRow { const char* name; int id, nvar, ncvar, nparams, native; };
@@ -133,6 +154,7 @@ extern "C" hb_status hb_noalloc_run_csr_sweep(
     if (n_params < mr->nparams || n_params > 24 || !params) return nfail(HB_ERR_INVALID_CONFIG, "wrong number of model parameters");
     if (nnodes < 1 || nnodes > 1024 || n_sweep < 1 || n_steps < 1 || !(dt > 0.0))
         return nfail(HB_ERR_INVALID_CONFIG, "nnodes must be 1..1024, n_sweep >= 1, n_steps >= 1, dt > 0");
+    if (n_steps > (int64_t)0x7fffffff) return nfail(HB_ERR_UNSUPPORTED, "n_steps above 2^31-1");
     if (max_delay < 0 || max_delay > 65535 || nnz < 0) return nfail(HB_ERR_INVALID_CONFIG, "max_delay must be 0..65535");
     if (!d_x0 || !d_indptr || (nnz > 0 && (!d_indices || !d_delays || !d_weights)) || !d_final_states || !d_tavg || !sweep_values)
         return nfail(HB_ERR_INVALID_STATE, "a required pointer is NULL");
@@ -155,6 +177,7 @@ extern "C" hb_status hb_noalloc_run_csr_sweep(
     const size_t o_edges = off;    off = align256(off + (size_t)std::max<int64_t>(nnz, 1) * 4);
     const size_t o_eoff = off;     off = align256(off + (size_t)std::max<int64_t>(nnz, 1) * 4);
     const size_t o_flags = off;    off = align256(off + 16);
+    const size_t o_empty = off;    off = align256(off + ((size_t)nnodes + 1) * 4);
     const size_t o_ring = off;     off = align256(off + (size_t)B * ring_stride * 4);
     if (off > (size_t)HB_NOALLOC_SCRATCH_BYTES) {
         char msg[256];
@@ -179,7 +202,9 @@ extern "C" hb_status hb_noalloc_run_csr_sweep(
     if (sweep_sub_idx != 0 && !coupling_sweep) return nfail(HB_ERR_INVALID_CONFIG, "sweep_sub_idx must be 0 or -1");
     if (coupling_sweep && (sweep_param_idx < 0 || sweep_param_idx >= n_coupling_params))
         return nfail(HB_ERR_INVALID_CONFIG, "coupling sweep index out of range");
-    const bool native = !coupling_sweep && sweep_param_idx == mr->native;
+    if (!coupling_sweep && sweep_param_idx != mr->native)
+        return nfail(HB_ERR_INVALID_CONFIG, "a model-parameter sweep takes the model's native sweep index only");
+    const bool native = !coupling_sweep;
     std::vector<float> cpb(coupling_params, coupling_params + std::max(0, n_coupling_params));
     for (int b = 0; b < B; b++) {
         float* row = &prow[(size_t)b * HB_PSTRIDE];
@@ -250,10 +275,8 @@ extern "C" hb_status hb_noalloc_run_csr_sweep(
                                                                         reinterpret_cast<uint32_t*>(scratch + o_edges),
                                                                         reinterpret_cast<int*>(scratch + o_eoff), d_flags);
         if ((s = cu(cudaGetLastError()))) return s;
-        int hflags[4] = {0, 0, 0, 0};
-        if ((s = cu(cudaMemcpyAsync(hflags, d_flags, 16, cudaMemcpyDeviceToHost, st)))) return s;
-        if ((s = cu(cudaStreamSynchronize(st)))) return s;  // also retires the host-to-device copies above
-        if (hflags[1]) return nfail(HB_ERR_INVALID_CONFIG, "malformed CSR input: bad indptr, a source index >= nnodes or a delay > max_delay");
+        guard_kernel<<<1, 256, 0, st>>>(d_net, reinterpret_cast<int*>(scratch + o_empty), nnodes, d_flags);
+        if ((s = cu(cudaGetLastError()))) return s;
         const int64_t n = (int64_t)B * nnodes * nvar;
         replicate_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_x0, nnodes * nvar, B, d_final_states);
         if ((s = cu(cudaGetLastError()))) return s;
@@ -271,10 +294,9 @@ extern "C" hb_status hb_noalloc_run_csr_sweep(
     a.load_ring = 0; a.store_ring = 0;
     a.flags = d_flags; a.check_finite = 0;
     a.bold.n = 0;
-    if (n_steps > (int64_t)0x7fffffff) return nfail(HB_ERR_UNSUPPORTED, "n_steps above 2^31-1");
     if ((s = cu(hb_launch_resident(mr->id, cfk == HBC_KURAMOTO ? 1 : 0, d_net, a, B, threads, smem, st)))) return s;
     const int64_t n = (int64_t)B * nnodes * nvar;
-    scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_tavg, n, 1.0f / (float)n_steps);
+    finish_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_tavg, d_final_states, n, 1.0f / (float)n_steps, d_flags);
     if ((s = cu(cudaGetLastError()))) return s;
     return HB_OK;
 }

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_kernel(const DevNet* __restr
 
     float prm[HB_PSTRIDE];
     {
-        const float* pr = net.sub[k].params + (size_t)b * HB_PSTRIDE;
+        const float* pr = hb_param_row(net.sub[k], b, nn);
 #pragma unroll
         for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
     }
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_fast_kernel(const DevNet* __
 
     float prm[HB_PSTRIDE];
     {
-        const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+        const float* pr = hb_param_row(net.sub[0], b, nn);
 #pragma unroll
         for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
     }
@@ -939,8 +939,8 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 // wait for the phase of parity `parity` with an iteration limit; false when the limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); it++) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = 1 << 22) {
+    for (int it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
@@ -1031,6 +1031,7 @@ template <int MODEL, int PRE, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) uint64_t noise_bar[2];  // bulk-copy completion of the two noise buffers
+    __shared__ __align__(8) uint64_t unset_bar;     // HB_RUN_TEST_UNSET_WAIT: a barrier nothing completes
     __shared__ DevNet net;
     {
         const int* src = reinterpret_cast<const int*>(gnet);
@@ -1107,6 +1108,13 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
         mbar_init(&noise_bar[0], 1);
         mbar_init(&noise_bar[1], 1);
         mbar_init_fence();
+    }
+    // test hook: one bounded wait on a barrier phase that nothing completes; it gives up after 4096
+    // polls and reports the timeout like a real one, and the run then proceeds unchanged
+    if (a.test_unset_wait && t == 0) {
+        mbar_init(&unset_bar, 1);
+        mbar_init_fence();
+        if (!mbar_wait(&unset_bar, 0, 1 << 12)) atomicOr(a.flags + 1, 4);
     }
 
     // consumers publish x_{s0} before the first barrier
@@ -1271,7 +1279,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
         const float rowsum = (has_rowsums && active) ? P.rowsums[n] : 0.0f;
         float prm[HB_PSTRIDE];
         {
-            const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+            const float* pr = hb_param_row(net.sub[0], b, active ? n : 0);
 #pragma unroll
             for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
         }

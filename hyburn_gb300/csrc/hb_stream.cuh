@@ -319,6 +319,12 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
     uint32_t* s_edges = reinterpret_cast<uint32_t*>(smem + off);
     off += (size_t)a.smem_edges * 4;
     float* s_ew = reinterpret_cast<float*>(smem + off);
+    off += (size_t)a.smem_edges * 4;
+    off = (off + 15) & ~(size_t)15;
+    // with several nodes per consumer thread, every node's parameter row [nm][PU] (its node row when the
+    // subnetwork has per-node parameters, else the point's row)
+    constexpr int PU = c_nparams_used(MODEL);
+    float* s_prm = reinterpret_cast<float*>(smem + off);
 
     // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176)
     if (a.s0 == 0) {
@@ -367,6 +373,8 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
         }
         if (active[q]) stream_publish<PRE, NCV, PCH>(ring, n, RPX, RP, (int)(a.s0 % RP), x[q]);
     }
+    if (NPT > 1)
+        for (int i = t; i < nm * PU; i += nthreads) s_prm[i] = hb_param_row(net.sub[0], b, i / PU)[i % PU];
     __syncthreads();
 
     if (!is_consumer) {
@@ -467,11 +475,11 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
     } else {
         // ================= consumers =================
         const int sweep_form = net.sub[0].sweep_form;
-        float prm[HB_PSTRIDE];
+        float prm[HB_PSTRIDE];  // one node per thread: its row in registers
         {
-            const float* pr = net.sub[0].params + (size_t)b * HB_PSTRIDE;
+            const float* pr = hb_param_row(net.sub[0], b, active[0] ? t : 0);
 #pragma unroll
-            for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (i < c_nparams_used(MODEL)) ? pr[i] : 0.0f;
+            for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (NPT == 1 && i < PU) ? pr[i] : 0.0f;
         }
         float rowsum[NPT];
 #pragma unroll
@@ -539,7 +547,8 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                         else if (a.stream_noise_smem) nz[v] = nbuf[(size_t)j * nm * NVAR + n * NVAR + v] * net.noise_scale[v];
                         else nz[v] = __ldcs(noise_base + (size_t)(it0 + j) * nstride + n * NVAR + v) * net.noise_scale[v];
                     }
-                    stream_node_step<MODEL>(P, cp, integ, prm, sweep_form, rowsum[q], gx, nz, x[q], dt, dt_half, h2, h6);
+                    const float* pq = NPT == 1 ? prm : s_prm + (size_t)n * PU;
+                    stream_node_step<MODEL>(P, cp, integ, pq, sweep_form, rowsum[q], gx, nz, x[q], dt, dt_half, h2, h6);
 #pragma unroll
                     for (int v = 0; v < NVAR; v++) tv[q][v] = tv[q][v] + x[q][v];
                     if (a.traj) {

@@ -21,7 +21,7 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 from . import _abi
-from .config import (BackendError, InvalidConfig, InvalidState, IOError_, NonFinite, SimConfig,
+from .config import (BackendError, DeviceTimeout, InvalidConfig, InvalidState, IOError_, NonFinite, SimConfig,
                      SimulationError, Unsupported, resolve_initial_state)
 
 
@@ -82,7 +82,7 @@ _ERRORS = {
     _abi.HB_ERR_IO: IOError_,
     _abi.HB_ERR_CUDA: BackendError,
     _abi.HB_ERR_NONFINITE: NonFinite,
-    _abi.HB_ERR_TIMEOUT: BackendError,
+    _abi.HB_ERR_TIMEOUT: DeviceTimeout,
     _abi.HB_ERR_UNSUPPORTED: Unsupported,
 }
 
@@ -120,7 +120,8 @@ class OrderAdjointResult:
     """Time-averaged Kuramoto order parameter and its gradients (hb_engine_adjoint_order)."""
     loss: np.ndarray      # [n_sweep]
     d_gain: np.ndarray    # [n_sweep] dL/da, the coupling scale
-    d_omega: np.ndarray   # [n_sweep] dL/domega
+    d_omega: np.ndarray   # [n_sweep] dL/domega for a shift of every node's omega (sum of d_omega_node)
+    d_omega_node: Optional[np.ndarray] = None  # [n_sweep, nnodes] dL/domega_i
     forward_ms: float = 0.0
     prepare_ms: float = 0.0
     reverse_ms: float = 0.0
@@ -284,16 +285,18 @@ class BatchHybridEngine:
     def adjoint_order(self, gain_values, n_steps: int, run_flags: int = 0) -> OrderAdjointResult:
         """Kuramoto: loss = time average of the order parameter R over n_steps from the initial state
         (the engine is reset), with the coupling scale a = gain_values[b] per point; gradients with
-        respect to a and omega by the discrete adjoint on the GPU."""
+        respect to a and to omega (per node, and for a shift of all nodes) by the discrete adjoint on the GPU."""
         g = np.ascontiguousarray(np.asarray(gain_values, np.float32))
         B = self.n_sweep
+        n = self.config.network.subnetworks[0].nnodes
         loss, dg, dw = (np.zeros(B, np.float64) for _ in range(3))
+        dwn = np.zeros((B, n), np.float64)
         out = _abi.hb_order_adjoint_out()
         dp = C.POINTER(C.c_double)
-        out.loss, out.d_gain, out.d_omega = (a.ctypes.data_as(dp) for a in (loss, dg, dw))
+        out.loss, out.d_gain, out.d_omega, out.d_omega_node = (a.ctypes.data_as(dp) for a in (loss, dg, dw, dwn))
         st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), int(run_flags), C.byref(out))
         raise_for(st, self._lib.hb_last_error().decode())
-        return OrderAdjointResult(loss, dg, dw, out.forward_ms, out.prepare_ms, out.reverse_ms)
+        return OrderAdjointResult(loss, dg, dw, dwn, out.forward_ms, out.prepare_ms, out.reverse_ms)
 
     def adjoint_fc(self, gain_values, n_steps: int, target_fc, checkpoint_every: int = 500,
                    return_y: bool = False) -> AdjointResult:

@@ -116,32 +116,44 @@ def batched_sweep(n_steps: int = 20_000, n_points: int = 128, n: int = 74, seed:
 
 
 def mpr_grid(n_nodes: int, n_points: int, n_steps: int, seed: int, dt: float = 0.05,
-             bold: bool = True) -> Tuple[SimConfig, dict]:
+             bold: bool = True, eta_per_point: bool = True) -> Tuple[SimConfig, dict]:
     """One size of the uneven-batching MPR workload: N nodes, a (G, eta) grid over n_points,
-    sparse delayed Linear coupling (U[10,200] mm at 3 mm/ms), RK4, BOLD at TR 2 s."""
+    sparse delayed Linear coupling (U[10,200] mm at 3 mm/ms), RK4, BOLD at TR 2 s.
+
+    The grid has n_eta = the largest divisor of n_points not above its square root values of eta in
+    [-6, -3] and n_points / n_eta values of the coupling scale G in [0, 1]; point b = iG * n_eta + i_eta.
+    G is swept per point as the Linear coupling scale (``values``); eta enters through per-point
+    parameter tables (``node_params`` [n_points, N, 7]) when eta_per_point is set."""
     c = connectome(n_nodes, 0.2, seed)
     delays = tract_lengths_to_delays(c.lengths, 3.0, dt)
     params = list(DEFAULT_PARAMS["MontbrioPazoRoxin"])
     mons = [MonitorConfig("Bold", tr=2.0, bold_period=10)] if bold else []
     rng = np.random.default_rng(seed)
     x0 = np.stack([rng.uniform(0.0, 1.0, n_nodes), rng.uniform(-2.0, 0.0, n_nodes)], 1).astype(np.float32)
+    n_eta = max(d for d in range(1, int(np.sqrt(n_points)) + 1) if n_points % d == 0)
+    n_g = n_points // n_eta
+    g = np.linspace(0.0, 1.0, n_g).astype(np.float32)
+    eta = np.linspace(-6.0, -3.0, n_eta).astype(np.float32)
+    sub = SubnetworkConfig("MontbrioPazoRoxin", n_nodes, x0.ravel().tolist(), params)
+    if eta_per_point:
+        rows = np.tile(np.asarray(params, np.float32), (n_points, n_nodes, 1))
+        rows[:, :, 2] = np.repeat(np.tile(eta, n_g), n_nodes).reshape(n_points, n_nodes)
+        sub.node_params = rows
     cfg = SimConfig(
         sim_length=n_steps * dt, dt=dt, integrator="rk4", nsig=0.0, monitors=mons,
         network=NetworkConfig(
-            subnetworks=[SubnetworkConfig("MontbrioPazoRoxin", n_nodes, x0.ravel().tolist(), params)],
+            subnetworks=[sub],
             projections=[ProjectionConfig(0, 0, c.csr_weights(), conn_type="csr", delays=delays,
                                           coupling_fn="Linear", coupling_params=[1.0], cvar_map="0:0")]))
-    side = int(round(np.sqrt(n_points)))
-    g = np.linspace(0.0, 1.0, max(side, 1)).astype(np.float32)
-    eta = np.linspace(-6.0, -3.0, max(n_points // max(side, 1), 1)).astype(np.float32)
-    return cfg, {"n_sweep": n_points, "G": g.tolist(), "eta": eta.tolist(), "n_steps": n_steps,
-                 "max_delay": int(max(delays)), "min_delay": int(min(delays))}
+    return cfg, {"n_sweep": n_points, "G": g.tolist(), "eta": eta.tolist(), "values": np.repeat(g, n_eta).tolist(),
+                 "n_steps": n_steps, "max_delay": int(max(delays)), "min_delay": int(min(delays))}
 
 
 def kuramoto_scale(n: int = 1000, n_points: int = 256, n_steps: int = 100_000, seed: int = 5,
-                   density: float = 0.05, bold: bool = True) -> Tuple[SimConfig, dict]:
+                   density: float = 0.05, bold: bool = True, omega_per_node: bool = True) -> Tuple[SimConfig, dict]:
     """Kuramoto, 1000-node 5% CSR connectome, delays from U[10,250] mm at 5 mm/ms, dt 0.1,
-    256 points over the coupling scale G, natural frequencies omega ~ N(0,1) per node."""
+    256 points over the coupling scale G, natural frequencies omega ~ N(0,1) per node (``node_params``
+    [n, 1]; with omega_per_node off every node keeps the model's omega = 1)."""
     c = connectome(n, density, seed, 10.0, 250.0)
     dt = 0.1
     delays = tract_lengths_to_delays(c.lengths, 5.0, dt)
@@ -155,6 +167,8 @@ def kuramoto_scale(n: int = 1000, n_points: int = 256, n_steps: int = 100_000, s
             projections=[ProjectionConfig(0, 0, c.csr_weights(), conn_type="csr", delays=delays,
                                           coupling_fn="Kuramoto", coupling_params=[1.0], cvar_map="0:0")]))
     omega = rng.standard_normal(n).astype(np.float32)
+    if omega_per_node:
+        cfg.network.subnetworks[0].node_params = omega.reshape(n, 1)
     values = np.linspace(0.0, 2.0, n_points).astype(np.float32).tolist()
     return cfg, {"n_sweep": n_points, "values": values, "n_steps": n_steps, "omega": omega,
                  "max_delay": int(max(delays)), "min_delay": int(min(delays))}
@@ -179,3 +193,22 @@ def jr_fc_adjoint(n_steps: int = 20_000, n_points: int = 64, n: int = 74, seed: 
     gains = np.linspace(0.5, 1.5, n_points).astype(np.float32)
     return cfg, {"gains": gains, "connectome": c, "min_delay": int(min(delays)), "max_delay": int(max(delays))}
 
+
+
+def jr_target_fc(cfg: SimConfig, n_steps: int, gain: float = 1.0, seed: int = 40) -> np.ndarray:
+    """Target FC of the FC-adjoint workload: Pearson FC of y1 - y2 of a forward run of the same network
+    with coupling gain `gain` from an initial state drawn with `seed` (computed on the GPU)."""
+    import copy
+
+    from .engine import BatchHybridEngine, SweepParam
+    from ._abi import HB_SEM_DELAY_RING
+
+    c = copy.deepcopy(cfg)
+    sub = c.network.subnetworks[0]
+    rng = np.random.default_rng(seed)
+    ranges = [(-0.5, 0.5), (0.0, 20.0), (0.0, 20.0), (-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0)]
+    sub.initial_state = np.stack([rng.uniform(lo, hi, sub.nnodes) for lo, hi in ranges], 1).astype(np.float32).ravel().tolist()
+    eng = BatchHybridEngine.from_config(c, 1, semantics=HB_SEM_DELAY_RING)
+    r = eng.adjoint_fc([gain], n_steps, np.eye(sub.nnodes, dtype=np.float32), checkpoint_every=500)
+    eng.close()
+    return np.asarray(r.fc[0], np.float32)

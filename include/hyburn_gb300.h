@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define HB_ABI_VERSION 1
+#define HB_ABI_VERSION 2
 
 /* ---- status codes: src/error.rs:6-25 (SimulationError) + device-side codes ---- */
 typedef int32_t hb_status;
@@ -93,6 +93,10 @@ typedef int32_t hb_status;
  * hb_engine_fc_features, with no host copy (the reference copies each step to the host,
  * engine.rs:779-782); HB_ERR_UNSUPPORTED when it does not fit the device's free memory */
 #define HB_RUN_DEVICE_TRAJECTORY (1u << 29)
+/* test hook of the bounded device-side waits: the warp-specialised pipeline kernel also waits once on
+ * an mbarrier phase that nothing completes; the wait gives up after a fixed number of polls, the run
+ * finishes unchanged and returns HB_ERR_TIMEOUT. Other kernels ignore the flag. */
+#define HB_RUN_TEST_UNSET_WAIT (1u << 30)
 /* resident kernel: threads per node sharing its edge list (1, 2, 4 or 8); 0 lets the engine choose */
 #define HB_RUN_LANES(n) ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : 0) << 12)
 
@@ -107,6 +111,13 @@ typedef struct hb_subnet_desc {
     int32_t      n_params;
     const float* initial_state;  /* one point, [nnodes*nmodes, nvar] node-major (engine.rs:239-243) */
     int64_t      n_initial_state;
+    /* Extension (the reference takes one parameter row per subnetwork); NULL / 0 for none.
+     * Parameter rows per node, [nnodes*nmodes][n_params] shared by all sweep points or
+     * [n_sweep][nnodes*nmodes][n_params] one table per point. They replace `params` node by node;
+     * a swept model parameter (the native sweep index, or the per-point overrides of a multi-parameter
+     * sweep) still takes its sweep value at every node. */
+    const float* node_params;
+    int64_t      n_node_params;
 } hb_subnet_desc;
 
 /* One projection: ProjectionConfig (src/config.rs:158-184). */
@@ -230,23 +241,28 @@ hb_status hb_engine_prepare(hb_engine* engine, int32_t sub_idx, int32_t param_id
 hb_status hb_engine_execute_prepared(hb_engine* engine);
 
 /* ---- one sweep without any device allocation (no counterpart in the reference) ----
- * For callers that cannot call cudaMalloc: a host framework whose own arena owns all device
- * memory, or a loop that must not pay cudaMalloc's implicit device synchronisation. It runs the
- * hot-path shape — one subnetwork coupled to itself through one CSR projection with one delay
- * per edge (ring-buffer semantics of HB_SEM_DELAY_RING), shared noise, no monitors — on inputs
- * and outputs the caller already holds in device memory:
+ * For callers that cannot call cudaMalloc: a host framework whose own caching allocator or arena
+ * owns the device's memory (a foreign allocation fails once the arena has reserved the device, or
+ * fragments it), or code running where allocating is not allowed. It runs the hot-path shape —
+ * one subnetwork coupled to itself through one CSR projection with one delay per edge
+ * (ring-buffer semantics of HB_SEM_DELAY_RING), shared noise, no monitors — on inputs and outputs
+ * the caller already holds in device memory:
  *   d_x0 [nnodes*nvar] (one point, node-major), CSR rows = target nodes: d_indptr [nnodes+1]
  *   (int32), d_indices / d_delays / d_weights [nnz], d_noise [n_steps, nnodes*nvar] standard
  *   normal draws (stochastic integrators only), outputs d_final_states / d_tavg
  *   [n_sweep, nnodes, nvar]. Host arrays: model and coupling parameters, nsig, sweep_values.
- * sweep_sub_idx 0 sweeps model parameter sweep_param_idx (the model's native sweep index only,
- * as the batch engine), -1 sweeps coupling parameter sweep_param_idx.
+ * sweep_sub_idx 0 sweeps model parameter sweep_param_idx, which must be the model's native sweep
+ * index (the batch engine's dfun.rs:49-72; any other index is HB_ERR_INVALID_CONFIG here), -1
+ * sweeps coupling parameter sweep_param_idx.
  * Network tables and the history ring live in one static device array of
  * HB_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until exit; sweeps needing
  * more are rejected with HB_ERR_UNSUPPORTED. The first call on a device resolves that array's
- * address and should come before any stream capture. All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller. Returns after the work is
- * enqueued on cuda_stream (the inputs' validation waits for a small packing kernel). */
+ * address. All calls share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. The call returns once its work is enqueued on cuda_stream and makes no explicit
+ * synchronisation (its parameter tables are copied from pageable host memory, which the driver
+ * stages and for which it may wait on the stream). The CSR input (indptr monotone from 0 to nnz,
+ * source indices below nnodes, delays at most max_delay) is checked on the device: a malformed
+ * one makes the run use no edges and fills both outputs with NaN. */
 #define HB_NOALLOC_SCRATCH_BYTES (64u << 20)
 hb_status hb_noalloc_run_csr_sweep(
     const char* model, const float* params, int32_t n_params, int32_t nnodes, const float* d_x0,
@@ -322,8 +338,10 @@ hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int3
  * with per-edge delays (HB_SEM_DELAY_RING), Kuramoto coupling and deterministic Heun: the engine is
  * reset and runs n_steps with the coupling scale a = gain_values[b] for sweep point b, keeping
  * every step's phase on the device; loss_b = (1/n_steps) sum_{t=1..n_steps} R_b(t) with
- * R = |mean_j exp(i theta_j)|. Outputs (any pointer may be NULL): loss, d_gain = dL/da and
- * d_omega = dL/domega, [n_sweep] each, and the device times of the forward run, the preparation
+ * R = |mean_j exp(i theta_j)|. Omega may be one value per node (hb_subnet_desc.node_params). Outputs (any
+ * pointer may be NULL): loss, d_gain = dL/da and d_omega = dL/domega (the gradient with respect to a
+ * shift of every node's omega), [n_sweep] each, d_omega_node = dL/domega_i [n_sweep][nnodes], and the
+ * device times of the forward run, the preparation
  * (sin / cos rows, order parameter) and the reverse sweep. run_flags (HB_RUN_*) choose the forward's
  * kernel form as for hb_engine_run_sweep; the pipeline and streamed-history forms also hand the
  * coupling sums of every step to the reverse sweep, which otherwise gathers them again. The phase
@@ -332,7 +350,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* engine, const float* gain_values, int3
 typedef struct hb_order_adjoint_out {
     double* loss;
     double* d_gain;
-    double* d_omega;
+    double* d_omega;       /* [n_sweep]: dL/domega for one omega shared by all nodes (the sum of d_omega_node) */
+    double* d_omega_node;  /* [n_sweep][nnodes]: dL/domega_i per node (omega per node from hb_subnet_desc.node_params) */
     float   forward_ms, prepare_ms, reverse_ms;
 } hb_order_adjoint_out;
 hb_status hb_engine_adjoint_order(hb_engine* engine, const float* gain_values, int32_t n_values, int64_t n_steps,

@@ -573,6 +573,8 @@ typedef struct {
     float params[32];
     int nparams;
     float* x0; /* [nm*nvar] */
+    float* node_params;  /* extension of this engine: [nm][nparams] or [B][nm][nparams] rows per node, or NULL */
+    int node_pp;         /* node_params holds one table per sweep point */
 } osub;
 
 enum { W_MEAN = 0, W_DIAG, W_DENSE, W_CSR };
@@ -624,6 +626,7 @@ typedef struct {
 typedef struct {
     int mode;                 /* 0 none, 1 native sweep form, 2 per-point params */
     real* pp;                 /* [B][nparams] */
+    char swept[32];           /* parameters that pp overrides (they override per-node rows too) */
 } osweep;
 
 /* per-point coupling functions of swept projections (an extension: the reference cannot sweep
@@ -690,6 +693,16 @@ EXPORT oengine* HBO(engine_create)(const hb_sim_desc* d, int32_t n_sweep, int32_
         if (s->n_initial_state != (int64_t)o->nm * o->nvar) { set_err("subnetwork %d: initial state has %lld values, expected %d", i, (long long)s->n_initial_state, o->nm * o->nvar); *status = HB_ERR_INVALID_CONFIG; HBO(engine_destroy)(e); return NULL; }
         o->x0 = malloc(sizeof(float) * o->nm * o->nvar);
         memcpy(o->x0, s->initial_state, sizeof(float) * o->nm * o->nvar);
+        if (s->n_node_params > 0) {
+            int64_t per = (int64_t)o->nm * s->n_params;
+            if (!s->node_params || (s->n_node_params != per && s->n_node_params != per * n_sweep)) {
+                set_err("subnetwork %d: node_params has %lld values", i, (long long)s->n_node_params);
+                *status = HB_ERR_INVALID_CONFIG; HBO(engine_destroy)(e); return NULL;
+            }
+            o->node_params = malloc(sizeof(float) * (size_t)s->n_node_params);
+            memcpy(o->node_params, s->node_params, sizeof(float) * (size_t)s->n_node_params);
+            o->node_pp = s->n_node_params != per || n_sweep == 1;
+        }
     }
     /* horizon: engine.rs:253-257 (batch) / construction.rs:596-601 (ring) */
     int max_delay = 0;
@@ -827,7 +840,7 @@ static void free_results(oengine* e) {
 
 EXPORT void HBO(engine_destroy)(oengine* e) {
     if (!e) return;
-    for (int i = 0; i < e->nsub; i++) { free(e->sub[i].x0); free(e->x[i]); free(e->hist[i]); }
+    for (int i = 0; i < e->nsub; i++) { free(e->sub[i].x0); free(e->sub[i].node_params); free(e->x[i]); free(e->hist[i]); }
     for (int p = 0; p < e->nproj && e->proj; p++) {
         oproj* o = &e->proj[p];
         free(o->dense); free(o->csr_w); free(o->csr_idx); free(o->csr_ptr); free(o->edelay); free(o->rowsums);
@@ -967,7 +980,18 @@ static void dfun_sub(const oengine* e, int i, const osweep* sw, int b, const rea
     int sweep_form = 0;
     if (sw[i].mode == 0) { for (int k = 0; k < S->nparams; k++) p[k] = S->params[k]; }
     else { for (int k = 0; k < S->nparams; k++) p[k] = sw[i].pp[(size_t)b * S->nparams + k]; sweep_form = (sw[i].mode == 1); }
-    for (int n = 0; n < S->nm; n++) dfun_node(S->model, p, sweep_form, x + n * S->nvar, cpl + n * S->ncvar, dx + n * S->nvar);
+    if (!S->node_params) {
+        for (int n = 0; n < S->nm; n++) dfun_node(S->model, p, sweep_form, x + n * S->nvar, cpl + n * S->ncvar, dx + n * S->nvar);
+        return;
+    }
+    /* per-node rows (an extension: the reference has one row per subnetwork): the node's row, with the
+     * swept parameters of point b taking their sweep values as above */
+    real q[32];
+    for (int n = 0; n < S->nm; n++) {
+        const float* nr = S->node_params + ((size_t)(S->node_pp ? b : 0) * S->nm + n) * S->nparams;
+        for (int k = 0; k < S->nparams; k++) q[k] = (sw[i].mode != 0 && sw[i].swept[k]) ? p[k] : (real)nr[k];
+        dfun_node(S->model, q, sweep_form, x + n * S->nvar, cpl + n * S->ncvar, dx + n * S->nvar);
+    }
 }
 
 static void clamp_sub(const osub* S, real* x) {
@@ -1233,6 +1257,7 @@ EXPORT int32_t HBO(engine_run_sweep)(oengine* e, int32_t sub_idx, int32_t param_
     } else if (param_idx == k_native_sweep[e->sub[sub_idx].model]) {
         const osub* S = &e->sub[sub_idx];
         sw[sub_idx].mode = 1;
+        sw[sub_idx].swept[param_idx] = 1;
         sw[sub_idx].pp = malloc(sizeof(real) * (size_t)e->n_sweep * S->nparams);
         for (int b = 0; b < e->n_sweep; b++) {
             for (int k = 0; k < S->nparams; k++) sw[sub_idx].pp[(size_t)b * S->nparams + k] = S->params[k];
@@ -1293,6 +1318,8 @@ EXPORT int32_t HBO(engine_run_sweep_multi)(oengine* e, const hb_sweep_point* dim
             int d0 = 0; while (dims[d0].sub_idx != i) d0++;
             sw[i].mode = (dims[d0].param_idx == k_native_sweep[S->model]) ? 1 : 0;
         }
+        for (int d = 0; d < n_dims && sw[i].mode != 0; d++)
+            if (dims[d].sub_idx == i && dims[d].param_idx >= 0 && dims[d].param_idx < S->nparams) sw[i].swept[dims[d].param_idx] = 1;
     }
     e->r_params = malloc(sizeof(float) * (size_t)B * n_dims);
     e->r_params_len = (int64_t)B * n_dims;
@@ -1339,7 +1366,7 @@ EXPORT int32_t HBO(dfun)(const char* model, const float* params, int32_t n_param
                          const float* state, const float* coupling, int32_t n, float* out) {
     int m = model_from_name(model);
     if (m < 0) { set_err("Unknown model: %s", model ? model : "(null)"); return HB_ERR_INVALID_CONFIG; }
-    real p[32], x[8], c[4], dx[8];
+    real p[32], x[8], c[4], dx[8] = {0};
     for (int k = 0; k < n_params && k < 32; k++) p[k] = params[k];
     for (int i = 0; i < n; i++) {
         for (int v = 0; v < k_nvar[m]; v++) x[v] = state[i * k_nvar[m] + v];

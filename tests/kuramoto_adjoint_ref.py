@@ -11,7 +11,8 @@ the coupling held over the step (engine.rs:710-720: both stages see the same c),
 [0, 2 pi) after the step.
 
 Loss: L = (1 / T) sum_{t=1..T} R(t), R = |mean_j exp(i th_j)| (the time-averaged order parameter).
-Gradients: dL/da (the coupling scale) and dL/domega (the model's omega, one value per sweep point).
+Gradients: dL/da (the coupling scale) and dL/domega: per node when omega is one value per node
+(an array), else for the one omega all nodes share.
 """
 import numpy as np
 
@@ -46,7 +47,8 @@ def order_loss(th):
 
 
 def adjoint(theta0, omega, a, indptr, indices, weights, delays, dt, n_steps):
-    """Loss and (dL/da, dL/domega) by the discrete adjoint of the forward above."""
+    """Loss and (dL/da, dL/domega) by the discrete adjoint of the forward above; dL/domega is a vector
+    over nodes when omega is an array."""
     n = theta0.shape[0]
     th, S, C = forward(theta0, omega, a, indptr, indices, weights, delays, dt, n_steps)
     T = n_steps
@@ -57,13 +59,13 @@ def adjoint(theta0, omega, a, indptr, indices, weights, delays, dt, n_steps):
     rows = np.repeat(np.arange(n), np.diff(indptr))
     lam = src[T - 1].copy()                      # lambda(T)
     nu_c, nu_s = np.zeros((T, n)), np.zeros((T, n))
-    g_a, g_w = 0.0, 0.0
+    g_a, g_w = 0.0, np.zeros(n)
     k = a / n
     for s in range(T - 1, -1, -1):
         ci, si = np.cos(th[s]), np.sin(th[s])
         q = k * (-si * S[s] - ci * C[s])            # dc_i / dth_i
         g_a += dt * float(np.sum(lam * (ci * S[s] - si * C[s]))) / n
-        g_w += dt * float(np.sum(lam))
+        g_w += dt * lam
         nu_c[s] = lam * dt * k * ci
         nu_s[s] = lam * dt * k * si
         if s == 0:
@@ -78,4 +80,4 @@ def adjoint(theta0, omega, a, indptr, indices, weights, delays, dt, n_steps):
         new += np.cos(th[s]) * np.bincount(indices, weights=pc, minlength=n)
         new += np.sin(th[s]) * np.bincount(indices, weights=ps, minlength=n)
         lam = new
-    return order_loss(th), g_a, g_w
+    return order_loss(th), g_a, (g_w if np.ndim(omega) else float(np.sum(g_w)))
