@@ -61,6 +61,20 @@ HB_RUN_DEVICE_TRAJECTORY = 1 << 29
 HB_RUN_TEST_UNSET_WAIT = 1 << 30
 
 
+def HB_RUN_STREAM_CLUSTER(n: int) -> int:
+    """Streamed-history kernel: CTAs per sweep point (a thread-block cluster splitting its nodes)."""
+    return {1: 1, 2: 2, 4: 3, 8: 4}.get(int(n), 0) << 4
+
+
+# the run flags that choose a kernel form or its lane counts (what the autotuner chooses)
+HB_RUN_KERNEL_CHOICE = (HB_RUN_FORCE_RESIDENT | HB_RUN_FORCE_BLOCKED | HB_RUN_GLOBAL_RING | HB_RUN_GENERIC | (0x7 << 4)
+                        | (0xF << 12)
+                        | HB_RUN_TWO_PHASE | HB_RUN_NO_PIPE | HB_RUN_STREAM | HB_RUN_NO_STREAM | (0xF << 20)
+                        | (0x7 << 24) | HB_RUN_STREAM_PREFETCH | HB_RUN_PIPE_WIDE)
+# the streamed-history kernel's form within those: nodes per consumer thread and L2 prefetch
+HB_RUN_STREAM_FORM = (0x7 << 24) | HB_RUN_STREAM_PREFETCH
+
+
 def HB_RUN_LANES(n: int) -> int:
     return {1: 1, 2: 2, 4: 3, 8: 4}.get(n, 0) << 12
 

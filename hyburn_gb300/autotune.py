@@ -6,9 +6,11 @@ the generic resident kernel otherwise) with fixed lane counts. `tune` instead ru
 form for a short probe on a scratch engine built from the same configuration, keeps the fastest,
 and caches the run flags under a key of the network's shape:
 (model, nodes, edges, smallest and largest delay, sweep points, integrator, semantics, monitors).
-Later runs of the same shape read the cache (`best_run_flags`). Results are those of the chosen
-kernel form, which all agree with the CPU oracle within the parity tolerance; only the time
-differs.
+Later runs of the same shape read the cache (`best_run_flags`): BatchHybridEngine does so by default
+for every run that forces no kernel form (its `tune` option: "cache", "auto" to tune an untuned
+shape on its first run, "off"), and GroupedSweep takes the tuned streamed-history form when its
+members agree on one. Results are those of the chosen kernel form, which all agree with the CPU
+oracle within the parity tolerance; only the time differs.
 
 Cache file: $HYBURN_GB300_TUNE_CACHE, else ~/.cache/hyburn_gb300/tune.json.
 """
@@ -80,7 +82,7 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
 
 def _measure(config: SimConfig, n_sweep: int, semantics: int, param: SweepParam, values, n_steps: int,
              run_flags: int, noise, repeats: int) -> float:
-    eng = BatchHybridEngine.from_config(config, n_sweep, semantics=semantics)
+    eng = BatchHybridEngine.from_config(config, n_sweep, semantics=semantics, tune="off")
     try:
         eng.prepare(param, values, n_steps, noise=noise, run_flags=run_flags)
         eng.execute_prepared()

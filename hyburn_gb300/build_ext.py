@@ -19,6 +19,9 @@ LIB = os.path.join(OUT_DIR, "libhyburn_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
+    ("hb_queue_1.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_queue_2.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_queue_4.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_1.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_2.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_4.cu", ["--fmad=false", "-lineinfo"]),

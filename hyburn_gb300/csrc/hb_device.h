@@ -143,6 +143,7 @@ struct RunArgs {
     int stream_rp;        // streamed-history kernel: ring positions per node (time t at t mod stream_rp)
     int stream_noise_smem;// streamed-history kernel: noise rows staged through shared memory
     int stream_prefetch;  // streamed-history kernel: prefetch the history run of the edge this many lane strides ahead (0: off)
+    int stream_cluster;   // streamed-history kernel: CTAs per sweep point (a thread-block cluster splitting its nodes; 0 or 1: one)
     int load_ring;        // copy the global ring into shared memory at launch start
     int store_ring;       // copy the shared ring back at launch end
     int* flags;           // [0]: non-finite seen, [1]: bounds error
@@ -151,12 +152,13 @@ struct RunArgs {
     DevBold bold;
 };
 
-// one network's sweep inside a grouped launch of the streamed-history kernel
+// one network's sweep inside a grouped launch of the streamed-history work-queue kernel
 struct StreamJob {
     const DevNet* net;
     RunArgs args;
-    int first_block;   // first block of this job in the grouped grid
-    int n_points;      // its sweep points (one block each)
+    int first_block;   // first work item of this job (items are numbered job by job)
+    int n_points;      // its sweep points (one work item each)
+    int model, pre;    // model id and coupling pre() form (0: identity, 1: [sin, cos]) of its kernel path
 };
 
 // the FC-loss adjoint's buffers and sizes (hb_adjoint.cu); device pointers

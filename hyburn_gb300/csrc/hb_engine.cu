@@ -36,12 +36,15 @@ int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
 cudaError_t hb_launch_single(int model, int m, const DevNet* d_net, const RunArgs& a, int B, cudaStream_t st);
-cudaError_t hb_launch_stream_group_1(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-cudaError_t hb_launch_stream_group_2(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_group_budget_1(int model, int pre);
-int hb_stream_group_budget_2(int model, int pre);
-int hb_stream_group_budget_4(int model, int pre);
+cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_1(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_2(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_4(int threads, size_t smem);
+int hb_stream_queue_budget_1();
+int hb_stream_queue_budget_2();
+int hb_stream_queue_budget_4();
 cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int phase, cudaStream_t st);
 // hb_io.cu
 hb_status hb_io_make_dirs(const std::string& dir);
@@ -681,13 +684,28 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     else if (edge_bytes + part_bytes <= smem_cap) { edges_in_smem = 1; }
     size_t smem = (ring_in_smem ? ((ring_bytes + 15) & ~(size_t)15) : 0) + (edges_in_smem ? edge_bytes : 0) + part_bytes + 16;
     // ---- streamed-history pipeline: per-edge delays whose history does not fit shared memory ----
-    int stream_npt = 0, stream_pl = 1, stream_rp = 0, stream_noise_smem = 0, stream_edges = 0;
+    int stream_npt = 0, stream_pl = 1, stream_rp = 0, stream_noise_smem = 0, stream_edges = 0, stream_cluster = 1;
     size_t stream_smem = 0;
     if (fast >= 0 && e->projs[0].dmode == HBD_EDGE && e->dmin >= 2 * HB_STREAM_K - 1 && !(run_flags & HB_RUN_NO_STREAM) &&
         (!ring_in_smem || (run_flags & HB_RUN_STREAM)) && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE) &&
         !(run_flags & HB_RUN_GLOBAL_RING)) {
-        const int nm0 = e->subs[0].nm, nvar0 = e->subs[0].nvar;
+        const int nm_all = e->subs[0].nm, nvar0 = e->subs[0].nvar;
         const int pch = (fast == 1) ? 2 : e->subs[0].ncvar;
+        // CTAs per point: a thread-block cluster splitting the point's nodes (HB_RUN_STREAM_CLUSTER), so
+        // that fewer points are in flight and their histories stay in L2
+        {
+            const int v = (int)((run_flags >> 4) & 0x7);
+            stream_cluster = v == 0 ? 1 : 1 << (v - 1);
+            if (stream_cluster > 8 || stream_cluster > nm_all)
+                return fail(HB_ERR_INVALID_STATE, "HB_RUN_STREAM_CLUSTER: 1, 2, 4 or 8 CTAs per point, at most one per node");
+        }
+        const int SC = stream_cluster;
+        const int nm0 = (nm_all + SC - 1) / SC;  // nodes of the largest slice
+        size_t slice_edges = 0;
+        for (int r = 0; r < SC; r++) {
+            const int a0 = (int)(((long long)nm_all * r) / SC), a1 = (int)(((long long)nm_all * (r + 1)) / SC);
+            slice_edges = std::max(slice_edges, (size_t)(e->projs[0].rowptr[a1] - e->projs[0].rowptr[a0]));
+        }
         // nodes per consumer thread: one (512 threads) for up to 96 nodes, else two (1024 threads, at
         // least 256 producers); four (768 threads, two edge windows in flight per producer) on request
         auto fits = [&](int k, int nt) { return ((nm0 + k - 1) / k + 31) / 32 * 32 + (nt == 512 ? 128 : 256) <= nt; };
@@ -704,20 +722,20 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
             const size_t gx_b = (size_t)2 * HB_STREAM_K * nm0 * pch * 4;
             const size_t nz_b = any_stoch ? (size_t)2 * HB_STREAM_K * nm0 * nvar0 * 4 : 0;
             const size_t rp_b = ((size_t)(nm0 + 1) * 4 + 15) & ~(size_t)15;
-            const size_t ed_b = e->projs[0].edges.size() * 8;
+            const size_t ed_b = slice_edges * 8;
             const size_t pr_b = stream_prm_bytes(e->kernel_model, nm0, npt);
             if (gx_b + rp_b + pr_b + 16 <= cap) {
                 stream_npt = npt;
                 stream_noise_smem = (nz_b > 0 && gx_b + nz_b + rp_b + pr_b + 16 <= cap) ? 1 : 0;
                 size_t used = gx_b + (stream_noise_smem ? nz_b : 0) + rp_b + pr_b + 16;
-                if (used + ed_b <= cap) { stream_edges = (int)e->projs[0].edges.size(); used += ed_b; }
+                if (used + ed_b + 16 <= cap) { stream_edges = (int)slice_edges; used += ed_b + 16; }
                 stream_smem = used;
                 const int n_cons = ((nm0 + npt - 1) / npt + 31) / 32 * 32;
                 const int n_prod = threads - n_cons;
                 while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
                 e->threads = threads;
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
-                const size_t words = (size_t)B * nm0 * (stream_rp + 2 * HB_STREAM_K) * pch;
+                const size_t words = (size_t)B * nm_all * (stream_rp + 2 * HB_STREAM_K) * pch;
                 CUDA_TRY(e->sring.ensure(words));
                 e->last_kind = 4;
             }
@@ -827,6 +845,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     a.stream_rp = stream_rp;
     a.stream_noise_smem = stream_noise_smem;
     a.stream_prefetch = (run_flags & HB_RUN_STREAM_PREFETCH) ? 2 : 0;
+    a.stream_cluster = stream_npt ? stream_cluster : 1;
     if (stream_npt) { a.ring = e->sring.p; a.ring_in_smem = 0; }
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
@@ -1792,6 +1811,7 @@ struct hb_group {
     };
     std::vector<Member> m;
     DBuf<StreamJob> jobs;
+    DBuf<int> counter;   // the work queue's next item
     cudaStream_t own = nullptr, user = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1806,6 +1826,7 @@ struct hb_group {
         if (ev1) cudaEventDestroy(ev1);
         for (auto& mm : m) { mm.noise.release(); for (auto& b : mm.bw_init) b.release(); }
         jobs.release();
+        counter.release();
         if (own) cudaStreamDestroy(own);
     }
 };
@@ -1835,7 +1856,6 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     CUDA_TRY(cudaEventCreate(&g->ev0));
     CUDA_TRY(cudaEventCreate(&g->ev1));
     g->m.resize(n);
-    int model = -2, fast = -2;
     size_t smem = 0;
     for (int i = 0; i < n; i++) {
         const hb_group_member& mb = members[i];
@@ -1854,14 +1874,15 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
             CUDA_TRY(cudaMemcpy(gm.noise.p, mb.noise, (size_t)mb.noise_len * 4, cudaMemcpyHostToDevice));
             noise_dev = gm.noise.p;
         }
-        const uint32_t flags = (mb.run_flags & ~(uint32_t)(0x7u << 24)) | HB_RUN_STREAM | HB_RUN_STREAM_NPT(npt);
+        // the work-queue kernel runs every point in one CTA (no clusters)
+        const uint32_t flags = (mb.run_flags & ~(uint32_t)(0x7u << 24) & ~(uint32_t)(0x7u << 4)) | HB_RUN_STREAM |
+                               HB_RUN_STREAM_NPT(npt);
         if ((s = run_setup(e, gm.T, mb.n_steps, flags, nullptr, noise_dev ? noise_dev : e->x0.p, nullptr, gm.P))) return s;
         if (gm.P.stream_npt != npt)
             return fail(HB_ERR_UNSUPPORTED, "member %d cannot run in the streamed-history kernel (one subnetwork, one sparse "
                         "projection with per-edge delays >= %d steps)", i, 2 * HB_STREAM_K - 1);
-        if (model == -2) { model = e->kernel_model; fast = gm.P.fast; }
-        else if (model != e->kernel_model || fast != gm.P.fast)
-            return fail(HB_ERR_UNSUPPORTED, "group members must share the model and the coupling pre() form");
+        if (e->kernel_model < 0 || (gm.P.fast == 1 && e->subs[0].ncvar != 1))
+            return fail(HB_ERR_UNSUPPORTED, "member %d: no streamed-history kernel path for its model and coupling", i);
         smem = std::max(smem, gm.P.stream_smem);
         gm.P.a.s0 = 0;
         gm.P.a.n_steps = (int)mb.n_steps;
@@ -1882,8 +1903,7 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
         }
         CUDA_TRY(cudaStreamSynchronize(e->stream()));
     }
-    const int budget = npt == 1 ? hb_stream_group_budget_1(model, fast)
-                     : npt == 2 ? hb_stream_group_budget_2(model, fast) : hb_stream_group_budget_4(model, fast);
+    const int budget = npt == 1 ? hb_stream_queue_budget_1() : npt == 2 ? hb_stream_queue_budget_2() : hb_stream_queue_budget_4();
     if (budget < 0 || smem + 64 > (size_t)budget) return fail(HB_ERR_UNSUPPORTED, "grouped launch: shared memory budget exceeded");
     // jobs, longest points first
     std::vector<int> order(n);
@@ -1899,12 +1919,18 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
         jobs[k].args = gm.P.a;
         jobs[k].first_block = blocks;
         jobs[k].n_points = gm.e->B;
+        jobs[k].model = gm.e->kernel_model;
+        jobs[k].pre = gm.P.fast;
         blocks += gm.e->B;
     }
     CUDA_TRY(g->jobs.ensure(n));
+    CUDA_TRY(g->counter.ensure(1));
     CUDA_TRY(cudaMemcpy(g->jobs.p, jobs.data(), n * sizeof(StreamJob), cudaMemcpyHostToDevice));
     const int threads = npt == 1 ? 512 : npt == 2 ? 1024 : 768;
-    // the whole run as one graph: member resets, the grouped launch, batch-mean BOLD reductions
+    const int grid = npt == 1 ? hb_stream_queue_grid_1(threads, smem) : npt == 2 ? hb_stream_queue_grid_2(threads, smem)
+                                                                      : hb_stream_queue_grid_4(threads, smem);
+    if (grid < 1) return fail(HB_ERR_CUDA, "grouped launch: cannot size the work-queue grid");
+    // the whole run as one graph: member resets, the queue counter, the grouped launch, batch-mean BOLD reductions
     cudaStream_t st = g->stream();
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaSuccess;
@@ -1916,11 +1942,12 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
             ce = cudaMemcpyAsync(e->bold[k].bw.p, gm.bw_init[k].p, gm.bw_init[k].n * 4, cudaMemcpyDeviceToDevice, st);
     }
     // external event records become nodes of the graph, so the replay times the launch itself
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(g->counter.p, 0, sizeof(int), st);
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev0, st, cudaEventRecordExternal);
     if (ce == cudaSuccess)
-        ce = npt == 1 ? hb_launch_stream_group_1(model, fast, g->jobs.p, n, blocks, threads, smem, st)
-           : npt == 2 ? hb_launch_stream_group_2(model, fast, g->jobs.p, n, blocks, threads, smem, st)
-                      : hb_launch_stream_group_4(model, fast, g->jobs.p, n, blocks, threads, smem, st);
+        ce = npt == 1 ? hb_launch_stream_queue_1(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st)
+           : npt == 2 ? hb_launch_stream_queue_2(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st)
+                      : hb_launch_stream_queue_4(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st);
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev1, st, cudaEventRecordExternal);
     for (auto& gm : g->m) {
         for (int mo = 0; mo < gm.P.n_bold_active && !gm.P.bold_pp && ce == cudaSuccess; mo++) {

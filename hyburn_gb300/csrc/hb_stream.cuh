@@ -228,6 +228,46 @@ __device__ __forceinline__ void stream_edge_prefetch(const float* ring, const ui
     prefetch_l2(qp + (HB_STREAM_K * PCH - 1));
 }
 
+// ---- one sweep point split over the CTAs of a thread-block cluster ----
+#define HB_BAR_CONS 5  // named barrier of the consumer threads alone
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// every thread of every CTA of the cluster (release / acquire at cluster scope)
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
+// arrive (release at cluster scope) on the mbarrier at the same shared-memory offset in CTA `rank`
+__device__ __forceinline__ void mbar_arrive_remote(const uint64_t* bar, uint32_t rank) {
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_addr(bar)), "r"(rank));
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(ra) : "memory");
+}
+// wait (acquire at cluster scope) for the phase of parity `parity`, with an iteration limit; false
+// when the limit ran out
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// consumers of a cluster-split point after finishing block `blk`: their history writes made visible at
+// cluster scope, then one arrival per CTA on every CTA's barrier of the block's parity
+__device__ __forceinline__ void stream_signal_block(uint64_t* hbar, int blk, int C, int n_cons) {
+    fence_cluster();
+    named_sync(HB_BAR_CONS, n_cons);
+    if (threadIdx.x == 0)
+        for (int r = 0; r < C; r++) mbar_arrive_remote(hbar + (blk & 1), (uint32_t)r);
+}
+
 // Consumer steps for Heun (deterministic or stochastic) with Linear coupling delivered directly, no
 // trajectory and no BOLD, one node per thread: one straight-line loop with the operations of
 // stream_node_step in the same order.
@@ -235,35 +275,35 @@ template <int MODEL, bool STOCH, bool SF, bool NOISE_SMEM>
 __device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, const float* prm, const float* cp,
                                                            const float* nscale, float dt, float dt_half,
                                                            const float* gxbuf, const float* nzbuf, const float* noise_g,
-                                                           size_t nstride, float* ring, int n, bool active, int nm,
+                                                           size_t nstride, float* ring, int n, int l, bool active, int ns,
                                                            int RPX, int RP, int wpos, int n_steps, int n_blocks,
-                                                           int nthreads) {
+                                                           int nthreads, int C, uint64_t* hbar, int n_cons) {
     constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL), K = HB_STREAM_K;
     const float ca = cp[0], cb = cp[1];
-    float ns[NVAR];
+    float nsc[NVAR];
 #pragma unroll
-    for (int v = 0; v < NVAR; v++) ns[v] = nscale[v];
+    for (int v = 0; v < NVAR; v++) nsc[v] = nscale[v];
     for (int blk = 0; blk < n_blocks; blk++) {
         const int buf = blk & 1;
         named_sync(HB_BAR_FULL0 + buf, nthreads);
         const int it0 = blk * K;
         const int nb = (n_steps - it0) < K ? (n_steps - it0) : K;
-        const float* gb = gxbuf + (size_t)buf * K * nm * NCV + (size_t)n * NCV;
-        const float* nbuf = nzbuf + (size_t)buf * K * nm * NVAR + (size_t)n * NVAR;
+        const float* gb = gxbuf + (size_t)buf * K * ns * NCV + (size_t)l * NCV;
+        const float* nbuf = nzbuf + (size_t)buf * K * ns * NVAR + (size_t)l * NVAR;
 #pragma unroll 1
         for (int j = 0; j < nb; j++) {
             const int pos = wpos;
             wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
             if (!active) continue;  // threads past the last node only take part in the barriers
             float cc[2] = {0.0f, 0.0f};
-            cc[0] = gb[(size_t)j * nm * NCV] * ca + cb;
-            if (NCV > 1) cc[1] = gb[(size_t)j * nm * NCV + 1] * ca + cb;
+            cc[0] = gb[(size_t)j * ns * NCV] * ca + cb;
+            if (NCV > 1) cc[1] = gb[(size_t)j * ns * NCV + 1] * ca + cb;
             float nz[NVAR];
 #pragma unroll
             for (int v = 0; v < NVAR; v++) {
                 if (!STOCH) nz[v] = 0.0f;
-                else if (NOISE_SMEM) nz[v] = nbuf[(size_t)j * nm * NVAR + v] * ns[v];
-                else nz[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * ns[v];
+                else if (NOISE_SMEM) nz[v] = nbuf[(size_t)j * ns * NVAR + v] * nsc[v];
+                else nz[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * nsc[v];
             }
             float k1[NVAR], k2[NVAR], tmp[NVAR];
             dfun(MODEL, prm, SF ? 1 : 0, x, cc, k1);
@@ -281,40 +321,48 @@ __device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, 
         }
         __threadfence_block();
         named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+        if (C > 1) stream_signal_block(hbar, blk, C, n_cons);
     }
 }
 
-// the whole run of sweep point b of one network (one CTA)
+// copy of a network description into shared memory by all threads of the block (no barrier)
+__device__ __forceinline__ void stream_load_net(DevNet& net, const DevNet* __restrict__ gnet) {
+    const int* src = reinterpret_cast<const int*>(gnet);
+    int* dst = reinterpret_cast<int*>(&net);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
+}
+
+// One sweep point b of a network, or with a.stream_cluster = C > 1 the slice of its nodes that CTA
+// `rank` of the point's cluster owns. `net` is the block's shared-memory copy of the network's
+// description, filled by the caller and published with a block barrier before this call.
 template <int MODEL, int PRE, int NPT, int MAXT>
-__device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, const RunArgs& a, const int b) {
+__device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, const int b, const int rank) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ DevNet net;
-    {
-        const int* src = reinterpret_cast<const int*>(gnet);
-        int* dst = reinterpret_cast<int*>(&net);
-        for (int i = threadIdx.x; i < (int)(sizeof(DevNet) / 4); i += blockDim.x) dst[i] = src[i];
-    }
+    __shared__ __align__(8) uint64_t hist_bar[2];  // cluster-split: all CTAs finished an even / odd block
     constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
     constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
     constexpr int K = HB_STREAM_K;
     constexpr int UNR = (MAXT > 768) ? 1 : 2;  // edges in flight per producer thread (register budget)
     constexpr int DB = (MAXT > 768) ? 1 : 8;   // edge descriptors loaded per batch (register budget)
     const int t = threadIdx.x, nthreads = blockDim.x;
-    const int nm = gnet->sub[0].nm;
+    const int nm = net.sub[0].nm;  // nodes of the network (history rows)
+    const int C = a.stream_cluster > 1 ? a.stream_cluster : 1;
+    const int n0 = (int)(((long long)nm * rank) / C);                  // this CTA's nodes n0 .. n0 + ns - 1
+    const int ns = (int)(((long long)nm * (rank + 1)) / C) - n0;
     const int RP = a.stream_rp, RPX = RP + 2 * K;
-    const int n_cons = (((nm + NPT - 1) / NPT + 31) >> 5) << 5;
+    const int n_cons = (((ns + NPT - 1) / NPT + 31) >> 5) << 5;
     const int n_prod = nthreads - n_cons;
     float* ring = a.ring + (size_t)b * nm * RPX * PCH;
 
-    // shared layout: gx buffers [2][K][nm][PCH] | noise buffers [2][K][nm*NVAR] | rowptr | edges | weights
+    // shared layout: gx buffers [2][K][ns][PCH] | noise buffers [2][K][ns*NVAR] | rowptr | edges | weights
     size_t off = 0;
     float* gxbuf = reinterpret_cast<float*>(smem);
-    off += (size_t)2 * K * nm * PCH * sizeof(float);
+    off += (size_t)2 * K * ns * PCH * sizeof(float);
     float* nzbuf = reinterpret_cast<float*>(smem + off);
-    if (a.stream_noise_smem) off += (size_t)2 * K * nm * NVAR * sizeof(float);
+    if (a.stream_noise_smem) off += (size_t)2 * K * ns * NVAR * sizeof(float);
     off = (off + 15) & ~(size_t)15;
     int* s_rowptr = reinterpret_cast<int*>(smem + off);
-    off += (size_t)(nm + 1) * 4;
+    off += (size_t)(ns + 1) * 4;
     off = (off + 15) & ~(size_t)15;
     uint32_t* s_edges = reinterpret_cast<uint32_t*>(smem + off);
     off += (size_t)a.smem_edges * 4;
@@ -326,19 +374,28 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
     constexpr int PU = c_nparams_used(MODEL);
     float* s_prm = reinterpret_cast<float*>(smem + off);
 
-    // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176)
+    // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176);
+    // each CTA clears its own nodes' rows
     if (a.s0 == 0) {
-        float4* r4 = reinterpret_cast<float4*>(ring);
-        const size_t n4 = ((size_t)nm * RPX * PCH) >> 2;
+        float4* r4 = reinterpret_cast<float4*>(ring + (size_t)n0 * RPX * PCH);
+        const size_t n4 = ((size_t)ns * RPX * PCH) >> 2;
         for (size_t i = t; i < n4; i += nthreads) r4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (C > 1 && t == 0) {
+        mbar_init(&hist_bar[0], (uint32_t)C);
+        mbar_init(&hist_bar[1], (uint32_t)C);
+        mbar_init_fence();
     }
     __syncthreads();
     const DevProj& P = net.proj[0];
-    for (int i = t; i <= nm; i += nthreads) s_rowptr[i] = P.rowptr[i];
+    // row bounds of this CTA's target nodes; relative to the shared-memory copy of its edges when
+    // they fit there
     const bool edges_smem = a.smem_edges > 0;
+    const int e_first = P.rowptr[n0];
+    for (int i = t; i <= ns; i += nthreads) s_rowptr[i] = P.rowptr[n0 + i] - (edges_smem ? e_first : 0);
     if (edges_smem) {
-        const int nnz = P.rowptr[P.ntgt];
-        for (int i = t; i < nnz; i += nthreads) { s_edges[i] = P.edges[i]; s_ew[i] = P.ew[i]; }
+        const int cnt = P.rowptr[n0 + ns] - e_first;
+        for (int i = t; i < cnt; i += nthreads) { s_edges[i] = P.edges[e_first + i]; s_ew[i] = P.ew[e_first + i]; }
     }
     const uint32_t* __restrict__ ed = edges_smem ? s_edges : P.edges;
     const float* __restrict__ ew = edges_smem ? s_ew : P.ew;
@@ -357,14 +414,14 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
     const bool is_consumer = t < n_cons;
     const bool first_launch_of_run = (a.s0 == a.run_s0);
 
-    // consumer state: nodes t, t + n_cons, ...
+    // consumer state: local nodes t, t + n_cons, ... (network nodes n0 + those)
     float x[NPT][NVAR], tv[NPT][NVAR];
     size_t st_base[NPT];
     bool active[NPT];
 #pragma unroll
     for (int q = 0; q < NPT; q++) {
-        const int n = t + q * n_cons;
-        active[q] = is_consumer && n < nm;
+        const int n = n0 + t + q * n_cons;
+        active[q] = is_consumer && t + q * n_cons < ns;
         st_base[q] = (size_t)b * net.state_len + (size_t)(active[q] ? n : 0) * NVAR;
 #pragma unroll
         for (int v = 0; v < NVAR; v++) {
@@ -374,25 +431,32 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
         if (active[q]) stream_publish<PRE, NCV, PCH>(ring, n, RPX, RP, (int)(a.s0 % RP), x[q]);
     }
     if (NPT > 1)
-        for (int i = t; i < nm * PU; i += nthreads) s_prm[i] = hb_param_row(net.sub[0], b, i / PU)[i % PU];
-    __syncthreads();
+        for (int i = t; i < ns * PU; i += nthreads) s_prm[i] = hb_param_row(net.sub[0], b, n0 + i / PU)[i % PU];
+    // the history every CTA of the point reads (cleared rows, the published start state) and the
+    // barriers of the cluster are ready
+    if (C > 1) cluster_barrier();
+    else __syncthreads();
 
     if (!is_consumer) {
         // ================= producers =================
         const int p = t - n_cons;
         const int PL = a.pipe_lanes;  // threads per node (power of two <= 8)
         const int pf = a.stream_prefetch;
-        const int items = nm * PL;
+        const int items = ns * PL;
         const int rounds = (items + n_prod - 1) / n_prod;
-        const int row_len = nm * NVAR;
+        const int row_len = ns * NVAR;  // this CTA's part of a noise row
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
+            // block blk reads the history up to the first step of block blk - 1, which every CTA of the
+            // point has published once it finished block blk - 2
+            if (C > 1 && blk >= 2 && !mbar_wait_cluster(&hist_bar[(blk - 2) & 1], (uint32_t)(((blk - 2) >> 1) & 1)))
+                atomicOr(a.flags + 1, 4);
             const int it0 = blk * K;
             const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
             const int64_t sb = a.s0 + it0;
             const int sbm = (int)(sb % RP);
-            float* gb = gxbuf + (size_t)buf * K * nm * PCH;
+            float* gb = gxbuf + (size_t)buf * K * ns * PCH;
             for (int r = 0; r < rounds; r++) {
                 const int item = p + r * n_prod;
                 const int node = item / PL, lane = item - (item / PL) * PL;
@@ -401,7 +465,7 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                 for (int j = 0; j < K; j++)
 #pragma unroll
                     for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
-                if (node < nm) {
+                if (node < ns) {
                     const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
                     if constexpr (DB == 1) {
 #pragma unroll UNR
@@ -441,19 +505,19 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
 #pragma unroll
                         for (int c = 0; c < PCH; c++) acc[j][c] += __shfl_xor_sync(0xffffffffu, acc[j][c], o);
                 }
-                if (node < nm && lane == 0) {
+                if (node < ns && lane == 0) {
 #pragma unroll
                     for (int j = 0; j < K; j++)
                         if (j < nb) {
 #pragma unroll
-                            for (int c = 0; c < PCH; c++) gb[((size_t)j * nm + node) * PCH + c] = acc[j][c];
+                            for (int c = 0; c < PCH; c++) gb[((size_t)j * ns + node) * PCH + c] = acc[j][c];
                         }
                 }
             }
             if (stoch && a.stream_noise_smem) {
                 float* nbuf = nzbuf + (size_t)buf * K * row_len;
-                const float* src = noise_base + (size_t)it0 * nstride;
-                if (!a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                const float* src = noise_base + (size_t)it0 * nstride + (size_t)n0 * NVAR;
+                if (C == 1 && !a.noise_per_point && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
                     const int total = nb * row_len, n4 = total >> 2;
                     const float4* s4 = reinterpret_cast<const float4*>(src);
                     float4* d4 = reinterpret_cast<float4*>(nbuf);
@@ -477,13 +541,13 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
         const int sweep_form = net.sub[0].sweep_form;
         float prm[HB_PSTRIDE];  // one node per thread: its row in registers
         {
-            const float* pr = hb_param_row(net.sub[0], b, active[0] ? t : 0);
+            const float* pr = hb_param_row(net.sub[0], b, active[0] ? n0 + t : 0);
 #pragma unroll
             for (int i = 0; i < HB_PSTRIDE; i++) prm[i] = (NPT == 1 && i < PU) ? pr[i] : 0.0f;
         }
         float rowsum[NPT];
 #pragma unroll
-        for (int q = 0; q < NPT; q++) rowsum[q] = (P.has_rowsums && active[q]) ? P.rowsums[t + q * n_cons] : 0.0f;
+        for (int q = 0; q < NPT; q++) rowsum[q] = (P.has_rowsums && active[q]) ? P.rowsums[n0 + t + q * n_cons] : 0.0f;
         const float dt = net.dt, dt_half = net.dt_half, h2 = net.dt_h2, h6 = net.dt_sixth;
         const int N0 = a.bold.n0;
         float bacc[NPT][HB_MAX_BOLD];
@@ -496,7 +560,7 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                 bcnt[q][m] = 0;
                 if (m < a.bold.n) {
                     bcnt[q][m] = (int)((a.s0 - a.run_s0) % a.bold.period[m]);
-                    if (active[q] && !first_launch_of_run) bacc[q][m] = a.bold.acc[m][(size_t)b * N0 + t + q * n_cons];
+                    if (active[q] && !first_launch_of_run) bacc[q][m] = a.bold.acc[m][(size_t)b * N0 + n0 + t + q * n_cons];
                 }
             }
         int64_t s = a.s0;
@@ -505,14 +569,14 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
                               P.cfk == HBC_LINEAR && P.direct && P.pc == NCV && !P.has_rowsums && a.traj == nullptr &&
                               a.bold.n == 0;
         if (straight) {
-            const int n = t;
+            const int n = n0 + t;
             float nscale[8];
 #pragma unroll
             for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
             const bool ns_smem = a.stream_noise_smem != 0;
             float* x0 = x[0];
             float* tv0 = tv[0];
-#define HB_SC(ST, SF, NS) stream_consume_heun_linear<MODEL, ST, SF, NS>(x0, tv0, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n, active[0], nm, RPX, RP, wpos, a.n_steps, n_blocks, nthreads)
+#define HB_SC(ST, SF, NS) stream_consume_heun_linear<MODEL, ST, SF, NS>(x0, tv0, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n, t, active[0], ns, RPX, RP, wpos, a.n_steps, n_blocks, nthreads, C, hist_bar, n_cons)
             if (integ == HBI_HEUN_STOCH) {
                 if (ns_smem) { if (sweep_form) HB_SC(true, true, true); else HB_SC(true, false, true); }
                 else { if (sweep_form) HB_SC(true, true, false); else HB_SC(true, false, false); }
@@ -526,17 +590,17 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
             named_sync(HB_BAR_FULL0 + buf, nthreads);
             const int it0 = blk * K;
             const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
-            const float* gb = gxbuf + (size_t)buf * K * nm * PCH;
-            const float* nbuf = nzbuf + (size_t)buf * K * nm * NVAR;
+            const float* gb = gxbuf + (size_t)buf * K * ns * PCH;
+            const float* nbuf = nzbuf + (size_t)buf * K * ns * NVAR;
 #pragma unroll 1
             for (int j = 0; j < nb; j++, s++) {
 #pragma unroll
                 for (int q = 0; q < NPT; q++) {
                     if (!active[q]) continue;
-                    const int n = t + q * n_cons;
+                    const int l = t + q * n_cons, n = n0 + l;  // local and network node
                     float gx[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                    for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * nm + n) * PCH + c];
+                    for (int c = 0; c < PCH; c++) gx[c] = gb[((size_t)j * ns + l) * PCH + c];
                     if (PCH == 2 && a.gx_out)
                         __stcs(reinterpret_cast<float2*>(a.gx_out) + ((size_t)(it0 + j) * B + b) * nm + n,
                                make_float2(gx[0], gx[PCH - 1]));
@@ -544,10 +608,10 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
 #pragma unroll
                     for (int v = 0; v < NVAR; v++) {
                         if (!stoch) nz[v] = 0.0f;
-                        else if (a.stream_noise_smem) nz[v] = nbuf[(size_t)j * nm * NVAR + n * NVAR + v] * net.noise_scale[v];
+                        else if (a.stream_noise_smem) nz[v] = nbuf[(size_t)j * ns * NVAR + l * NVAR + v] * net.noise_scale[v];
                         else nz[v] = __ldcs(noise_base + (size_t)(it0 + j) * nstride + n * NVAR + v) * net.noise_scale[v];
                     }
-                    const float* pq = NPT == 1 ? prm : s_prm + (size_t)n * PU;
+                    const float* pq = NPT == 1 ? prm : s_prm + (size_t)l * PU;
                     stream_node_step<MODEL>(P, cp, integ, pq, sweep_form, rowsum[q], gx, nz, x[q], dt, dt_half, h2, h6);
 #pragma unroll
                     for (int v = 0; v < NVAR; v++) tv[q][v] = tv[q][v] + x[q][v];
@@ -563,6 +627,7 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
             }
             __threadfence_block();
             named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+            if (C > 1) stream_signal_block(hist_bar, blk, C, n_cons);
         }
 #pragma unroll
         for (int q = 0; q < NPT; q++) {
@@ -577,61 +642,114 @@ __device__ __forceinline__ void stream_point(const DevNet* __restrict__ gnet, co
             if (a.check_finite && bad) atomicOr(a.flags, 1);
 #pragma unroll
             for (int m = 0; m < HB_MAX_BOLD; m++)
-                if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + t + q * n_cons] = bacc[q][m];
+                if (m < a.bold.n) a.bold.acc[m][(size_t)b * N0 + n0 + t + q * n_cons] = bacc[q][m];
         }
     }
+    // no CTA of a cluster-split point leaves while another may still arrive on its barriers
+    if (C > 1) cluster_barrier();
 }
 
 template <int MODEL, int PRE, int NPT, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __restrict__ gnet, RunArgs a) {
-    stream_point<MODEL, PRE, NPT, MAXT>(gnet, a, (int)blockIdx.x);
+    __shared__ DevNet net;
+    stream_load_net(net, gnet);
+    __syncthreads();
+    // a cluster of a.stream_cluster CTAs per point (consecutive blocks), else one CTA per point
+    const int C = a.stream_cluster > 1 ? a.stream_cluster : 1;
+    stream_point<MODEL, PRE, NPT, MAXT>(net, a, (int)blockIdx.x / C, C > 1 ? (int)cluster_rank() : 0);
 }
 
-// Several networks' sweeps in one launch: block i runs point i - first_block of the job whose
-// range holds i. Jobs are ordered by decreasing work per point, so the block scheduler starts the
-// longest points first and fills the machine with the short ones as SMs free up.
+// one (model, coupling pre() form) path of the work-queue kernel
 template <int MODEL, int PRE, int NPT, int MAXT>
-__global__ void __launch_bounds__(MAXT, 1) stream_group_kernel(const StreamJob* __restrict__ jobs, int n_jobs) {
+__device__ __forceinline__ void stream_queue_item(DevNet& net, const RunArgs& a, int b) {
+    stream_point<MODEL, PRE, NPT, MAXT>(net, a, b, 0);
+}
+
+// Several networks' sweeps — different models, node counts, connectomes, delays and step counts — in
+// one launch of a persistent kernel: each block takes the next (job, point) item from a device counter
+// until the items run out, and runs it through the path of the job's model and coupling form. Items
+// are numbered job by job with the jobs ordered by decreasing work per point, so the longest points
+// start first and the short ones fill the SMs that finish early (greedy longest-first scheduling).
+// The counter is zeroed before every launch.
+template <int NPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) stream_queue_kernel(const StreamJob* __restrict__ jobs, int n_jobs, int n_items,
+                                                              int* __restrict__ counter) {
+    __shared__ DevNet net;
     __shared__ RunArgs sa;
-    __shared__ int sj;
-    if (threadIdx.x == 0) {
-        int j = 0;
-        while (j + 1 < n_jobs && (int)blockIdx.x >= jobs[j + 1].first_block) j++;
-        sj = j;
+    __shared__ int s_item, s_job;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int it = atomicAdd(counter, 1);
+            int j = 0;
+            while (j + 1 < n_jobs && it >= jobs[j + 1].first_block) j++;
+            s_item = it;
+            s_job = j;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const StreamJob* J = jobs + s_job;
+        {
+            const int* src = reinterpret_cast<const int*>(&J->args);
+            int* dst = reinterpret_cast<int*>(&sa);
+            for (int i = threadIdx.x; i < (int)(sizeof(RunArgs) / 4); i += blockDim.x) dst[i] = src[i];
+        }
+        stream_load_net(net, J->net);
+        __syncthreads();
+        const int b = it - J->first_block;
+        switch (J->model * 2 + (J->pre == PRE_KURA ? 1 : 0)) {
+        case 0: stream_queue_item<0, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 1: stream_queue_item<0, PRE_KURA, NPT, MAXT>(net, sa, b); break;
+        case 2: stream_queue_item<1, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 4: stream_queue_item<2, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 5: stream_queue_item<2, PRE_KURA, NPT, MAXT>(net, sa, b); break;
+        case 6: stream_queue_item<3, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 7: stream_queue_item<3, PRE_KURA, NPT, MAXT>(net, sa, b); break;
+        case 8: stream_queue_item<4, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 9: stream_queue_item<4, PRE_KURA, NPT, MAXT>(net, sa, b); break;
+        case 10: stream_queue_item<5, PRE_ID, NPT, MAXT>(net, sa, b); break;
+        case 11: stream_queue_item<5, PRE_KURA, NPT, MAXT>(net, sa, b); break;
+        default: break;  // MontbrioPazoRoxin has two coupling variables: no [sin, cos] form (refused on the host)
+        }
+        __syncthreads();  // shared memory and the item slot are reused by the next item
     }
-    __syncthreads();
-    const StreamJob* J = jobs + sj;
-    {
-        const int* src = reinterpret_cast<const int*>(&J->args);
-        int* dst = reinterpret_cast<int*>(&sa);
-        for (int i = threadIdx.x; i < (int)(sizeof(RunArgs) / 4); i += blockDim.x) dst[i] = src[i];
-    }
-    __syncthreads();
-    stream_point<MODEL, PRE, NPT, MAXT>(J->net, sa, (int)blockIdx.x - J->first_block);
 }
 
-template <int MODEL, int PRE, int NPT, int MAXT>
-int stream_group_max_dynamic_smem() {
+template <int NPT, int MAXT>
+int stream_queue_max_dynamic_smem() {
     static int cached = -1;
     if (cached >= 0) return cached;
     int dev = 0, optin = 0;
     cudaFuncAttributes fa;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
-    if (cudaFuncGetAttributes(&fa, stream_group_kernel<MODEL, PRE, NPT, MAXT>) != cudaSuccess) return -1;
+    if (cudaFuncGetAttributes(&fa, stream_queue_kernel<NPT, MAXT>) != cudaSuccess) return -1;
     int maxdyn = optin - (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(stream_group_kernel<MODEL, PRE, NPT, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+    if (cudaFuncSetAttribute(stream_queue_kernel<NPT, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
         return -1;
     cached = maxdyn;
     return cached;
 }
 
-template <int MODEL, int PRE, int NPT, int MAXT>
-cudaError_t launch_stream_group(const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st) {
-    int maxdyn = stream_group_max_dynamic_smem<MODEL, PRE, NPT, MAXT>();
+// persistent grid: as many blocks of the queue kernel as fit on the device at once
+template <int NPT, int MAXT>
+int stream_queue_grid(int threads, size_t smem) {
+    if (stream_queue_max_dynamic_smem<NPT, MAXT>() < 0) return -1;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stream_queue_kernel<NPT, MAXT>, threads, smem) != cudaSuccess) return -1;
+    return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+template <int NPT, int MAXT>
+cudaError_t launch_stream_queue(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads,
+                                size_t smem, cudaStream_t st) {
+    int maxdyn = stream_queue_max_dynamic_smem<NPT, MAXT>();
     if (maxdyn < 0) return cudaErrorInvalidConfiguration;
-    if ((long long)smem > maxdyn || threads > MAXT) return cudaErrorInvalidValue;
-    stream_group_kernel<MODEL, PRE, NPT, MAXT><<<blocks, threads, smem, st>>>(d_jobs, n_jobs);
+    if ((long long)smem > maxdyn || threads > MAXT || blocks < 1) return cudaErrorInvalidValue;
+    if (blocks > n_items) blocks = n_items;
+    stream_queue_kernel<NPT, MAXT><<<blocks, threads, smem, st>>>(d_jobs, n_jobs, n_items, counter);
     return cudaGetLastError();
 }
 
@@ -656,8 +774,25 @@ cudaError_t launch_stream(const DevNet* d_net, const RunArgs& a, int B, int thre
     int maxdyn = stream_max_dynamic_smem<MODEL, PRE, NPT, MAXT>();
     if (maxdyn < 0) return cudaErrorInvalidConfiguration;
     if ((long long)smem > maxdyn || threads > MAXT) return cudaErrorInvalidValue;
-    stream_pipe_kernel<MODEL, PRE, NPT, MAXT><<<B, threads, smem, st>>>(d_net, a);
-    return cudaGetLastError();
+    const int C = a.stream_cluster > 1 ? a.stream_cluster : 1;
+    if (C == 1) {
+        stream_pipe_kernel<MODEL, PRE, NPT, MAXT><<<B, threads, smem, st>>>(d_net, a);
+        return cudaGetLastError();
+    }
+    if (C > 8) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(B * C));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stream_pipe_kernel<MODEL, PRE, NPT, MAXT>, d_net, a);
 }
 
 }  // namespace hb
@@ -669,12 +804,15 @@ cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const Ru
 int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
-cudaError_t hb_launch_stream_group_1(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-cudaError_t hb_launch_stream_group_2(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-cudaError_t hb_launch_stream_group_4(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_group_budget_1(int model, int pre);
-int hb_stream_group_budget_2(int model, int pre);
-int hb_stream_group_budget_4(int model, int pre);
+cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_1(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_2(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
+int hb_stream_queue_grid_4(int threads, size_t smem);
+int hb_stream_queue_budget_1();
+int hb_stream_queue_budget_2();
+int hb_stream_queue_budget_4();
 
 #define HB_STREAM_UNIT(NPT_, MAXT_)                                                                                  \
     cudaError_t hb_launch_stream_##NPT_(int model, int pre, const DevNet* d_net, const RunArgs& a, int B,            \
@@ -703,31 +841,13 @@ int hb_stream_group_budget_4(int model, int pre);
         int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
         if (i < 0 || i >= 12) return -1;                                                                             \
         return tab[i]();                                                                                             \
-    }                                                                                                                \
-    cudaError_t hb_launch_stream_group_##NPT_(int model, int pre, const StreamJob* d_jobs, int n_jobs, int blocks,   \
-                                              int threads, size_t smem, cudaStream_t st) {                           \
-        using F = cudaError_t (*)(const StreamJob*, int, int, int, size_t, cudaStream_t);                            \
-        static const F tab[12] = {                                                                                   \
-            hb::launch_stream_group<0, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<0, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::launch_stream_group<1, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<1, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::launch_stream_group<2, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<2, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::launch_stream_group<3, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<3, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::launch_stream_group<4, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<4, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::launch_stream_group<5, hb::PRE_ID, NPT_, MAXT_>, hb::launch_stream_group<5, hb::PRE_KURA, NPT_, MAXT_>}; \
-        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
-        if (i < 0 || i >= 12) return cudaErrorInvalidValue;                                                          \
-        return tab[i](d_jobs, n_jobs, blocks, threads, smem, st);                                                    \
-    }                                                                                                                \
-    int hb_stream_group_budget_##NPT_(int model, int pre) {                                                          \
-        using G = int (*)();                                                                                         \
-        static const G tab[12] = {                                                                                   \
-            hb::stream_group_max_dynamic_smem<0, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<0, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::stream_group_max_dynamic_smem<1, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<1, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::stream_group_max_dynamic_smem<2, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<2, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::stream_group_max_dynamic_smem<3, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<3, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::stream_group_max_dynamic_smem<4, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<4, hb::PRE_KURA, NPT_, MAXT_>, \
-            hb::stream_group_max_dynamic_smem<5, hb::PRE_ID, NPT_, MAXT_>, hb::stream_group_max_dynamic_smem<5, hb::PRE_KURA, NPT_, MAXT_>}; \
-        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
-        if (i < 0 || i >= 12) return -1;                                                                             \
-        return tab[i]();                                                                                             \
     }
+
+// one translation unit per (NPT, MAXT) for the work-queue kernel of grouped launches
+#define HB_QUEUE_UNIT(NPT_, MAXT_)                                                                                   \
+    cudaError_t hb_launch_stream_queue_##NPT_(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter,        \
+                                              int blocks, int threads, size_t smem, cudaStream_t st) {               \
+        return hb::launch_stream_queue<NPT_, MAXT_>(d_jobs, n_jobs, n_items, counter, blocks, threads, smem, st);    \
+    }                                                                                                                \
+    int hb_stream_queue_budget_##NPT_() { return hb::stream_queue_max_dynamic_smem<NPT_, MAXT_>(); }                  \
+    int hb_stream_queue_grid_##NPT_(int threads, size_t smem) { return hb::stream_queue_grid<NPT_, MAXT_>(threads, smem); }

@@ -157,11 +157,36 @@ class BatchHybridEngine:
         raise_for(st, self._lib.hb_last_error().decode())
         self._h = h
         self.models = [s.model for s in config.network.subnetworks]
+        self.tune = "cache"
+        self.tuned_flags: Optional[int] = None  # the autotuner's choice the last run used, if any
+
+    def _with_tuned(self, run_flags: int, param: Optional[SweepParam] = None, values=None) -> int:
+        """run_flags plus the autotuner's cached kernel choice for this shape, unless the caller chose a
+        kernel form itself or tuning is off."""
+        self.tuned_flags = None
+        if self.tune == "off" or (run_flags & _abi.HB_RUN_KERNEL_CHOICE):
+            return run_flags
+        from . import autotune
+        f = autotune.best_run_flags(self.config, self.n_sweep, self.semantics)
+        if f is None and self.tune == "auto" and param is not None:
+            f, _ = autotune.tune(self.config, self.n_sweep, param, values, self.semantics)
+        self.tuned_flags = f
+        return run_flags | (f or 0)
 
     @classmethod
-    def from_config(cls, config: SimConfig, n_sweep: int, device=None, semantics: int = 0) -> "BatchHybridEngine":
-        """BatchHybridEngine::from_config (engine.rs:145-471)."""
-        return cls(config, n_sweep, semantics)
+    def from_config(cls, config: SimConfig, n_sweep: int, device=None, semantics: int = 0,
+                    tune: str = "cache") -> "BatchHybridEngine":
+        """BatchHybridEngine::from_config (engine.rs:145-471).
+
+        `tune` selects how a run that forces no kernel form picks one: "cache" (default) uses the
+        autotuner's cached choice for this network shape when there is one, else the engine's fixed
+        rules; "auto" also measures the candidates on the first run of an untuned shape
+        (hyburn_gb300.autotune.tune) and caches the winner; "off" always uses the fixed rules."""
+        eng = cls(config, n_sweep, semantics)
+        if tune not in ("cache", "auto", "off"):
+            raise ValueError(f"tune must be 'cache', 'auto' or 'off', not {tune!r}")
+        eng.tune = tune
+        return eng
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -210,6 +235,7 @@ class BatchHybridEngine:
         writes the run's tavg_sub{i}.npy files there (cli.rs:961-970, hb_engine_write_tavg)."""
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        run_flags = self._with_tuned(run_flags, param, vals)
         r = C.c_void_p()
         st = self._lib.hb_engine_run_sweep(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals),
                                            vals.size, int(n_steps), int(run_flags), nptr, nlen, C.byref(r))
@@ -231,6 +257,7 @@ class BatchHybridEngine:
         """BatchHybridEngine::run_sweep_multi (engine.rs:845-851)."""
         arr, keep = _abi.sweep_points(spec.points)
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        run_flags = self._with_tuned(run_flags)
         r = C.c_void_p()
         st = self._lib.hb_engine_run_sweep_multi(self._h, arr, len(spec.points), int(n_steps), int(run_flags),
                                                  nptr, nlen, C.byref(r))
@@ -294,6 +321,7 @@ class BatchHybridEngine:
         out = _abi.hb_order_adjoint_out()
         dp = C.POINTER(C.c_double)
         out.loss, out.d_gain, out.d_omega, out.d_omega_node = (a.ctypes.data_as(dp) for a in (loss, dg, dw, dwn))
+        run_flags = self._with_tuned(run_flags)
         st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), int(run_flags), C.byref(out))
         raise_for(st, self._lib.hb_last_error().decode())
         return OrderAdjointResult(loss, dg, dw, dwn, out.forward_ms, out.prepare_ms, out.reverse_ms)
@@ -324,6 +352,7 @@ class BatchHybridEngine:
     def prepare(self, param: SweepParam, param_values, n_steps: int, noise=None, run_flags: int = 0) -> None:
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
+        run_flags = self._with_tuned(run_flags, param, vals)
         st = self._lib.hb_engine_prepare(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals), vals.size,
                                          int(n_steps), int(run_flags), nptr, nlen)
         raise_for(st, self._lib.hb_last_error().decode())
@@ -350,6 +379,15 @@ class GroupedSweep:
     def __init__(self, members, run_flags: int = 0, stream_handle: Optional[int] = None):
         self._lib = _abi.load_library()
         self._engines = [m[0] for m in members]
+        if not (run_flags & _abi.HB_RUN_KERNEL_CHOICE):
+            # the autotuner's streamed-history form (nodes per consumer thread, L2 prefetch) when every
+            # tuned member chose the same one
+            from . import autotune
+            picks = {f & _abi.HB_RUN_STREAM_FORM for f in
+                     (autotune.best_run_flags(e.config, e.n_sweep, e.semantics) for e in self._engines
+                      if e.tune != "off") if f is not None and f & _abi.HB_RUN_STREAM}
+            if len(picks) == 1:
+                run_flags |= picks.pop()
         keep = []
         arr = (_abi.hb_group_member * len(members))()
         for i, (eng, param, values, n_steps, noise) in enumerate(members):

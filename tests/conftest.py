@@ -7,6 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# engines consult the autotuner's cache by default; the tests use a cache of their own (empty unless
+# a test tunes into it) so that a user's cached choices do not change which kernel a test exercises
+os.environ.setdefault("HYBURN_GB300_TUNE_CACHE", os.path.join(ROOT, ".pytest_cache", "hyburn_gb300_tune.json"))
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")

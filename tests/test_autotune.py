@@ -8,9 +8,7 @@ from hyburn_gb300.config import Unsupported
 from cases import single_model
 
 
-def test_tune_picks_the_fastest_candidate_and_caches_it(tmp_path, monkeypatch):
-    monkeypatch.setenv("HYBURN_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
-    autotune._MEMO.clear()
+def test_tune_picks_the_fastest_candidate_and_caches_it(tune_cache):
     cfg = single_model("Generic2dOscillator", 24, "heun", "Linear", (0.1,), weights="csr", delays="per_edge_long")
     names = [n for n, _ in autotune.candidates(cfg, HB_SEM_DELAY_RING)]
     assert names[0] == "engine" and any("pipeline" in n for n in names) and any("streamed" in n for n in names)
@@ -31,14 +29,53 @@ def test_tune_picks_the_fastest_candidate_and_caches_it(tmp_path, monkeypatch):
     assert autotune.best_run_flags(cfg, 4, HB_SEM_DELAY_RING) is None    # another shape
 
 
-@pytest.mark.gpu
-def test_tuned_flags_run_and_match_the_oracle(tmp_path, monkeypatch):
-    from test_parity_gpu import compare
-    from hyburn_gb300 import inputs
+@pytest.fixture
+def tune_cache(tmp_path, monkeypatch):
+    """A private tuning cache; the in-process memo is cleared before and after so no tuned choice
+    leaks into other tests."""
     monkeypatch.setenv("HYBURN_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
     autotune._MEMO.clear()
+    yield tmp_path / "tune.json"
+    autotune._MEMO.clear()
+
+
+@pytest.mark.gpu
+def test_tuned_flags_run_and_match_the_oracle(tune_cache):
+    from test_parity_gpu import compare
+    from hyburn_gb300 import inputs
     cfg, meta = inputs.batched_sweep(n_steps=600, n_points=16)
     flags, times = autotune.tune(cfg, 16, SweepParam(-1, 0), meta["values"], HB_SEM_DELAY_RING, probe_steps=400)
     assert len(times) >= 8 and all(t > 0 for t in times.values())
     nz = inputs.standard_normal((600, 148), 5)
     compare(cfg, 16, SweepParam(-1, 0), meta["values"], 600, semantics=HB_SEM_DELAY_RING, noise=nz, run_flags=flags)
+
+
+@pytest.mark.gpu
+def test_engine_uses_the_tuned_choice_by_default(tune_cache):
+    """A cached choice (here made to pick the per-step kernel with two lanes, kind 2) is what a default
+    run uses; tune="off" and an explicit kernel choice bypass it; tune="auto" tunes an untuned shape."""
+    from hyburn_gb300 import BatchHybridEngine, inputs
+    cfg, meta = inputs.batched_sweep(n_steps=300, n_points=5, nsig=0.0, integrator="heun")
+    want = dict(autotune.candidates(cfg, HB_SEM_DELAY_RING))["per-step lanes 2"]
+
+    def fake(config, n_sweep, semantics, param, values, n_steps, flags, noise, repeats):
+        return 1.0 if flags == want else 2.0
+
+    autotune.tune(cfg, 5, SweepParam(-1, 0), meta["values"], HB_SEM_DELAY_RING, measure=fake)
+    eng = BatchHybridEngine.from_config(cfg, 5, semantics=HB_SEM_DELAY_RING)
+    a = eng.run_sweep(SweepParam(-1, 0), meta["values"], 300)
+    assert eng.tuned_flags == want and eng.last_kernel_time()[2] == 2
+    off = BatchHybridEngine.from_config(cfg, 5, semantics=HB_SEM_DELAY_RING, tune="off")
+    b = off.run_sweep(SweepParam(-1, 0), meta["values"], 300)
+    assert off.tuned_flags is None and off.last_kernel_time()[2] == 3
+    eng.reset()
+    eng.run_sweep(SweepParam(-1, 0), meta["values"], 300, run_flags=HB_RUN_STREAM)
+    assert eng.tuned_flags is None and eng.last_kernel_time()[2] == 4
+    import numpy as np
+    assert np.allclose(a.final_states[0], b.final_states[0], rtol=1e-5, atol=1e-6)
+    # an untuned shape with tune="auto": measured on its first run, then cached
+    cfg6, meta6 = inputs.batched_sweep(n_steps=300, n_points=6, nsig=0.0, integrator="heun")
+    assert autotune.best_run_flags(cfg6, 6, HB_SEM_DELAY_RING) is None
+    auto = BatchHybridEngine.from_config(cfg6, 6, semantics=HB_SEM_DELAY_RING, tune="auto")
+    auto.run_sweep(SweepParam(-1, 0), meta6["values"], 300)
+    assert auto.tuned_flags is not None and autotune.best_run_flags(cfg6, 6, HB_SEM_DELAY_RING) == auto.tuned_flags

@@ -1,5 +1,6 @@
-"""Grouped launch (hb_group_*): several engines' sweeps with different node counts, delays, sweep
-values and step counts in one launch of the streamed-history kernel, replayed from a CUDA graph.
+"""Grouped launch (hb_group_*): several engines' sweeps with different models, node counts, delays,
+sweep values and step counts in one launch of the streamed-history work-queue kernel, replayed from a
+CUDA graph.
 Each member's results must equal the oracle's run of that member alone (same tolerances as the
 other parity tests), on the first and on a repeated execution."""
 import numpy as np
@@ -59,13 +60,41 @@ def test_group_stochastic_members():
     _check(members, HB_SEM_DELAY_RING, g.results())
 
 
-def test_group_rejects_mixed_models_and_short_delays():
-    a = single_model("MontbrioPazoRoxin", 20, "rk4", "Linear", (0.3,), weights="csr", delays="per_edge_long", dt=0.05)
-    b = single_model("Generic2dOscillator", 20, "heun", "Linear", (0.3,), weights="csr", delays="per_edge_long")
-    ea = BatchHybridEngine.from_config(a, 2, semantics=HB_SEM_DELAY_RING)
-    eb = BatchHybridEngine.from_config(b, 2, semantics=HB_SEM_DELAY_RING)
-    with pytest.raises(Unsupported, match="share the model"):
-        GroupedSweep([(ea, SweepParam(0, 4), [0.0, 0.1], 50, None), (eb, SweepParam(0, 1), [0.0, 0.1], 50, None)])
+@pytest.mark.parametrize("npt", [0, 4])
+def test_group_mixed_models_one_launch(npt):
+    """Generic2dOscillator, MontbrioPazoRoxin, JansenRit and Kuramoto (the [sin, cos] coupling form)
+    networks with different sizes, step counts, integrators and parameter tables in one launch of the
+    work-queue kernel; each member equals the oracle's run of it alone, on two executions."""
+    sem = HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT
+    mons = [MonitorConfig("Bold", tr=0.004, bold_period=10)]
+    members = []
+    g2 = single_model("Generic2dOscillator", 30, "heun_stochastic", "Linear", (0.2,), weights="csr", delays="per_edge_long",
+                      nsig=1e-3, seed=1, monitors=mons)
+    members.append((g2, 3, SweepParam(-1, 0), [0.0, 0.1, 0.2], 240, noise_for(g2, 240, 3, False, 7)))
+    mpr = single_model("MontbrioPazoRoxin", 52, "rk4", "Linear", (0.3,), weights="csr", delays="per_edge_long", dt=0.05,
+                       seed=2, monitors=mons)
+    p = np.asarray(mpr.network.subnetworks[0].params, np.float32)
+    rows = np.tile(p, (2, 52, 1))
+    rows[1, :, 2] = -4.0
+    mpr.network.subnetworks[0].node_params = rows
+    members.append((mpr, 2, SweepParam(-1, 0), [0.2, 0.6], 300, None))
+    jr = single_model("JansenRit", 24, "heun", "Sigmoidal", (0.0, 0.1, 0.0, 1.0, 0.05), weights="csr",
+                      delays="per_edge_long", seed=3)
+    members.append((jr, 2, SweepParam(-1, 3), [0.5, 1.5], 160, None))
+    ku = single_model("Kuramoto", 40, "heun", "Kuramoto", (1.5,), weights="csr", delays="per_edge_long", seed=4)
+    ku.network.subnetworks[0].node_params = np.random.default_rng(4).standard_normal((40, 1)).astype(np.float32)
+    members.append((ku, 3, SweepParam(-1, 0), [0.5, 1.0, 2.0], 200, None))
+    engines = [BatchHybridEngine.from_config(c, n, semantics=sem) for c, n, *_ in members]
+    g = GroupedSweep([(e, m[2], m[3], m[4], m[5]) for e, m in zip(engines, members)],
+                     run_flags=HB_RUN_STREAM_NPT(npt) if npt else 0)
+    for _ in range(2):
+        g.execute()
+        _check(members, sem, g.results())
+    assert engines[0].last_kernel_time()[2] == 5
+    g.close()
+
+
+def test_group_rejects_short_delays():
     c = single_model("Generic2dOscillator", 20, "heun", "Linear", (0.3,), weights="csr", delays="per_edge")
     ec = BatchHybridEngine.from_config(c, 2, semantics=HB_SEM_DELAY_RING)
     with pytest.raises(Unsupported, match="streamed-history"):

@@ -108,3 +108,48 @@ def test_history_layout_cannot_change_mid_simulation():
     eng.reset()
     eng.run_sweep(SweepParam(0, 1), [0.0, 0.1], 50)
     assert np.isfinite(eng.states[0]).all()
+
+
+@pytest.mark.parametrize("C", [2, 4, 8])
+@pytest.mark.parametrize("npt", [1, 2])
+def test_stream_cluster_split_kuramoto(C, npt):
+    """One point's 1000 nodes split over a cluster of C CTAs (HB_RUN_STREAM_CLUSTER): the CTAs read
+    each other's history through global memory after each block's cluster-scope signal; per-node
+    omega, per-point BOLD, with and without one node per consumer thread."""
+    from hyburn_gb300 import inputs
+    from hyburn_gb300._abi import HB_RUN_STREAM_CLUSTER
+    cfg, meta = inputs.kuramoto_scale(n=1000, n_points=3, n_steps=200, bold=True)
+    cfg.monitors[0].tr = 0.005
+    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 1.0, 2.0], 200, rtol=2e-5,
+                           semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT,
+                           run_flags=HB_RUN_STREAM_CLUSTER(C) | HB_RUN_STREAM_NPT(npt))
+    assert kind(eng) == STREAM_KIND
+
+
+@pytest.mark.parametrize("C", [2, 8])
+def test_stream_cluster_split_stochastic_chunked(C):
+    """Uneven slices (74 nodes over C CTAs), shared noise staged per slice, trajectories, runs split
+    across calls: the same results as the oracle."""
+    from hyburn_gb300 import inputs
+    from hyburn_gb300._abi import HB_RUN_STREAM_CLUSTER
+    cfg, meta = inputs.batched_sweep(n_steps=500, n_points=6)
+    eng = BatchHybridEngine.from_config(cfg, 6, semantics=HB_SEM_DELAY_RING)
+    ora = OracleEngine.from_config(cfg, 6, semantics=HB_SEM_DELAY_RING)
+    for n in (300, 77):
+        nz = inputs.standard_normal((n, 148), n)
+        flags = HB_RUN_STREAM | HB_RUN_STREAM_CLUSTER(C)
+        g = eng.run_sweep_with_trajectory(SweepParam(-1, 0), meta["values"], n, noise=nz, run_flags=flags)
+        o = ora.run_sweep_with_trajectory(SweepParam(-1, 0), meta["values"], n, noise=nz)
+        close(g.final_states[0], o.final_states[0], what=f"final after {n}")
+        close(g.tavg[0], o.tavg[0], what=f"tavg after {n}")
+        close(g.trajectories[0], o.trajectories[0], what=f"trajectory after {n}")
+        assert kind(eng) == STREAM_KIND
+
+
+def test_stream_cluster_split_mpr_500_nodes():
+    from hyburn_gb300 import inputs
+    from hyburn_gb300._abi import HB_RUN_STREAM_CLUSTER
+    cfg, meta = inputs.mpr_grid(500, 3, 150, seed=3)
+    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 0.5, 1.0], 150, semantics=HB_SEM_DELAY_RING,
+                           run_flags=HB_RUN_STREAM_CLUSTER(4))
+    assert kind(eng) == STREAM_KIND
