@@ -75,6 +75,9 @@ struct DevProj {
     float cp[HB_NCP];
     const float* cp_pp;   // [B][HB_NCP] when the coupling parameters are swept, else nullptr
     const int* rowptr;    // [ntgt + 1]
+    const int* porder;    // producer order of the target nodes (pipeline and streamed-history kernels): per node slice,
+                          // the slice's local node ids by decreasing in-degree, so that a warp's lanes get similar
+                          // edge counts; nullptr for the identity
     const uint32_t* edges; // (delay << 16) | src node
     const int* eoff;       // ring offset of each edge: src column - delay * cols (per-edge mode) or src column
     const float* ew;

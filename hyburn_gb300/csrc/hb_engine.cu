@@ -295,6 +295,7 @@ struct hb_engine {
     int hist_R = 0;           // ring length (slots) of the time-major history the last run left
     std::vector<DBuf<float>> d_params;
     std::vector<DBuf<float>> d_node_params;
+    DBuf<int> porder;           // producer node order of the last run's pipeline / streamed-history kernel
     DBuf<int> flags_buf;
     std::vector<BoldHost> bold;
     cudaStream_t own_stream = nullptr, user_stream = nullptr;
@@ -723,7 +724,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
             const size_t nz_b = any_stoch ? (size_t)2 * HB_STREAM_K * nm0 * nvar0 * 4 : 0;
             const size_t rp_b = ((size_t)(nm0 + 1) * 4 + 15) & ~(size_t)15;
             const size_t ed_b = slice_edges * 8;
-            const size_t pr_b = stream_prm_bytes(e->kernel_model, nm0, npt);
+            const size_t pr_b = stream_prm_bytes(e->kernel_model, nm0, npt) + (size_t)nm0 * 4 + 16;  // + producer order
             if (gx_b + rp_b + pr_b + 16 <= cap) {
                 stream_npt = npt;
                 stream_noise_smem = (nz_b > 0 && gx_b + nz_b + rp_b + pr_b + 16 <= cap) ? 1 : 0;
@@ -755,6 +756,26 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         for (size_t p = 0; p < e->projs.size(); p++) {
             if (e->projs[p].kind == W_SPARSE && edges_in_smem) { e->net.proj[p].smem_edges = (int)off; off += e->projs[p].edges.size(); }
             else e->net.proj[p].smem_edges = -1;
+            e->net.proj[p].porder = nullptr;
+        }
+        // producer order of the pipeline and streamed-history kernels: each node slice's nodes by
+        // decreasing in-degree (a warp's lanes then walk similar numbers of edges; every node's own sum
+        // is unchanged)
+        if (pipe >= 0 || stream_npt) {
+            const HostProj& hp = e->projs[0];
+            const int nmo = e->subs[0].nm, SC = stream_npt ? stream_cluster : 1;
+            std::vector<int> order(nmo);
+            for (int r = 0; r < SC; r++) {
+                const int a0 = (int)(((long long)nmo * r) / SC), a1 = (int)(((long long)nmo * (r + 1)) / SC);
+                for (int i = a0; i < a1; i++) order[i] = i - a0;
+                std::stable_sort(order.begin() + a0, order.begin() + a1, [&](int x, int y) {
+                    return hp.rowptr[a0 + x + 1] - hp.rowptr[a0 + x] > hp.rowptr[a0 + y + 1] - hp.rowptr[a0 + y];
+                });
+            }
+            CUDA_TRY(e->porder.ensure(nmo));
+            CUDA_TRY(cudaMemcpyAsync(e->porder.p, order.data(), nmo * sizeof(int), cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaStreamSynchronize(st));  // `order` is released at scope end
+            e->net.proj[0].porder = e->porder.p;
         }
         CUDA_TRY(cudaMemcpyAsync(e->d_net, &e->net, sizeof(DevNet), cudaMemcpyHostToDevice, st));
     }
@@ -1427,7 +1448,7 @@ void hb_engine_destroy(hb_engine* e) {
     e->traj.release(); e->dtraj.release();
     e->fe_fc.release(); e->fe_feat.release(); e->fe_fcd.release(); e->fe_fcds.release(); e->fe_ut.release();
     e->fe_part.release(); e->fe_mv.release();
-    e->means.release(); e->flags_buf.release();
+    e->means.release(); e->flags_buf.release(); e->porder.release();
     if (e->d_net) cudaFree(e->d_net);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);

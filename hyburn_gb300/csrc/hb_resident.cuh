@@ -974,11 +974,9 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
         const int nb = (n_steps - blk * PK) < PK ? (n_steps - blk * PK) : PK;
         const float* gb = gxbuf + (size_t)buf * PK * nm * NCV + (size_t)n * NCV;
         const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR + (size_t)n * NVAR;
-#pragma unroll 1
-        for (int j = 0; j < nb; j++) {
-            slot = (slot + 1 == R) ? 0 : slot + 1;
-            if (!active) continue;  // threads past the last node only take part in the barriers
-            float cc[2] = {0.0f, 0.0f};
+        // the coupling term and the scaled noise of a step depend only on the block's shared-memory
+        // buffers: each is computed one step ahead, off the state's dependency chain (same arithmetic)
+        auto ahead = [&](int j, float* ccv, float* nzv) {
 #pragma unroll
             for (int c = 0; c < NCV; c++) {
                 const float g = gb[(size_t)j * nm * NCV + c];
@@ -986,14 +984,27 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
                     const float sh = (g + (-c2)) / c4;
                     const float ex = -(sh * c3);
                     const float den = expf(ex) + 1.0f;
-                    cc[c] = (1.0f / den) * (cb - ca) + ca;
+                    ccv[c] = (1.0f / den) * (cb - ca) + ca;
                 } else {
-                    cc[c] = g * ca + cb;
+                    ccv[c] = g * ca + cb;
                 }
             }
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) nzv[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
+        };
+        float cc_next[2] = {0.0f, 0.0f}, nz_next[NVAR];
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) nz_next[v] = 0.0f;
+        if (active && nb > 0) ahead(0, cc_next, nz_next);
+#pragma unroll 1
+        for (int j = 0; j < nb; j++) {
+            slot = (slot + 1 == R) ? 0 : slot + 1;
+            if (!active) continue;  // threads past the last node only take part in the barriers
+            float cc[2] = {cc_next[0], cc_next[1]};
             float nz[NVAR];
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) nz[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
+            for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v];
+            if (j + 1 < nb) ahead(j + 1, cc_next, nz_next);
             float k1[NVAR], k2[NVAR], tmp[NVAR];
             dfun(MODEL, prm, SWEEP_FORM ? 1 : 0, x, cc, k1);
             if (STOCH) {
@@ -1141,7 +1152,8 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
         const int row_len = nm * NVAR;
         // node-major assignment for the steady state: node p / PL, lane p % PL (PL a power of two)
         const int PL = a.pipe_lanes;
-        const int pnode = p / PL, plane = p - (p / PL) * PL;
+        const int pslot = p / PL, plane = p - (p / PL) * PL;
+        const int pnode = (P.porder && pslot < nm) ? P.porder[pslot] : pslot;
         const bool pactive = pnode < nm;
         const int pe0 = pactive ? s_rowptr[pnode] : 0, pe1 = pactive ? s_rowptr[pnode + 1] : 0;
         const int early_until = (dmode == HBD_EDGE) ? maxd : P.delay;

@@ -247,25 +247,41 @@ __device__ __forceinline__ void mbar_arrive_remote(const uint64_t* bar, uint32_t
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_addr(bar)), "r"(rank));
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(ra) : "memory");
 }
-// wait (acquire at cluster scope) for the phase of parity `parity`, with an iteration limit; false
-// when the limit ran out
-__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); it++) {
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// wait (acquire at cluster scope) for the phase of parity `parity`, for at most 200 ms; false when the
+// time ran out. After a timeout in the block (*gave_up set) later waits return at once, so a fault in
+// the cluster's signalling costs one bounded wait, not one per block.
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* gave_up) {
+    if (*gave_up) return false;
+    const uint64_t t0 = global_ns();
+    for (;;) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
         if (done) return true;
+        if (global_ns() - t0 > 200000000ull || *gave_up) {
+            *gave_up = 1;
+            return false;
+        }
     }
-    return false;
 }
+// The CTAs of a cluster-split point signal each finished block on four barriers (block mod 4) in every
+// CTA. A barrier's phase then only ever collects one arrival per CTA for the same block: a CTA can
+// arrive for block j + 4 only after its producers saw every CTA's arrival for block j + 2, which each CTA
+// made after its arrivals for block j.
+#define HB_HIST_BARS 4
 // consumers of a cluster-split point after finishing block `blk`: their history writes made visible at
-// cluster scope, then one arrival per CTA on every CTA's barrier of the block's parity
+// cluster scope, then one arrival per CTA on every CTA's barrier of the block
 __device__ __forceinline__ void stream_signal_block(uint64_t* hbar, int blk, int C, int n_cons) {
     fence_cluster();
     named_sync(HB_BAR_CONS, n_cons);
     if (threadIdx.x == 0)
-        for (int r = 0; r < C; r++) mbar_arrive_remote(hbar + (blk & 1), (uint32_t)r);
+        for (int r = 0; r < C; r++) mbar_arrive_remote(hbar + (blk & (HB_HIST_BARS - 1)), (uint32_t)r);
 }
 
 // Consumer steps for Heun (deterministic or stochastic) with Linear coupling delivered directly, no
@@ -290,21 +306,32 @@ __device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, 
         const int nb = (n_steps - it0) < K ? (n_steps - it0) : K;
         const float* gb = gxbuf + (size_t)buf * K * ns * NCV + (size_t)l * NCV;
         const float* nbuf = nzbuf + (size_t)buf * K * ns * NVAR + (size_t)l * NVAR;
+        // the coupling term and the scaled noise of a step are computed one step ahead, off the state's
+        // dependency chain (same arithmetic)
+        auto ahead = [&](int j, float* ccv, float* nzv) {
+            ccv[0] = gb[(size_t)j * ns * NCV] * ca + cb;
+            if (NCV > 1) ccv[1] = gb[(size_t)j * ns * NCV + 1] * ca + cb;
+#pragma unroll
+            for (int v = 0; v < NVAR; v++) {
+                if (!STOCH) nzv[v] = 0.0f;
+                else if (NOISE_SMEM) nzv[v] = nbuf[(size_t)j * ns * NVAR + v] * nsc[v];
+                else nzv[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * nsc[v];
+            }
+        };
+        float cc_next[2] = {0.0f, 0.0f}, nz_next[NVAR];
+#pragma unroll
+        for (int v = 0; v < NVAR; v++) nz_next[v] = 0.0f;
+        if (active && nb > 0) ahead(0, cc_next, nz_next);
 #pragma unroll 1
         for (int j = 0; j < nb; j++) {
             const int pos = wpos;
             wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
             if (!active) continue;  // threads past the last node only take part in the barriers
-            float cc[2] = {0.0f, 0.0f};
-            cc[0] = gb[(size_t)j * ns * NCV] * ca + cb;
-            if (NCV > 1) cc[1] = gb[(size_t)j * ns * NCV + 1] * ca + cb;
+            float cc[2] = {cc_next[0], cc_next[1]};
             float nz[NVAR];
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) {
-                if (!STOCH) nz[v] = 0.0f;
-                else if (NOISE_SMEM) nz[v] = nbuf[(size_t)j * ns * NVAR + v] * nsc[v];
-                else nz[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * nsc[v];
-            }
+            for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v];
+            if (j + 1 < nb) ahead(j + 1, cc_next, nz_next);
             float k1[NVAR], k2[NVAR], tmp[NVAR];
             dfun(MODEL, prm, SF ? 1 : 0, x, cc, k1);
 #pragma unroll
@@ -338,7 +365,8 @@ __device__ __forceinline__ void stream_load_net(DevNet& net, const DevNet* __res
 template <int MODEL, int PRE, int NPT, int MAXT>
 __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, const int b, const int rank) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ __align__(8) uint64_t hist_bar[2];  // cluster-split: all CTAs finished an even / odd block
+    __shared__ __align__(8) uint64_t hist_bar[HB_HIST_BARS];  // cluster-split: all CTAs finished block j (j mod 4)
+    __shared__ int hist_gave_up;                              // cluster-split: a wait on hist_bar timed out
     constexpr int NVAR = c_nvar(MODEL), NCV = c_ncvar(MODEL);
     constexpr int PCH = (PRE == PRE_KURA) ? 2 : NCV;
     constexpr int K = HB_STREAM_K;
@@ -373,6 +401,9 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
     // subnetwork has per-node parameters, else the point's row)
     constexpr int PU = c_nparams_used(MODEL);
     float* s_prm = reinterpret_cast<float*>(smem + off);
+    if (NPT > 1) off += (size_t)ns * PU * 4;
+    off = (off + 15) & ~(size_t)15;
+    int* s_porder = reinterpret_cast<int*>(smem + off);  // [ns] producer order of the slice's nodes
 
     // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176);
     // each CTA clears its own nodes' rows
@@ -382,8 +413,8 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
         for (size_t i = t; i < n4; i += nthreads) r4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (C > 1 && t == 0) {
-        mbar_init(&hist_bar[0], (uint32_t)C);
-        mbar_init(&hist_bar[1], (uint32_t)C);
+        for (int q = 0; q < HB_HIST_BARS; q++) mbar_init(&hist_bar[q], (uint32_t)C);
+        hist_gave_up = 0;
         mbar_init_fence();
     }
     __syncthreads();
@@ -432,6 +463,7 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
     }
     if (NPT > 1)
         for (int i = t; i < ns * PU; i += nthreads) s_prm[i] = hb_param_row(net.sub[0], b, n0 + i / PU)[i % PU];
+    for (int i = t; i < ns; i += nthreads) s_porder[i] = P.porder ? P.porder[n0 + i] : i;
     // the history every CTA of the point reads (cleared rows, the published start state) and the
     // barriers of the cluster are ready
     if (C > 1) cluster_barrier();
@@ -450,7 +482,8 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             if (blk >= 2) named_sync(HB_BAR_EMPTY0 + buf, nthreads);
             // block blk reads the history up to the first step of block blk - 1, which every CTA of the
             // point has published once it finished block blk - 2
-            if (C > 1 && blk >= 2 && !mbar_wait_cluster(&hist_bar[(blk - 2) & 1], (uint32_t)(((blk - 2) >> 1) & 1)))
+            if (C > 1 && blk >= 2 &&
+                !mbar_wait_cluster(&hist_bar[(blk - 2) & (HB_HIST_BARS - 1)], (uint32_t)(((blk - 2) >> 2) & 1), &hist_gave_up))
                 atomicOr(a.flags + 1, 4);
             const int it0 = blk * K;
             const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
@@ -459,7 +492,8 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             float* gb = gxbuf + (size_t)buf * K * ns * PCH;
             for (int r = 0; r < rounds; r++) {
                 const int item = p + r * n_prod;
-                const int node = item / PL, lane = item - (item / PL) * PL;
+                const int islot = item / PL, lane = item - (item / PL) * PL;
+                const int node = islot < ns ? s_porder[islot] : islot;
                 float acc[K][PCH];
 #pragma unroll
                 for (int j = 0; j < K; j++)
