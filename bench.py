@@ -48,6 +48,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def peaks_tf32():
+    """Dense TF32 tensor rate: half the measured bf16 burst rate."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]) / 2.0
+    except Exception:
+        return 1900.0 / 2.0
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons while the timed region runs: one `nvidia-smi -lms 20`
     process started (and seen answering) before the region, stopped after it; only the samples that
@@ -446,6 +455,42 @@ def run_other_workload(args):
                                 "gradients": "coupling scale, omega per node", "trajectory": "kept in HBM"},
                         adjoint={"forward_ms": parts[0], "prepare_ms": parts[1], "reverse_ms": parts[2],
                                  "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
+        elif args.workload == "dense":
+            # undelayed all-to-all dense coupling (the reference's batched matrix product, engine.rs:609-620):
+            # G2DO, 74 nodes, weights U[0, 1) / 74 off the diagonal, Linear coupling swept over the points,
+            # Heun, 2 000 steps; the tensor-core path (HB_RUN_DENSE_TC) beside the engine's CUDA-core kernel
+            from hyburn_gb300._abi import HB_RUN_DENSE_TC
+            from hyburn_gb300.config import NetworkConfig, ProjectionConfig, SimConfig, SubnetworkConfig
+            T, n, B = args.run_steps or 2_000, 74, args.dense_points
+            rng = np.random.default_rng(7)
+            w = (rng.uniform(0.0, 1.0, (n, n)) / n).astype(np.float32)
+            np.fill_diagonal(w, 0.0)
+            cfg = SimConfig(sim_length=T * 0.1, dt=0.1, integrator="heun", nsig=0.0, network=NetworkConfig(
+                [SubnetworkConfig("Generic2dOscillator", n, inputs.uniform_state(n, 2, 7), list(inputs.G2DO_BENCH_PARAMS))],
+                [ProjectionConfig(0, 0, w.tolist(), coupling_fn="Linear", coupling_params=[0.1])]))
+            vals = np.linspace(0.0, 0.2, B).astype(np.float32)
+            res = {}
+            for name, flags in (("tensor_core", HB_RUN_DENSE_TC), ("cuda_core", 0)):
+                eng = BatchHybridEngine.from_config(cfg, B, tune="off")
+                eng.prepare(SweepParam(-1, 0), vals, T, run_flags=flags)
+                res[name] = _time_prepared(eng, args.steps, args.warmup)
+                eng.close()
+            ms, kind = res["tensor_core"]
+            ns = B * n * T
+            np_, kp = (n + 15) // 16 * 16, (n + 7) // 8 * 8
+            issued = 3 * 2 * ((B + 127) // 128 * 128) * np_ * kp * T  # flops the tensor cores execute (3 x TF32, padded)
+            useful = 2 * B * n * n * T
+            line.update(metric="node-steps/s", value=ns / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+                        config={"workload": f"g2do-{n}n-{B}pt-dense-undelayed-heun-{T}steps", "kernel_kind": kind},
+                        dense={"tensor_core_ms": ms, "cuda_core_ms": res["cuda_core"][0],
+                               "cuda_core_kernel_kind": res["cuda_core"][1],
+                               "cuda_core_node_steps_per_s": ns / (res["cuda_core"][0] / 1e3),
+                               "speedup_over_cuda_core": res["cuda_core"][0] / ms},
+                        roofline={"bound": "tensor", "achieved": issued / (ms / 1e3) / 1e12,
+                                  "peak": peaks_tf32(), "unit": "TFLOP/s",
+                                  "frac": issued / (ms / 1e3) / 1e12 / peaks_tf32(),
+                                  "peak_kind": "half the measured dense bf16 burst (TF32 runs at half the bf16 rate)",
+                                  "useful_tflops": useful / (ms / 1e3) / 1e12, "traffic": None})
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -535,7 +580,9 @@ def main():
     ap.add_argument("--pipe-lanes", type=int, default=0, help="pipeline producer threads per node (0: engine's choice)")
     ap.add_argument("--stream-cluster", type=int, default=0,
                     help="streamed-history kernel: CTAs per sweep point, 1/2/4/8 (0: engine's choice)")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint", "fc"],
+    ap.add_argument("--dense-points", type=int, default=1024, help="dense workload: sweep points")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint",
+                                                          "fc", "dense"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()

@@ -37,6 +37,7 @@ HB_SEM_HYBRID_INTEGRATOR = 1 << 4
 
 HB_RUN_TRAJECTORY = 1 << 0
 HB_RUN_CHECK_FINITE = 1 << 1
+HB_RUN_DENSE_TC = 1 << 2
 HB_RUN_FORCE_RESIDENT = 1 << 8
 HB_RUN_FORCE_BLOCKED = 1 << 9
 HB_RUN_GLOBAL_RING = 1 << 10
@@ -67,7 +68,7 @@ def HB_RUN_STREAM_CLUSTER(n: int) -> int:
 
 
 # the run flags that choose a kernel form or its lane counts (what the autotuner chooses)
-HB_RUN_KERNEL_CHOICE = (HB_RUN_FORCE_RESIDENT | HB_RUN_FORCE_BLOCKED | HB_RUN_GLOBAL_RING | HB_RUN_GENERIC | (0x7 << 4)
+HB_RUN_KERNEL_CHOICE = (HB_RUN_DENSE_TC | HB_RUN_FORCE_RESIDENT | HB_RUN_FORCE_BLOCKED | HB_RUN_GLOBAL_RING | HB_RUN_GENERIC | (0x7 << 4)
                         | (0xF << 12)
                         | HB_RUN_TWO_PHASE | HB_RUN_NO_PIPE | HB_RUN_STREAM | HB_RUN_NO_STREAM | (0xF << 20)
                         | (0x7 << 24) | HB_RUN_STREAM_PREFETCH | HB_RUN_PIPE_WIDE)

@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
     ("hb_queue_1.cu", ["--fmad=false", "-lineinfo"]),
+    ("hb_dense_tc.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_queue_2.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_queue_4.cu", ["--fmad=false", "-lineinfo"]),
     ("hb_stream_1.cu", ["--fmad=false", "-lineinfo"]),

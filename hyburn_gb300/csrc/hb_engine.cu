@@ -36,6 +36,11 @@ int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
 cudaError_t hb_launch_single(int model, int m, const DevNet* d_net, const RunArgs& a, int B, cudaStream_t st);
+// hb_dense_tc.cu
+int hb_dense_tc_tmem_columns(int model, int nm);
+void hb_dense_tc_tiles(const float* w, int nm, int NP, int KP, float* out);
+cudaError_t hb_launch_dense_tc(int model, const DevNet* d_net, const RunArgs& a, int B, const float* wtiles, int NP, int KP,
+                               int NPN, cudaStream_t st);
 cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
 int hb_stream_queue_grid_1(int threads, size_t smem);
 cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
@@ -295,6 +300,7 @@ struct hb_engine {
     int hist_R = 0;           // ring length (slots) of the time-major history the last run left
     std::vector<DBuf<float>> d_params;
     std::vector<DBuf<float>> d_node_params;
+    DBuf<float> dtc;            // the tensor-core path's W in its shared-memory layout (hi and lo TF32 parts)
     DBuf<int> porder;           // producer node order of the last run's pipeline / streamed-history kernel
     DBuf<int> flags_buf;
     std::vector<BoldHost> bold;
@@ -560,6 +566,7 @@ struct RunPlan {
     bool noise_on_device = false, any_stoch = false, record = false, bold_pp = false, dev_traj = false;
     int64_t noise_rows_per_step = 0, chunk = 0;
     int B = 0, N0 = 0, n_bold_active = 0, stream_npt = 0, fast = -1, pipe = -1, pipe_maxt = 512, single_m = 0;
+    int dense_tc = 0, tc_np = 0, tc_kp = 0, tc_npn = 0;  // tensor-core path for undelayed dense coupling
     size_t smem = 0, stream_smem = 0;
     RunArgs a;
     std::vector<std::vector<double>> new_times;
@@ -609,6 +616,44 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         e->threads = off;
     }
     // ---- kernel choice: the specialised single-projection form when the network allows it ----
+    // ---- tensor-core path for undelayed dense coupling (HB_RUN_DENSE_TC), engine.rs:609-620 ----
+    int dense_tc = 0, tc_np = 0, tc_kp = 0, tc_npn = 0;
+    if (run_flags & HB_RUN_DENSE_TC) {
+        const char* why = nullptr;
+        const int km = e->kernel_model;
+        if (e->subs.size() != 1 || e->projs.size() != 1) why = "one subnetwork and one projection";
+        else {
+            const HostProj& hp = e->projs[0];
+            const int nm = e->subs[0].nm;
+            const int k = hp.cf.kind;
+            if (hp.kind != W_SPARSE || hp.src != 0 || hp.tgt != 0) why = "a Dense or CSR projection of the subnetwork onto itself";
+            else if (hp.delay != 0 || hp.maxd != 0) why = "no delay";
+            else if (!(k == HBC_LINEAR || k == HBC_SIGMOIDAL || k == HBC_SCALED_LINEAR) || hp.diff_mode == 2 || !hp.direct ||
+                     hp.ncv != 1 || hp.pc != 1)
+                why = "Linear, Sigmoidal or ScaledLinear coupling from and into the first coupling variable";
+            else if (!(km == HBM_G2DO || km == HBM_RWW || km == HBM_JR || km == HBM_WC))
+                why = "a model with one coupling variable (Generic2dOscillator, ReducedWongWang, JansenRit, WilsonCowan)";
+            else if (nm > 112 || hb_dense_tc_tmem_columns(km, nm) > 512)
+                why = "at most 112 nodes, with the state and its running sum within tensor memory";
+            else if (!e->subs[0].node_params.empty()) why = "one parameter row per point (no node_params)";
+            else if ((!e->bold_removed && !e->bold.empty()) || (run_flags & (HB_RUN_TRAJECTORY | HB_RUN_DEVICE_TRAJECTORY)) ||
+                     e->cs_out)
+                why = "no monitors and no trajectory";
+            if (!why) {
+                tc_np = (nm + 15) / 16 * 16;
+                tc_kp = (nm + 7) / 8 * 8;
+                tc_npn = tc_np;
+                std::vector<float> w((size_t)nm * nm, 0.0f), tiles((size_t)2 * tc_np * tc_kp);
+                for (int i = 0; i < nm; i++)
+                    for (int q = hp.rowptr[i]; q < hp.rowptr[i + 1]; q++) w[(size_t)i * nm + (hp.edges[q] & 0xffffu)] = hp.ew[q];
+                hb_dense_tc_tiles(w.data(), nm, tc_np, tc_kp, tiles.data());
+                CUDA_TRY(e->dtc.ensure(tiles.size()));
+                CUDA_TRY(cudaMemcpy(e->dtc.p, tiles.data(), tiles.size() * 4, cudaMemcpyHostToDevice));
+                dense_tc = 1;
+            }
+        }
+        if (why) return fail(HB_ERR_UNSUPPORTED, "HB_RUN_DENSE_TC needs %s", why);
+    }
     int fast = -1;
     if (e->subs.size() == 1 && e->projs.size() == 1 && e->projs[0].kind == W_SPARSE && !(run_flags & HB_RUN_GENERIC)) {
         const int k = e->projs[0].cf.kind;
@@ -743,7 +788,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         }
     }
     {
-        const int layout = stream_npt ? 1 : 0;
+        const int layout = dense_tc ? 3 : stream_npt ? 1 : 0;
         if (e->step > 0 && (layout != e->hist_layout || (layout == 1 && stream_rp != e->hist_rp) ||
                             (layout == 0 && R_run != e->hist_R)))
             return fail(HB_ERR_UNSUPPORTED, "this run would change the history layout of a started simulation; reset the engine first");
@@ -892,6 +937,11 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     P.pipe = pipe;
     P.pipe_maxt = pipe_maxt;
     P.single_m = single_m;
+    P.dense_tc = dense_tc;
+    P.tc_np = tc_np;
+    P.tc_kp = tc_kp;
+    P.tc_npn = tc_npn;
+    if (dense_tc) e->last_kind = 8;
     P.smem = smem;
     P.stream_smem = stream_smem;
     P.a = a;
@@ -931,7 +981,8 @@ hb_status run_launch(hb_engine* e, RunPlan& P, hb_result* res) {
         a.traj = (record || dev_traj) ? traj_dst : nullptr;
         a.gx_out = e->cs_out ? e->cs_out + (size_t)c0 * B * e->subs[0].nm * 2 : nullptr;
         CUDA_TRY(cudaEventRecord(e->ev0, st));
-        if (P.single_m) CUDA_TRY(hb_launch_single(e->kernel_model, P.single_m, e->d_net, a, B, st));
+        if (P.dense_tc) CUDA_TRY(hb_launch_dense_tc(e->kernel_model, e->d_net, a, B, e->dtc.p, P.tc_np, P.tc_kp, P.tc_npn, st));
+        else if (P.single_m) CUDA_TRY(hb_launch_single(e->kernel_model, P.single_m, e->d_net, a, B, st));
         else if (stream_npt == 1) CUDA_TRY(hb_launch_stream_1(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 2) CUDA_TRY(hb_launch_stream_2(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
         else if (stream_npt == 4) CUDA_TRY(hb_launch_stream_4(e->kernel_model, fast, e->d_net, a, B, e->threads, stream_smem, st));
@@ -1448,7 +1499,7 @@ void hb_engine_destroy(hb_engine* e) {
     e->traj.release(); e->dtraj.release();
     e->fe_fc.release(); e->fe_feat.release(); e->fe_fcd.release(); e->fe_fcds.release(); e->fe_ut.release();
     e->fe_part.release(); e->fe_mv.release();
-    e->means.release(); e->flags_buf.release(); e->porder.release();
+    e->means.release(); e->flags_buf.release(); e->porder.release(); e->dtc.release();
     if (e->d_net) cudaFree(e->d_net);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);

@@ -71,6 +71,11 @@ typedef int32_t hb_status;
 /* ---- run flags (hb_engine_run_* `run_flags`) ---- */
 #define HB_RUN_TRAJECTORY   (1u << 0) /* run_sweep_with_trajectory (engine.rs:487-494) */
 #define HB_RUN_CHECK_FINITE (1u << 1) /* fail with HB_ERR_NONFINITE if a state becomes NaN/Inf */
+/* undelayed dense coupling (the batched matrix product of engine.rs:609-620) on the tensor cores: 128 sweep
+   points per CTA, X * W^T by tcgen05.mma in three TF32 products (FP32 accumulation). For one subnetwork coupled
+   to itself through one projection without delay, Linear / Sigmoidal / ScaledLinear coupling, a model with one
+   coupling variable, up to 112 nodes, no monitors, trajectories or node_params; HB_ERR_UNSUPPORTED otherwise. */
+#define HB_RUN_DENSE_TC     (1u << 2)
 #define HB_RUN_FORCE_RESIDENT (1u << 8) /* kernel choice: point-resident persistent kernel */
 #define HB_RUN_FORCE_BLOCKED  (1u << 9) /* kernel choice: time-blocked tiled kernel */
 #define HB_RUN_GLOBAL_RING    (1u << 10) /* resident kernel: keep the history ring in global memory */

@@ -110,3 +110,51 @@ def test_adjoint_checkpoint_interval_changes_only_summation_rounding(integrator)
     assert np.array_equal(r1.loss, r2.loss)
     for f in ("d_gain", "d_A", "d_B", "d_a"):
         np.testing.assert_allclose(getattr(r1, f), getattr(r2, f), rtol=1e-5, atol=1e-9 * np.abs(getattr(r2, f)).max())
+
+
+def test_adjoint_at_fc_workload_scale_with_checkpoints_every_500_steps():
+    """The FC-adjoint workload's own network (JansenRit, 74 nodes, 20 % CSR, delays 37-666 steps,
+    Sigmoidal coupling) for 2 000 steps with checkpoints every 500 steps, against a target FC of a
+    seeded forward run. The FP64 restatement of the adjoint is pinned to central differences
+    (h = 1e-6) on the gain and on six nodes' A, B, a; the GPU gradients are then compared with it on
+    all 74 nodes: gain, A and B within 1e-4 (2-norm relative), a within 5e-4 (its conditioning, as
+    above)."""
+    from hyburn_gb300 import inputs
+    n, T, K, h = 74, 2000, 500, 1e-6
+    gains = [0.8, 1.2]
+    cfg, meta = inputs.jr_fc_adjoint(T, len(gains), n)
+    sub, pr = cfg.network.subnetworks[0], cfg.network.projections[0]
+    w = pr.weights
+    net = (np.asarray(w["indptr"]), np.asarray(w["indices"]), np.asarray(w["data"], np.float64),
+           np.asarray(pr.delays, np.int64))
+    x0 = np.asarray(sub.initial_state, np.float64).reshape(n, 6)
+    rng = np.random.default_rng(40)
+    ranges = [(-0.5, 0.5), (0.0, 20.0), (0.0, 20.0), (-1.0, 1.0), (-1.0, 1.0), (-1.0, 1.0)]
+    x_t = np.stack([rng.uniform(lo, hi, n) for lo, hi in ranges], 1)
+    cp = lambda g: (0.0, 0.1, 0.0, g, 0.05)
+    target = np.corrcoef(ar.forward(ar.params_dict(sub.params, n), x_t, *net, "Sigmoidal", cp(1.0), cfg.dt, T).T)
+    eng = BatchHybridEngine.from_config(cfg, len(gains), semantics=HB_SEM_DELAY_RING)
+    r = eng.adjoint_fc(gains, T, target.astype(np.float32), checkpoint_every=K)
+    base = {k: float(sub.params[i]) for i, k in enumerate(("A", "B", "a"))}
+    nodes = [0, 13, 27, 41, 55, 73]
+
+    def L(gain, **kw):
+        return ar.fc_loss(ar.forward(ar.params_dict(sub.params, n, **kw), x0, *net, "Sigmoidal", cp(gain), cfg.dt, T),
+                          target)[0]
+
+    for b, gain in enumerate(gains):
+        l64, gG, gA, gB, ga = ar.adjoint(ar.params_dict(sub.params, n), x0, *net, cp(gain), cfg.dt, T, target)
+        fd_g = (L(gain + h) - L(gain - h)) / (2 * h)
+        assert abs(gG - fd_g) <= 1e-6 * abs(fd_g), (gG, fd_g)
+        for name, g64 in (("A", gA), ("B", gB), ("a", ga)):
+            for i in nodes:
+                vp, vm = np.full(n, base[name]), np.full(n, base[name])
+                vp[i] += h
+                vm[i] -= h
+                fd = (L(gain, **{name: vp}) - L(gain, **{name: vm})) / (2 * h)
+                assert abs(g64[i] - fd) <= 1e-5 * abs(fd) + 1e-9, (name, i, g64[i], fd)
+        assert abs(r.loss[b] - l64) <= 1e-4 * abs(l64)
+        errs = {"gain": abs(r.d_gain[b] - gG) / abs(gG), "A": rel(r.d_A[b], gA), "B": rel(r.d_B[b], gB),
+                "a": rel(r.d_a[b], ga)}
+        print(f"point {b}: relative errors against the FP64 adjoint {errs}")
+        assert errs["gain"] <= 1e-4 and errs["A"] <= 1e-4 and errs["B"] <= 1e-4 and errs["a"] <= 5e-4, errs
