@@ -58,7 +58,8 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
     """Run-flag sets worth measuring for this network (the engine's own choice is the first)."""
     out = [("engine", 0)]
     projs = config.network.projections
-    single_sparse = (len(config.network.subnetworks) == 1 and len(projs) == 1 and isinstance(projs[0].weights, dict))
+    single_sparse = (len(config.network.subnetworks) == 1 and len(projs) == 1 and
+                     not isinstance(projs[0].weights, (int, float)))
     per_edge = bool(single_sparse and (semantics & _abi.HB_SEM_DELAY_RING) and projs[0].delays and
                     len(projs[0].delays) > 1)
     dmin = min(projs[0].delays) if per_edge else 0
@@ -74,6 +75,15 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
                             _abi.HB_RUN_NO_STREAM | _abi.HB_RUN_PIPE_WIDE | _abi.HB_RUN_PIPE_LANES(pl)))
             for npt in (1, 2, 4):
                 out.append((f"streamed history {npt} node(s) per thread", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_NPT(npt)))
+            # CTAs per point: a point's nodes split over a cluster (fewer points in flight, histories in L2)
+            nodes = config.network.subnetworks[0].nnodes
+            for c in (2, 4, 8):
+                if nodes >= 16 * c:
+                    out.append((f"streamed history, {c} CTAs per point", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_CLUSTER(c)))
+        undelayed = not projs[0].delays or max(projs[0].delays) == 0
+        if undelayed and projs[0].coupling_fn in ("Linear", "Sigmoidal", "ScaledLinear"):
+            # 128 points per CTA: the coupling as a tensor-core matrix product
+            out.append(("tensor-core dense coupling, 128 points per CTA", _abi.HB_RUN_DENSE_TC))
     else:
         for lanes in (1, 2, 4, 8):
             out.append((f"generic lanes {lanes}", _abi.HB_RUN_GENERIC | _abi.HB_RUN_LANES(lanes)))
