@@ -38,6 +38,7 @@ HB_SEM_HYBRID_INTEGRATOR = 1 << 4
 HB_RUN_TRAJECTORY = 1 << 0
 HB_RUN_CHECK_FINITE = 1 << 1
 HB_RUN_DENSE_TC = 1 << 2
+HB_RUN_EXACT_SUMS = 1 << 3
 HB_RUN_FORCE_RESIDENT = 1 << 8
 HB_RUN_FORCE_BLOCKED = 1 << 9
 HB_RUN_GLOBAL_RING = 1 << 10

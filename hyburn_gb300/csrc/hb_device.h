@@ -152,6 +152,7 @@ struct RunArgs {
     int* flags;           // [0]: non-finite seen, [1]: bounds error
     int check_finite;
     int test_unset_wait;  // pipeline kernel: one bounded wait on a barrier nothing completes (timeout test)
+    int exact_sums;       // coupling sums term by term in edge order, product and sum rounded apart (HB_RUN_EXACT_SUMS)
     DevBold bold;
 };
 

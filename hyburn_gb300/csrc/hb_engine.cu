@@ -587,6 +587,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     // ---- thread layout: `lanes` threads per node share its edge list ----
     {
         int forced = (int)((run_flags >> 12) & 0xf);
+        if (run_flags & HB_RUN_EXACT_SUMS) forced = 1;  // one thread per node: its sum in edge order
         std::vector<int> lanes(e->subs.size(), 1);
         for (size_t i = 0; i < e->subs.size(); i++) {
             if (forced) { lanes[i] = 1 << (forced - 1); continue; }
@@ -687,7 +688,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         const int nm0 = e->subs[0].nm;
         const int n_cons = (nm0 + 31) / 32 * 32;
         auto prod_of = [&](int pl) { return std::max(64, (nm0 * pl + 31) / 32 * 32); };
-        const int forced_pl = (int)((run_flags >> 20) & 0xf);
+        const int forced_pl = (run_flags & HB_RUN_EXACT_SUMS) ? 1 : (int)((run_flags >> 20) & 0xf);
         if (forced_pl && ((forced_pl & (forced_pl - 1)) != 0 || forced_pl > 8))
             return fail(HB_ERR_INVALID_STATE, "pipeline producer lanes must be 1, 2, 4 or 8");
         const bool wide = (run_flags & HB_RUN_PIPE_WIDE) || n_cons + 256 > 512 ||
@@ -778,7 +779,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
                 stream_smem = used;
                 const int n_cons = ((nm0 + npt - 1) / npt + 31) / 32 * 32;
                 const int n_prod = threads - n_cons;
-                while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
+                while (!(run_flags & HB_RUN_EXACT_SUMS) && stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
                 e->threads = threads;
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
                 const size_t words = (size_t)B * nm_all * (stream_rp + 2 * HB_STREAM_K) * pch;
@@ -916,6 +917,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     a.flags = e->flags_buf.p;
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
     a.test_unset_wait = (run_flags & HB_RUN_TEST_UNSET_WAIT) ? 1 : 0;
+    a.exact_sums = (run_flags & HB_RUN_EXACT_SUMS) ? 1 : 0;
     a.bold = db;
 
     P.n_steps = n_steps;

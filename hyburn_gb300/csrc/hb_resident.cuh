@@ -16,6 +16,7 @@
 // Template parameters: MODEL (a fixed model id, or -1 for networks mixing models) and MAXT
 // (the launch bound, which sets the register budget).
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include "hb_models.cuh"
 
@@ -1178,34 +1179,33 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
 #pragma unroll
                     for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
                 const int base = slb * cols + doff;
-                for (int e = pe0 + plane; e < pe1; e += PL) {
-                    int a0 = base + eo[e];
-                    a0 = a0 < 0 ? a0 + ring_words : a0;
-                    const float w = ew[e];
-                    if (a0 + (PK - 1) * cols < ring_words) {
-#pragma unroll
-                        for (int j = 0; j < PK; j++) {
-                            const float v = ring[a0 + j * cols];
-                            if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
-                            else {
-                                acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
-                                if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[a0 + j * cols + 1], acc[j][PCH - 1]);
-                            }
-                        }
-                    } else {
+                // EXACT (HB_RUN_EXACT_SUMS, one lane per node): each term rounded as a product and then a sum,
+                // in edge order, as the reference; otherwise fused multiply-adds
+                auto edge_loop = [&](auto exact_tag) {
+                    constexpr bool EXACT = decltype(exact_tag)::value;
+                    for (int e = pe0 + plane; e < pe1; e += PL) {
+                        int a0 = base + eo[e];
+                        a0 = a0 < 0 ? a0 + ring_words : a0;
+                        const float w = ew[e];
+                        const bool whole = a0 + (PK - 1) * cols < ring_words;
 #pragma unroll
                         for (int j = 0; j < PK; j++) {
                             int aj = a0 + j * cols;
-                            aj = aj >= ring_words ? aj - ring_words : aj;
+                            if (!whole) aj = aj >= ring_words ? aj - ring_words : aj;
                             const float v = ring[aj];
                             if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
-                            else {
+                            else if (EXACT) {
+                                acc[j][0] = acc[j][0] + w * v;
+                                if (NCV > 1) acc[j][PCH - 1] = acc[j][PCH - 1] + w * ring[aj + 1];
+                            } else {
                                 acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
                                 if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[aj + 1], acc[j][PCH - 1]);
                             }
                         }
                     }
-                }
+                };
+                if (a.exact_sums) edge_loop(std::true_type());
+                else edge_loop(std::false_type());
                 for (int o = PL >> 1; o > 0; o >>= 1) {
 #pragma unroll
                     for (int j = 0; j < PK; j++)

@@ -194,9 +194,9 @@ __device__ __forceinline__ void stream_window(const float* q, float (&v)[HB_STRE
 
 // One edge's contribution to the K coupling sums of a block: the window of its source's history
 // starting `delay` steps before the block's first step, times the weight, added to acc (fused
-// multiply-adds: the regrouped sum). At step 0 the edge also reads the current state
-// (runtime.rs:166-170).
-template <int PCH>
+// multiply-adds: the regrouped sum; with EXACT a rounded product and a rounded sum per term, the
+// reference's operations). At step 0 the edge also reads the current state (runtime.rs:166-170).
+template <int PCH, bool EXACT = false>
 __device__ __forceinline__ void stream_edge_acc(const float* ring, uint32_t m, float w, int sbm, int RP, int RPX,
                                                 bool first_step, float (&acc)[HB_STREAM_K][PCH]) {
     const int d = (int)(m >> 16), src = (int)(m & 0xffffu);
@@ -207,7 +207,7 @@ __device__ __forceinline__ void stream_edge_acc(const float* ring, uint32_t m, f
 #pragma unroll
     for (int j = 0; j < HB_STREAM_K; j++)
 #pragma unroll
-        for (int c = 0; c < PCH; c++) acc[j][c] = __fmaf_rn(w, v[j][c], acc[j][c]);
+        for (int c = 0; c < PCH; c++) acc[j][c] = EXACT ? acc[j][c] + w * v[j][c] : __fmaf_rn(w, v[j][c], acc[j][c]);
     if (first_step) {
         const float* q0 = ring + (size_t)src * RPX * PCH;
 #pragma unroll
@@ -505,7 +505,8 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
 #pragma unroll UNR
                         for (int e = e0 + lane; e < e1; e += PL) {
                             if (pf) stream_edge_prefetch<PCH>(ring, ed, e + pf * PL, e1, sbm, RP, RPX);
-                            stream_edge_acc<PCH>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
+                            if (a.exact_sums) stream_edge_acc<PCH, true>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
+                            else stream_edge_acc<PCH>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
                         }
                     } else {
                         // the edge descriptors DB at a time, loaded together, so that their latency is
@@ -528,7 +529,8 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
 #pragma unroll
                                 for (int q = 0; q + 1 < DB; q++) { mb[q] = mb[q + 1]; wb[q] = wb[q + 1]; }
                                 if (pf) stream_edge_prefetch<PCH>(ring, ed, eb + (u + pf) * PL, e1, sbm, RP, RPX);
-                                stream_edge_acc<PCH>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                                if (a.exact_sums) stream_edge_acc<PCH, true>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                                else stream_edge_acc<PCH>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
                             }
                         }
                     }
@@ -570,6 +572,10 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             }
             named_arrive(HB_BAR_FULL0 + buf, nthreads);
         }
+        // the consumers' arrivals on EMPTY after the last two blocks have no producer block to wait for
+        // them; they are matched here, so that the named barriers end the point as they started (the
+        // work-queue kernel runs several points in one CTA)
+        for (int q = n_blocks - 2 > 0 ? n_blocks - 2 : 0; q < n_blocks; q++) named_sync(HB_BAR_EMPTY0 + (q & 1), nthreads);
     } else {
         // ================= consumers =================
         const int sweep_form = net.sub[0].sweep_form;

@@ -76,6 +76,12 @@ typedef int32_t hb_status;
    to itself through one projection without delay, Linear / Sigmoidal / ScaledLinear coupling, a model with one
    coupling variable, up to 112 nodes, no monitors, trajectories or node_params; HB_ERR_UNSUPPORTED otherwise. */
 #define HB_RUN_DENSE_TC     (1u << 2)
+/* sparse coupling sums in the reference's order: one thread per target node adds its edges' terms in CSR order,
+   each product and each sum rounded (no fused multiply-add), as the reference's per-edge loop
+   (runtime.rs:162-204); slower than the default, which splits a node's edges over lanes and fuses the
+   multiply-adds (results agree within the FP32 rounding of the sum). With it, a model without transcendental
+   functions reproduces the FP32 reference arithmetic bit for bit. */
+#define HB_RUN_EXACT_SUMS   (1u << 3)
 #define HB_RUN_FORCE_RESIDENT (1u << 8) /* kernel choice: point-resident persistent kernel */
 #define HB_RUN_FORCE_BLOCKED  (1u << 9) /* kernel choice: time-blocked tiled kernel */
 #define HB_RUN_GLOBAL_RING    (1u << 10) /* resident kernel: keep the history ring in global memory */

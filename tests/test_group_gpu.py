@@ -99,3 +99,23 @@ def test_group_rejects_short_delays():
     ec = BatchHybridEngine.from_config(c, 2, semantics=HB_SEM_DELAY_RING)
     with pytest.raises(Unsupported, match="streamed-history"):
         GroupedSweep([(ec, SweepParam(0, 1), [0.0, 0.1], 50, None)])
+
+
+@pytest.mark.parametrize("big", [False, True])
+def test_group_many_points_per_cta(big):
+    """More work items than resident CTAs (about 150 on the device): each CTA of the persistent
+    work-queue kernel runs several points one after another and must leave its barriers and shared
+    memory as it found them. big: a 150-node member moves the launch to two nodes per consumer thread."""
+    members = []
+    sizes = [(20, 200, 240), (28, 200, 300)] + ([(150, 40, 160)] if big else [])
+    for i, (n, pts, steps) in enumerate(sizes):
+        cfg = single_model("MontbrioPazoRoxin", n, "rk4", "Linear", (0.3,), weights="csr", delays="per_edge_long",
+                           dt=0.05, seed=10 + i)
+        vals = np.linspace(-1.0, 0.5, pts).astype(np.float32).tolist()
+        members.append((cfg, pts, SweepParam(0, 4), vals, steps, None))
+    engines = [BatchHybridEngine.from_config(c, p, semantics=HB_SEM_DELAY_RING) for c, p, *_ in members]
+    g = GroupedSweep([(e, m[2], m[3], m[4], m[5]) for e, m in zip(engines, members)])
+    for _ in range(2):
+        g.execute()
+        _check(members, HB_SEM_DELAY_RING, g.results())
+    g.close()

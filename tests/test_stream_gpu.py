@@ -110,19 +110,18 @@ def test_history_layout_cannot_change_mid_simulation():
     assert np.isfinite(eng.states[0]).all()
 
 
-@pytest.mark.parametrize("C", [2, 4, 8])
-@pytest.mark.parametrize("npt", [1, 2])
+@pytest.mark.parametrize("C,npt", [(2, 2), (4, 1), (4, 2), (8, 1), (8, 2)])
 def test_stream_cluster_split_kuramoto(C, npt):
     """One point's 1000 nodes split over a cluster of C CTAs (HB_RUN_STREAM_CLUSTER): the CTAs read
     each other's history through global memory after each block's cluster-scope signal; per-node
-    omega, per-point BOLD, with and without one node per consumer thread."""
+    omega, per-point BOLD, with one (where a slice fits 512 threads) and two nodes per consumer thread."""
     from hyburn_gb300 import inputs
     from hyburn_gb300._abi import HB_RUN_STREAM_CLUSTER
     cfg, meta = inputs.kuramoto_scale(n=1000, n_points=3, n_steps=200, bold=True)
     cfg.monitors[0].tr = 0.005
     eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 1.0, 2.0], 200, rtol=2e-5,
                            semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT,
-                           run_flags=HB_RUN_STREAM_CLUSTER(C) | HB_RUN_STREAM_NPT(npt))
+                           run_flags=HB_RUN_STREAM | HB_RUN_STREAM_CLUSTER(C) | HB_RUN_STREAM_NPT(npt))
     assert kind(eng) == STREAM_KIND
 
 
