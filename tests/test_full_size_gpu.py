@@ -4,9 +4,10 @@ Two forms of the check. With HB_RUN_EXACT_SUMS the engine adds every coupling te
 order with separately rounded products and sums; for models without transcendental functions it must
 then equal the FP32 oracle bit for bit, at any length. In the default form the coupling sums are
 regrouped (lanes, fused multiply-adds); over tens of thousands of deterministic steps the two FP32
-roundings drift apart by more than rel 1e-5 in a few elements, so there the bound is the FP32
-arithmetic itself: the engine may be no farther from the FP32 oracle than the FP32 oracle is from the
-FP64 one (largest absolute difference over the output). Shorter runs keep rel 1e-5 / abs 1e-6.
+roundings drift apart by more than rel 1e-5 in a few elements (measured: 6.8e-5 in one of 18 944
+temporal averages of the deterministic benchmark sweep), so there the bound is the FP32 arithmetic
+itself: the engine may be no farther from the FP32 oracle than twice the FP32 oracle's distance from
+the FP64 one (largest absolute difference over the output), with rel 1e-5 / abs 1e-6 as the floor.
 
 - The 128-point, 74-node G2DO sweep with per-edge delays, 20 000 Heun steps: deterministic and with
   the shared seeded draws of the benchmark.
@@ -46,10 +47,13 @@ def _mpr_member(n, seed, T, G, eta, tr=2.0):
 
 
 def within_fp32_error(g, o32, o64, what):
-    """The engine's distance from the FP32 oracle is at most the FP32 oracle's own distance from FP64."""
+    """The engine and the FP32 oracle are two FP32 roundings of the same run, each about as far from the
+    FP64 run as the other: the engine's largest distance from the FP32 oracle may be twice the FP32
+    oracle's largest distance from FP64, and never needs to be below the usual rel 1e-5 / abs 1e-6."""
     g, o32, o64 = (np.asarray(v, np.float64) for v in (g, o32, o64))
     dg, d32 = np.abs(g - o32).max(), np.abs(o32 - o64).max()
-    assert dg <= d32, f"{what}: engine differs from the FP32 oracle by {dg:.3g}, the FP32 oracle from FP64 by {d32:.3g}"
+    bound = max(2.0 * d32, 1e-6 + 1e-5 * np.abs(o32).max())
+    assert dg <= bound, f"{what}: engine differs from the FP32 oracle by {dg:.3g}, the FP32 oracle from FP64 by {d32:.3g}"
 
 
 @pytest.mark.parametrize("stochastic", [False, True])
