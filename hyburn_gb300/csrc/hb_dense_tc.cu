@@ -157,7 +157,6 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     const uint32_t tD = tlane, tX = tlane + (uint32_t)NP, tV = tlane + (uint32_t)(NP + NVAR * NPN);
     const DevProj& P = net.proj[0];
     const int integ = net.sub[0].integ, sweep_form = net.sub[0].sweep_form;
-    const bool stoch = (integ == HBI_EULER_STOCH || integ == HBI_HEUN_STOCH || integ == HBI_RK4_STOCH);
     float prm[HB_PSTRIDE];
     {
         const float* pr = net.sub[0].params + (size_t)bb * HB_PSTRIDE;
@@ -203,57 +202,71 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     const uint32_t sbo = (uint32_t)(KP >> 2) << 7;
     const uint32_t s_whi = smem_addr(whi), s_wlo = smem_addr(wlo), s_ahi = smem_addr(ahi), s_alo = smem_addr(alo);
     bool bad = false;
-    for (int s = 0; s < a.n_steps; s++) {
-        // X of this step visible to the tensor core; the last step's reads of D finished
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        if (t == 0) {
+    // the step loop with the integrator fixed at compile time: only that integrator's code is live in the
+    // instruction cache while the 16 node updates of a chunk run unrolled
+    auto run_steps = [&](auto integ_tag) {
+        constexpr int IG = decltype(integ_tag)::value;
+        constexpr bool STOCH = IG == HBI_EULER_STOCH || IG == HBI_HEUN_STOCH || IG == HBI_RK4_STOCH;
+        for (int s = 0; s < a.n_steps; s++) {
+            // X of this step visible to the tensor core; the last step's reads of D finished
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (t == 0) {
+                tc_fence_after();
+                const int nk = KP >> 3;
+                for (int kk = 0; kk < nk; kk++)
+                    tc_mma(tD, smem_desc(s_ahi + kk * 256, 128, sbo), smem_desc(s_whi + kk * 256, 128, sbo), idesc, kk > 0);
+                for (int kk = 0; kk < nk; kk++)
+                    tc_mma(tD, smem_desc(s_ahi + kk * 256, 128, sbo), smem_desc(s_wlo + kk * 256, 128, sbo), idesc, 1);
+                for (int kk = 0; kk < nk; kk++)
+                    tc_mma(tD, smem_desc(s_alo + kk * 256, 128, sbo), smem_desc(s_whi + kk * 256, 128, sbo), idesc, 1);
+                tc_commit(&mma_bar);
+            }
+            if (!mbar_wait(&mma_bar, (uint32_t)(s & 1))) atomicOr(a.flags + 1, 4);
             tc_fence_after();
-            const int nk = KP >> 3;
-            for (int kk = 0; kk < nk; kk++)
-                tc_mma(tD, smem_desc(s_ahi + kk * 256, 128, sbo), smem_desc(s_whi + kk * 256, 128, sbo), idesc, kk > 0);
-            for (int kk = 0; kk < nk; kk++)
-                tc_mma(tD, smem_desc(s_ahi + kk * 256, 128, sbo), smem_desc(s_wlo + kk * 256, 128, sbo), idesc, 1);
-            for (int kk = 0; kk < nk; kk++)
-                tc_mma(tD, smem_desc(s_alo + kk * 256, 128, sbo), smem_desc(s_whi + kk * 256, 128, sbo), idesc, 1);
-            tc_commit(&mma_bar);
-        }
-        if (!mbar_wait(&mma_bar, (uint32_t)(s & 1))) atomicOr(a.flags + 1, 4);
-        tc_fence_after();
-        for (int c = 0; c < NPN; c += TC_CH) {
-            float dr[TC_CH], xr[TC_CH * NVAR], vr[TC_CH * NVAR], x0[TC_CH];
-            tc_ld16(tD + (uint32_t)c, dr);
+            for (int c = 0; c < NPN; c += TC_CH) {
+                float dr[TC_CH], xr[TC_CH * NVAR], vr[TC_CH * NVAR], x0[TC_CH];
+                tc_ld16(tD + (uint32_t)c, dr);
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) {
-                tc_ld16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-                tc_ld16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
-            }
-            tc_wait_ld();
-#pragma unroll
-            for (int i = 0; i < TC_CH; i++) {
-                const int n = c + i;
-                float* x = xr + i * NVAR;
-                if (active && n < N) {
-                    float gx[4] = {dr[i], 0.0f, 0.0f, 0.0f};
-                    float nz[NVAR];
-#pragma unroll
-                    for (int v = 0; v < NVAR; v++)
-                        nz[v] = stoch ? noise_base[(size_t)s * nstride + (size_t)n * NVAR + v] * net.noise_scale[v] : 0.0f;
-                    stream_node_step<MODEL>(P, cp, integ, prm, sweep_form, 0.0f, gx, nz, x, dt, dt_half, h2, h6);
-#pragma unroll
-                    for (int v = 0; v < NVAR; v++) vr[i * NVAR + v] = vr[i * NVAR + v] + x[v];
+                for (int v = 0; v < NVAR; v++) {
+                    tc_ld16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
+                    tc_ld16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
                 }
-                x0[i] = (active && n < N) ? x[0] : 0.0f;
-            }
+                tc_wait_ld();
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) {
-                tc_st16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-                tc_st16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
+                for (int i = 0; i < TC_CH; i++) {
+                    const int n = c + i;
+                    float* x = xr + i * NVAR;
+                    if (active && n < N) {
+                        float gx[4] = {dr[i], 0.0f, 0.0f, 0.0f};
+                        float nz[NVAR];
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++)
+                            nz[v] = STOCH ? noise_base[(size_t)s * nstride + (size_t)n * NVAR + v] * net.noise_scale[v] : 0.0f;
+                        stream_node_step<MODEL>(P, cp, IG, prm, sweep_form, 0.0f, gx, nz, x, dt, dt_half, h2, h6);
+#pragma unroll
+                        for (int v = 0; v < NVAR; v++) vr[i * NVAR + v] = vr[i * NVAR + v] + x[v];
+                    }
+                    x0[i] = (active && n < N) ? x[0] : 0.0f;
+                }
+#pragma unroll
+                for (int v = 0; v < NVAR; v++) {
+                    tc_st16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
+                    tc_st16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
+                }
+                write_x_row(ahi, alo, t, c, KP, x0);
             }
-            write_x_row(ahi, alo, t, c, KP, x0);
+            tc_wait_st();
         }
-        tc_wait_st();
+    };
+    switch (integ) {
+    case HBI_HEUN_DET: run_steps(std::integral_constant<int, HBI_HEUN_DET>()); break;
+    case HBI_HEUN_STOCH: run_steps(std::integral_constant<int, HBI_HEUN_STOCH>()); break;
+    case HBI_EULER: run_steps(std::integral_constant<int, HBI_EULER>()); break;
+    case HBI_EULER_STOCH: run_steps(std::integral_constant<int, HBI_EULER_STOCH>()); break;
+    case HBI_RK4: run_steps(std::integral_constant<int, HBI_RK4>()); break;
+    default: run_steps(std::integral_constant<int, HBI_RK4_STOCH>()); break;
     }
     // state and running sums out
     for (int c = 0; c < NPN; c += TC_CH) {
