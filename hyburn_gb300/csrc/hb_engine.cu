@@ -742,7 +742,19 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         // that fewer points are in flight and their histories stay in L2
         {
             const int v = (int)((run_flags >> 4) & 0x7);
-            stream_cluster = v == 0 ? 1 : 1 << (v - 1);
+            if (v == 0) {
+                // engine's choice: split each point over a cluster when the histories of the points in flight
+                // (one CTA per SM) would not fit in about 96 MB of the 129 MB L2, keeping 64 nodes per CTA
+                int dev = 0, sms = 152;
+                if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                const int rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
+                const double hist = (double)nm_all * (rp + 2 * HB_STREAM_K) * pch * 4;
+                stream_cluster = 1;
+                for (int c = 2; c <= 8; c *= 2) {
+                    if (std::min<double>(B, (double)sms / (c / 2)) * hist <= 96e6 || nm_all / c < 64) break;
+                    stream_cluster = c;
+                }
+            } else stream_cluster = 1 << (v - 1);
             if (stream_cluster > 8 || stream_cluster > nm_all)
                 return fail(HB_ERR_INVALID_STATE, "HB_RUN_STREAM_CLUSTER: 1, 2, 4 or 8 CTAs per point, at most one per node");
         }
@@ -1950,7 +1962,7 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
         }
         // the work-queue kernel runs every point in one CTA (no clusters)
         const uint32_t flags = (mb.run_flags & ~(uint32_t)(0x7u << 24) & ~(uint32_t)(0x7u << 4)) | HB_RUN_STREAM |
-                               HB_RUN_STREAM_NPT(npt);
+                               HB_RUN_STREAM_NPT(npt) | HB_RUN_STREAM_CLUSTER(1);
         if ((s = run_setup(e, gm.T, mb.n_steps, flags, nullptr, noise_dev ? noise_dev : e->x0.p, nullptr, gm.P))) return s;
         if (gm.P.stream_npt != npt)
             return fail(HB_ERR_UNSUPPORTED, "member %d cannot run in the streamed-history kernel (one subnetwork, one sparse "

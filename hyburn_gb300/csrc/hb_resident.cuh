@@ -975,9 +975,11 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
         const int nb = (n_steps - blk * PK) < PK ? (n_steps - blk * PK) : PK;
         const float* gb = gxbuf + (size_t)buf * PK * nm * NCV + (size_t)n * NCV;
         const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR + (size_t)n * NVAR;
-        // the coupling term and the scaled noise of a step depend only on the block's shared-memory
-        // buffers: each is computed one step ahead, off the state's dependency chain (same arithmetic)
-        auto ahead = [&](int j, float* ccv, float* nzv) {
+#pragma unroll 1
+        for (int j = 0; j < nb; j++) {
+            slot = (slot + 1 == R) ? 0 : slot + 1;
+            if (!active) continue;  // threads past the last node only take part in the barriers
+            float cc[2] = {0.0f, 0.0f};
 #pragma unroll
             for (int c = 0; c < NCV; c++) {
                 const float g = gb[(size_t)j * nm * NCV + c];
@@ -985,27 +987,14 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
                     const float sh = (g + (-c2)) / c4;
                     const float ex = -(sh * c3);
                     const float den = expf(ex) + 1.0f;
-                    ccv[c] = (1.0f / den) * (cb - ca) + ca;
+                    cc[c] = (1.0f / den) * (cb - ca) + ca;
                 } else {
-                    ccv[c] = g * ca + cb;
+                    cc[c] = g * ca + cb;
                 }
             }
-#pragma unroll
-            for (int v = 0; v < NVAR; v++) nzv[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
-        };
-        float cc_next[2] = {0.0f, 0.0f}, nz_next[NVAR];
-#pragma unroll
-        for (int v = 0; v < NVAR; v++) nz_next[v] = 0.0f;
-        if (active && nb > 0) ahead(0, cc_next, nz_next);
-#pragma unroll 1
-        for (int j = 0; j < nb; j++) {
-            slot = (slot + 1 == R) ? 0 : slot + 1;
-            if (!active) continue;  // threads past the last node only take part in the barriers
-            float cc[2] = {cc_next[0], cc_next[1]};
             float nz[NVAR];
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v];
-            if (j + 1 < nb) ahead(j + 1, cc_next, nz_next);
+            for (int v = 0; v < NVAR; v++) nz[v] = STOCH ? nbuf[(size_t)j * nm * NVAR + v] * ns[v] : 0.0f;
             float k1[NVAR], k2[NVAR], tmp[NVAR];
             dfun(MODEL, prm, SWEEP_FORM ? 1 : 0, x, cc, k1);
             if (STOCH) {
@@ -1183,23 +1172,30 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                 // in edge order, as the reference; otherwise fused multiply-adds
                 auto edge_loop = [&](auto exact_tag) {
                     constexpr bool EXACT = decltype(exact_tag)::value;
+                    auto term = [&](int j, float w, int aj) {
+                        const float v = ring[aj];
+                        if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
+                        else if (EXACT) {
+                            acc[j][0] = acc[j][0] + w * v;
+                            if (NCV > 1) acc[j][PCH - 1] = acc[j][PCH - 1] + w * ring[aj + 1];
+                        } else {
+                            acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
+                            if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[aj + 1], acc[j][PCH - 1]);
+                        }
+                    };
                     for (int e = pe0 + plane; e < pe1; e += PL) {
                         int a0 = base + eo[e];
                         a0 = a0 < 0 ? a0 + ring_words : a0;
                         const float w = ew[e];
-                        const bool whole = a0 + (PK - 1) * cols < ring_words;
+                        if (a0 + (PK - 1) * cols < ring_words) {
 #pragma unroll
-                        for (int j = 0; j < PK; j++) {
-                            int aj = a0 + j * cols;
-                            if (!whole) aj = aj >= ring_words ? aj - ring_words : aj;
-                            const float v = ring[aj];
-                            if (PRE == PRE_KURA) { acc[j][0] += w * sinf(v); acc[j][PCH - 1] += w * cosf(v); }
-                            else if (EXACT) {
-                                acc[j][0] = acc[j][0] + w * v;
-                                if (NCV > 1) acc[j][PCH - 1] = acc[j][PCH - 1] + w * ring[aj + 1];
-                            } else {
-                                acc[j][0] = __fmaf_rn(w, v, acc[j][0]);
-                                if (NCV > 1) acc[j][PCH - 1] = __fmaf_rn(w, ring[aj + 1], acc[j][PCH - 1]);
+                            for (int j = 0; j < PK; j++) term(j, w, a0 + j * cols);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < PK; j++) {
+                                int aj = a0 + j * cols;
+                                aj = aj >= ring_words ? aj - ring_words : aj;
+                                term(j, w, aj);
                             }
                         }
                     }

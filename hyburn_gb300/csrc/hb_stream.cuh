@@ -306,32 +306,21 @@ __device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, 
         const int nb = (n_steps - it0) < K ? (n_steps - it0) : K;
         const float* gb = gxbuf + (size_t)buf * K * ns * NCV + (size_t)l * NCV;
         const float* nbuf = nzbuf + (size_t)buf * K * ns * NVAR + (size_t)l * NVAR;
-        // the coupling term and the scaled noise of a step are computed one step ahead, off the state's
-        // dependency chain (same arithmetic)
-        auto ahead = [&](int j, float* ccv, float* nzv) {
-            ccv[0] = gb[(size_t)j * ns * NCV] * ca + cb;
-            if (NCV > 1) ccv[1] = gb[(size_t)j * ns * NCV + 1] * ca + cb;
-#pragma unroll
-            for (int v = 0; v < NVAR; v++) {
-                if (!STOCH) nzv[v] = 0.0f;
-                else if (NOISE_SMEM) nzv[v] = nbuf[(size_t)j * ns * NVAR + v] * nsc[v];
-                else nzv[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * nsc[v];
-            }
-        };
-        float cc_next[2] = {0.0f, 0.0f}, nz_next[NVAR];
-#pragma unroll
-        for (int v = 0; v < NVAR; v++) nz_next[v] = 0.0f;
-        if (active && nb > 0) ahead(0, cc_next, nz_next);
 #pragma unroll 1
         for (int j = 0; j < nb; j++) {
             const int pos = wpos;
             wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
             if (!active) continue;  // threads past the last node only take part in the barriers
-            float cc[2] = {cc_next[0], cc_next[1]};
+            float cc[2] = {0.0f, 0.0f};
+            cc[0] = gb[(size_t)j * ns * NCV] * ca + cb;
+            if (NCV > 1) cc[1] = gb[(size_t)j * ns * NCV + 1] * ca + cb;
             float nz[NVAR];
 #pragma unroll
-            for (int v = 0; v < NVAR; v++) nz[v] = nz_next[v];
-            if (j + 1 < nb) ahead(j + 1, cc_next, nz_next);
+            for (int v = 0; v < NVAR; v++) {
+                if (!STOCH) nz[v] = 0.0f;
+                else if (NOISE_SMEM) nz[v] = nbuf[(size_t)j * ns * NVAR + v] * nsc[v];
+                else nz[v] = __ldcs(noise_g + (size_t)(it0 + j) * nstride + (size_t)n * NVAR + v) * nsc[v];
+            }
             float k1[NVAR], k2[NVAR], tmp[NVAR];
             dfun(MODEL, prm, SF ? 1 : 0, x, cc, k1);
 #pragma unroll
