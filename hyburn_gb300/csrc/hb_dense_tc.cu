@@ -14,10 +14,13 @@
 // no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix, core matrices K-adjacent at 128
 // bytes, 8-row groups at KP / 4 * 128 bytes), in shared memory; W is arranged on the host once. Tensor
 // memory holds, for lane = point, the accumulator D (NP columns), the state x [node][var] and its
-// running sum over the run (NPN * nvar columns each, NPN = N rounded up to 16). After the product of a
-// step each thread reads its point's row of D, applies the coupling post-function and the integrator
-// stages node by node (the same operations in the same order as the other kernels; the coupling is
-// held over the stages, engine.rs:697-771), writes the new state back and rebuilds its row of X.
+// running sum over the run (NPN * nvar columns each, NPN = N rounded up to 16). The CTA runs four
+// warpgroups; a warp may only touch the 32 tensor-memory lanes of its quarter (warp % 4), so thread
+// (warpgroup g, row r) owns point r and the 8-node chunks g, g + 4, g + 8, ... of that point. After the
+// product of a step each thread reads its chunks of its point's row of D, applies the coupling
+// post-function and the integrator stages node by node (the same operations in the same order as the
+// other kernels; the coupling is held over the stages, engine.rs:697-771), writes the new state back
+// and rebuilds its part of the row of X.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,7 +32,8 @@ namespace hb {
 namespace {
 
 constexpr int TC_M = 128;    // sweep points per CTA (the MMA's M)
-constexpr int TC_CH = 16;    // nodes per tensor-memory chunk
+constexpr int TC_WG = 4;     // warpgroups per CTA, splitting each point's nodes
+constexpr int TC_CH = 8;     // nodes per tensor-memory chunk
 
 // byte offset of element (row r, column k) in the K-major no-swizzle core-matrix layout with KP columns
 __device__ __forceinline__ uint32_t cm_off(int r, int k, int KP) {
@@ -67,30 +71,25 @@ __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sy
 __device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// 16 consecutive tensor-memory columns of this thread's lane
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
+// 8 consecutive tensor-memory columns of this thread's lane
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
 #pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
-__device__ __forceinline__ void tc_st16(uint32_t taddr, const float* v) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
-        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])),
-          "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
-          "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-          "r"(__float_as_uint(v[15]))
-        : "memory");
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const float* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                   "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                   "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
 }
 
-// this thread's row of X for nodes c .. c + 15 (value v of node c + i in v[i]; zero past the last node)
+// this thread's row of X for nodes c .. c + 7 (value v of node c + i in v[i]; zero past the last node)
 __device__ __forceinline__ void write_x_row(unsigned char* ahi, unsigned char* alo, int row, int c, int KP, const float* v) {
 #pragma unroll
     for (int q = 0; q < TC_CH; q += 4) {
@@ -112,7 +111,7 @@ __device__ __forceinline__ void write_x_row(unsigned char* ahi, unsigned char* a
 }
 
 template <int MODEL>
-__global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restrict__ gnet, RunArgs a,
+__global__ void __launch_bounds__(TC_M * TC_WG, 1) dense_tc_kernel(const DevNet* __restrict__ gnet, RunArgs a,
                                                            const float* __restrict__ wtiles, int NP, int KP, int NPN,
                                                            int ncols) {
     extern __shared__ __align__(128) unsigned char smem[];  // W_hi | W_lo | X_hi | X_lo
@@ -123,6 +122,7 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
         reinterpret_cast<int*>(&net)[i] = reinterpret_cast<const int*>(gnet)[i];
     constexpr int NVAR = c_nvar(MODEL);
     const int t = threadIdx.x, warp = t >> 5;
+    const int row = ((warp & 3) << 5) | (t & 31), grp = warp >> 2;  // point row of the tile, node-chunk group
     const size_t wbytes = (size_t)NP * KP * 4, abytes = (size_t)TC_M * KP * 4;
     unsigned char* whi = smem;
     unsigned char* wlo = smem + wbytes;
@@ -150,10 +150,11 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     tc_fence_after();
 
     const int N = net.sub[0].nm, B = net.B;
-    const int b = blockIdx.x * TC_M + t;  // this thread's sweep point (row of the tile)
+    const int b = blockIdx.x * TC_M + row;  // this thread's sweep point
     const bool active = b < B;
     const int bb = active ? b : 0;
-    const uint32_t tlane = tmem_base_s + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tlane = tmem_base_s + ((uint32_t)((warp & 3) * 32) << 16);
+    const int c_first = grp * TC_CH, c_step = TC_WG * TC_CH;
     const uint32_t tD = tlane, tX = tlane + (uint32_t)NP, tV = tlane + (uint32_t)(NP + NVAR * NPN);
     const DevProj& P = net.proj[0];
     const int integ = net.sub[0].integ, sweep_form = net.sub[0].sweep_form;
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     const bool first_launch_of_run = (a.s0 == a.run_s0);
 
     // the start state and running sums into tensor memory, X of the first step into shared memory
-    for (int c = 0; c < NPN; c += TC_CH) {
+    for (int c = c_first; c < NPN; c += c_step) {
         float xr[TC_CH * NVAR], vr[TC_CH * NVAR], x0[TC_CH];
 #pragma unroll
         for (int i = 0; i < TC_CH; i++) {
@@ -191,10 +192,10 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
         }
 #pragma unroll
         for (int v = 0; v < NVAR; v++) {
-            tc_st16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-            tc_st16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
+            tc_st8(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
+            tc_st8(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
         }
-        write_x_row(ahi, alo, t, c, KP, x0);
+        write_x_row(ahi, alo, row, c, KP, x0);
     }
     tc_wait_st();
 
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     const uint32_t s_whi = smem_addr(whi), s_wlo = smem_addr(wlo), s_ahi = smem_addr(ahi), s_alo = smem_addr(alo);
     bool bad = false;
     // the step loop with the integrator fixed at compile time: only that integrator's code is live in the
-    // instruction cache while the 16 node updates of a chunk run unrolled
+    // instruction cache while the 8 node updates of a chunk run unrolled
     auto run_steps = [&](auto integ_tag) {
         constexpr int IG = decltype(integ_tag)::value;
         constexpr bool STOCH = IG == HBI_EULER_STOCH || IG == HBI_HEUN_STOCH || IG == HBI_RK4_STOCH;
@@ -225,14 +226,11 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
             }
             if (!mbar_wait(&mma_bar, (uint32_t)(s & 1))) atomicOr(a.flags + 1, 4);
             tc_fence_after();
-            for (int c = 0; c < NPN; c += TC_CH) {
-                float dr[TC_CH], xr[TC_CH * NVAR], vr[TC_CH * NVAR], x0[TC_CH];
-                tc_ld16(tD + (uint32_t)c, dr);
+            for (int c = c_first; c < NPN; c += c_step) {
+                float dr[TC_CH], xr[TC_CH * NVAR], x0[TC_CH];
+                tc_ld8(tD + (uint32_t)c, dr);
 #pragma unroll
-                for (int v = 0; v < NVAR; v++) {
-                    tc_ld16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-                    tc_ld16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
-                }
+                for (int v = 0; v < NVAR; v++) tc_ld8(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
                 tc_wait_ld();
 #pragma unroll
                 for (int i = 0; i < TC_CH; i++) {
@@ -245,17 +243,23 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
                         for (int v = 0; v < NVAR; v++)
                             nz[v] = STOCH ? noise_base[(size_t)s * nstride + (size_t)n * NVAR + v] * net.noise_scale[v] : 0.0f;
                         stream_node_step<MODEL>(P, cp, IG, prm, sweep_form, 0.0f, gx, nz, x, dt, dt_half, h2, h6);
-#pragma unroll
-                        for (int v = 0; v < NVAR; v++) vr[i * NVAR + v] = vr[i * NVAR + v] + x[v];
                     }
                     x0[i] = (active && n < N) ? x[0] : 0.0f;
                 }
 #pragma unroll
+                for (int v = 0; v < NVAR; v++) tc_st8(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
+                write_x_row(ahi, alo, row, c, KP, x0);
+                // running sums, one variable block at a time (padded nodes and rows past the batch hold
+                // zero states, so adding them changes nothing)
+#pragma unroll
                 for (int v = 0; v < NVAR; v++) {
-                    tc_st16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-                    tc_st16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
+                    float vr[TC_CH];
+                    tc_ld8(tV + (uint32_t)(c * NVAR + v * TC_CH), vr);
+                    tc_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < TC_CH; i++) vr[i] = vr[i] + xr[v * TC_CH + i];
+                    tc_st8(tV + (uint32_t)(c * NVAR + v * TC_CH), vr);
                 }
-                write_x_row(ahi, alo, t, c, KP, x0);
             }
             tc_wait_st();
         }
@@ -269,12 +273,12 @@ __global__ void __launch_bounds__(TC_M, 1) dense_tc_kernel(const DevNet* __restr
     default: run_steps(std::integral_constant<int, HBI_RK4_STOCH>()); break;
     }
     // state and running sums out
-    for (int c = 0; c < NPN; c += TC_CH) {
+    for (int c = c_first; c < NPN; c += c_step) {
         float xr[TC_CH * NVAR], vr[TC_CH * NVAR];
 #pragma unroll
         for (int v = 0; v < NVAR; v++) {
-            tc_ld16(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
-            tc_ld16(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
+            tc_ld8(tX + (uint32_t)(c * NVAR + v * TC_CH), xr + v * TC_CH);
+            tc_ld8(tV + (uint32_t)(c * NVAR + v * TC_CH), vr + v * TC_CH);
         }
         tc_wait_ld();
 #pragma unroll
@@ -308,7 +312,7 @@ cudaError_t launch_dense_tc(const DevNet* d_net, const RunArgs& a, int B, const 
     const size_t smem = (size_t)2 * NP * KP * 4 + (size_t)2 * TC_M * KP * 4;
     cudaError_t e = cudaFuncSetAttribute(dense_tc_kernel<MODEL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dense_tc_kernel<MODEL><<<(B + TC_M - 1) / TC_M, TC_M, smem, st>>>(d_net, a, wtiles, NP, KP, NPN, ncols);
+    dense_tc_kernel<MODEL><<<(B + TC_M - 1) / TC_M, TC_M * TC_WG, smem, st>>>(d_net, a, wtiles, NP, KP, NPN, ncols);
     return cudaGetLastError();
 }
 

@@ -791,7 +791,13 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
                 stream_smem = used;
                 const int n_cons = ((nm0 + npt - 1) / npt + 31) / 32 * 32;
                 const int n_prod = threads - n_cons;
-                while (!(run_flags & HB_RUN_EXACT_SUMS) && stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
+                const int forced_pl = (int)((run_flags >> 20) & 0xf);
+                if (forced_pl && ((forced_pl & (forced_pl - 1)) != 0 || forced_pl > 8))
+                    return fail(HB_ERR_INVALID_STATE, "producer lanes must be 1, 2, 4 or 8");
+                if (run_flags & HB_RUN_EXACT_SUMS) stream_pl = 1;
+                else if (forced_pl) stream_pl = forced_pl;
+                else
+                    while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
                 e->threads = threads;
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
                 const size_t words = (size_t)B * nm_all * (stream_rp + 2 * HB_STREAM_K) * pch;

@@ -90,7 +90,9 @@ typedef int32_t hb_status;
 #define HB_RUN_NO_PIPE        (1u << 17) /* do not use the warp-specialised producer/consumer pipeline */
 #define HB_RUN_STREAM         (1u << 18) /* keep the history in HBM (streamed-history pipeline) even when it fits shared memory */
 #define HB_RUN_NO_STREAM      (1u << 19) /* never use the streamed-history pipeline */
-/* pipeline kernel: producer threads per node (1, 2, 4 or 8); 0 lets the engine choose */
+/* pipeline and streamed-history kernels: producer threads per node (1, 2, 4 or 8; a streamed-history
+   CTA with fewer producers than nodes x lanes runs its producers over several rounds per block); 0 lets
+   the engine choose. HB_RUN_EXACT_SUMS overrides it with one. */
 #define HB_RUN_PIPE_LANES(n)  ((uint32_t)((n) & 0xf) << 20)
 /* streamed-history kernel: nodes per consumer thread (1: 512 threads, 2: 1024 threads, 4: 768 threads
    with two edge windows in flight per producer; 0 lets the engine choose). A grouped launch uses 4 when
