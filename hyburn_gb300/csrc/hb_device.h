@@ -153,6 +153,8 @@ struct RunArgs {
     int check_finite;
     int test_unset_wait;  // pipeline kernel: one bounded wait on a barrier nothing completes (timeout test)
     int exact_sums;       // coupling sums term by term in edge order, product and sum rounded apart (HB_RUN_EXACT_SUMS)
+    int stream_wgather;   // streamed-history kernel: warp-cooperative gathers (a warp per node, 8 lanes per edge
+                          // window; 0: one thread per edge window)
     DevBold bold;
 };
 

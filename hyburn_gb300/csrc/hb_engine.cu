@@ -732,6 +732,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     size_t smem = (ring_in_smem ? ((ring_bytes + 15) & ~(size_t)15) : 0) + (edges_in_smem ? edge_bytes : 0) + part_bytes + 16;
     // ---- streamed-history pipeline: per-edge delays whose history does not fit shared memory ----
     int stream_npt = 0, stream_pl = 1, stream_rp = 0, stream_noise_smem = 0, stream_edges = 0, stream_cluster = 1;
+    int stream_wgather = 0;
     size_t stream_smem = 0;
     if (fast >= 0 && e->projs[0].dmode == HBD_EDGE && e->dmin >= 2 * HB_STREAM_K - 1 && !(run_flags & HB_RUN_NO_STREAM) &&
         (!ring_in_smem || (run_flags & HB_RUN_STREAM)) && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE) &&
@@ -799,6 +800,14 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
                 else
                     while (stream_pl < 8 && nm0 * stream_pl * 2 <= n_prod) stream_pl *= 2;
                 e->threads = threads;
+                // warp-cooperative gathers (unless the reference's summation order or a producer lane count
+                // is asked for) when the slice's edge lists sit in shared memory and the nodes' rows fill most
+                // of the warp's 32-edge chunks (a mean in-degree of at least 24). With the edge lists in
+                // global memory each chunk's descriptor load would precede its window loads on the critical
+                // path, and one thread per window keeps more loads in flight there.
+                if (!(run_flags & HB_RUN_EXACT_SUMS) && !((run_flags >> 20) & 0xf) && stream_edges > 0 &&
+                    e->projs[0].edges.size() >= (size_t)24 * nm_all)
+                    stream_wgather = 1;
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
                 const size_t words = (size_t)B * nm_all * (stream_rp + 2 * HB_STREAM_K) * pch;
                 CUDA_TRY(e->sring.ensure(words));
@@ -936,6 +945,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     a.check_finite = (run_flags & HB_RUN_CHECK_FINITE) ? 1 : 0;
     a.test_unset_wait = (run_flags & HB_RUN_TEST_UNSET_WAIT) ? 1 : 0;
     a.exact_sums = (run_flags & HB_RUN_EXACT_SUMS) ? 1 : 0;
+    a.stream_wgather = stream_npt ? stream_wgather : 0;
     a.bold = db;
 
     P.n_steps = n_steps;

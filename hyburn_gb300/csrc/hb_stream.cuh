@@ -240,8 +240,8 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
-__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
 // arrive (release at cluster scope) on the mbarrier at the same shared-memory offset in CTA `rank`
+__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive_remote(const uint64_t* bar, uint32_t rank) {
     uint32_t ra;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_addr(bar)), "r"(rank));
@@ -255,15 +255,20 @@ __device__ __forceinline__ uint64_t global_ns() {
 // wait (acquire at cluster scope) for the phase of parity `parity`, for at most 200 ms; false when the
 // time ran out. After a timeout in the block (*gave_up set) later waits return at once, so a fault in
 // the cluster's signalling costs one bounded wait, not one per block.
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
 __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* gave_up) {
+    if (mbar_try_cluster(bar, parity)) return true;  // the common case: no clock read
     if (*gave_up) return false;
     const uint64_t t0 = global_ns();
     for (;;) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
-        if (done) return true;
+        if (mbar_try_cluster(bar, parity)) return true;
+        __nanosleep(64);  // a waiting warp leaves the issue slots to the consumers
         if (global_ns() - t0 > 200000000ull || *gave_up) {
             *gave_up = 1;
             return false;
@@ -276,12 +281,12 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity
 // made after its arrivals for block j.
 #define HB_HIST_BARS 4
 // consumers of a cluster-split point after finishing block `blk`: their history writes made visible at
-// cluster scope, then one arrival per CTA on every CTA's barrier of the block
+// cluster scope, then one arrival per CTA on every CTA's barrier of the block, made by C consumer threads
+// in parallel
 __device__ __forceinline__ void stream_signal_block(uint64_t* hbar, int blk, int C, int n_cons) {
     fence_cluster();
     named_sync(HB_BAR_CONS, n_cons);
-    if (threadIdx.x == 0)
-        for (int r = 0; r < C; r++) mbar_arrive_remote(hbar + (blk & (HB_HIST_BARS - 1)), (uint32_t)r);
+    if ((int)threadIdx.x < C) mbar_arrive_remote(hbar + (blk & (HB_HIST_BARS - 1)), threadIdx.x);
 }
 
 // Consumer steps for Heun (deterministic or stochastic) with Linear coupling delivered directly, no
@@ -339,6 +344,119 @@ __device__ __forceinline__ void stream_consume_heun_linear(float* x, float* tv, 
         named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
         if (C > 1) stream_signal_block(hbar, blk, C, n_cons);
     }
+}
+
+// steps from absolute step s (included) to the next step at which stream_bold_sample emits: a monitor's
+// window of period steps closes (its count `cnt` before step s), or the run's last step closes a partial
+// window
+__device__ __forceinline__ int stream_bold_until(const RunArgs& a, const int* cnt, int64_t s) {
+    int u = 0x7fffffff;
+    bool partial = false;
+#pragma unroll
+    for (int m = 0; m < HB_MAX_BOLD; m++)
+        if (m < a.bold.n) {
+            u = min(u, a.bold.period[m] - cnt[m]);
+            partial |= a.bold.partial[m] > 0;
+        }
+    if (partial) u = min(u, (int)(a.run_steps - (s - a.run_s0)));
+    return u;
+}
+
+// the Kuramoto phase wrap x - floor(x / 2pi) * 2pi (clamp(), dfun.rs:170-239). For 0 < x < 2pi the
+// quotient rounds to a value below 1 (x <= 2pi - 2^-21 gives x / 2pi <= 1 - 2^-24 after rounding), so
+// the floor is 0 and the result is x itself: the division runs only when the phase left that interval.
+__device__ __forceinline__ float kura_wrap(float v) {
+    const float two_pi = 2.0f * 3.14159265358979323846f;
+    if (v > 0.0f && v < two_pi) return v;
+    return v - floorf(v / two_pi) * two_pi;
+}
+
+// Consumer steps for the Kuramoto model with Kuramoto coupling delivered directly and Heun integration
+// (deterministic or stochastic), NPT nodes per thread, no trajectory and no coupling-sum output: the
+// operations of stream_node_step in the same order, with two exact shortcuts. The corrector's derivative
+// equals the predictor's (c + omega does not depend on the phase, dfun.rs:480-492), so the predictor
+// state is not formed; and the sin / cos of the phase that post() takes (coupling.rs:323-399) are the
+// values the previous step published (sinf / cosf of the same float), so each step evaluates them once.
+// Per-point BOLD is sampled as in the general loop.
+template <int NPT, bool STOCH, bool NOISE_SMEM>
+__device__ __forceinline__ void stream_consume_kuramoto(float (&x)[NPT][1], float (&tv)[NPT][1], const bool (&active)[NPT],
+                                                        const float (&om)[NPT], float cpk, float nsc, float dt_half,
+                                                        const float* gxbuf, const float* nzbuf, const float* noise_g,
+                                                        size_t nstride, float* ring, int n0, int t, int n_cons, int ns,
+                                                        int RPX, int RP, int wpos, int64_t s, const RunArgs& a, int b, int B,
+                                                        float (&bacc)[NPT][HB_MAX_BOLD], int (&bcnt)[NPT][HB_MAX_BOLD],
+                                                        int n_blocks, int nthreads, int C, uint64_t* hbar) {
+    constexpr int K = HB_STREAM_K;
+    float sn[NPT], cs[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; q++) { sn[q] = sinf(x[q][0]); cs[q] = cosf(x[q][0]); }
+    // BOLD: the window sums grow every step; the window counts and the emissions (stream_bold_sample) are
+    // settled only at the steps where a monitor's window closes or the run's last step emits a partial
+    // window. `until` counts the steps to the next such step (the current one included); `pend` the steps
+    // whose counts are not yet added.
+    const bool bold = a.bold.n > 0;
+    int until = bold ? stream_bold_until(a, bcnt[0], s) : 0, pend = 0;
+    for (int blk = 0; blk < n_blocks; blk++) {
+        const int buf = blk & 1;
+        named_sync(HB_BAR_FULL0 + buf, nthreads);
+        const int it0 = blk * K;
+        const int nb = (a.n_steps - it0) < K ? (a.n_steps - it0) : K;
+        const float2* gb = reinterpret_cast<const float2*>(gxbuf) + (size_t)buf * K * ns;
+        const float* nbuf = nzbuf + (size_t)buf * K * ns;
+#pragma unroll 1
+        for (int j = 0; j < nb; j++, s++) {
+            const int pos = wpos;
+            wpos = (wpos + 1 == RP) ? 0 : wpos + 1;
+#pragma unroll
+            for (int q = 0; q < NPT; q++) {
+                if (!active[q]) continue;
+                const int l = t + q * n_cons, n = n0 + l;
+                const float2 g = gb[(size_t)j * ns + l];
+                float nz = 0.0f;
+                if (STOCH) nz = (NOISE_SMEM ? nbuf[(size_t)j * ns + l] : __ldcs(noise_g + (size_t)(it0 + j) * nstride + n)) * nsc;
+                const float ct = cs[q] * g.x;
+                const float st = sn[q] * g.y;
+                const float cc = (ct - st) * cpk;
+                const float k1 = cc + om[q];
+                float xn = STOCH ? (x[q][0] + (k1 + k1) * dt_half) + nz : x[q][0] + (k1 + k1) * dt_half;
+                xn = kura_wrap(xn);
+                x[q][0] = xn;
+                tv[q][0] = tv[q][0] + xn;
+                if (bold) {
+                    if (until == 1) {
+#pragma unroll
+                        for (int m = 0; m < HB_MAX_BOLD; m++) bcnt[q][m] += pend;
+                        stream_bold_sample(a, b, B, n, s, xn, bacc[q], bcnt[q]);
+                    } else {
+#pragma unroll
+                        for (int m = 0; m < HB_MAX_BOLD; m++)
+                            if (m < a.bold.n) bacc[q][m] = bacc[q][m] + xn;
+                    }
+                }
+                sn[q] = sinf(xn);
+                cs[q] = cosf(xn);
+                float* r = ring + ((size_t)n * RPX + pos) * 2;
+                *reinterpret_cast<float2*>(r) = make_float2(sn[q], cs[q]);
+                if (pos < K) *reinterpret_cast<float2*>(r + (size_t)RP * 2) = make_float2(sn[q], cs[q]);
+            }
+            if (bold) {
+                if (until == 1) {
+                    pend = 0;
+                    until = stream_bold_until(a, bcnt[0], s + 1);
+                } else {
+                    pend++;
+                    until--;
+                }
+            }
+        }
+        __threadfence_block();
+        named_arrive(HB_BAR_EMPTY0 + buf, nthreads);
+        if (C > 1) stream_signal_block(hbar, blk, C, n_cons);
+    }
+#pragma unroll
+    for (int q = 0; q < NPT; q++)
+#pragma unroll
+        for (int m = 0; m < HB_MAX_BOLD; m++) bcnt[q][m] += pend;
 }
 
 // copy of a network description into shared memory by all threads of the block (no barrier)
@@ -479,64 +597,135 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             const int64_t sb = a.s0 + it0;
             const int sbm = (int)(sb % RP);
             float* gb = gxbuf + (size_t)buf * K * ns * PCH;
-            for (int r = 0; r < rounds; r++) {
-                const int item = p + r * n_prod;
-                const int islot = item / PL, lane = item - (item / PL) * PL;
-                const int node = islot < ns ? s_porder[islot] : islot;
-                float acc[K][PCH];
-#pragma unroll
-                for (int j = 0; j < K; j++)
-#pragma unroll
-                    for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
-                if (node < ns) {
+            if (a.stream_wgather) {
+                // warp-cooperative gather: warp w takes the slice's nodes w, w + nwarp, ... in producer order
+                // (decreasing in-degree), 32 of the node's edges at a time. Lane j decodes edge j of the chunk
+                // (history offset of its window, weight); the window of chunk edge k = 4u + slot is then read
+                // by the 8 lanes of that slot, lane (slot, stp) taking entry stp (step stp of the block), so
+                // one load instruction covers 4 edges as 4 runs of 32 PCH contiguous bytes; each lane sums
+                // its step over its slot's edges, and the 4 slots' sums are added by shuffles.
+                const int lane = t & 31, wid = p >> 5, nwarp = n_prod >> 5;
+                const int slot = lane >> 3, stp = lane & (K - 1);
+                for (int i = wid; i < ns; i += nwarp) {
+                    const int node = s_porder[i];
                     const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
-                    if constexpr (DB == 1) {
-#pragma unroll UNR
-                        for (int e = e0 + lane; e < e1; e += PL) {
-                            if (pf) stream_edge_prefetch<PCH>(ring, ed, e + pf * PL, e1, sbm, RP, RPX);
-                            if (a.exact_sums) stream_edge_acc<PCH, true>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
-                            else stream_edge_acc<PCH>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
+                    float acc[PCH];
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) acc[c] = 0.0f;
+                    for (int eb = e0; eb < e1; eb += 32) {
+                        const int cnt = (e1 - eb) < 32 ? (e1 - eb) : 32;
+                        // lanes past the row read entries RP + K .. RP + 2K - 1 of row 0, which nothing writes
+                        // (cleared when a run starts), with weight 0
+                        uint32_t off = (uint32_t)(RP + K) * PCH, src = 0;
+                        float w = 0.0f;
+                        if (lane < cnt) {
+                            const uint32_t m = ed[eb + lane];
+                            int pos = sbm - (int)(m >> 16);
+                            pos += (pos < 0) ? RP : 0;
+                            src = m & 0xffffu;
+                            off = (src * (uint32_t)RPX + (uint32_t)pos) * PCH;
+                            w = ew[eb + lane];
                         }
-                    } else {
-                        // the edge descriptors DB at a time, loaded together, so that their latency is
-                        // paid once per batch instead of before every window read; the batch is
-                        // consumed in order by rotating it through registers
-                        for (int eb = e0 + lane; eb < e1; eb += DB * PL) {
-                            uint32_t mb[DB];
-                            float wb[DB];
+                        float v[8][PCH], wk[8];
 #pragma unroll
-                            for (int u = 0; u < DB; u++) {
-                                const int e = eb + u * PL;
-                                mb[u] = (e < e1) ? ed[e] : 0u;
-                                wb[u] = (e < e1) ? ew[e] : 0.0f;
-                            }
-                            const int cnt = (e1 - eb + PL - 1) / PL < DB ? (e1 - eb + PL - 1) / PL : DB;
-#pragma unroll UNR
-                            for (int u = 0; u < cnt; u++) {
-                                const uint32_t m = mb[0];
-                                const float w = wb[0];
+                        for (int u = 0; u < 8; u++) {
+                            const int k = 4 * u + slot;  // lanes with k >= cnt read the zero entries
+                            const uint32_t o = __shfl_sync(0xffffffffu, off, k) + (uint32_t)(stp * PCH);
+                            wk[u] = __shfl_sync(0xffffffffu, w, k);
+                            if (PCH == 2) {
+                                const float2 f = *reinterpret_cast<const float2*>(ring + o);
+                                v[u][0] = f.x;
+                                v[u][PCH - 1] = f.y;
+                            } else v[u][0] = ring[o];
+                        }
 #pragma unroll
-                                for (int q = 0; q + 1 < DB; q++) { mb[q] = mb[q + 1]; wb[q] = wb[q + 1]; }
-                                if (pf) stream_edge_prefetch<PCH>(ring, ed, eb + (u + pf) * PL, e1, sbm, RP, RPX);
-                                if (a.exact_sums) stream_edge_acc<PCH, true>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
-                                else stream_edge_acc<PCH>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                        for (int u = 0; u < 8; u++)
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) acc[c] = __fmaf_rn(wk[u], v[u][c], acc[c]);
+                        if (sb == 0) {
+                            // step 0 also reads the current state (runtime.rs:166-170)
+#pragma unroll
+                            for (int u = 0; u < 8; u++) {
+                                const int k = 4 * u + slot;
+                                const uint32_t sk = __shfl_sync(0xffffffffu, src, k);
+                                if (stp == 0 && k < cnt) {
+                                    const float* q0 = ring + (size_t)sk * RPX * PCH;
+#pragma unroll
+                                    for (int c = 0; c < PCH; c++) acc[c] += wk[u] * q0[c];
+                                }
                             }
                         }
                     }
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) {
+                        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
+                        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+                    }
+                    if (slot == 0 && stp < nb) {
+#pragma unroll
+                        for (int c = 0; c < PCH; c++) gb[((size_t)stp * ns + node) * PCH + c] = acc[c];
+                    }
                 }
-                for (int o = PL >> 1; o > 0; o >>= 1) {
+            } else {
+                for (int r = 0; r < rounds; r++) {
+                    const int item = p + r * n_prod;
+                    const int islot = item / PL, lane = item - (item / PL) * PL;
+                    const int node = islot < ns ? s_porder[islot] : islot;
+                    float acc[K][PCH];
 #pragma unroll
                     for (int j = 0; j < K; j++)
 #pragma unroll
-                        for (int c = 0; c < PCH; c++) acc[j][c] += __shfl_xor_sync(0xffffffffu, acc[j][c], o);
-                }
-                if (node < ns && lane == 0) {
+                        for (int c = 0; c < PCH; c++) acc[j][c] = 0.0f;
+                    if (node < ns) {
+                        const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
+                        if constexpr (DB == 1) {
+#pragma unroll UNR
+                            for (int e = e0 + lane; e < e1; e += PL) {
+                                if (pf) stream_edge_prefetch<PCH>(ring, ed, e + pf * PL, e1, sbm, RP, RPX);
+                                if (a.exact_sums) stream_edge_acc<PCH, true>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
+                                else stream_edge_acc<PCH>(ring, ed[e], ew[e], sbm, RP, RPX, sb == 0, acc);
+                            }
+                        } else {
+                            // the edge descriptors DB at a time, loaded together, so that their latency is
+                            // paid once per batch instead of before every window read; the batch is
+                            // consumed in order by rotating it through registers
+                            for (int eb = e0 + lane; eb < e1; eb += DB * PL) {
+                                uint32_t mb[DB];
+                                float wb[DB];
 #pragma unroll
-                    for (int j = 0; j < K; j++)
-                        if (j < nb) {
+                                for (int u = 0; u < DB; u++) {
+                                    const int e = eb + u * PL;
+                                    mb[u] = (e < e1) ? ed[e] : 0u;
+                                    wb[u] = (e < e1) ? ew[e] : 0.0f;
+                                }
+                                const int cnt = (e1 - eb + PL - 1) / PL < DB ? (e1 - eb + PL - 1) / PL : DB;
+#pragma unroll UNR
+                                for (int u = 0; u < cnt; u++) {
+                                    const uint32_t m = mb[0];
+                                    const float w = wb[0];
 #pragma unroll
-                            for (int c = 0; c < PCH; c++) gb[((size_t)j * ns + node) * PCH + c] = acc[j][c];
+                                    for (int q = 0; q + 1 < DB; q++) { mb[q] = mb[q + 1]; wb[q] = wb[q + 1]; }
+                                    if (pf) stream_edge_prefetch<PCH>(ring, ed, eb + (u + pf) * PL, e1, sbm, RP, RPX);
+                                    if (a.exact_sums) stream_edge_acc<PCH, true>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                                    else stream_edge_acc<PCH>(ring, m, w, sbm, RP, RPX, sb == 0, acc);
+                                }
+                            }
                         }
+                    }
+                    for (int o = PL >> 1; o > 0; o >>= 1) {
+#pragma unroll
+                        for (int j = 0; j < K; j++)
+#pragma unroll
+                            for (int c = 0; c < PCH; c++) acc[j][c] += __shfl_xor_sync(0xffffffffu, acc[j][c], o);
+                    }
+                    if (node < ns && lane == 0) {
+#pragma unroll
+                        for (int j = 0; j < K; j++)
+                            if (j < nb) {
+#pragma unroll
+                                for (int c = 0; c < PCH; c++) gb[((size_t)j * ns + node) * PCH + c] = acc[j][c];
+                            }
+                    }
                 }
             }
             if (stoch && a.stream_noise_smem) {
@@ -614,7 +803,24 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             }
 #undef HB_SC
         }
-        for (int blk = 0; blk < (straight ? 0 : n_blocks); blk++) {
+        const bool kura = MODEL == HBM_KURAMOTO && PRE == PRE_KURA && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) &&
+                          P.cfk == HBC_KURAMOTO && P.direct && a.traj == nullptr && a.gx_out == nullptr;
+        if constexpr (MODEL == HBM_KURAMOTO && PRE == PRE_KURA) {
+            if (kura) {
+                float om[NPT];
+#pragma unroll
+                for (int q = 0; q < NPT; q++) om[q] = NPT == 1 ? prm[0] : s_prm[(size_t)(active[q] ? t + q * n_cons : 0) * PU];
+                const float nsc = net.noise_scale[0];
+#define HB_SK(ST, NS) stream_consume_kuramoto<NPT, ST, NS>(x, tv, active, om, cp[1], nsc, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n0, t, n_cons, ns, RPX, RP, wpos, s, a, b, B, bacc, bcnt, n_blocks, nthreads, C, hist_bar)
+                if (integ == HBI_HEUN_STOCH) {
+                    if (a.stream_noise_smem) HB_SK(true, true);
+                    else HB_SK(true, false);
+                } else HB_SK(false, false);
+#undef HB_SK
+            }
+        }
+        const bool general = !straight && !(kura && MODEL == HBM_KURAMOTO && PRE == PRE_KURA);
+        for (int blk = 0; blk < (general ? n_blocks : 0); blk++) {
             const int buf = blk & 1;
             named_sync(HB_BAR_FULL0 + buf, nthreads);
             const int it0 = blk * K;
