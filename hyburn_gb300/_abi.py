@@ -65,7 +65,7 @@ HB_RUN_TEST_UNSET_WAIT = 1 << 30
 
 def HB_RUN_STREAM_CLUSTER(n: int) -> int:
     """Streamed-history kernel: CTAs per sweep point (a thread-block cluster splitting its nodes)."""
-    return {1: 1, 2: 2, 4: 3, 8: 4}.get(int(n), 0) << 4
+    return {1: 1, 2: 2, 4: 3, 8: 4, 3: 5, 5: 6, 6: 7}.get(int(n), 0) << 4
 
 
 # the run flags that choose a kernel form or its lane counts (what the autotuner chooses)

@@ -77,7 +77,7 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
                 out.append((f"streamed history {npt} node(s) per thread", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_NPT(npt)))
             # CTAs per point: a point's nodes split over a cluster (fewer points in flight, histories in L2)
             nodes = config.network.subnetworks[0].nnodes
-            for c in (2, 4, 8):
+            for c in (2, 4, 5, 6, 8):
                 if nodes >= 16 * c:
                     out.append((f"streamed history, {c} CTAs per point", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_CLUSTER(c)))
         undelayed = not projs[0].delays or max(projs[0].delays) == 0

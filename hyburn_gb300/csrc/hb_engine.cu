@@ -35,6 +35,9 @@ cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const Ru
 int hb_stream_budget_1(int model, int pre);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
+int hb_stream_clusters_1(int model, int pre, int C, int threads, size_t smem);
+int hb_stream_clusters_2(int model, int pre, int C, int threads, size_t smem);
+int hb_stream_clusters_4(int model, int pre, int C, int threads, size_t smem);
 cudaError_t hb_launch_single(int model, int m, const DevNet* d_net, const RunArgs& a, int B, cudaStream_t st);
 // hb_dense_tc.cu
 int hb_dense_tc_tmem_columns(int model, int nm);
@@ -739,25 +742,59 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
         !(run_flags & HB_RUN_GLOBAL_RING)) {
         const int nm_all = e->subs[0].nm, nvar0 = e->subs[0].nvar;
         const int pch = (fast == 1) ? 2 : e->subs[0].ncvar;
+        // consumer threads per CTA: one node per thread (512 threads) for up to 96 nodes, else two (1024
+        // threads, at least 256 producers); four (768 threads, two edge windows in flight per producer) on
+        // request
+        const int want = (int)((run_flags >> 24) & 0x7);
+        auto plan_threads = [&](int nmx, int& np_, int& nt_) {
+            auto fits = [&](int k, int nt) { return ((nmx + k - 1) / k + 31) / 32 * 32 + (nt == 512 ? 128 : 256) <= nt; };
+            np_ = 0;
+            nt_ = 0;
+            if (want == 1 || (want == 0 && nmx <= 96)) { if (fits(1, 512)) { np_ = 1; nt_ = 512; } }
+            else if (want == 4) { if (fits(4, 768)) { np_ = 4; nt_ = 768; } }
+            else if (fits(2, 1024)) { np_ = 2; nt_ = 1024; }
+        };
         // CTAs per point: a thread-block cluster splitting the point's nodes (HB_RUN_STREAM_CLUSTER), so
         // that fewer points are in flight and their histories stay in L2
         {
+            static const int code_to_c[8] = {0, 1, 2, 4, 8, 3, 5, 6};
             const int v = (int)((run_flags >> 4) & 0x7);
             if (v == 0) {
-                // engine's choice: split each point over a cluster when the histories of the points in flight
-                // (one CTA per SM) would not fit in about 96 MB of the 129 MB L2, keeping 64 nodes per CTA
+                // engine's choice among 1..6 and 8 CTAs per point (at least 64 nodes per CTA): the size whose
+                // resident clusters (one point each, as the device's cluster occupancy reports them) keep the
+                // histories in flight within about 100 MB of the 129 MB L2, then the most SMs busy
                 int dev = 0, sms = 152;
                 if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
                 const int rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
                 const double hist = (double)nm_all * (rp + 2 * HB_STREAM_K) * pch * 4;
+                static const int cand[7] = {1, 2, 3, 4, 5, 6, 8};
+                double best = -1.0;
+                bool best_fit = false;
                 stream_cluster = 1;
-                for (int c = 2; c <= 8; c *= 2) {
-                    if (std::min<double>(B, (double)sms / (c / 2)) * hist <= 96e6 || nm_all / c < 64) break;
-                    stream_cluster = c;
+                for (int c : cand) {
+                    if (c > 1 && nm_all / c < 64) continue;
+                    const int nmx = (nm_all + c - 1) / c;
+                    int np_ = 0, nt_ = 0;
+                    plan_threads(nmx, np_, nt_);
+                    if (!np_) continue;
+                    const size_t smem_est = (size_t)2 * HB_STREAM_K * nmx * pch * 4 + (size_t)nmx * 16 + 1024;
+                    const int cap = c == 1 ? sms
+                                  : np_ == 1 ? hb_stream_clusters_1(e->kernel_model, fast, c, nt_, smem_est)
+                                  : np_ == 2 ? hb_stream_clusters_2(e->kernel_model, fast, c, nt_, smem_est)
+                                             : hb_stream_clusters_4(e->kernel_model, fast, c, nt_, smem_est);
+                    if (cap <= 0) continue;
+                    const double inflight = std::min<double>(B, cap);
+                    const bool fit = inflight * hist <= 100e6;
+                    const double score = inflight * c;  // SMs busy
+                    if (best < 0 || (fit && !best_fit) || (fit == best_fit && score > best)) {
+                        best = score;
+                        best_fit = fit;
+                        stream_cluster = c;
+                    }
                 }
-            } else stream_cluster = 1 << (v - 1);
+            } else stream_cluster = code_to_c[v];
             if (stream_cluster > 8 || stream_cluster > nm_all)
-                return fail(HB_ERR_INVALID_STATE, "HB_RUN_STREAM_CLUSTER: 1, 2, 4 or 8 CTAs per point, at most one per node");
+                return fail(HB_ERR_INVALID_STATE, "HB_RUN_STREAM_CLUSTER: 1 to 6 or 8 CTAs per point, at most one per node");
         }
         const int SC = stream_cluster;
         const int nm0 = (nm_all + SC - 1) / SC;  // nodes of the largest slice
@@ -766,14 +803,8 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
             const int a0 = (int)(((long long)nm_all * r) / SC), a1 = (int)(((long long)nm_all * (r + 1)) / SC);
             slice_edges = std::max(slice_edges, (size_t)(e->projs[0].rowptr[a1] - e->projs[0].rowptr[a0]));
         }
-        // nodes per consumer thread: one (512 threads) for up to 96 nodes, else two (1024 threads, at
-        // least 256 producers); four (768 threads, two edge windows in flight per producer) on request
-        auto fits = [&](int k, int nt) { return ((nm0 + k - 1) / k + 31) / 32 * 32 + (nt == 512 ? 128 : 256) <= nt; };
-        const int want = (int)((run_flags >> 24) & 0x7);
         int npt = 0, threads = 0;
-        if (want == 1 || (want == 0 && nm0 <= 96)) { if (fits(1, 512)) { npt = 1; threads = 512; } }
-        else if (want == 4) { if (fits(4, 768)) { npt = 4; threads = 768; } }
-        else if (fits(2, 1024)) { npt = 2; threads = 1024; }
+        plan_threads(nm0, npt, threads);
         const int sbudget = npt == 1 ? hb_stream_budget_1(e->kernel_model, fast)
                           : npt == 2 ? hb_stream_budget_2(e->kernel_model, fast)
                           : npt == 4 ? hb_stream_budget_4(e->kernel_model, fast) : -1;

@@ -1004,6 +1004,29 @@ int stream_max_dynamic_smem() {
     return cached;
 }
 
+// thread-block clusters of C CTAs that can be resident at once (one point each), or -1
+template <int MODEL, int PRE, int NPT, int MAXT>
+int stream_cluster_capacity(int C, int threads, size_t smem) {
+    if (stream_max_dynamic_smem<MODEL, PRE, NPT, MAXT>() < 0) return -1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(C * 64));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, stream_pipe_kernel<MODEL, PRE, NPT, MAXT>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return n;
+}
+
 template <int MODEL, int PRE, int NPT, int MAXT>
 cudaError_t launch_stream(const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st) {
     int maxdyn = stream_max_dynamic_smem<MODEL, PRE, NPT, MAXT>();
@@ -1037,6 +1060,9 @@ cudaError_t hb_launch_stream_1(int model, int pre, const DevNet* d_net, const Ru
 cudaError_t hb_launch_stream_2(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 cudaError_t hb_launch_stream_4(int model, int pre, const DevNet* d_net, const RunArgs& a, int B, int threads, size_t smem, cudaStream_t st);
 int hb_stream_budget_1(int model, int pre);
+int hb_stream_clusters_1(int model, int pre, int C, int threads, size_t smem);
+int hb_stream_clusters_2(int model, int pre, int C, int threads, size_t smem);
+int hb_stream_clusters_4(int model, int pre, int C, int threads, size_t smem);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
 cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
@@ -1063,6 +1089,19 @@ int hb_stream_queue_budget_4();
         int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
         if (i < 0 || i >= 12) return cudaErrorInvalidValue;                                                          \
         return tab[i](d_net, a, B, threads, smem, st);                                                               \
+    }                                                                                                                \
+    int hb_stream_clusters_##NPT_(int model, int pre, int C, int threads, size_t smem) {                             \
+        using H = int (*)(int, int, size_t);                                                                         \
+        static const H tab[12] = {                                                                                   \
+            hb::stream_cluster_capacity<0, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<0, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_cluster_capacity<1, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<1, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_cluster_capacity<2, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<2, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_cluster_capacity<3, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<3, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_cluster_capacity<4, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<4, hb::PRE_KURA, NPT_, MAXT_>, \
+            hb::stream_cluster_capacity<5, hb::PRE_ID, NPT_, MAXT_>, hb::stream_cluster_capacity<5, hb::PRE_KURA, NPT_, MAXT_>}; \
+        int i = model * 2 + (pre == hb::PRE_KURA ? 1 : 0);                                                           \
+        if (i < 0 || i >= 12) return -1;                                                                             \
+        return tab[i](C, threads, smem);                                                                             \
     }                                                                                                                \
     int hb_stream_budget_##NPT_(int model, int pre) {                                                                \
         using G = int (*)();                                                                                         \

@@ -98,11 +98,14 @@ typedef int32_t hb_status;
    with two edge windows in flight per producer; 0 lets the engine choose). A grouped launch uses 4 when
    every member asks for it. */
 #define HB_RUN_STREAM_NPT(n)  ((uint32_t)((n) & 0x7) << 24)
-/* streamed-history kernel: CTAs per sweep point (1, 2, 4 or 8; 0 lets the engine choose). With more than
-   one, each point's nodes are split over a thread-block cluster of that many CTAs, so that fewer points
-   are in flight and their histories stay in L2; the CTAs of a point exchange the history through
-   global memory and signal each finished block of steps to each other. Grouped launches use one. */
-#define HB_RUN_STREAM_CLUSTER(n) ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : 0) << 4)
+/* streamed-history kernel: CTAs per sweep point (1, 2, 3, 4, 5, 6 or 8; 0 lets the engine choose). With
+   more than one, each point's nodes are split over a thread-block cluster of that many CTAs, so that fewer
+   points are in flight and their histories stay in L2; the CTAs of a point exchange the history through
+   global memory and signal each finished block of steps to each other. The engine's choice takes the
+   size whose resident clusters keep the histories in flight within about 100 MB of L2 with the most SMs
+   busy. Grouped launches use one. */
+#define HB_RUN_STREAM_CLUSTER(n) \
+    ((uint32_t)((n) == 1 ? 1 : (n) == 2 ? 2 : (n) == 4 ? 3 : (n) == 8 ? 4 : (n) == 3 ? 5 : (n) == 5 ? 6 : (n) == 6 ? 7 : 0) << 4)
 /* streamed-history kernel: prefetch the history runs of upcoming edges into L2 */
 #define HB_RUN_STREAM_PREFETCH (1u << 27)
 /* warp-specialised pipeline: use its 1024-thread form (room for eight producer threads per node) */

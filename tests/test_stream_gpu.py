@@ -110,7 +110,7 @@ def test_history_layout_cannot_change_mid_simulation():
     assert np.isfinite(eng.states[0]).all()
 
 
-@pytest.mark.parametrize("C,npt", [(2, 2), (4, 1), (4, 2), (8, 1), (8, 2)])
+@pytest.mark.parametrize("C,npt", [(2, 2), (3, 2), (4, 1), (4, 2), (5, 2), (6, 2), (8, 1), (8, 2)])
 def test_stream_cluster_split_kuramoto(C, npt):
     """One point's 1000 nodes split over a cluster of C CTAs (HB_RUN_STREAM_CLUSTER): the CTAs read
     each other's history through global memory after each block's cluster-scope signal; per-node
@@ -125,7 +125,7 @@ def test_stream_cluster_split_kuramoto(C, npt):
     assert kind(eng) == STREAM_KIND
 
 
-@pytest.mark.parametrize("C", [2, 8])
+@pytest.mark.parametrize("C", [2, 6, 8])
 def test_stream_cluster_split_stochastic_chunked(C):
     """Uneven slices (74 nodes over C CTAs), shared noise staged per slice, trajectories, runs split
     across calls: the same results as the oracle."""
