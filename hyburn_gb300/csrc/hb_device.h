@@ -210,6 +210,7 @@ struct HbKuraAdjLaunch {
     const float* traj;   // [T][B][N] phases after each step
     const float* x0;     // [B][N] initial phases
     int B, N, T, K;      // K: steps per reverse block (<= 8 and <= every delay)
+    int maxd;            // largest edge delay
     float dt;
     const float* k;      // [B] the coupling's a / N as the engine resolves it
     const int* rowptr; const uint32_t* edges; const float* ew;          // CSR by target

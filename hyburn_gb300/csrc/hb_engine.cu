@@ -723,7 +723,8 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     // engine's ring (longest delay + their barrier interval)
     const int R_run = pipe >= 0 ? std::max(e->H, 1) + 1 : e->R;
     e->net.R = R_run;
-    const size_t ring_bytes = (size_t)R_run * e->cols * 4;
+    // (the pipeline's ring in shared memory carries 8 mirror slots, one block of steps, after its R slots)
+    const size_t ring_bytes = (size_t)(R_run + (pipe >= 0 ? 8 : 0)) * e->cols * 4;
     size_t edges = 0;
     for (auto& hp : e->projs) if (hp.kind == W_SPARSE) edges += hp.edges.size();
     const size_t edge_bytes = ((edges * 8) + 15) & ~(size_t)15;
@@ -1794,6 +1795,7 @@ hb_status hb_engine_adjoint_order(hb_engine* e, const float* gain_values, int32_
     HbKuraAdjLaunch L;
     memset(&L, 0, sizeof L);
     L.traj = e->dtraj.p; L.x0 = e->x0.p; L.B = B; L.N = N; L.T = T; L.K = K; L.dt = e->net.dt; L.k = d_k.p;
+    L.maxd = hp.maxd;
     L.rowptr = hp.d_rowptr; L.edges = hp.d_edges; L.ew = hp.d_ew;
     L.cptr = d_cptr.p; L.ctgt = d_ctgt.p; L.cdel = d_cdel.p; L.cw = d_cw.p;
     L.sc = d_sc.p; L.z = d_z.p; L.nu = d_nu.p; L.loss = d_loss.p; L.gA = d_gA.p; L.gW = d_gW.p; L.gWn = d_gWn.p;

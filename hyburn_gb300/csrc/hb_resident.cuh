@@ -962,7 +962,7 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
                                                          const float* gxbuf, const float* nzbuf, float* ring,
                                                          int n, bool active, int nm, int cols, int R, int slot,
                                                          int n_steps, int n_blocks, int nthreads, uint64_t* nbar,
-                                                         int* err, float* traj, size_t traj_stride) {
+                                                         int* err, float* traj, size_t traj_stride, bool mirror) {
     constexpr int PK = HB_PIPE_K;
     const float ca = cp[0], cb = cp[1], c2 = cp[2], c3 = cp[3], c4 = cp[4];
     float ns[NVAR];
@@ -1018,6 +1018,10 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
             for (int v = 0; v < NVAR; v++) tv[v] = tv[v] + x[v];
             ring[slot * cols + n * NCV] = x[0];
             if (NCV > 1) ring[slot * cols + n * NCV + 1] = x[1];
+            if (mirror && slot < PK) {
+                ring[(slot + R) * cols + n * NCV] = x[0];
+                if (NCV > 1) ring[(slot + R) * cols + n * NCV + 1] = x[1];
+            }
             if (traj) {
                 float* tr = traj + (size_t)(blk * PK + j) * traj_stride;
 #pragma unroll
@@ -1055,7 +1059,10 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
     // shared layout: ring | gx buffers [2][PK][nm][PCH] | noise buffers [2][PK][nm*NVAR] | edges
     size_t off = 0;
     float* ring;
-    if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)ring_words * sizeof(float); }
+    // a ring in shared memory carries PK mirror slots after its R slots (slot R + q holds slot q), so that
+    // a producer's window of PK consecutive slots never wraps
+    const bool mirror = a.ring_in_smem != 0;
+    if (a.ring_in_smem) { ring = reinterpret_cast<float*>(smem); off = (size_t)(ring_words + PK * cols) * sizeof(float); }
     else ring = a.ring + (size_t)b * ring_stride;
     off = (off + 15) & ~(size_t)15;
     float* gxbuf = reinterpret_cast<float*>(smem + off);
@@ -1079,6 +1086,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
         const int n4 = ring_words >> 2;
         for (int i = t; i < n4; i += nthreads) r4[i] = g[i];
         for (int i = (n4 << 2) + t; i < ring_words; i += nthreads) ring[i] = a.ring[(size_t)b * ring_stride + i];
+        for (int i = t; i < PK * cols; i += nthreads) ring[ring_words + i] = a.ring[(size_t)b * ring_stride + i];
     }
     for (int i = t; i <= nm; i += nthreads) s_rowptr[i] = P.rowptr[i];
     const bool edges_smem = P.smem_edges >= 0;
@@ -1133,6 +1141,10 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
     if (active) {
         ring[slot * cols + n * NCV] = x[0];
         if (NCV > 1) ring[slot * cols + n * NCV + 1] = x[1];
+        if (mirror && slot < PK) {
+            ring[(slot + R) * cols + n * NCV] = x[0];
+            if (NCV > 1) ring[(slot + R) * cols + n * NCV + 1] = x[1];
+        }
     }
     __syncthreads();
 
@@ -1187,7 +1199,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                         int a0 = base + eo[e];
                         a0 = a0 < 0 ? a0 + ring_words : a0;
                         const float w = ew[e];
-                        if (a0 + (PK - 1) * cols < ring_words) {
+                        if (mirror || a0 + (PK - 1) * cols < ring_words) {
 #pragma unroll
                             for (int j = 0; j < PK; j++) term(j, w, a0 + j * cols);
                         } else {
@@ -1316,7 +1328,7 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
 #pragma unroll
             for (int v = 0; v < 8; v++) nscale[v] = net.noise_scale[v];
             uint64_t* nb_ = use_bulk ? noise_bar : nullptr;
-#define HB_STRAIGHT(ST, SF, CF) pipe_consume_heun_linear<MODEL, NVAR, NCV, ST, SF, CF>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, nb_, a.flags + 1, trj, trs)
+#define HB_STRAIGHT(ST, SF, CF) pipe_consume_heun_linear<MODEL, NVAR, NCV, ST, SF, CF>(x, tv, prm, cp, nscale, dt, dt_half, gxbuf, nzbuf, ring, n, active, nm, cols, R, slot, a.n_steps, n_blocks, nthreads, nb_, a.flags + 1, trj, trs, mirror)
             if (cfk == HBC_SIGMOIDAL) {
                 if (integ == HBI_HEUN_STOCH) { if (sweep_form) HB_STRAIGHT(true, true, HBC_SIGMOIDAL); else HB_STRAIGHT(true, false, HBC_SIGMOIDAL); }
                 else { if (sweep_form) HB_STRAIGHT(false, true, HBC_SIGMOIDAL); else HB_STRAIGHT(false, false, HBC_SIGMOIDAL); }
@@ -1458,6 +1470,10 @@ __global__ void __launch_bounds__(MAXT, 1) resident_pipe_kernel(const DevNet* __
                     sl1 = sl1 >= R ? sl1 - R : sl1;
                     ring[sl1 * cols + n * NCV] = x[0];
                     if (NCV > 1) ring[sl1 * cols + n * NCV + 1] = x[1];
+                    if (mirror && sl1 < PK) {
+                        ring[(sl1 + R) * cols + n * NCV] = x[0];
+                        if (NCV > 1) ring[(sl1 + R) * cols + n * NCV + 1] = x[1];
+                    }
                 }
                 slot = (slot + 1 == R) ? 0 : slot + 1;
             }
