@@ -975,8 +975,11 @@ __device__ __forceinline__ void pipe_consume_heun_linear(float* x, float* tv, co
         const int nb = (n_steps - blk * PK) < PK ? (n_steps - blk * PK) : PK;
         const float* gb = gxbuf + (size_t)buf * PK * nm * NCV + (size_t)n * NCV;
         const float* nbuf = nzbuf + (size_t)buf * PK * nm * NVAR + (size_t)n * NVAR;
-#pragma unroll 1
-        for (int j = 0; j < nb; j++) {
+        // the block's steps unrolled: the shared-memory reads of every step's coupling sums and draws
+        // do not depend on the state, so they can issue ahead of the state's dependency chain
+#pragma unroll
+        for (int j = 0; j < PK; j++) {
+            if (j >= nb) break;
             slot = (slot + 1 == R) ? 0 : slot + 1;
             if (!active) continue;  // threads past the last node only take part in the barriers
             float cc[2] = {0.0f, 0.0f};
