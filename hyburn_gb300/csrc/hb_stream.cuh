@@ -372,18 +372,20 @@ __device__ __forceinline__ float kura_wrap(float v) {
 }
 
 // Consumer steps for the Kuramoto model with Kuramoto coupling delivered directly and Heun integration
-// (deterministic or stochastic), NPT nodes per thread, no trajectory and no coupling-sum output: the
-// operations of stream_node_step in the same order, with two exact shortcuts. The corrector's derivative
+// (deterministic or stochastic), NPT nodes per thread, writing the trajectory and the coupling sums when
+// asked (as the general loop does): the operations of stream_node_step in the same order, with two exact
+// shortcuts. The corrector's derivative
 // equals the predictor's (c + omega does not depend on the phase, dfun.rs:480-492), so the predictor
 // state is not formed; and the sin / cos of the phase that post() takes (coupling.rs:323-399) are the
 // values the previous step published (sinf / cosf of the same float), so each step evaluates them once.
 // Per-point BOLD is sampled as in the general loop.
-template <int NPT, bool STOCH, bool NOISE_SMEM>
+template <int NPT, bool STOCH, bool NOISE_SMEM, bool OUTS>
 __device__ __forceinline__ void stream_consume_kuramoto(float (&x)[NPT][1], float (&tv)[NPT][1], const bool (&active)[NPT],
                                                         const float (&om)[NPT], float cpk, float nsc, float dt_half,
                                                         const float* gxbuf, const float* nzbuf, const float* noise_g,
                                                         size_t nstride, float* ring, int n0, int t, int n_cons, int ns,
                                                         int RPX, int RP, int wpos, int64_t s, const RunArgs& a, int b, int B,
+                                                        int N, size_t state_len,
                                                         float (&bacc)[NPT][HB_MAX_BOLD], int (&bcnt)[NPT][HB_MAX_BOLD],
                                                         int n_blocks, int nthreads, int C, uint64_t* hbar) {
     constexpr int K = HB_STREAM_K;
@@ -412,6 +414,7 @@ __device__ __forceinline__ void stream_consume_kuramoto(float (&x)[NPT][1], floa
                 if (!active[q]) continue;
                 const int l = t + q * n_cons, n = n0 + l;
                 const float2 g = gb[(size_t)j * ns + l];
+                if (OUTS && a.gx_out) __stcs(reinterpret_cast<float2*>(a.gx_out) + ((size_t)(it0 + j) * B + b) * N + n, g);
                 float nz = 0.0f;
                 if (STOCH) nz = (NOISE_SMEM ? nbuf[(size_t)j * ns + l] : __ldcs(noise_g + (size_t)(it0 + j) * nstride + n)) * nsc;
                 const float ct = cs[q] * g.x;
@@ -422,6 +425,7 @@ __device__ __forceinline__ void stream_consume_kuramoto(float (&x)[NPT][1], floa
                 xn = kura_wrap(xn);
                 x[q][0] = xn;
                 tv[q][0] = tv[q][0] + xn;
+                if (OUTS && a.traj) __stcs(a.traj + ((size_t)(it0 + j) * B + b) * state_len + n, xn);
                 if (bold) {
                     if (until == 1) {
 #pragma unroll
@@ -804,19 +808,21 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
 #undef HB_SC
         }
         const bool kura = MODEL == HBM_KURAMOTO && PRE == PRE_KURA && (integ == HBI_HEUN_STOCH || integ == HBI_HEUN_DET) &&
-                          P.cfk == HBC_KURAMOTO && P.direct && a.traj == nullptr && a.gx_out == nullptr;
+                          P.cfk == HBC_KURAMOTO && P.direct;
         if constexpr (MODEL == HBM_KURAMOTO && PRE == PRE_KURA) {
             if (kura) {
                 float om[NPT];
 #pragma unroll
                 for (int q = 0; q < NPT; q++) om[q] = NPT == 1 ? prm[0] : s_prm[(size_t)(active[q] ? t + q * n_cons : 0) * PU];
                 const float nsc = net.noise_scale[0];
-#define HB_SK(ST, NS) stream_consume_kuramoto<NPT, ST, NS>(x, tv, active, om, cp[1], nsc, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n0, t, n_cons, ns, RPX, RP, wpos, s, a, b, B, bacc, bcnt, n_blocks, nthreads, C, hist_bar)
+#define HB_SK(ST, NS) if (a.traj || a.gx_out) stream_consume_kuramoto<NPT, ST, NS, true>(HB_SK_ARGS); else stream_consume_kuramoto<NPT, ST, NS, false>(HB_SK_ARGS)
+#define HB_SK_ARGS x, tv, active, om, cp[1], nsc, dt_half, gxbuf, nzbuf, noise_base, nstride, ring, n0, t, n_cons, ns, RPX, RP, wpos, s, a, b, B, nm, (size_t)net.state_len, bacc, bcnt, n_blocks, nthreads, C, hist_bar
                 if (integ == HBI_HEUN_STOCH) {
                     if (a.stream_noise_smem) HB_SK(true, true);
                     else HB_SK(true, false);
                 } else HB_SK(false, false);
 #undef HB_SK
+#undef HB_SK_ARGS
             }
         }
         const bool general = !straight && !(kura && MODEL == HBM_KURAMOTO && PRE == PRE_KURA);
