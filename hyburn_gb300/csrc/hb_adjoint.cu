@@ -58,6 +58,9 @@ struct AdjArgs {
     float* ck_ring;       // [n_ck][B][R*N]
     float* scratch;       // [B][CK][N][8]  x(s), g(s) of the segment being reversed
     float* mu_ring;       // [B][R*N]
+    float* lam_g;         // [B][N*6] lambda carried between the segments' reverse launches
+    int seg_begin, seg_end, seg_last;  // the segment one reverse or re-computation launch covers (seg_last: the
+                                       // run's last segment, where the reverse starts)
     // statistics
     const float* target;  // [N][N] target FC
     float* mean;          // [B][N]
@@ -502,12 +505,24 @@ __device__ __forceinline__ void bar_arrive(int id, int count) { asm volatile("ba
 // over. The values read for block k + 1 are at least K steps old when block k starts, so the
 // consumers of block k never write them. Per step the same operations in the same order as
 // forward_steps (mode 0).
+constexpr int ADJ_BAR_CONS = 5;  // named barrier of the consumer threads alone
+
+// The forward steps [s_begin, s_end) as a producer / consumer pipeline, when every delay is at least
+// 2K - 1 steps: the first n_cons threads are consumers (thread t integrates node t), the others
+// producers (L lanes per node) that gather block k + 1's coupling sums into one of two buffers while
+// the consumers integrate block k from the other; named barriers hand the buffers over. The values
+// read for block k + 1 are at least K steps old when block k starts, so the consumers of block k never
+// write them. Per step the same operations in the same order as forward_steps. mode 0: the run's
+// forward (y(t); every step's x, g when store_all, else a checkpoint of the state and the ring at each
+// multiple of CK, taken by the consumers before they write the block); mode 1: re-computation of one
+// segment from its checkpoint, keeping x(s), g(s) in the scratch (rows relative to s_begin).
 template <bool RK4>
 __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, const AdjTables& tb, int b, int L,
-                                  float* x, const float* prm, const float* cp, int n_cons) {
-    const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K, T = A.T;
+                                  float* x, const float* prm, const float* cp, int n_cons, int s_begin, int s_end,
+                                  int mode) {
+    const int N = A.N, R = A.R, RN = A.R * A.N, K = A.K;
     const int t = threadIdx.x, nthreads = blockDim.x;
-    const int n_blocks = (T + K - 1) / K;
+    const int n_blocks = (s_end - s_begin + K - 1) / K;
     if (t >= n_cons) {
         const int p = t - n_cons;
         const int gi = p / L, gl = p - (p / L) * L;
@@ -516,7 +531,7 @@ __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, c
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             if (blk >= 2) bar_sync(ADJ_BAR_EMPTY0 + buf, nthreads);
-            const int s0 = blk * K, nb = (T - s0) < K ? (T - s0) : K;
+            const int s0 = s_begin + blk * K, nb = (s_end - s0) < K ? (s_end - s0) : K;
             float* gb = gbuf2 + (size_t)buf * K * N;
             int slot = s0 % R;
             for (int j = 0; j < nb; j++) {
@@ -543,21 +558,35 @@ __device__ void forward_pipelined(float* ring, float* gbuf2, const AdjArgs& A, c
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             bar_sync(ADJ_BAR_FULL0 + buf, nthreads);
-            const int s0 = blk * K, nb = (T - s0) < K ? (T - s0) : K;
+            const int s0 = s_begin + blk * K, nb = (s_end - s0) < K ? (s_end - s0) : K;
+            if (mode == 0 && !A.store_all && s0 % A.CK == 0) {
+                // checkpoint: the ring holds every time before s0 and no consumer has written block s0 yet
+                const int k = s0 / A.CK;
+                float* cr = A.ck_ring + ((size_t)k * A.B + b) * (size_t)RN;
+                for (int q = t; q < RN; q += n_cons) cr[q] = ring[q];
+                if (uact) {
+                    float* cs = A.ck_state + ((size_t)k * A.B + b) * N * NV + (size_t)t * NV;
+#pragma unroll
+                    for (int v = 0; v < NV; v++) cs[v] = x[v];
+                }
+                bar_sync(ADJ_BAR_CONS, n_cons);
+            }
             const float* gb = gbuf2 + (size_t)buf * K * N;
             if (uact) {
                 int slot = s0 % R;
                 for (int j = 0; j < nb; j++) {
                     const int s = s0 + j;
                     const float g = gb[j * N + t];
-                    float* sc = A.scratch + (((size_t)b * A.CK + s) * N + t) * 8;
+                    if (mode == 1 || A.store_all) {
+                        float* sc = A.scratch + (((size_t)b * A.CK + (s - s_begin)) * N + t) * 8;
 #pragma unroll
-                    for (int v = 0; v < NV; v++) sc[v] = x[v];
-                    sc[6] = g;
+                        for (int v = 0; v < NV; v++) sc[v] = x[v];
+                        sc[6] = g;
+                    }
                     adj_step<RK4>(A, prm, x, coupling_post(A.cfk, cp, g));
                     const int next = (slot + 1 == R) ? 0 : slot + 1;
                     ring[next * N + t] = x[0];
-                    A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
+                    if (mode == 0) A.Y[((size_t)s * A.B + b) * N + t] = x[1] - x[2];
                     slot = next;
                 }
             }
@@ -584,10 +613,32 @@ __global__ void adj_forward_kernel(const DevNet* __restrict__ gnet, AdjArgs A, i
     if (uact) ring[threadIdx.x] = x[0];
     if (n_cons > 0) {
         __syncthreads();
-        forward_pipelined<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons);
+        forward_pipelined<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons, 0, A.T, 0);
     } else {
         forward_steps<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, 0, A.T, 0);
     }
+}
+
+// Re-computation of one checkpoint segment [A.seg_begin, A.seg_end) as the forward's pipeline, from
+// the segment's checkpoint (state and ring), keeping x(s), g(s) in the scratch for the reverse.
+template <bool RK4>
+__global__ void adj_recompute_kernel(const DevNet* __restrict__ gnet, AdjArgs A, int L, int n_cons) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* ring = reinterpret_cast<float*>(smem);
+    const int b = blockIdx.x, N = A.N, RN = A.R * A.N;
+    const int seg = A.seg_begin / A.CK;
+    const DevNet& net = *gnet;
+    float prm[13], cp[8], x[NV];
+    load_params(net, b, prm, cp);
+    const float* cr = A.ck_ring + ((size_t)seg * A.B + b) * (size_t)RN;
+    for (int q = threadIdx.x; q < RN; q += blockDim.x) ring[q] = cr[q];
+    const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, false);
+    float* gbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + tables_size(N, A.rowptr[N]) + 15) & ~(size_t)15));
+    const bool uact = (int)threadIdx.x < N;
+#pragma unroll
+    for (int v = 0; v < NV; v++) x[v] = uact ? A.ck_state[((size_t)seg * A.B + b) * N * NV + threadIdx.x * NV + v] : 0.0f;
+    __syncthreads();
+    forward_pipelined<RK4>(ring, gbuf, A, tb, b, L, x, prm, cp, n_cons, A.seg_begin, A.seg_end, 1);
 }
 
 // ---- statistics of y, FC, loss, and the coefficients of dL/dy ----
@@ -904,9 +955,13 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
     const int nnz = A.rowptr[N];
     const AdjTables tb = stage_tables(A, smem, (size_t)RN * 4, true);
     float* pbuf = reinterpret_cast<float*>(smem + (((size_t)RN * 4 + 2 * tables_size(N, nnz) + 15) & ~(size_t)15));
-    for (int q = threadIdx.x; q < RN; q += nthreads) ring[q] = 0.0f;  // mu of steps past the end reads 0
+    // the segment [sb, se) of this launch: the run's last segment starts from mu = 0 (steps past the end
+    // read 0) and lambda = dL/dx(T - 1); earlier segments continue the later ones' mu ring and lambda
+    const int sb = A.seg_begin, se = A.seg_end;
+    float* mu_g = A.mu_ring + (size_t)b * RN;
+    for (int q = threadIdx.x; q < RN; q += nthreads) ring[q] = A.seg_last ? 0.0f : mu_g[q];
     __syncthreads();
-    const int n_blocks = (T + K - 1) / K;
+    const int n_blocks = (se - sb + K - 1) / K;
     double gG = 0.0;
     bool owner = false;
     if ((int)threadIdx.x >= n_cons) {
@@ -917,7 +972,7 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             if (blk >= 2) bar_sync(ADJ_BAR_EMPTY0 + buf, nthreads);
-            const int s_top = T - 1 - blk * K, nb = (s_top + 1) < K ? (s_top + 1) : K;
+            const int s_top = se - 1 - blk * K, nb = (s_top - sb + 1) < K ? (s_top - sb + 1) : K;
             float* pb = pbuf + (size_t)buf * K * N;
             for (int j = 0; j < nb; j++) {
                 const int s = s_top - j;
@@ -943,15 +998,20 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
 #pragma unroll
         for (int v = 0; v < NV; v++) lam[v] = 0.0f;
         if (act) {
-            const float sT = A.S[((size_t)(T - 1) * A.B + b) * N + i];
-            lam[1] = sT;
-            lam[2] = -sT;
+            if (A.seg_last) {
+                const float sT = A.S[((size_t)(T - 1) * A.B + b) * N + i];
+                lam[1] = sT;
+                lam[2] = -sT;
+            } else {
+#pragma unroll
+                for (int v = 0; v < NV; v++) lam[v] = A.lam_g[((size_t)b * N + i) * NV + v];
+            }
         }
         float sA = 0.0f, sB = 0.0f, sa = 0.0f, sG = 0.0f;
         for (int blk = 0; blk < n_blocks; blk++) {
             const int buf = blk & 1;
             bar_sync(ADJ_BAR_FULL0 + buf, nthreads);
-            const int s_top = T - 1 - blk * K, nb = (s_top + 1) < K ? (s_top + 1) : K;
+            const int s_top = se - 1 - blk * K, nb = (s_top - sb + 1) < K ? (s_top - sb + 1) : K;
             const float* pb = pbuf + (size_t)buf * K * N;
             for (int g = 0; g < nb; g += L) {
                 const int s_hi = s_top - g;
@@ -959,7 +1019,7 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
                 float src_mine = 0.0f;
                 const int sl = s_hi - lane;
                 if (act && g + lane < nb) {
-                    const float* sc = A.scratch + (((size_t)b * A.CK + sl) * N + i) * 8;
+                    const float* sc = A.scratch + (((size_t)b * A.CK + (sl - sb)) * N + i) * 8;
                     float xs[NV];
 #pragma unroll
                     for (int v = 0; v < NV; v++) xs[v] = sc[v];
@@ -992,12 +1052,23 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
             }
             bar_arrive(ADJ_BAR_EMPTY0 + buf, nthreads);
         }
+        // FP32 sums within the segment, FP64 across segments
         if (owner) {
-            A.gA[(size_t)b * N + i] = (double)sA;
-            A.gB[(size_t)b * N + i] = (double)sB;
-            A.ga[(size_t)b * N + i] = (double)sa;
+            const size_t gi = (size_t)b * N + i;
+            A.gA[gi] = (A.seg_last ? 0.0 : A.gA[gi]) + (double)sA;
+            A.gB[gi] = (A.seg_last ? 0.0 : A.gB[gi]) + (double)sB;
+            A.ga[gi] = (A.seg_last ? 0.0 : A.ga[gi]) + (double)sa;
             gG = (double)sG;
+            if (sb > 0) {
+#pragma unroll
+                for (int v = 0; v < NV; v++) A.lam_g[gi * NV + v] = lam[v];
+            }
         }
+    }
+    // the mu ring for the next (earlier) segment
+    if (sb > 0) {
+        __syncthreads();
+        for (int q = threadIdx.x; q < RN; q += nthreads) mu_g[q] = ring[q];
     }
     // gain gradient: sum over nodes, a tree over the next power of two of the block (zeros past it)
     __syncthreads();
@@ -1012,7 +1083,7 @@ __global__ void __launch_bounds__(ADJ_PIPE_MAXT, 1) adj_backward_pipe_kernel(con
         for (int q = threadIdx.x; q < o; q += nthreads) red[q] += red[q + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) A.gG[b] = red[0];
+    if (threadIdx.x == 0) A.gG[b] = (A.seg_last ? 0.0 : A.gG[b]) + red[0];
 }
 
 }  // namespace
@@ -1027,6 +1098,8 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
     A.x0 = L.x0; A.rowptr = L.rowptr; A.edges = L.edges; A.ew = L.ew;
     A.cptr = L.cptr; A.ctgt = L.ctgt; A.cdel = L.cdel; A.cw = L.cw;
     A.Y = L.Y; A.S = L.S; A.ck_state = L.ck_state; A.ck_ring = L.ck_ring; A.scratch = L.scratch; A.mu_ring = L.mu_ring;
+    A.lam_g = L.lam_g;
+    A.seg_begin = 0; A.seg_end = L.T; A.seg_last = 1;
     A.target = L.target; A.mean = L.mean; A.sdev = L.sdev; A.coef = L.coef; A.rk = L.rk; A.M = L.M; A.fc = L.fc;
     A.loss = L.loss; A.gG = L.gG; A.gA = L.gA; A.gB = L.gB; A.ga = L.ga;
     // lanes per node: a power of two up to 4 within 1024 threads; the block a power of two for the
@@ -1071,13 +1144,67 @@ cudaError_t hb_launch_adjoint(const DevNet* d_net, const HbAdjointLaunch& L, int
         int max_sm = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (L.store_all && L.n_ck == 1 && L.dmin >= 2 * L.K && L.K % rl == 0 && pthreads <= ADJ_PIPE_MAXT &&
-            psm <= (size_t)max_sm) {
+        if (L.pipelined && L.dmin >= 2 * L.K && L.K % rl == 0 && pthreads <= ADJ_PIPE_MAXT && psm <= (size_t)max_sm) {
             auto kp = L.rk4 ? adj_backward_pipe_kernel<true> : adj_backward_pipe_kernel<false>;
             if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm) != cudaSuccess)
                 return cudaGetLastError();
-            kp<<<L.B, pthreads, psm, st>>>(d_net, A, rl, pc);
-            return cudaGetLastError();
+            if (L.store_all) {
+                kp<<<L.B, pthreads, psm, st>>>(d_net, A, rl, pc);
+                return cudaGetLastError();
+            }
+            // checkpointed: the segments last to first, each re-computed from its checkpoint by the forward
+            // pipeline into one of two scratch buffers, then reversed. The re-computation of segment k - 1
+            // runs on a second stream, on SMs the reverse of segment k leaves idle (one CTA per point each),
+            // so only the last segment's re-computation adds to the reverse time.
+            const int n_cons = (L.N + 31) / 32 * 32;
+            const int fthreads = n_cons + (L.N * lanes + 31) / 32 * 32;
+            const size_t fsm = ring_bytes + tab1 + 2 * gbuf_bytes;
+            auto kr = L.rk4 ? adj_recompute_kernel<true> : adj_recompute_kernel<false>;
+            if (cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm) != cudaSuccess)
+                return cudaGetLastError();
+            const size_t seg_floats = (size_t)L.B * L.CK * L.N * 8;
+            auto seg_args = [&](int seg) {
+                AdjArgs a2 = A;
+                a2.seg_begin = seg * L.CK;
+                a2.seg_end = (seg + 1) * L.CK < L.T ? (seg + 1) * L.CK : L.T;
+                a2.seg_last = seg == L.n_ck - 1 ? 1 : 0;
+                a2.scratch = L.scratch + (size_t)(seg & 1) * seg_floats;
+                return a2;
+            };
+            cudaStream_t s2 = nullptr;
+            cudaEvent_t ev_start = nullptr, rc[2] = {nullptr, nullptr}, bk[2] = {nullptr, nullptr};
+            cudaError_t ce = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+            if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming);
+            for (int q = 0; q < 2 && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&rc[q], cudaEventDisableTiming);
+            for (int q = 0; q < 2 && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&bk[q], cudaEventDisableTiming);
+            if (ce == cudaSuccess) ce = cudaEventRecord(ev_start, st);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(s2, ev_start, 0);
+            const int last = L.n_ck - 1;
+            if (ce == cudaSuccess) {
+                kr<<<L.B, fthreads, fsm, s2>>>(d_net, seg_args(last), lanes, n_cons);
+                ce = cudaGetLastError();
+            }
+            if (ce == cudaSuccess) ce = cudaEventRecord(rc[last & 1], s2);
+            for (int seg = last; seg >= 0 && ce == cudaSuccess; seg--) {
+                ce = cudaStreamWaitEvent(st, rc[seg & 1], 0);
+                if (ce != cudaSuccess) break;
+                kp<<<L.B, pthreads, psm, st>>>(d_net, seg_args(seg), rl, pc);
+                ce = cudaGetLastError();
+                if (ce == cudaSuccess) ce = cudaEventRecord(bk[seg & 1], st);
+                if (ce == cudaSuccess && seg > 0) {
+                    // the buffer of segment seg - 1 was last read by the reverse of segment seg + 1
+                    ce = cudaStreamWaitEvent(s2, bk[(seg - 1) & 1], 0);
+                    if (ce == cudaSuccess) {
+                        kr<<<L.B, fthreads, fsm, s2>>>(d_net, seg_args(seg - 1), lanes, n_cons);
+                        ce = cudaGetLastError();
+                    }
+                    if (ce == cudaSuccess) ce = cudaEventRecord(rc[(seg - 1) & 1], s2);
+                }
+            }
+            for (auto* ev : {&ev_start, &rc[0], &rc[1], &bk[0], &bk[1]})
+                if (*ev) cudaEventDestroy(*ev);
+            if (s2) cudaStreamDestroy(s2);
+            return ce;
         }
         int rthreads = 32;
         while (rthreads < L.N * rl) rthreads *= 2;

@@ -171,7 +171,7 @@ struct StreamJob {
 struct HbAdjointLaunch {
     int B, N, T, R, K, CK, n_ck, cfk, gain_idx, nnz, store_all;
     int slices;        // time slices of the moment pass (hb_adjoint_moment_slices)
-    int pipelined;     // forward as a producer / consumer pipeline (store_all and every delay >= 2K - 1)
+    int pipelined;     // forward, re-computation and reverse as producer / consumer pipelines (every delay >= 2K - 1)
     int dmin;          // smallest edge delay (steps)
     int rk4;           // deterministic RK4 (else Heun)
     float dt_h2, dt_sixth;
@@ -180,6 +180,7 @@ struct HbAdjointLaunch {
     const int* rowptr; const uint32_t* edges; const float* ew;
     const int* cptr; const int* ctgt; const int* cdel; const float* cw;
     float *Y, *S, *ck_state, *ck_ring, *scratch, *mu_ring;
+    float* lam_g;      // [B][N*6] lambda between the checkpoint segments' reverse launches
     const float* target;
     float *mean, *sdev, *coef, *rk, *M, *fc;
     double *loss, *gG, *gA, *gB, *ga;

@@ -2153,7 +2153,7 @@ void hb_group_destroy(hb_group* g) { delete g; }
 
 struct AdjWorkspace {
     DBuf<int> cptr, ctgt, cdel;
-    DBuf<float> cw, Y, S, ck_state, ck_ring, scratch, mu_ring, target, mean, sdev, coef, rk, M, fc;
+    DBuf<float> cw, Y, S, ck_state, ck_ring, scratch, mu_ring, lam, target, mean, sdev, coef, rk, M, fc;
     DBuf<double> loss, gG, gA, gB, ga, moments;
 };
 
@@ -2236,7 +2236,9 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     CUDA_TRY(W->Y.ensure(TBN)); CUDA_TRY(W->S.ensure(TBN));
     CUDA_TRY(W->ck_state.ensure(store_all ? 1 : (size_t)n_ck * B * N * 6));
     CUDA_TRY(W->ck_ring.ensure(store_all ? 1 : (size_t)n_ck * B * R * N));
-    CUDA_TRY(W->scratch.ensure((size_t)B * CK * N * 8));
+    // the re-computation of one segment overlaps the reverse of the next: two segment buffers
+    CUDA_TRY(W->scratch.ensure((size_t)B * CK * N * 8 * (store_all ? 1 : 2)));
+    CUDA_TRY(W->lam.ensure((size_t)B * N * 6));
     CUDA_TRY(W->mu_ring.ensure((size_t)B * R * N));
     CUDA_TRY(W->target.ensure((size_t)N * N));
     CUDA_TRY(cudaMemcpyAsync(W->target.p, target_fc, (size_t)N * N * 4, cudaMemcpyHostToDevice, st));
@@ -2262,7 +2264,8 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     L.ga = W->ga.p;
     L.moments = W->moments.p;
     L.slices = hb_adjoint_moment_slices(B, T);
-    L.pipelined = (store_all && dmin >= 2 * K - 1) ? 1 : 0;
+    L.pipelined = dmin >= 2 * K - 1 ? 1 : 0;
+    L.lam_g = W->lam.p;
     L.dmin = dmin;
     cudaEvent_t ev[4];
     for (auto& v : ev) CUDA_TRY(cudaEventCreate(&v));
@@ -2291,7 +2294,7 @@ hb_status hb_engine_adjoint_fc(hb_engine* e, const float* gain_values, int32_t n
     if (out->d_a) CUDA_TRY(cudaMemcpy(out->d_a, W->ga.p, (size_t)B * N * 8, cudaMemcpyDeviceToHost));
     if (out->fc) CUDA_TRY(cudaMemcpy(out->fc, W->fc.p, (size_t)B * N * N * 4, cudaMemcpyDeviceToHost));
     if (out->y) CUDA_TRY(cudaMemcpy(out->y, W->Y.p, TBN * 4, cudaMemcpyDeviceToHost));
-    for (auto* b : {&W->Y, &W->S, &W->ck_state, &W->ck_ring, &W->scratch, &W->mu_ring, &W->target, &W->mean, &W->sdev,
+    for (auto* b : {&W->Y, &W->S, &W->ck_state, &W->ck_ring, &W->scratch, &W->mu_ring, &W->lam, &W->target, &W->mean, &W->sdev,
                     &W->coef, &W->rk, &W->M, &W->fc, &W->cw})
         b->release();
     W->cptr.release(); W->ctgt.release(); W->cdel.release();
