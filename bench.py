@@ -446,7 +446,9 @@ def run_other_workload(args):
                 ns += 128 * n * T
                 bytes_ += 128 * T * (8.0 * nnz + 8.0 * n)
             from hyburn_gb300._abi import HB_RUN_PIPE_LANES
-            g = GroupedSweep(members, run_flags=HB_RUN_PIPE_LANES(args.pipe_lanes))
+            from hyburn_gb300._abi import HB_RUN_STREAM_CLUSTER
+            g = GroupedSweep(members, run_flags=HB_RUN_PIPE_LANES(args.pipe_lanes) |
+                             (HB_RUN_STREAM_CLUSTER(args.stream_cluster) if args.stream_cluster else 0))
             for _ in range(args.warmup):
                 g.execute()
             times = []
@@ -458,7 +460,8 @@ def run_other_workload(args):
                         config={"workload": f"mpr-68/84/164/400n-x128pt-(G16xeta8)-csr20pct-per-edge-delays-rk4-dt0.05-bold-"
                                             f"{T}steps (of 1200000), one grouped launch", "kernel_kind": 5,
                                 "grid": "per size: G in linspace(0, 1, 16) x eta in linspace(-6, -3, 8)",
-                                "producer_lanes_per_node": args.pipe_lanes or "engine's choice"},
+                                "producer_lanes_per_node": args.pipe_lanes or "engine's choice",
+                                "ctas_per_point_of_split_members": args.stream_cluster or "engine's choice"},
                         roofline={"bound": "hbm", "achieved": bytes_ / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": bytes_ / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bytes_ / ns, "traffic": None})
@@ -611,7 +614,8 @@ def main():
     ap.add_argument("--pipe-lanes", type=int, default=0,
                     help="pipeline and streamed-history kernels: producer threads per node (0: engine's choice)")
     ap.add_argument("--stream-cluster", type=int, default=0,
-                    help="streamed-history kernel: CTAs per sweep point, 1/2/4/8 (0: engine's choice)")
+                    help="streamed-history kernel: CTAs per sweep point, 1-6 or 8 (0: the engine's choice); "
+                         "uneven workload: the grouped launch's cluster size (0: the engine's choice)")
     ap.add_argument("--dense-points", type=int, default=1024, help="dense workload: sweep points")
     ap.add_argument("--stream-npt", type=int, default=0,
                     help="streamed-history kernel: nodes per consumer thread, 1/2/4 (0: engine's choice)")

@@ -165,6 +165,8 @@ struct StreamJob {
     int first_block;   // first work item of this job (items are numbered job by job)
     int n_points;      // its sweep points (one work item each)
     int model, pre;    // model id and coupling pre() form (0: identity, 1: [sin, cos]) of its kernel path
+    int split;         // 1: each work item is one point split over the launch's cluster (args.stream_cluster
+                       // = the cluster size); 0: each item is cluster-size points, one per CTA
 };
 
 // the FC-loss adjoint's buffers and sizes (hb_adjoint.cu); device pointers

@@ -44,12 +44,12 @@ int hb_dense_tc_tmem_columns(int model, int nm);
 void hb_dense_tc_tiles(const float* w, int nm, int NP, int KP, float* out);
 cudaError_t hb_launch_dense_tc(int model, const DevNet* d_net, const RunArgs& a, int B, const float* wtiles, int NP, int KP,
                                int NPN, cudaStream_t st);
-cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_1(int threads, size_t smem);
-cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_2(int threads, size_t smem);
-cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_4(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_1(int threads, size_t smem, int C);
+cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_2(int threads, size_t smem, int C);
+cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_4(int threads, size_t smem, int C);
 int hb_stream_queue_budget_1();
 int hb_stream_queue_budget_2();
 int hb_stream_queue_budget_4();
@@ -1985,6 +1985,34 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     bool want4 = true;
     for (int i = 0; i < n; i++) want4 = want4 && ((members[i].run_flags >> 24) & 0x7) == 4;
     const int npt = want4 && max_nm <= 2048 ? 4 : max_nm <= 96 ? 1 : 2;
+    const int threads = npt == 1 ? 512 : npt == 2 ? 1024 : 768;
+    // cluster size of the launch: the size the members ask for (HB_RUN_STREAM_CLUSTER, the first member's
+    // request), else the largest of 4, 3, 2 that leaves the member with the most work at least 100 nodes
+    // per CTA, else one CTA per point. (On the uneven MPR grid, 68 / 84 / 164 / 400 nodes: 4 gives 5.80e9
+    // node-steps/s against 5.23e9 for one CTA per point; 6 CTAs, 67 nodes each, 4.77e9.) Members with
+    // at least 100 nodes per CTA at that size run each point split over a cluster (their histories in
+    // flight shrink by the cluster size); the others run one point per CTA, cluster-size points per item.
+    int Cq = 1;
+    {
+        static const int code_to_c[8] = {0, 1, 2, 4, 8, 3, 5, 6};
+        const int v = (int)((members[0].run_flags >> 4) & 0x7);
+        if (v) Cq = code_to_c[v];
+        else {
+            int big = 0;
+            for (int i = 1; i < n; i++)
+                if ((double)members[i].engine->subs[0].nm * members[i].engine->B * members[i].n_steps >
+                    (double)members[big].engine->subs[0].nm * members[big].engine->B * members[big].n_steps)
+                    big = i;
+            const int nmb = members[big].engine->subs[0].nm;
+            for (int c = 4; c >= 2 && Cq == 1; c--)
+                if (nmb / c >= 100) Cq = c;
+        }
+        if (Cq > 1) {
+            const int cap = npt == 1 ? hb_stream_queue_grid_1(threads, 48 * 1024, Cq)
+                          : npt == 2 ? hb_stream_queue_grid_2(threads, 48 * 1024, Cq) : hb_stream_queue_grid_4(threads, 48 * 1024, Cq);
+            if (cap <= 0) return fail(HB_ERR_UNSUPPORTED, "grouped launch: no cluster of %d CTAs fits the device", Cq);
+        }
+    }
     std::unique_ptr<hb_group> g(new hb_group());
     if (cuda_stream) g->user = (cudaStream_t)cuda_stream;
     else CUDA_TRY(cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking));
@@ -2009,9 +2037,11 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
             CUDA_TRY(cudaMemcpy(gm.noise.p, mb.noise, (size_t)mb.noise_len * 4, cudaMemcpyHostToDevice));
             noise_dev = gm.noise.p;
         }
-        // the work-queue kernel runs every point in one CTA (no clusters)
+        // a member with at least 100 nodes per CTA at the launch's cluster size runs its points split over
+        // a cluster; the others one point per CTA
+        const int mc = (Cq > 1 && e->subs[0].nm / Cq >= 100) ? Cq : 1;
         const uint32_t flags = (mb.run_flags & ~(uint32_t)(0x7u << 24) & ~(uint32_t)(0x7u << 4)) | HB_RUN_STREAM |
-                               HB_RUN_STREAM_NPT(npt) | HB_RUN_STREAM_CLUSTER(1);
+                               HB_RUN_STREAM_NPT(npt) | HB_RUN_STREAM_CLUSTER(mc);
         if ((s = run_setup(e, gm.T, mb.n_steps, flags, nullptr, noise_dev ? noise_dev : e->x0.p, nullptr, gm.P))) return s;
         if (gm.P.stream_npt != npt)
             return fail(HB_ERR_UNSUPPORTED, "member %d cannot run in the streamed-history kernel (one subnetwork, one sparse "
@@ -2040,30 +2070,34 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     }
     const int budget = npt == 1 ? hb_stream_queue_budget_1() : npt == 2 ? hb_stream_queue_budget_2() : hb_stream_queue_budget_4();
     if (budget < 0 || smem + 64 > (size_t)budget) return fail(HB_ERR_UNSUPPORTED, "grouped launch: shared memory budget exceeded");
-    // jobs, longest points first
+    // jobs, longest work per CTA first; a split member's item is one point over a cluster, another
+    // member's item is Cq points, one per CTA
+    auto is_split = [&](int i) { return Cq > 1 && g->m[i].P.a.stream_cluster == Cq; };
+    auto work = [&](int i) {
+        return (double)g->m[i].e->subs[0].nm * members[i].n_steps / (is_split(i) ? Cq : 1);
+    };
     std::vector<int> order(n);
     for (int i = 0; i < n; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return (double)g->m[x].e->subs[0].nm * members[x].n_steps > (double)g->m[y].e->subs[0].nm * members[y].n_steps;
-    });
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
     std::vector<StreamJob> jobs(n);
     int blocks = 0;
     for (int k = 0; k < n; k++) {
         hb_group::Member& gm = g->m[order[k]];
+        const bool sp = is_split(order[k]);
         jobs[k].net = gm.e->d_net;
         jobs[k].args = gm.P.a;
         jobs[k].first_block = blocks;
         jobs[k].n_points = gm.e->B;
         jobs[k].model = gm.e->kernel_model;
         jobs[k].pre = gm.P.fast;
-        blocks += gm.e->B;
+        jobs[k].split = sp ? 1 : 0;
+        blocks += sp ? gm.e->B : (gm.e->B + Cq - 1) / Cq;
     }
     CUDA_TRY(g->jobs.ensure(n));
     CUDA_TRY(g->counter.ensure(1));
     CUDA_TRY(cudaMemcpy(g->jobs.p, jobs.data(), n * sizeof(StreamJob), cudaMemcpyHostToDevice));
-    const int threads = npt == 1 ? 512 : npt == 2 ? 1024 : 768;
-    const int grid = npt == 1 ? hb_stream_queue_grid_1(threads, smem) : npt == 2 ? hb_stream_queue_grid_2(threads, smem)
-                                                                      : hb_stream_queue_grid_4(threads, smem);
+    const int grid = npt == 1 ? hb_stream_queue_grid_1(threads, smem, Cq) : npt == 2 ? hb_stream_queue_grid_2(threads, smem, Cq)
+                                                                          : hb_stream_queue_grid_4(threads, smem, Cq);
     if (grid < 1) return fail(HB_ERR_CUDA, "grouped launch: cannot size the work-queue grid");
     // the whole run as one graph: member resets, the queue counter, the grouped launch, batch-mean BOLD reductions
     cudaStream_t st = g->stream();
@@ -2080,9 +2114,9 @@ hb_status hb_group_prepare(const hb_group_member* members, int32_t n, void* cuda
     if (ce == cudaSuccess) ce = cudaMemsetAsync(g->counter.p, 0, sizeof(int), st);
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev0, st, cudaEventRecordExternal);
     if (ce == cudaSuccess)
-        ce = npt == 1 ? hb_launch_stream_queue_1(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st)
-           : npt == 2 ? hb_launch_stream_queue_2(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st)
-                      : hb_launch_stream_queue_4(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, st);
+        ce = npt == 1 ? hb_launch_stream_queue_1(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, Cq, st)
+           : npt == 2 ? hb_launch_stream_queue_2(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, Cq, st)
+                      : hb_launch_stream_queue_4(g->jobs.p, n, blocks, g->counter.p, grid, threads, smem, Cq, st);
     if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(g->ev1, st, cudaEventRecordExternal);
     for (auto& gm : g->m) {
         for (int mo = 0; mo < gm.P.n_bold_active && !gm.P.bold_pp && ce == cudaSuccess; mo++) {

@@ -900,31 +900,51 @@ __global__ void __launch_bounds__(MAXT, 1) stream_pipe_kernel(const DevNet* __re
     stream_point<MODEL, PRE, NPT, MAXT>(net, a, (int)blockIdx.x / C, C > 1 ? (int)cluster_rank() : 0);
 }
 
-// one (model, coupling pre() form) path of the work-queue kernel
-template <int MODEL, int PRE, int NPT, int MAXT>
-__device__ __forceinline__ void stream_queue_item(DevNet& net, const RunArgs& a, int b) {
-    stream_point<MODEL, PRE, NPT, MAXT>(net, a, b, 0);
-}
 
 // Several networks' sweeps — different models, node counts, connectomes, delays and step counts — in
-// one launch of a persistent kernel: each block takes the next (job, point) item from a device counter
-// until the items run out, and runs it through the path of the job's model and coupling form. Items
-// are numbered job by job with the jobs ordered by decreasing work per point, so the longest points
-// start first and the short ones fill the SMs that finish early (greedy longest-first scheduling).
-// The counter is zeroed before every launch.
+// one launch of a persistent kernel: each block (or thread-block cluster) takes the next work item from
+// a device counter until the items run out, and runs it through the path of the job's model and
+// coupling form. Items are numbered job by job with the jobs ordered by decreasing work per item, so
+// the longest start first and the short ones fill the SMs that finish early (greedy longest-first
+// scheduling). The counter is zeroed before every launch.
+// Launched with clusters of C CTAs, a job marked split gives each item one point whose nodes the C
+// CTAs share (stream_point's cluster form: fewer points in flight, histories in L2); another job's item
+// is C consecutive points, one per CTA. The cluster's first CTA takes the item and the others read it
+// from its shared memory after a cluster barrier; every item ends with a cluster barrier.
+__device__ __forceinline__ uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ int ld_remote_int(const int* p, uint32_t rank) {
+    uint32_t ra;
+    int v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_addr(p)), "r"(rank));
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(ra) : "memory");
+    return v;
+}
 template <int NPT, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) stream_queue_kernel(const StreamJob* __restrict__ jobs, int n_jobs, int n_items,
                                                               int* __restrict__ counter) {
     __shared__ DevNet net;
     __shared__ RunArgs sa;
     __shared__ int s_item, s_job;
+    const int C = (int)cluster_size();
+    const int rank = C > 1 ? (int)cluster_rank() : 0;
     for (;;) {
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && rank == 0) {
             const int it = atomicAdd(counter, 1);
             int j = 0;
             while (j + 1 < n_jobs && it >= jobs[j + 1].first_block) j++;
             s_item = it;
             s_job = j;
+        }
+        if (C > 1) {
+            cluster_barrier();
+            if (threadIdx.x == 0 && rank != 0) {
+                s_item = ld_remote_int(&s_item, 0);
+                s_job = ld_remote_int(&s_job, 0);
+            }
         }
         __syncthreads();
         const int it = s_item;
@@ -937,23 +957,32 @@ __global__ void __launch_bounds__(MAXT, 1) stream_queue_kernel(const StreamJob* 
         }
         stream_load_net(net, J->net);
         __syncthreads();
-        const int b = it - J->first_block;
-        switch (J->model * 2 + (J->pre == PRE_KURA ? 1 : 0)) {
-        case 0: stream_queue_item<0, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 1: stream_queue_item<0, PRE_KURA, NPT, MAXT>(net, sa, b); break;
-        case 2: stream_queue_item<1, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 4: stream_queue_item<2, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 5: stream_queue_item<2, PRE_KURA, NPT, MAXT>(net, sa, b); break;
-        case 6: stream_queue_item<3, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 7: stream_queue_item<3, PRE_KURA, NPT, MAXT>(net, sa, b); break;
-        case 8: stream_queue_item<4, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 9: stream_queue_item<4, PRE_KURA, NPT, MAXT>(net, sa, b); break;
-        case 10: stream_queue_item<5, PRE_ID, NPT, MAXT>(net, sa, b); break;
-        case 11: stream_queue_item<5, PRE_KURA, NPT, MAXT>(net, sa, b); break;
-        default: break;  // MontbrioPazoRoxin has two coupling variables: no [sin, cos] form (refused on the host)
+        const bool split = C > 1 && J->split;
+        const int local = it - J->first_block;
+        const int b = split ? local : local * C + rank;
+        if (b < J->n_points) {
+            const int r = split ? rank : 0;
+            switch (J->model * 2 + (J->pre == PRE_KURA ? 1 : 0)) {
+            case 0: stream_point<0, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 1: stream_point<0, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
+            case 2: stream_point<1, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 4: stream_point<2, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 5: stream_point<2, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
+            case 6: stream_point<3, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 7: stream_point<3, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
+            case 8: stream_point<4, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 9: stream_point<4, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
+            case 10: stream_point<5, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
+            case 11: stream_point<5, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
+            default: break;  // MontbrioPazoRoxin has two coupling variables: no [sin, cos] form (refused on the host)
+            }
         }
+        // a split point ends with stream_point's cluster barrier; the other items end with one here
+        if (C > 1 && !split) cluster_barrier();
         __syncthreads();  // shared memory and the item slot are reused by the next item
     }
+    // no CTA leaves while another may still read the first CTA's item slot
+    if (C > 1) cluster_barrier();
 }
 
 template <int NPT, int MAXT>
@@ -972,10 +1001,29 @@ int stream_queue_max_dynamic_smem() {
     return cached;
 }
 
-// persistent grid: as many blocks of the queue kernel as fit on the device at once
+// persistent grid: as many blocks (clusters of C blocks) of the queue kernel as fit on the device at once
 template <int NPT, int MAXT>
-int stream_queue_grid(int threads, size_t smem) {
+int stream_queue_grid(int threads, size_t smem, int C) {
     if (stream_queue_max_dynamic_smem<NPT, MAXT>() < 0) return -1;
+    if (C > 1) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(C * 64));
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, stream_queue_kernel<NPT, MAXT>, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        return n * C;
+    }
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
@@ -985,13 +1033,31 @@ int stream_queue_grid(int threads, size_t smem) {
 
 template <int NPT, int MAXT>
 cudaError_t launch_stream_queue(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads,
-                                size_t smem, cudaStream_t st) {
+                                size_t smem, int C, cudaStream_t st) {
     int maxdyn = stream_queue_max_dynamic_smem<NPT, MAXT>();
     if (maxdyn < 0) return cudaErrorInvalidConfiguration;
-    if ((long long)smem > maxdyn || threads > MAXT || blocks < 1) return cudaErrorInvalidValue;
-    if (blocks > n_items) blocks = n_items;
-    stream_queue_kernel<NPT, MAXT><<<blocks, threads, smem, st>>>(d_jobs, n_jobs, n_items, counter);
-    return cudaGetLastError();
+    if ((long long)smem > maxdyn || threads > MAXT || blocks < 1 || C < 1 || C > 8) return cudaErrorInvalidValue;
+    if (C == 1) {
+        if (blocks > n_items) blocks = n_items;
+        stream_queue_kernel<NPT, MAXT><<<blocks, threads, smem, st>>>(d_jobs, n_jobs, n_items, counter);
+        return cudaGetLastError();
+    }
+    if (blocks / C > n_items) blocks = n_items * C;
+    blocks = blocks / C * C;
+    if (blocks < C) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, stream_queue_kernel<NPT, MAXT>, d_jobs, n_jobs, n_items, counter);
 }
 
 template <int MODEL, int PRE, int NPT, int MAXT>
@@ -1071,12 +1137,12 @@ int hb_stream_clusters_2(int model, int pre, int C, int threads, size_t smem);
 int hb_stream_clusters_4(int model, int pre, int C, int threads, size_t smem);
 int hb_stream_budget_2(int model, int pre);
 int hb_stream_budget_4(int model, int pre);
-cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_1(int threads, size_t smem);
-cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_2(int threads, size_t smem);
-cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, cudaStream_t st);
-int hb_stream_queue_grid_4(int threads, size_t smem);
+cudaError_t hb_launch_stream_queue_1(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_1(int threads, size_t smem, int C);
+cudaError_t hb_launch_stream_queue_2(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_2(int threads, size_t smem, int C);
+cudaError_t hb_launch_stream_queue_4(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter, int blocks, int threads, size_t smem, int C, cudaStream_t st);
+int hb_stream_queue_grid_4(int threads, size_t smem, int C);
 int hb_stream_queue_budget_1();
 int hb_stream_queue_budget_2();
 int hb_stream_queue_budget_4();
@@ -1126,8 +1192,10 @@ int hb_stream_queue_budget_4();
 // one translation unit per (NPT, MAXT) for the work-queue kernel of grouped launches
 #define HB_QUEUE_UNIT(NPT_, MAXT_)                                                                                   \
     cudaError_t hb_launch_stream_queue_##NPT_(const StreamJob* d_jobs, int n_jobs, int n_items, int* counter,        \
-                                              int blocks, int threads, size_t smem, cudaStream_t st) {               \
-        return hb::launch_stream_queue<NPT_, MAXT_>(d_jobs, n_jobs, n_items, counter, blocks, threads, smem, st);    \
+                                              int blocks, int threads, size_t smem, int C, cudaStream_t st) {        \
+        return hb::launch_stream_queue<NPT_, MAXT_>(d_jobs, n_jobs, n_items, counter, blocks, threads, smem, C, st); \
     }                                                                                                                \
     int hb_stream_queue_budget_##NPT_() { return hb::stream_queue_max_dynamic_smem<NPT_, MAXT_>(); }                  \
-    int hb_stream_queue_grid_##NPT_(int threads, size_t smem) { return hb::stream_queue_grid<NPT_, MAXT_>(threads, smem); }
+    int hb_stream_queue_grid_##NPT_(int threads, size_t smem, int C) {                                               \
+        return hb::stream_queue_grid<NPT_, MAXT_>(threads, smem, C);                                                 \
+    }

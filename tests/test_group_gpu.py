@@ -119,3 +119,48 @@ def test_group_many_points_per_cta(big):
         g.execute()
         _check(members, HB_SEM_DELAY_RING, g.results())
     g.close()
+
+
+@pytest.mark.parametrize("sem", [HB_SEM_DELAY_RING, HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT])
+@pytest.mark.parametrize("exact", [True, False])
+def test_group_large_member_split_over_a_cluster(sem, exact):
+    """Clusters of 4 CTAs (the launch's choice for a 400-node member): its 6 points run split over a
+    cluster (100 nodes per CTA), while the 30- and 70-node members run 4 points per cluster, one per CTA;
+    the MPR grid's (G, eta) tables,
+    different step counts, a first and a repeated execution.
+    exact (HB_RUN_EXACT_SUMS, the reference's summation order): every member's states equal the FP32
+    oracle's bit for bit (no transcendental functions in MPR; BOLD to the usual tolerance).
+    Default (regrouped, fused sums): this grid's last point amplifies the reordering of its 80-term
+    sums to about 3e-5 relative over the 160 RK4 steps (the one-CTA form of the same run reaches
+    1.2e-5), so the default form is held to 5e-5."""
+    from hyburn_gb300 import inputs
+    from hyburn_gb300._abi import HB_RUN_EXACT_SUMS, HB_RUN_STREAM_CLUSTER
+    mons = [MonitorConfig("Bold", tr=0.004, bold_period=10)]
+    members = []
+    cfg, meta = inputs.mpr_grid(400, 6, 160, seed=7, bold=False)
+    if sem & HB_SEM_BOLD_PER_POINT:
+        cfg.monitors = mons
+    members.append((cfg, 6, SweepParam(-1, 0), meta["values"], 160, None))
+    for i, (n, pts, steps) in enumerate([(30, 5, 200), (70, 7, 120)]):
+        c = single_model("MontbrioPazoRoxin", n, "rk4", "Linear", (0.3,), weights="csr", delays="per_edge_long",
+                         monitors=mons if sem & HB_SEM_BOLD_PER_POINT else [], dt=0.05, seed=20 + i)
+        vals = np.linspace(-1.0, 0.5, pts).astype(np.float32).tolist()
+        members.append((c, pts, SweepParam(0, 4), vals, steps, None))
+    engines = [BatchHybridEngine.from_config(c, p, semantics=sem) for c, p, *_ in members]
+    g = GroupedSweep([(e, m[2], m[3], m[4], m[5]) for e, m in zip(engines, members)],
+                     run_flags=(HB_RUN_EXACT_SUMS if exact else 0) | HB_RUN_STREAM_CLUSTER(4))
+    for _ in range(2):
+        g.execute()
+        for (cfg_m, n_pts, param, vals, n_steps, noise), r in zip(members, g.results()):
+            o = OracleEngine.from_config(cfg_m, n_pts, semantics=sem).run_sweep(param, vals, n_steps, noise=noise)
+            what = f"{cfg_m.network.subnetworks[0].nnodes} nodes"
+            if exact:
+                assert np.array_equal(r.final_states[0], o.final_states[0]), what
+                assert np.array_equal(r.tavg[0], o.tavg[0]), what
+            else:
+                close(r.final_states[0], o.final_states[0], rtol=5e-5, what=f"final ({what})")
+                close(r.tavg[0], o.tavg[0], rtol=5e-5, what=f"tavg ({what})")
+            if o.bold is not None:
+                for m in range(len(o.bold)):
+                    close(r.bold[m], o.bold[m], atol=BOLD_ATOL, what="bold")
+    g.close()
