@@ -175,3 +175,28 @@ def test_new_entry_points_reject_null_arguments_without_a_gpu():
     oa = _abi.hb_order_adjoint_out()
     assert lib.hb_engine_adjoint_order(None, None, 0, 10, 0, C.byref(oa)) == _abi.HB_ERR_INVALID_STATE
     assert b"NULL" in lib.hb_last_error() or b"null" in lib.hb_last_error()
+
+
+def test_run_flag_macros_match_the_header():
+    """The Python mirror's run-flag helpers give the same bits as the C header's macros: the header
+    is compiled with a one-line C program per value (gcc, no GPU)."""
+    import os
+    import subprocess
+    import tempfile
+    from hyburn_gb300 import _abi
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    cases = [("HB_RUN_STREAM_CLUSTER", c, _abi.HB_RUN_STREAM_CLUSTER(c)) for c in (1, 2, 3, 4, 5, 6, 8)]
+    cases += [("HB_RUN_STREAM_NPT", n, _abi.HB_RUN_STREAM_NPT(n)) for n in (1, 2, 4)]
+    cases += [("HB_RUN_PIPE_LANES", n, _abi.HB_RUN_PIPE_LANES(n)) for n in (1, 2, 4, 8)]
+    src = "#include <stdio.h>\n#include \"hyburn_gb300.h\"\nint main(void) {\n"
+    src += "".join(f'  printf("%u\\n", (unsigned){m}({v}));\n' for m, v, _ in cases) + "  return 0;\n}\n"
+    with tempfile.TemporaryDirectory() as d:
+        c_path, exe = os.path.join(d, "flags.c"), os.path.join(d, "flags")
+        with open(c_path, "w") as f:
+            f.write(src)
+        subprocess.run(["gcc", "-std=c99", "-I", inc, c_path, "-o", exe], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    assert [int(x) for x in out] == [py for _, _, py in cases]
+    # distinct codes for the distinct cluster sizes
+    codes = [_abi.HB_RUN_STREAM_CLUSTER(c) for c in (1, 2, 3, 4, 5, 6, 8)]
+    assert len(set(codes)) == len(codes) and 0 not in codes
