@@ -74,6 +74,31 @@ def issue_roofline(prof, n_run, kern_ms, clocks, hbm):
     return out
 
 
+def dense_roofline(B, T, ms, clocks, tensor):
+    """Roofline of the tensor-core dense kernel on the roof that binds it, instruction issue of its FP32
+    epilogue: warp instructions of one launch (the committed one-launch ncu counts per CTA and step,
+    profiles/dense_tc_kernel_counts.json, times the launch's CTAs and steps) over the event time, against
+    one warp instruction per cycle on the 4 schedulers of every SM at the sampled SM clock. The tensor
+    pipe's figures ride along as `tensor`."""
+    prof = os.path.join(ROOT, "profiles", "dense_tc_kernel_counts.json")
+    out = {"bound": "issue", "unit": "G warp-instructions/s", "tensor": tensor, "traffic": None}
+    try:
+        d = json.load(open(prof))
+    except Exception:
+        out.update(achieved=None, peak=None, frac=None, note="instruction counts not recorded")
+        return out
+    ctas = (B + 127) // 128
+    inst = ctas * (d["warp_instructions_per_cta_step"] * T + d["warp_instructions_startup_per_cta"])
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak = 4.0 * 152 * mhz * 1e6 / 1e9
+    achieved = inst / (ms / 1e3) / 1e9
+    out.update(achieved=achieved, peak=peak, frac=achieved / peak, sms_with_work=ctas,
+               frac_of_sms_with_work=achieved / (peak * min(ctas, 152) / 152),
+               issue_active_ncu=d.get("issue_active_pct"), tensor_pipe_active_ncu=d.get("tensor_pipe_active_pct"),
+               peak_kind="4 schedulers x 152 SMs x %.0f MHz (sampled)" % mhz)
+    return out
+
+
 def peaks_tf32():
     """Dense TF32 tensor rate: half the measured bf16 burst rate."""
     try:
@@ -520,11 +545,12 @@ def run_other_workload(args):
                                "cuda_core_kernel_kind": res["cuda_core"][1],
                                "cuda_core_node_steps_per_s": ns / (res["cuda_core"][0] / 1e3),
                                "speedup_over_cuda_core": res["cuda_core"][0] / ms},
-                        roofline={"bound": "tensor", "achieved": issued / (ms / 1e3) / 1e12,
+                        roofline=dense_roofline(B, T, ms, None, {
+                                  "bound": "tensor", "achieved": issued / (ms / 1e3) / 1e12,
                                   "peak": peaks_tf32(), "unit": "TFLOP/s",
                                   "frac": issued / (ms / 1e3) / 1e12 / peaks_tf32(),
                                   "peak_kind": "half the measured dense bf16 burst (TF32 runs at half the bf16 rate)",
-                                  "useful_tflops": useful / (ms / 1e3) / 1e12, "traffic": None})
+                                  "useful_tflops": useful / (ms / 1e3) / 1e12, "traffic": None}))
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -595,6 +621,11 @@ def run_other_workload(args):
                         adjoint={"forward_ms": parts[0], "statistics_ms": parts[1], "reverse_ms": parts[2],
                                  "plain_forward_ms": fwd_ms, "fwd_plus_adjoint_over_forward": ms / fwd_ms})
     line["clocks"] = clk.summary()
+    if args.workload == "dense" and line.get("roofline", {}).get("bound") == "issue":
+        # the issue peak at the SM clock sampled during the timed region
+        r = line["roofline"]
+        line["roofline"] = dense_roofline(args.dense_points, args.run_steps or 2_000, line["ms_per_step"],
+                                          line["clocks"], r["tensor"])
     print(json.dumps(line), flush=True)
 
 
