@@ -440,10 +440,11 @@ def run_other_workload(args):
             T = args.run_steps or 10_000
             cfg, meta = inputs.kuramoto_scale(n=1000, n_points=256, n_steps=T, bold=True)
             eng = BatchHybridEngine.from_config(cfg, 256, semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT)
-            from hyburn_gb300._abi import HB_RUN_PIPE_LANES, HB_RUN_STREAM_CLUSTER, HB_RUN_STREAM_NPT
+            from hyburn_gb300._abi import HB_RUN_PIPE_LANES, HB_RUN_STREAM_BULK, HB_RUN_STREAM_CLUSTER, HB_RUN_STREAM_NPT
             eng.prepare(SweepParam(-1, 0), meta["values"], T,
                         run_flags=(HB_RUN_STREAM_CLUSTER(args.stream_cluster) if args.stream_cluster else 0) |
-                        HB_RUN_STREAM_NPT(args.stream_npt) | HB_RUN_PIPE_LANES(args.pipe_lanes))
+                        HB_RUN_STREAM_NPT(args.stream_npt) | HB_RUN_PIPE_LANES(args.pipe_lanes) |
+                        (HB_RUN_STREAM_BULK if args.stream_bulk else 0))
             ms, kind = _time_prepared(eng, args.steps, args.warmup)
             nnz = sum(len(p.weights["data"]) for p in cfg.network.projections)
             bpns = 4.0 * nnz / 1000 + 4.0
@@ -454,7 +455,8 @@ def run_other_workload(args):
                                 "omega": "per node, N(0, 1) (seed 5)",
                                 "ctas_per_point": args.stream_cluster or "engine's choice",
                                 "nodes_per_consumer_thread": args.stream_npt or "engine's choice",
-                                "producer_lanes_per_node": args.pipe_lanes or "engine's choice"},
+                                "producer_lanes_per_node": args.pipe_lanes or "engine's choice",
+                                "windows_staged_by_bulk_copies": bool(args.stream_bulk)},
                         roofline={"bound": "hbm", "achieved": bpns * ns / (ms / 1e3) / 1e9, "peak": peak,
                                   "unit": "GB/s", "frac": bpns * ns / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
                                   "algorithmic_bytes_per_node_step": bpns, "traffic": None})
@@ -647,6 +649,8 @@ def main():
     ap.add_argument("--stream-cluster", type=int, default=0,
                     help="streamed-history kernel: CTAs per sweep point, 1-6 or 8 (0: the engine's choice); "
                          "uneven workload: the grouped launch's cluster size (0: the engine's choice)")
+    ap.add_argument("--stream-bulk", action="store_true",
+                    help="Kuramoto workload: stage the gathered windows by the bulk-copy engine (HB_RUN_STREAM_BULK)")
     ap.add_argument("--dense-points", type=int, default=1024, help="dense workload: sweep points")
     ap.add_argument("--stream-npt", type=int, default=0,
                     help="streamed-history kernel: nodes per consumer thread, 1/2/4 (0: engine's choice)")

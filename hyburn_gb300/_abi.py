@@ -58,6 +58,7 @@ def HB_RUN_STREAM_NPT(n: int) -> int:
 
 
 HB_RUN_STREAM_PREFETCH = 1 << 27
+HB_RUN_STREAM_BULK = 1 << 7
 HB_RUN_PIPE_WIDE = 1 << 28
 HB_RUN_DEVICE_TRAJECTORY = 1 << 29
 HB_RUN_TEST_UNSET_WAIT = 1 << 30
@@ -72,7 +73,7 @@ def HB_RUN_STREAM_CLUSTER(n: int) -> int:
 HB_RUN_KERNEL_CHOICE = (HB_RUN_DENSE_TC | HB_RUN_FORCE_RESIDENT | HB_RUN_FORCE_BLOCKED | HB_RUN_GLOBAL_RING | HB_RUN_GENERIC | (0x7 << 4)
                         | (0xF << 12)
                         | HB_RUN_TWO_PHASE | HB_RUN_NO_PIPE | HB_RUN_STREAM | HB_RUN_NO_STREAM | (0xF << 20)
-                        | (0x7 << 24) | HB_RUN_STREAM_PREFETCH | HB_RUN_PIPE_WIDE)
+                        | (0x7 << 24) | HB_RUN_STREAM_PREFETCH | HB_RUN_PIPE_WIDE | HB_RUN_STREAM_BULK)
 # the streamed-history kernel's form within those: nodes per consumer thread and L2 prefetch
 HB_RUN_STREAM_FORM = (0x7 << 24) | HB_RUN_STREAM_PREFETCH
 

@@ -155,6 +155,7 @@ struct RunArgs {
     int exact_sums;       // coupling sums term by term in edge order, product and sum rounded apart (HB_RUN_EXACT_SUMS)
     int stream_wgather;   // streamed-history kernel: warp-cooperative gathers (a warp per node, 8 lanes per edge
                           // window; 0: one thread per edge window)
+    int stream_bulk;      // warp-cooperative gathers staged by the bulk-copy engine (HB_RUN_STREAM_BULK)
     DevBold bold;
 };
 

@@ -736,7 +736,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     size_t smem = (ring_in_smem ? ((ring_bytes + 15) & ~(size_t)15) : 0) + (edges_in_smem ? edge_bytes : 0) + part_bytes + 16;
     // ---- streamed-history pipeline: per-edge delays whose history does not fit shared memory ----
     int stream_npt = 0, stream_pl = 1, stream_rp = 0, stream_noise_smem = 0, stream_edges = 0, stream_cluster = 1;
-    int stream_wgather = 0;
+    int stream_wgather = 0, stream_bulk = 0;
     size_t stream_smem = 0;
     if (fast >= 0 && e->projs[0].dmode == HBD_EDGE && e->dmin >= 2 * HB_STREAM_K - 1 && !(run_flags & HB_RUN_NO_STREAM) &&
         (!ring_in_smem || (run_flags & HB_RUN_STREAM)) && !((run_flags >> 12) & 0xf) && !(run_flags & HB_RUN_TWO_PHASE) &&
@@ -840,6 +840,18 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
                 if (!(run_flags & HB_RUN_EXACT_SUMS) && !((run_flags >> 20) & 0xf) && stream_edges > 0 &&
                     e->projs[0].edges.size() >= (size_t)24 * nm_all)
                     stream_wgather = 1;
+                // HB_RUN_STREAM_BULK: the warp gather's windows staged by the bulk-copy engine, 32 slots per
+                // producer warp (80 bytes for two channels, 48 for one) and one mbarrier per warp
+                if (run_flags & HB_RUN_STREAM_BULK) {
+                    if (!stream_wgather)
+                        return fail(HB_ERR_UNSUPPORTED, "HB_RUN_STREAM_BULK needs the warp-cooperative gather (edge lists in shared "
+                                    "memory, mean in-degree >= 24, no exact sums or producer lane count)");
+                    const size_t bulk_b = (size_t)(n_prod / 32) * (32 * (pch == 2 ? 80 : 48) + 8) + 16;
+                    if (stream_smem + bulk_b > cap)
+                        return fail(HB_ERR_UNSUPPORTED, "HB_RUN_STREAM_BULK: the staging area does not fit shared memory");
+                    stream_smem += bulk_b;
+                    stream_bulk = 1;
+                }
                 stream_rp = (e->projs[0].maxd + 2 * HB_STREAM_K + 2 + 7) / 8 * 8;
                 const size_t words = (size_t)B * nm_all * (stream_rp + 2 * HB_STREAM_K) * pch;
                 CUDA_TRY(e->sring.ensure(words));
@@ -978,6 +990,7 @@ hb_status run_setup(hb_engine* e, const RunTables& T, int64_t n_steps, uint32_t 
     a.test_unset_wait = (run_flags & HB_RUN_TEST_UNSET_WAIT) ? 1 : 0;
     a.exact_sums = (run_flags & HB_RUN_EXACT_SUMS) ? 1 : 0;
     a.stream_wgather = stream_npt ? stream_wgather : 0;
+    a.stream_bulk = stream_npt ? stream_bulk : 0;
     a.bold = db;
 
     P.n_steps = n_steps;

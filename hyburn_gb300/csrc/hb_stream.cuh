@@ -515,6 +515,12 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
     if (NPT > 1) off += (size_t)ns * PU * 4;
     off = (off + 15) & ~(size_t)15;
     int* s_porder = reinterpret_cast<int*>(smem + off);  // [ns] producer order of the slice's nodes
+    off += (size_t)ns * 4;
+    off = (off + 15) & ~(size_t)15;
+    // bulk-staged gathers: per producer warp 32 window slots of BSLOT bytes, then one mbarrier per warp
+    constexpr int BSLOT = PCH == 2 ? 80 : 48;  // an 8-step window from the 16-byte boundary at or below it
+    unsigned char* s_stage = smem + off;
+    uint64_t* s_sbar = reinterpret_cast<uint64_t*>(smem + off + (size_t)(n_prod >> 5) * 32 * BSLOT);
 
     // a fresh run starts from a zero history (zero rows after pre() for d > s, runtime.rs:166-176);
     // each CTA clears its own nodes' rows
@@ -583,6 +589,14 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
     if (!is_consumer) {
         // ================= producers =================
         const int p = t - n_cons;
+        uint32_t bulk_phase = 0;  // bulk-staged gathers: chunks this warp has staged (its mbarrier's phase)
+        if (a.stream_wgather && a.stream_bulk) {
+            if ((p & 31) == 0) {
+                mbar_init(s_sbar + (p >> 5), 1);
+                mbar_init_fence();
+            }
+            __syncwarp();
+        }
         const int PL = a.pipe_lanes;  // threads per node (power of two <= 8)
         const int pf = a.stream_prefetch;
         const int items = ns * PL;
@@ -601,7 +615,88 @@ __device__ __forceinline__ void stream_point(DevNet& net, const RunArgs& a, cons
             const int64_t sb = a.s0 + it0;
             const int sbm = (int)(sb % RP);
             float* gb = gxbuf + (size_t)buf * K * ns * PCH;
-            if (a.stream_wgather) {
+            if (a.stream_wgather && a.stream_bulk) {
+                // the warp-cooperative gather with each chunk's windows staged by the bulk-copy engine: lane j
+                // copies edge j's window (BSLOT bytes from the 16-byte boundary at or below its first entry,
+                // which stays inside the node's row) into its slot of the warp's staging area; lane 0 posts
+                // the chunk's byte count on the warp's mbarrier, whose phase completes when every copy has
+                // landed (bounded wait); the 8 lanes of a slot then read the window's entries from shared
+                // memory. The reads of one chunk finish (warp barrier, proxy fence) before the next chunk's
+                // copies overwrite the slots.
+                const int lane = t & 31, wid = p >> 5, nwarp = n_prod >> 5;
+                const int slot = lane >> 3, stp = lane & (K - 1);
+                unsigned char* stg = s_stage + (size_t)wid * 32 * BSLOT;
+                uint64_t* sbar = s_sbar + wid;
+                for (int i = wid; i < ns; i += nwarp) {
+                    const int node = s_porder[i];
+                    const int e0 = s_rowptr[node], e1 = s_rowptr[node + 1];
+                    float acc[PCH];
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) acc[c] = 0.0f;
+                    for (int eb = e0; eb < e1; eb += 32) {
+                        const int cnt = (e1 - eb) < 32 ? (e1 - eb) : 32;
+                        uint32_t src = 0, shift = 0;
+                        float w = 0.0f;
+                        if (lane == 0)
+                            asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                                         ::"r"(smem_addr(sbar)), "r"((uint32_t)(cnt * BSLOT)) : "memory");
+                        __syncwarp();
+                        if (lane < cnt) {
+                            const uint32_t m = ed[eb + lane];
+                            int pos = sbm - (int)(m >> 16);
+                            pos += (pos < 0) ? RP : 0;
+                            src = m & 0xffffu;
+                            const size_t off_f = ((size_t)src * RPX + (size_t)pos) * PCH;  // floats
+                            shift = (uint32_t)(off_f & 3);
+                            w = ew[eb + lane];
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                                         ::"r"(smem_addr(stg + lane * BSLOT)), "l"(ring + (off_f - shift)), "r"((uint32_t)BSLOT),
+                                           "r"(smem_addr(sbar))
+                                         : "memory");
+                        }
+                        if (!mbar_wait(sbar, bulk_phase & 1u)) atomicOr(a.flags + 1, 4);
+                        bulk_phase++;
+#pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            const int k = 4 * u + slot;
+                            const uint32_t shk = __shfl_sync(0xffffffffu, shift, k);
+                            const float wk = __shfl_sync(0xffffffffu, w, k);
+                            const float* q = reinterpret_cast<const float*>(stg + k * BSLOT) + shk + stp * PCH;
+                            if (k < cnt) {
+                                if (PCH == 2) {
+                                    acc[0] = __fmaf_rn(wk, q[0], acc[0]);
+                                    acc[PCH - 1] = __fmaf_rn(wk, q[1], acc[PCH - 1]);
+                                } else acc[0] = __fmaf_rn(wk, q[0], acc[0]);
+                            }
+                        }
+                        if (sb == 0) {
+                            // step 0 also reads the current state (runtime.rs:166-170)
+#pragma unroll
+                            for (int u = 0; u < 8; u++) {
+                                const int k = 4 * u + slot;
+                                const uint32_t sk = __shfl_sync(0xffffffffu, src, k);
+                                const float wk = __shfl_sync(0xffffffffu, w, k);
+                                if (stp == 0 && k < cnt) {
+                                    const float* q0 = ring + (size_t)sk * RPX * PCH;
+#pragma unroll
+                                    for (int c = 0; c < PCH; c++) acc[c] += wk * q0[c];
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+#pragma unroll
+                    for (int c = 0; c < PCH; c++) {
+                        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
+                        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+                    }
+                    if (slot == 0 && stp < nb) {
+#pragma unroll
+                        for (int c = 0; c < PCH; c++) gb[((size_t)stp * ns + node) * PCH + c] = acc[c];
+                    }
+                }
+            } else if (a.stream_wgather) {
                 // warp-cooperative gather: warp w takes the slice's nodes w, w + nwarp, ... in producer order
                 // (decreasing in-degree), 32 of the node's edges at a time. Lane j decodes edge j of the chunk
                 // (history offset of its window, weight); the window of chunk edge k = 4u + slot is then read

@@ -82,6 +82,10 @@ typedef int32_t hb_status;
    multiply-adds (results agree within the FP32 rounding of the sum). With it, a model without transcendental
    functions reproduces the FP32 reference arithmetic bit for bit. */
 #define HB_RUN_EXACT_SUMS   (1u << 3)
+/* streamed-history kernel, warp-cooperative gather: each lane stages its edge's window of history into
+   shared memory with the bulk-copy engine (cp.async.bulk, completion on a per-warp mbarrier, bounded
+   waits) instead of loading it; refused when the warp-cooperative gather is not in use */
+#define HB_RUN_STREAM_BULK    (1u << 7)
 #define HB_RUN_FORCE_RESIDENT (1u << 8) /* kernel choice: point-resident persistent kernel */
 #define HB_RUN_FORCE_BLOCKED  (1u << 9) /* kernel choice: time-blocked tiled kernel */
 #define HB_RUN_GLOBAL_RING    (1u << 10) /* resident kernel: keep the history ring in global memory */

@@ -7,7 +7,7 @@ import pytest
 from hyburn_gb300 import BatchHybridEngine, SweepParam
 from hyburn_gb300._abi import (HB_RUN_STREAM, HB_RUN_STREAM_NPT, HB_RUN_STREAM_PREFETCH, HB_SEM_BOLD_PER_POINT,
                                HB_SEM_DELAY_RING, HB_SEM_NOISE_PER_POINT)
-from hyburn_gb300.config import MonitorConfig
+from hyburn_gb300.config import MonitorConfig, Unsupported
 from oracle.hb_oracle import OracleEngine
 
 from cases import NATIVE_SWEEP, noise_for, single_model, sweep_values
@@ -151,4 +151,32 @@ def test_stream_cluster_split_mpr_500_nodes():
     cfg, meta = inputs.mpr_grid(500, 3, 150, seed=3)
     eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 0.5, 1.0], 150, semantics=HB_SEM_DELAY_RING,
                            run_flags=HB_RUN_STREAM_CLUSTER(4))
+    assert kind(eng) == STREAM_KIND
+
+
+@pytest.mark.parametrize("C", [4, 6])
+def test_stream_bulk_staged_gather_kuramoto(C):
+    """HB_RUN_STREAM_BULK: the warp-cooperative gather with every edge window staged into shared memory
+    by the bulk-copy engine (per-warp mbarrier, bounded waits), 4 and 6 CTAs per point (a slice's edge
+    lists must sit in shared memory); the [sin, cos] channels (80-byte slots), per-node omega, per-point
+    BOLD, against the oracle. One CTA per point is refused: its edge lists do not fit."""
+    from hyburn_gb300 import inputs
+    from hyburn_gb300._abi import HB_RUN_STREAM_BULK, HB_RUN_STREAM_CLUSTER
+    cfg, meta = inputs.kuramoto_scale(n=1000, n_points=3, n_steps=200, bold=True)
+    cfg.monitors[0].tr = 0.005
+    eng, _, _, _ = compare(cfg, 3, SweepParam(-1, 0), [0.0, 1.0, 2.0], 200, rtol=2e-5,
+                           semantics=HB_SEM_DELAY_RING | HB_SEM_BOLD_PER_POINT,
+                           run_flags=HB_RUN_STREAM | HB_RUN_STREAM_CLUSTER(C) | HB_RUN_STREAM_BULK)
+    assert kind(eng) == STREAM_KIND
+    with pytest.raises(Unsupported):
+        eng.run_sweep(SweepParam(-1, 0), [0.0, 1.0, 2.0], 20, run_flags=HB_RUN_STREAM | HB_RUN_STREAM_CLUSTER(1) | HB_RUN_STREAM_BULK)
+
+
+def test_stream_bulk_staged_gather_one_channel():
+    """HB_RUN_STREAM_BULK with one coupling channel (48-byte slots, windows starting at any 4-byte entry):
+    a 300-node Generic2dOscillator network with 20 % CSR coupling, split over 2 CTAs, against the oracle."""
+    from hyburn_gb300._abi import HB_RUN_STREAM_BULK, HB_RUN_STREAM_CLUSTER
+    cfg = single_model("Generic2dOscillator", 300, "heun", "Linear", (0.02,), weights="csr", delays="per_edge_long", seed=4)
+    eng, _, _, _ = compare(cfg, 2, SweepParam(-1, 0), [0.0, 0.5], 120, semantics=HB_SEM_DELAY_RING,
+                           run_flags=HB_RUN_STREAM | HB_RUN_STREAM_CLUSTER(2) | HB_RUN_STREAM_BULK)
     assert kind(eng) == STREAM_KIND
