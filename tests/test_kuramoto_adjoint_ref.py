@@ -58,11 +58,13 @@ def test_fp64_adjoint_matches_central_differences():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,T,dt,form", [(16, 300, 0.1, "pipe"), (40, 500, 0.05, "pipe"), (16, 300, 0.1, "stream"),
-                                        (40, 500, 0.05, "stream"), (16, 300, 0.1, "generic")])
+                                        (40, 500, 0.05, "stream"), (16, 300, 0.1, "generic"),
+                                        (128, 300, 0.1, "stream")])
 def test_gpu_order_adjoint_matches_central_differences(n, T, dt, form):
-    """hb_engine_adjoint_order against central differences (h = 1e-6) of the FP64 forward. The GPU
-    differentiates its FP32 trajectory, whose phases drift from the FP64 ones by ~1e-6 over these
-    runs: the loss agrees within 1e-4 (relative; measured 1e-5), each gradient within
+    """hb_engine_adjoint_order against central differences (h = 1e-6) of the FP64 forward. With 128
+    nodes and two points the streamed forward and the reverse sweep both split each point over a
+    2-CTA cluster (64 nodes per CTA). The GPU differentiates its FP32 trajectory, whose phases drift
+    from the FP64 ones by ~1e-6 over these runs: the loss agrees within 1e-4 (relative; measured 1e-5), each gradient within
     1e-4 |fd| + 2e-6 — the absolute floor covers gradients that nearly cancel (measured: dL/domega
     = -2.7e-4 off by 7.7e-7 on the 40-node case; elsewhere 3e-7 to 4e-5 relative)."""
     from hyburn_gb300 import BatchHybridEngine
