@@ -77,9 +77,12 @@ def candidates(config: SimConfig, semantics: int) -> List[Tuple[str, int]]:
                 out.append((f"streamed history {npt} node(s) per thread", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_NPT(npt)))
             # CTAs per point: a point's nodes split over a cluster (fewer points in flight, histories in L2)
             nodes = config.network.subnetworks[0].nnodes
-            for c in (2, 4, 5, 6, 8):
+            for c in (2, 3, 4, 5, 6, 8):
                 if nodes >= 16 * c:
                     out.append((f"streamed history, {c} CTAs per point", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_CLUSTER(c)))
+            # the warp gather's windows staged by the bulk-copy engine (the engine refuses it where the
+            # warp gather does not apply; such candidates are skipped)
+            out.append(("streamed history, bulk-staged windows", _abi.HB_RUN_STREAM | _abi.HB_RUN_STREAM_BULK))
         undelayed = not projs[0].delays or max(projs[0].delays) == 0
         if undelayed and projs[0].coupling_fn in ("Linear", "Sigmoidal", "ScaledLinear"):
             # 128 points per CTA: the coupling as a tensor-core matrix product
