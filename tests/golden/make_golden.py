@@ -16,12 +16,26 @@ The cases are the workloads' own shapes, cut to a few hundred steps:
 - ``kuramoto_1000n``: Kuramoto, 1000 nodes, 5 % CSR, delays up to 500 steps, per-node natural
   frequencies omega ~ N(0, 1), 3 coupling scales, BOLD on, 80 steps;
 - ``meanfield_<model>_<integrator>``: each of the six models under Heun-stochastic and RK4, 20
-  nodes, all-to-all scalar coupling, the model's native parameter swept over 4 points, 120 steps.
+  nodes, all-to-all scalar coupling, the model's native parameter swept over 4 points, 120 steps;
+- ``example_*``: the reference's own example configurations (``examples/*.toml`` with their
+  ``examples/init_*_74.npy`` initial states), loaded through this package's TOML reader, run for
+  their full ``sim_length`` the way its batch-sweep command runs them (``hyburn run -c <config>
+  --sweep <sweep>``, cli.rs:961-998): the G2DO and MPR sweep configurations over all 128 values of
+  their sweep files, and the other single-population and multi-population examples over the first
+  values of ``examples/sweep.toml`` or as one point. Their initial states are stored resolved, so the
+  fixtures do not need the reference tree.
+
+Short runs are compared element-wise (``bound`` "elementwise": rel/abs tolerances). The example runs
+are 10 000 to 100 000 steps, where two FP32 roundings of the same run drift apart by more than rel
+1e-5 in a few elements; they carry ``bound`` "fp32": the engine may be no farther from the FP32
+oracle than twice the FP32 oracle's largest distance from the FP64 twin (stored per output as
+``drift``), with the rel/abs tolerance as the floor.
 
 The engine's semantics follow the reference's ``BatchHybridEngine::run_sweep``
 (src/engine/batch_engine/engine.rs:477-842); the oracle restates it (oracle/hb_oracle.c).
 
-Run ``python tests/golden/make_golden.py`` from the repository root to rewrite every fixture.
+Run ``python tests/golden/make_golden.py`` from the repository root to rewrite every fixture (the
+``example_*`` cases read the reference tree, ``HYBURN_REFERENCE_TREE``, default /root/reference).
 """
 from __future__ import annotations
 
@@ -63,6 +77,12 @@ class GoldenCase:
     # True where the run has no transcendental function: the engine with the reference's summation
     # order (HB_RUN_EXACT_SUMS) must then reproduce the FP32 outputs bit for bit
     bitwise: bool
+    # "elementwise" (rtol/atol per element) or "fp32" (within twice the FP32 oracle's own distance
+    # from the FP64 twin, largest absolute difference per output)
+    bound: str
+    # largest |FP32 - FP64| of the oracle per output (final_i, tavg_i, bold_m)
+    drift: Dict[str, float]
+    source: str
     expected: Dict[str, np.ndarray]
 
 
@@ -163,6 +183,16 @@ def unpack_config(text: str, arrays) -> SimConfig:
                      speed=d["speed"], backend=d["backend"])
 
 
+def difference(key: str, a, b, cfg: SimConfig) -> np.ndarray:
+    """|a - b| element-wise in float64; Kuramoto final phases (kept in [0, 2 pi)) on the circle, where a
+    phase that wraps at a different step on the two sides is still the same phase."""
+    d = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    kind, _, idx = key.partition("_")
+    if kind == "final" and cfg.network.subnetworks[int(idx)].model == "Kuramoto":
+        d = np.minimum(d, np.abs(2.0 * np.pi - d))
+    return d
+
+
 def path_of(name: str) -> str:
     return os.path.join(HERE, f"{name}.npz")
 
@@ -176,7 +206,8 @@ def load_case(name: str) -> GoldenCase:
     noise = arrays.get("noise")
     return GoldenCase(name=name, cfg=cfg, n_sweep=meta["n_sweep"], param=SweepParam(*meta["param"]),
                       values=arrays["values"], n_steps=meta["n_steps"], semantics=meta["semantics"], noise=noise,
-                      rtol=meta["rtol"], atol=meta["atol"], bitwise=meta["bitwise"], expected=expected)
+                      rtol=meta["rtol"], atol=meta["atol"], bitwise=meta["bitwise"], bound=meta["bound"],
+                      drift=meta["drift"], source=meta["source"], expected=expected)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -238,6 +269,53 @@ for _m in MODELS:
         CASES[f"meanfield_{SHORT[_m]}_{_i}"] = _meanfield(_m, _i)
 
 
+REFERENCE_TREE = os.environ.get("HYBURN_REFERENCE_TREE", "/root/reference")
+
+
+def _example(config: str, sweep: Optional[str], n_points: int):
+    """One of the reference's example configurations, run for its full sim_length: over the first
+    n_points values of its sweep file, or (sweep None) as one point whose swept value is the model's
+    own native parameter."""
+    def make():
+        from cases import NATIVE_SWEEP
+        from hyburn_gb300.config import SweepConfig, parse_sweep_param, resolve_initial_state
+        cwd = os.getcwd()
+        os.chdir(REFERENCE_TREE)  # the examples name their initial-state files relative to the tree
+        try:
+            cfg = SimConfig.from_file(os.path.join("examples", config))
+            for s in cfg.network.subnetworks:
+                s.initial_state = np.asarray(resolve_initial_state(s), np.float64).tolist()
+            if sweep:
+                sw = SweepConfig.from_file(os.path.join("examples", sweep))
+                param = SweepParam(*parse_sweep_param(sw.parameter_name, cfg))
+                values = sw.generate_values()[:n_points]
+            else:
+                s0 = cfg.network.subnetworks[0]
+                param = SweepParam(0, NATIVE_SWEEP[s0.model])
+                values = [s0.params[param.param_idx]]
+        finally:
+            os.chdir(cwd)
+        n_steps = int(round(cfg.sim_length / cfg.dt))
+        src = f"examples/{config}" + (f" with examples/{sweep}" if sweep else "")
+        return dict(cfg=cfg, n_sweep=len(values), param=param, values=values, n_steps=n_steps, semantics=0,
+                    noise=None, rtol=1e-5, atol=1e-6, bitwise=False, bound="fp32", source=src)
+    return make
+
+
+EXAMPLES = {
+    "example_g2do_sweep": ("g2do_sweep.toml", "sweep.toml", 128),
+    "example_mpr_sweep": ("mpr_sweep.toml", "sweep_mpr.toml", 128),
+    "example_demo_sweep": ("demo.toml", "sweep.toml", 16),
+    "example_g2do_bold": ("g2do_bold.toml", "sweep.toml", 8),
+    "example_two_population_coupled": ("two_population_coupled.toml", "sweep.toml", 8),
+    "example_whole_brain_multi_model": ("whole_brain_multi_model.toml", "sweep.toml", 8),
+    "example_wilson_cowan_ring": ("wilson_cowan_ring.toml", None, 1),
+    "example_jansen_rit_evoked": ("jansen_rit_evoked.toml", None, 1),
+}
+for _n, (_c, _s, _p) in EXAMPLES.items():
+    CASES[_n] = _example(_c, _s, _p)
+
+
 def build_case(name: str) -> dict:
     """The case's inputs from the seeded generators (used to write fixtures, and by a CPU test that the
     generators still give the stored inputs)."""
@@ -249,18 +327,29 @@ def write_case(name: str) -> None:
     c = build_case(name)
     vals = np.asarray(c["values"], np.float32)
     text, arrays = pack_config(c["cfg"])
-    meta = {"n_sweep": c["n_sweep"], "param": [c["param"].sub_idx, c["param"].param_idx], "n_steps": c["n_steps"],
-            "semantics": c["semantics"], "rtol": c["rtol"], "atol": c["atol"], "bitwise": c["bitwise"]}
-    out = {}
-    for prec, tag in (("f32", ""), ("f64", "64")):
-        r = OracleEngine.from_config(c["cfg"], c["n_sweep"], semantics=c["semantics"], precision=prec).run_sweep(
-            c["param"], vals, c["n_steps"], noise=c["noise"])
+    bound = c.get("bound", "elementwise")
+    runs = {}
+    for prec in ("f32", "f64"):
+        r = OracleEngine.from_config(c["cfg"], c["n_sweep"], semantics=c["semantics"], precision=prec,
+                                     n_threads=os.cpu_count()).run_sweep(c["param"], vals, c["n_steps"],
+                                                                         noise=c["noise"])
         # the FP64 twin integrates in double and returns its outputs rounded to float
+        got = {}
         for i in range(len(r.final_states)):
-            out[f"out_final{tag}_{i}"] = np.asarray(r.final_states[i], np.float32)
-            out[f"out_tavg{tag}_{i}"] = np.asarray(r.tavg[i], np.float32)
+            got[f"final_{i}"] = np.asarray(r.final_states[i], np.float32)
+            got[f"tavg_{i}"] = np.asarray(r.tavg[i], np.float32)
         for m in range(len(r.bold or [])):
-            out[f"out_bold{tag}_{m}"] = np.asarray(r.bold[m], np.float32)
+            got[f"bold_{m}"] = np.asarray(r.bold[m], np.float32)
+        runs[prec] = got
+    drift = {k: float(np.max(difference(k, v, runs["f64"][k], c["cfg"])) if v.size else 0.0)
+             for k, v in runs["f32"].items()}
+    out = {f"out_{k}": v for k, v in runs["f32"].items()}
+    if bound == "elementwise":  # the long runs keep only the FP64 twin's drift, not its outputs
+        out.update({f"out_{k.replace('_', '64_', 1)}": v for k, v in runs["f64"].items()})
+    meta = {"n_sweep": c["n_sweep"], "param": [c["param"].sub_idx, c["param"].param_idx], "n_steps": c["n_steps"],
+            "semantics": c["semantics"], "rtol": c["rtol"], "atol": c["atol"], "bitwise": c["bitwise"],
+            "bound": bound, "drift": drift, "source": c.get("source", "seeded generators (hyburn_gb300.inputs, "
+                                                               "tests/cases.py)")}
     extra = {} if c["noise"] is None else {"noise": np.asarray(c["noise"], np.float32)}
     np.savez_compressed(path_of(name), meta=np.asarray(json.dumps(meta)), config=np.asarray(text), values=vals,
                         **arrays, **extra, **out)
