@@ -1055,8 +1055,10 @@ __global__ void __launch_bounds__(MAXT, 1) stream_queue_kernel(const StreamJob* 
         const bool split = C > 1 && J->split;
         const int local = it - J->first_block;
         const int b = split ? local : local * C + rank;
+        bool ran = false;  // stream_point ran (and, on a split item, ended with its cluster barrier)
         if (b < J->n_points) {
             const int r = split ? rank : 0;
+            ran = true;
             switch (J->model * 2 + (J->pre == PRE_KURA ? 1 : 0)) {
             case 0: stream_point<0, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
             case 1: stream_point<0, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
@@ -1069,11 +1071,13 @@ __global__ void __launch_bounds__(MAXT, 1) stream_queue_kernel(const StreamJob* 
             case 9: stream_point<4, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
             case 10: stream_point<5, PRE_ID, NPT, MAXT>(net, sa, b, r); break;
             case 11: stream_point<5, PRE_KURA, NPT, MAXT>(net, sa, b, r); break;
-            default: break;  // MontbrioPazoRoxin has two coupling variables: no [sin, cos] form (refused on the host)
+            default: ran = false; break;  // MontbrioPazoRoxin has two coupling variables: no [sin, cos] form (refused on the host)
             }
         }
-        // a split point ends with stream_point's cluster barrier; the other items end with one here
-        if (C > 1 && !split) cluster_barrier();
+        // a split point that ran ends with stream_point's cluster barrier; every other item ends with one
+        // here, so no rank reads the item slot of rank 0 after rank 0 has taken the next item (every rank
+        // of a split item sees the same point and job, so all of them take the same branch)
+        if (C > 1 && !(split && ran)) cluster_barrier();
         __syncthreads();  // shared memory and the item slot are reused by the next item
     }
     // no CTA leaves while another may still read the first CTA's item slot
