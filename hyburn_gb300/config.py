@@ -215,9 +215,14 @@ class SimConfig:
             integ = raw.get("integrator", "heun")
             if integ not in ("heun", "euler", "euler_stochastic", "heun_stochastic", "rk4", "rk4_stochastic"):
                 raise InvalidConfig(f"TOML parse error: unknown integrator kind: {integ}")
+            # NoiseMode deserialises from these two names only (integrator.rs:57-63); this engine takes its
+            # draws from the caller, so the mode names where they come from but changes no arithmetic
+            noise_mode = raw.get("noise_mode", "reproducible")
+            if noise_mode not in ("reproducible", "fast"):
+                raise InvalidConfig(f"TOML parse error: unknown noise mode: {noise_mode}")
             return SimConfig(sim_length=float(raw["sim_length"]), dt=float(raw["dt"]),
                              network=NetworkConfig(subs, projs), integrator=integ,
-                             noise_mode=raw.get("noise_mode", "reproducible"), monitors=mons,
+                             noise_mode=noise_mode, monitors=mons,
                              stimuli=raw.get("stimuli", []), nsig=raw.get("nsig", 0.0),
                              speed=float(raw.get("speed", 3.0)), backend=raw.get("backend", "ndarray"))
         except KeyError as e:
