@@ -180,6 +180,16 @@ def workload(n_steps=N_STEPS, n_points=N_POINTS):
     return cfg, meta, noise
 
 
+def workload_config(n_run=N_STEPS) -> dict:
+    """The benchmark workload as both arms' lines name it: the same keys and values on each."""
+    from hyburn_gb300 import inputs
+
+    _, meta = inputs.batched_sweep(n_steps=1, n_points=1)  # the delays depend on the connectome alone
+    return {"workload": WORKLOAD, "points_per_gpu": N_POINTS, "nodes": N_NODES, "steps_per_run": n_run,
+            "delays": f"per edge {meta['min_delay']}-{meta['max_delay']} steps",
+            "l2": "flushed (512 MiB write) between timed GPU iterations"}
+
+
 def algorithmic_bytes_per_node_step(meta, n_points=N_POINTS) -> float:
     """Delayed reads of the coupling variable (4 B per in-edge), the ring write (4 B) and the
     shared noise draws (2 x 4 B per node per step, read once for all points)."""
@@ -267,7 +277,7 @@ def run_reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "node-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "points": N_POINTS, "nodes": N_NODES, "steps_per_run": N_STEPS},
+            "config": workload_config(),
             "cpu_baseline": {"value": v, "unit": "node-steps/s", "cores": n_threads, "kind": "port",
                              "sample": sample, "note": CPU_BASELINE_NOTE},
             "e2e": {"value": v, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -765,9 +775,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "points_per_gpu": N_POINTS, "nodes": N_NODES, "steps_per_run": n_run,
-                   "delays": f"per edge {meta['min_delay']}-{meta['max_delay']} steps", "l2": "flushed (512 MiB write) between timed iterations",
-                   "kernel": KERNEL_NAMES.get(kind, str(kind)), "parallelism": f"sweep points sharded, {world} replica(s)"},
+        "config": workload_config(n_run),
+        "impl_detail": {"kernel": KERNEL_NAMES.get(kind, str(kind)), "parallelism": f"sweep points sharded, {world} replica(s)"},
         "roofline": issue_roofline(prof_d, n_run, kern_ms, clocks,
                                    {"bound": "hbm (notional: the history lives in shared memory)", "achieved": achieved,
                                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
