@@ -10,7 +10,9 @@ Later runs of the same shape read the cache (`best_run_flags`): BatchHybridEngin
 for every run that forces no kernel form (its `tune` option: "cache", "auto" to tune an untuned
 shape on its first run, "off"), and GroupedSweep takes the tuned streamed-history form when its
 members agree on one. Results are those of the chosen kernel form, which all agree with the CPU
-oracle within the parity tolerance; only the time differs.
+oracle within the parity tolerance; only the time differs. A cached form that the engine refuses for a
+particular run (one with options the key does not see, such as trajectories or per-node parameter
+tables) gives way to the fixed rules for that run.
 
 Cache file: $HYBURN_GB300_TUNE_CACHE, else ~/.cache/hyburn_gb300/tune.json.
 """

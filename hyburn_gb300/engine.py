@@ -173,6 +173,22 @@ class BatchHybridEngine:
         self.tuned_flags = f
         return run_flags | (f or 0)
 
+    def _run_tuned(self, call, run_flags: int, param: Optional[SweepParam] = None, values=None) -> int:
+        """call(flags), an entry point of the library returning its status, with the autotuner's cached
+        kernel choice added. The cache key is the network's shape; it does not see every option of a run
+        (trajectories, per-node parameter tables, device memory), so when the engine refuses the cached
+        choice for this run (HB_ERR_UNSUPPORTED) the call is made again with the caller's own flags, the
+        engine's fixed rules: a cache entry never turns a run those rules serve into an error. Returns the
+        flags of the call that ran."""
+        flags = self._with_tuned(run_flags, param, values)
+        st = call(flags)
+        if st == _abi.HB_ERR_UNSUPPORTED and flags != run_flags:
+            self.tuned_flags = None
+            flags = run_flags
+            st = call(flags)
+        raise_for(st, self._lib.hb_last_error().decode())
+        return flags
+
     @classmethod
     def from_config(cls, config: SimConfig, n_sweep: int, device=None, semantics: int = 0,
                     tune: str = "cache") -> "BatchHybridEngine":
@@ -235,11 +251,11 @@ class BatchHybridEngine:
         writes the run's tavg_sub{i}.npy files there (cli.rs:961-970, hb_engine_write_tavg)."""
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
-        run_flags = self._with_tuned(run_flags, param, vals)
         r = C.c_void_p()
-        st = self._lib.hb_engine_run_sweep(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals),
-                                           vals.size, int(n_steps), int(run_flags), nptr, nlen, C.byref(r))
-        raise_for(st, self._lib.hb_last_error().decode())
+        run_flags = self._run_tuned(
+            lambda f: self._lib.hb_engine_run_sweep(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals),
+                                                    vals.size, int(n_steps), int(f), nptr, nlen, C.byref(r)),
+            run_flags, param, vals)
         if output_dir is not None:
             st = self._lib.hb_engine_write_tavg(self._h, r, os.fsencode(output_dir))
             if st != _abi.HB_OK:
@@ -257,11 +273,11 @@ class BatchHybridEngine:
         """BatchHybridEngine::run_sweep_multi (engine.rs:845-851)."""
         arr, keep = _abi.sweep_points(spec.points)
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
-        run_flags = self._with_tuned(run_flags)
         r = C.c_void_p()
-        st = self._lib.hb_engine_run_sweep_multi(self._h, arr, len(spec.points), int(n_steps), int(run_flags),
-                                                 nptr, nlen, C.byref(r))
-        raise_for(st, self._lib.hb_last_error().decode())
+        run_flags = self._run_tuned(
+            lambda f: self._lib.hb_engine_run_sweep_multi(self._h, arr, len(spec.points), int(n_steps), int(f),
+                                                          nptr, nlen, C.byref(r)),
+            run_flags)
         return self._result(r, bool(run_flags & _abi.HB_RUN_TRAJECTORY))
 
     def run_sweep_multi_with_trajectory(self, spec: SweepSpec, n_steps: int, noise=None, run_flags: int = 0):
@@ -321,9 +337,8 @@ class BatchHybridEngine:
         out = _abi.hb_order_adjoint_out()
         dp = C.POINTER(C.c_double)
         out.loss, out.d_gain, out.d_omega, out.d_omega_node = (a.ctypes.data_as(dp) for a in (loss, dg, dw, dwn))
-        run_flags = self._with_tuned(run_flags)
-        st = self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), int(run_flags), C.byref(out))
-        raise_for(st, self._lib.hb_last_error().decode())
+        self._run_tuned(lambda f: self._lib.hb_engine_adjoint_order(self._h, _abi.f32p(g), g.size, int(n_steps), int(f),
+                                                                     C.byref(out)), run_flags)
         return OrderAdjointResult(loss, dg, dw, dwn, out.forward_ms, out.prepare_ms, out.reverse_ms)
 
     def adjoint_fc(self, gain_values, n_steps: int, target_fc, checkpoint_every: int = 500,
@@ -352,10 +367,9 @@ class BatchHybridEngine:
     def prepare(self, param: SweepParam, param_values, n_steps: int, noise=None, run_flags: int = 0) -> None:
         vals = np.ascontiguousarray(np.asarray(param_values, dtype=np.float32))
         nptr, nlen, _keep = self._noise_args(noise, n_steps)
-        run_flags = self._with_tuned(run_flags, param, vals)
-        st = self._lib.hb_engine_prepare(self._h, int(param.sub_idx), int(param.param_idx), _abi.f32p(vals), vals.size,
-                                         int(n_steps), int(run_flags), nptr, nlen)
-        raise_for(st, self._lib.hb_last_error().decode())
+        self._run_tuned(lambda f: self._lib.hb_engine_prepare(self._h, int(param.sub_idx), int(param.param_idx),
+                                                               _abi.f32p(vals), vals.size, int(n_steps), int(f), nptr, nlen),
+                        run_flags, param, vals)
 
     def execute_prepared(self) -> None:
         raise_for(self._lib.hb_engine_execute_prepared(self._h), self._lib.hb_last_error().decode())

@@ -79,3 +79,35 @@ def test_engine_uses_the_tuned_choice_by_default(tune_cache):
     auto = BatchHybridEngine.from_config(cfg6, 6, semantics=HB_SEM_DELAY_RING, tune="auto")
     auto.run_sweep(SweepParam(-1, 0), meta6["values"], 300)
     assert auto.tuned_flags is not None and autotune.best_run_flags(cfg6, 6, HB_SEM_DELAY_RING) == auto.tuned_flags
+
+
+def test_a_refused_cached_choice_falls_back_to_the_fixed_rules(monkeypatch):
+    """The cache key does not see every run option: when the engine refuses the cached kernel form for a
+    run (HB_ERR_UNSUPPORTED), the run is made again with the caller's flags; a refusal of a form the
+    caller chose is raised. (Host logic only: the library entry point is a fake.)"""
+    from hyburn_gb300 import BatchHybridEngine, _abi
+    eng = BatchHybridEngine.__new__(BatchHybridEngine)
+    eng.tune, eng.config, eng.n_sweep, eng.semantics, eng.tuned_flags = "cache", None, 4, 0, None
+
+    class Lib:
+        @staticmethod
+        def hb_last_error():
+            return b"refused"
+
+    eng._lib = Lib()
+    monkeypatch.setattr(autotune, "best_run_flags", lambda *a: HB_RUN_STREAM)
+    seen = []
+
+    def refuses_stream(f):
+        seen.append(f)
+        return _abi.HB_ERR_UNSUPPORTED if f & HB_RUN_STREAM else _abi.HB_OK
+
+    assert eng._run_tuned(refuses_stream, _abi.HB_RUN_TRAJECTORY) == _abi.HB_RUN_TRAJECTORY
+    assert seen == [HB_RUN_STREAM | _abi.HB_RUN_TRAJECTORY, _abi.HB_RUN_TRAJECTORY] and eng.tuned_flags is None
+    seen.clear()
+    with pytest.raises(Unsupported):
+        eng._run_tuned(refuses_stream, HB_RUN_STREAM)  # the caller's own choice: no cache, no second call
+    assert seen == [HB_RUN_STREAM]
+    assert eng._run_tuned(lambda f: _abi.HB_OK, 0) == HB_RUN_STREAM and eng.tuned_flags == HB_RUN_STREAM
+    eng.tune = "off"
+    assert eng._run_tuned(lambda f: _abi.HB_OK, 0) == 0 and eng.tuned_flags is None
