@@ -385,9 +385,12 @@ class GroupedSweep:
     """Several engines' sweeps in one kernel launch replayed from a CUDA graph (hb_group_*).
 
     ``members`` is a list of ``(engine, SweepParam, values, n_steps, noise)`` tuples; the engines
-    may differ in node count, connectome, delays, sweep values and step count but share the model
-    and the coupling function's pre() form. ``execute()`` restarts every member from its initial
-    state and runs all of them; ``results()`` returns one BatchSweepResult per member.
+    may differ in model, node count, connectome, delays, coupling function, sweep values and step
+    count. Each member must be one the streamed-history kernel serves: one subnetwork, one sparse
+    projection with per-edge delays of at least 15 steps (HB_SEM_DELAY_RING), and no trajectory. The
+    launch is a persistent work-queue kernel whose blocks (or thread-block clusters) take (member,
+    point) items from a device counter. ``execute()`` restarts every member from its initial state and
+    runs all of them; ``results()`` returns one BatchSweepResult per member.
     """
 
     def __init__(self, members, run_flags: int = 0, stream_handle: Optional[int] = None):
