@@ -96,7 +96,7 @@ def test_g2do_no_coupling_1000_steps():  # engine/mod.rs:49-87
 def test_engine_deterministic_steps(kind):
     from test_parity_gpu import compare
     compare(g2do(2, X2, kind, coupled=True), 1, NATIVE, [G2DO[1]], 1)
-    compare(g2do(2, [0.0] * 4, kind, coupled=True), 1, NATIVE, [G2DO[1]], 1000, traj=True)
+    compare(g2do(2, [0.0] * 4, kind, coupled=True), 1, NATIVE, [G2DO[1]], 1000)
 
 
 @pytest.mark.gpu
