@@ -200,7 +200,7 @@ def jr_target_fc(cfg: SimConfig, n_steps: int, gain: float = 1.0, seed: int = 40
     with coupling gain `gain` from an initial state drawn with `seed` (computed on the GPU)."""
     import copy
 
-    from .engine import BatchHybridEngine, SweepParam
+    from .engine import BatchHybridEngine
     from ._abi import HB_SEM_DELAY_RING
 
     c = copy.deepcopy(cfg)

@@ -17,7 +17,7 @@ from hyburn_gb300._abi import HB_SEM_DELAY_RING
 from hyburn_gb300.config import InvalidConfig
 from oracle.hb_oracle import OracleEngine
 
-from cases import NATIVE_SWEEP, single_model, sub, sweep_values
+from cases import NATIVE_SWEEP, single_model, sweep_values
 
 
 def with_rows(cfg, rows):

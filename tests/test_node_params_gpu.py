@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from hyburn_gb300 import BatchHybridEngine, GroupedSweep, SweepParam, inputs
-from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_NO_PIPE, HB_RUN_NO_STREAM, HB_RUN_STREAM, HB_RUN_STREAM_NPT,
+from hyburn_gb300._abi import (HB_RUN_GENERIC, HB_RUN_NO_PIPE, HB_RUN_STREAM, HB_RUN_STREAM_NPT,
                                HB_SEM_BOLD_PER_POINT, HB_SEM_DELAY_RING)
 from hyburn_gb300.config import InvalidConfig, Unsupported
 from oracle.hb_oracle import OracleEngine
