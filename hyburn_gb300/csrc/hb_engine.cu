@@ -93,6 +93,15 @@ const int k_other_nvar[] = {1, 2, 2, 2, 4, 4, 4, 3, 2, 6, 2, 2, 3, 5, 8, 12, 4, 
 const int k_other_ncvar[] = {1, 2, 2, 2, 4, 4, 4, 1, 1, 2, 1, 1, 1, 1, 3, 1, 2, 2, 4, 1, 1, 1};
 const int k_other_np[] = {1, 2, 3, 4, 5, 9, 9, 32, 12, 17, 19, 20, 13, 27, 28, 18, 8, 12, 14, 50, 50, 14};
 
+// the registry's names in its order, comma-separated: the list SimConfig::validate prints for an
+// unknown model (config.rs:297-303)
+std::string known_models() {
+    std::string out;
+    for (const ModelInfo& mi : k_models) out += (out.empty() ? "" : ", ") + std::string(mi.name);
+    for (const char* n : k_other_models) out += ", " + std::string(n);
+    return out;
+}
+
 int model_id(const char* name) {
     if (!name) return -1;
     for (int i = 0; i < 6; i++)
@@ -1209,11 +1218,13 @@ int32_t hb_abi_version(void) { return HB_ABI_VERSION; }
 const char* hb_last_error(void) { return g_err.c_str(); }
 
 hb_status hb_model_info(const char* model, int32_t* nvar, int32_t* ncvar, int32_t* n_params) {
+    if (!nvar || !ncvar || !n_params) return fail(HB_ERR_INVALID_STATE, "NULL output pointer");
     int m = model_id(model);
     if (m >= 0) { *nvar = k_models[m].nvar; *ncvar = k_models[m].ncvar; *n_params = k_models[m].nparams; return HB_OK; }
     for (int i = 0; i < 22; i++)
         if (model && !strcmp(model, k_other_models[i])) { *nvar = k_other_nvar[i]; *ncvar = k_other_ncvar[i]; *n_params = k_other_np[i]; return HB_OK; }
-    return fail(HB_ERR_INVALID_CONFIG, "Unknown model: %s", model ? model : "(null)");
+    return fail(HB_ERR_INVALID_CONFIG, "Unknown model '%s'. Known models: %s", model ? model : "(null)",
+                known_models().c_str());
 }
 
 hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** out) {
@@ -1248,7 +1259,8 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
             if (is_other_model(sd.model))
                 return bail(fail(HB_ERR_UNSUPPORTED, "model '%s' is not batch-native in the reference (per-point fallback); "
                                  "this engine implements the six batch-native models", sd.model));
-            return bail(fail(HB_ERR_INVALID_CONFIG, "Unknown model: %s", sd.model ? sd.model : "(null)"));
+            return bail(fail(HB_ERR_INVALID_CONFIG, "Unknown model '%s' in subnetwork %d. Known models: %s",
+                             sd.model ? sd.model : "(null)", i, known_models().c_str()));
         }
         if (sd.nnodes < 1 || sd.nmodes < 1) return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: nnodes and nmodes must be >= 1", i));
         s.nnodes = sd.nnodes; s.nmodes = sd.nmodes; s.nm = sd.nnodes * sd.nmodes;
