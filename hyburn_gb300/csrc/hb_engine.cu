@@ -1262,7 +1262,9 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
             return bail(fail(HB_ERR_INVALID_CONFIG, "Unknown model '%s' in subnetwork %d. Known models: %s",
                              sd.model ? sd.model : "(null)", i, known_models().c_str()));
         }
-        if (sd.nnodes < 1 || sd.nmodes < 1) return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: nnodes and nmodes must be >= 1", i));
+        // messages of SimConfig::validate (config.rs:305-309) where it checks the same thing
+        if (sd.nmodes < 1) return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: nmodes must be >= 1", i));
+        if (sd.nnodes < 1) return bail(fail(HB_ERR_INVALID_CONFIG, "Subnetwork %d: nnodes must be >= 1", i));
         s.nnodes = sd.nnodes; s.nmodes = sd.nmodes; s.nm = sd.nnodes * sd.nmodes;
         s.nvar = k_models[s.model].nvar; s.ncvar = k_models[s.model].ncvar;
         if (sd.n_params < k_models[s.model].nparams || sd.n_params > 24)
@@ -1334,10 +1336,16 @@ hb_status hb_engine_create(const hb_sim_desc* d, int32_t n_sweep, hb_engine** ou
             hp.kind = (d->flags & HB_SEM_SCALAR_DIAGONAL) ? W_DIAG : W_MEAN;
             hp.w = pd.scalar_weight;
             if (hp.kind == W_DIAG && hp.nsrc != hp.ntgt)
-                return bail(fail(HB_ERR_INVALID_CONFIG, "Scalar weights require src and tgt nnodes to match"));
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: scalar weights require src and tgt nnodes to match (%d != %d)",
+                                 p, S.nnodes, Tg.nnodes));
         } else if (pd.weights_kind == HB_WEIGHTS_DENSE) {
-            if (!pd.dense || pd.dense_rows != hp.ntgt || pd.dense_cols != hp.nsrc)
-                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: weights must be [%d x %d], got [%d x %d]", p, hp.ntgt, hp.nsrc, pd.dense_rows, pd.dense_cols));
+            if (!pd.dense) return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: dense weights pointer is NULL", p));
+            if (pd.dense_rows != hp.ntgt)  // config.rs:375-380
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: weights has %d rows, expected %d (tgt nnodes)", p,
+                                 pd.dense_rows, hp.ntgt));
+            if (pd.dense_cols != hp.nsrc)  // config.rs:381-388 (every row has dense_cols entries here)
+                return bail(fail(HB_ERR_INVALID_CONFIG, "Projection %d: weights row 0 has %d cols, expected %d (src nnodes)", p,
+                                 pd.dense_cols, hp.nsrc));
             hp.kind = W_SPARSE;
             dense.assign(pd.dense, pd.dense + (size_t)hp.ntgt * hp.nsrc);
         } else if (pd.weights_kind == HB_WEIGHTS_CSR) {

@@ -200,3 +200,35 @@ def test_run_flag_macros_match_the_header():
     # distinct codes for the distinct cluster sizes
     codes = [_abi.HB_RUN_STREAM_CLUSTER(c) for c in (1, 2, 3, 4, 5, 6, 8)]
     assert len(set(codes)) == len(codes) and 0 not in codes
+
+
+def _two_subnets(n0=4, n1=3, weights=0.5, conn="all_to_all", src=0, tgt=1, nmodes=1, params=None, x0=None):
+    from hyburn_gb300.config import NetworkConfig, ProjectionConfig, SubnetworkConfig
+    g = [1.0, 0.0, -2.0, -10.0, 0.0, 0.02, 3.0, 1.0, 0.0, 1.0, 1.0, 1.0]
+    subs = [SubnetworkConfig("Generic2dOscillator", n0, x0 if x0 is not None else [0.1] * (2 * n0 * nmodes),
+                             params or g, nmodes=nmodes),
+            SubnetworkConfig("Generic2dOscillator", n1, [0.1] * (2 * n1), g)]
+    return SimConfig(sim_length=10.0, dt=0.1, network=NetworkConfig(
+        subs, [ProjectionConfig(src, tgt, weights, conn_type=conn, coupling_fn="Linear", coupling_params=[0.1])]))
+
+
+@pytest.mark.parametrize("case,semantics", [
+    ("nmodes", 0), ("params", 0), ("initial_state", 0), ("src", 0), ("scalar_sizes", _abi.HB_SEM_SCALAR_DIAGONAL),
+    ("dense_rows", 0), ("csr_indptr", 0)])
+def test_boundary_errors_carry_the_reference_messages(case, semantics):
+    """Where hb_engine_create checks what SimConfig::validate checks (config.rs:286-429), a C caller gets
+    the same error kind and text that validate gives (here through the Python mirror's validate)."""
+    cfg = {
+        "nmodes": lambda: _two_subnets(nmodes=0, x0=[0.1] * 8),
+        "params": lambda: _two_subnets(params=[1.0] * 3),
+        "initial_state": lambda: _two_subnets(x0=[0.1] * 5),
+        "src": lambda: _two_subnets(src=3),
+        "scalar_sizes": lambda: _two_subnets(weights=0.5),
+        "dense_rows": lambda: _two_subnets(weights=[[1.0] * 4] * 2),
+        "csr_indptr": lambda: _two_subnets(weights={"data": [1.0], "indices": [0], "indptr": [0, 1]}, conn="csr"),
+    }[case]()
+    with pytest.raises(InvalidConfig) as want:
+        cfg.validate()
+    with pytest.raises(InvalidConfig) as got:
+        BatchHybridEngine.from_config(cfg, 2, semantics=semantics)
+    assert str(got.value) == str(want.value)
