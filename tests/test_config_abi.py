@@ -232,3 +232,27 @@ def test_boundary_errors_carry_the_reference_messages(case, semantics):
     with pytest.raises(InvalidConfig) as got:
         BatchHybridEngine.from_config(cfg, 2, semantics=semantics)
     assert str(got.value) == str(want.value)
+
+
+def test_last_error_is_per_thread():
+    """hb_last_error() is the calling thread's message (the header's contract): two threads set different
+    errors, then each reads its own after the other has set its."""
+    import threading
+    lib = _abi.load_library()
+    gate = threading.Barrier(2)
+    got = {}
+
+    def worker(name):
+        nv, nc, npar = C.c_int32(), C.c_int32(), C.c_int32()
+        assert lib.hb_model_info(name.encode(), C.byref(nv), C.byref(nc), C.byref(npar)) == _abi.HB_ERR_INVALID_CONFIG
+        gate.wait()  # both errors are set
+        gate.wait()
+        got[name] = lib.hb_last_error().decode()
+
+    ts = [threading.Thread(target=worker, args=(n,)) for n in ("ModelOfThreadA", "ModelOfThreadB")]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert "ModelOfThreadA" in got["ModelOfThreadA"] and "ModelOfThreadB" not in got["ModelOfThreadA"]
+    assert "ModelOfThreadB" in got["ModelOfThreadB"] and "ModelOfThreadA" not in got["ModelOfThreadB"]
