@@ -346,6 +346,7 @@ def load_library():
         "hb_engine_reset": (I32, [P]),
         "hb_engine_last_kernel_time": (I32, [P, C.POINTER(D), C.POINTER(I64), C.POINTER(I32)]),
         "hb_engine_set_stream": (I32, [P, P]),
+        "hb_engine_set_hybrid_integrator": (I32, [P, I32]),
         "hb_engine_prepare": (I32, [P, I32, I32, FP, I32, I64, U32, FP, I64]),
         "hb_engine_execute_prepared": (I32, [P]),
         "hb_group_prepare": (I32, [C.POINTER(hb_group_member), I32, P, C.POINTER(P)]),

@@ -1690,6 +1690,15 @@ hb_status hb_engine_last_kernel_time(const hb_engine* e, double* ms, int64_t* la
     return HB_OK;
 }
 
+hb_status hb_engine_set_hybrid_integrator(hb_engine* e, int32_t on) {
+    if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
+    if (on) e->flags |= HB_SEM_HYBRID_INTEGRATOR;
+    else e->flags &= ~(uint32_t)HB_SEM_HYBRID_INTEGRATOR;
+    // each subnetwork's integrator in the device network (uploaded with the tables of every run)
+    for (size_t i = 0; i < e->subs.size(); i++) e->net.sub[i].integ = eff_integrator(e, e->subs[i].model);
+    return HB_OK;
+}
+
 hb_status hb_engine_set_stream(hb_engine* e, void* stream) {
     if (!e) return fail(HB_ERR_INVALID_STATE, "NULL engine");
     if (e->own_stream) CUDA_TRY(cudaStreamSynchronize(e->own_stream));

@@ -156,6 +156,7 @@ class BatchHybridEngine:
         st = self._lib.hb_engine_create(C.byref(self._sd.desc), self.n_sweep, C.byref(h))
         raise_for(st, self._lib.hb_last_error().decode())
         self._h = h
+        self._hybrid = bool(self.semantics & _abi.HB_SEM_HYBRID_INTEGRATOR)
         self.models = [s.model for s in config.network.subnetworks]
         self.tune = "cache"
         self.tuned_flags: Optional[int] = None  # the autotuner's choice the last run used, if any
@@ -301,6 +302,18 @@ class BatchHybridEngine:
 
     def reset(self) -> None:
         raise_for(self._lib.hb_engine_reset(self._h), self._lib.hb_last_error().decode())
+
+    @property
+    def hybrid_integrator(self) -> bool:
+        """The public field `hybrid_integrator` (engine.rs:125): Heun for Generic2dOscillator
+        subnetworks and Euler for the others (engine.rs:697-702). Set it between runs, as callers of
+        the reference do after from_config; created from the HB_SEM_HYBRID_INTEGRATOR semantics flag."""
+        return bool(self._hybrid)
+
+    @hybrid_integrator.setter
+    def hybrid_integrator(self, on: bool) -> None:
+        raise_for(self._lib.hb_engine_set_hybrid_integrator(self._h, 1 if on else 0), self._lib.hb_last_error().decode())
+        self._hybrid = bool(on)
 
     def set_stream(self, stream_handle: Optional[int]) -> None:
         raise_for(self._lib.hb_engine_set_stream(self._h, C.c_void_p(stream_handle or 0)),

@@ -256,6 +256,14 @@ hb_status hb_engine_last_kernel_time(const hb_engine* engine, double* ms, int64_
  * restores the engine's own stream. */
 hb_status hb_engine_set_stream(hb_engine* engine, void* cuda_stream);
 
+/* Replaces an assignment to the public field `BatchHybridEngine::hybrid_integrator`
+ * (engine.rs:125, read by the step at engine.rs:697-702; callers set it after from_config, e.g.
+ * examples/bench/hyburn_bench_generic_cuda.rs:54). on != 0: Heun for Generic2dOscillator
+ * subnetworks and Euler for the others, whatever the configured integrator; 0: the configured
+ * integrator for every subnetwork. Same as creating the engine with or without
+ * HB_SEM_HYBRID_INTEGRATOR; takes effect at the next run or prepare. */
+hb_status hb_engine_set_hybrid_integrator(hb_engine* engine, int32_t on);
+
 /* ---- device-resident runs (inputs already in HBM; used to time the kernels alone) ---- */
 
 /* Upload the sweep values and noise of a run once; later `hb_engine_execute_prepared` calls

@@ -174,6 +174,7 @@ def test_new_entry_points_reject_null_arguments_without_a_gpu():
     assert lib.hb_engine_fc_features(None, 0, 0, 1, C.byref(out)) == _abi.HB_ERR_INVALID_STATE
     oa = _abi.hb_order_adjoint_out()
     assert lib.hb_engine_adjoint_order(None, None, 0, 10, 0, C.byref(oa)) == _abi.HB_ERR_INVALID_STATE
+    assert lib.hb_engine_set_hybrid_integrator(None, 1) == _abi.HB_ERR_INVALID_STATE
     assert b"NULL" in lib.hb_last_error() or b"null" in lib.hb_last_error()
 
 

@@ -213,6 +213,29 @@ def test_scalar_diagonal_and_hybrid_integrator():
     compare(cfg, 2, SweepParam(0, 1), [0.0, 0.2], 60, semantics=HB_SEM_SCALAR_DIAGONAL | HB_SEM_HYBRID_INTEGRATOR)
 
 
+def test_hybrid_integrator_set_after_creation():
+    """`engine.hybrid_integrator = true` after from_config, as the reference's callers do
+    (examples/bench/hyburn_bench_generic_cuda.rs:54): the same run as an engine created with the flag
+    (bit for bit) and as the oracle's; set back to false, the configured RK4 again."""
+    cfg = three_subnet_ring(8, "rk4")
+    p, v = SweepParam(0, 1), [0.0, 0.2]
+    eng = BatchHybridEngine.from_config(cfg, 2)
+    assert eng.hybrid_integrator is False
+    eng.hybrid_integrator = True
+    a = eng.run_sweep(p, v, 60)
+    b = BatchHybridEngine.from_config(cfg, 2, semantics=HB_SEM_HYBRID_INTEGRATOR).run_sweep(p, v, 60)
+    o = OracleEngine.from_config(cfg, 2, semantics=HB_SEM_HYBRID_INTEGRATOR).run_sweep(p, v, 60)
+    for i in range(3):
+        assert np.array_equal(a.final_states[i], b.final_states[i]) and np.array_equal(a.tavg[i], b.tavg[i])
+        close(a.final_states[i], o.final_states[i], what=f"hybrid final[{i}]")
+    eng.reset()
+    eng.hybrid_integrator = False
+    c = eng.run_sweep(p, v, 60)
+    d = BatchHybridEngine.from_config(cfg, 2).run_sweep(p, v, 60)
+    for i in range(3):
+        assert np.array_equal(c.final_states[i], d.final_states[i])
+
+
 @pytest.mark.parametrize("per_point", [False, True])
 @pytest.mark.parametrize("tr,period,n_steps", [(0.002, 10, 250), (0.0015, 10, 257), (0.001, 10, 200), (0.0025, 7, 101)])
 def test_bold_monitor(per_point, tr, period, n_steps):
