@@ -17,6 +17,9 @@ The cases are the workloads' own shapes, cut to a few hundred steps:
   frequencies omega ~ N(0, 1), 3 coupling scales, BOLD on, 80 steps;
 - ``meanfield_<model>_<integrator>``: each of the six models under Heun-stochastic and RK4, 20
   nodes, all-to-all scalar coupling, the model's native parameter swept over 4 points, 120 steps;
+- ``refbench_3subnet_*``: the generic-engine workload of the reference's batch-sweep benchmark (a
+  G2DO -> JansenRit -> WilsonCowan ring of 76 or 164 nodes per population, 1000 Heun steps), over 32
+  or 8 of its I values;
 - ``example_*``: the reference's own example configurations (``examples/*.toml`` with their
   ``examples/init_*_74.npy`` initial states), loaded through this package's TOML reader, run for
   their full ``sim_length`` the way its batch-sweep command runs them (``hyburn run -c <config>
@@ -301,6 +304,31 @@ def _example(config: str, sweep: Optional[str], n_points: int):
                     noise=None, rtol=1e-5, atol=1e-6, bitwise=False, bound="fp32", source=src)
     return make
 
+
+def _refbench(nnodes: int, n_points: int):
+    """The generic-engine workload of the reference's batch-sweep benchmark
+    (examples/bench/hyburn_bench_batch_sweep.rs:18-26, 72-150): a G2DO -> JansenRit -> WilsonCowan ring,
+    each subnetwork `nnodes` nodes from a zero state with its default parameters, all-to-all Scalar
+    weights 0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1 for 1000 steps, G2DO's I swept
+    as -0.5 + i / (n - 1) (the benchmark runs 1024 points; fewer here, with the same formula)."""
+    def make():
+        from hyburn_gb300.config import DEFAULT_PARAMS
+        n_steps, dt, w = 1000, 0.1, 0.01
+        subs = [SubnetworkConfig(m, nnodes, [0.0] * (nv * nnodes), list(DEFAULT_PARAMS[m]))
+                for m, nv in (("Generic2dOscillator", 2), ("JansenRit", 6), ("WilsonCowan", 2))]
+        projs = [ProjectionConfig(s, t, w, coupling_fn="Linear", coupling_params=[1.0], delays=[0])
+                 for s, t in ((0, 1), (1, 2), (2, 0))]
+        cfg = SimConfig(sim_length=n_steps * dt, dt=dt, integrator="heun", network=NetworkConfig(subs, projs))
+        f = np.float32
+        values = [float(f(-0.5) + f(i) * (f(1.0) / f(max(n_points - 1, 1)))) for i in range(n_points)]
+        return dict(cfg=cfg, n_sweep=n_points, param=SweepParam(0, 1), values=values, n_steps=n_steps, semantics=0,
+                    noise=None, rtol=1e-5, atol=1e-6, bitwise=False, bound="fp32",
+                    source="examples/bench/hyburn_bench_batch_sweep.rs (generic BatchHybridEngine workload)")
+    return make
+
+
+CASES["refbench_3subnet_76n"] = _refbench(76, 32)
+CASES["refbench_3subnet_164n"] = _refbench(164, 8)
 
 EXAMPLES = {
     "example_g2do_sweep": ("g2do_sweep.toml", "sweep.toml", 128),
