@@ -93,3 +93,46 @@ def test_engine_gpu_csr_matvec_basic(weights, conn):
     from hyburn_gb300 import BatchHybridEngine
     c = coupling_from_one_step(BatchHybridEngine, weights, conn)
     assert np.allclose(c, [4.0, 9.0, 1.0], rtol=1e-3), c
+
+
+def _random_pair(seed):
+    """A random network twice: dense weights and the same matrix as CSR (seeded)."""
+    from cases import sub
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(3, 12))
+    w = np.where(rng.random((n, n)) < 0.4, rng.uniform(0.1, 1.0, (n, n)), 0.0).astype(np.float32)
+    rows, cols = np.nonzero(w)
+    csr = {"data": w[rows, cols].tolist(), "indices": cols.tolist(),
+           "indptr": np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=n))]).tolist()}
+    fn, cp = [("Linear", [0.3, 0.01]), ("Sigmoidal", [0.0, 1.0, 0.0, 1.0, 1.0]), ("HyperbolicTangent", [0.1, 1.0, 0.2, 2.0]),
+              ("Difference", [0.05])][seed % 4]
+    integ = ["heun", "rk4", "euler"][seed % 3]
+    delay = [int(rng.integers(0, 6))]
+    return [SimConfig(sim_length=1.0, dt=0.1, integrator=integ,
+                      network=NetworkConfig([sub("Generic2dOscillator", n, seed)],
+                                            [ProjectionConfig(0, 0, weights, conn_type=conn, delays=delay,
+                                                              coupling_fn=fn, coupling_params=cp)]))
+            for weights, conn in ((w.tolist(), "all_to_all"), (csr, "csr"))]
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_csr_is_the_dense_matrix_it_stores(seed):
+    """The batch engine densifies CSR weights (engine.rs:298-322), so in its default delay semantics a
+    CSR projection and the dense matrix it stores give the same run bit for bit: random networks,
+    coupling functions, delays and integrators through the oracle."""
+    out = [oracle().from_config(cfg, 2).run_sweep(NATIVE, [0.0, 0.3], 40) for cfg in _random_pair(seed)]
+    assert np.array_equal(out[0].final_states[0], out[1].final_states[0])
+    assert np.array_equal(out[0].tavg[0], out[1].tavg[0])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(12))
+def test_engine_gpu_csr_is_the_dense_matrix_it_stores(seed):
+    """The same on the GPU: both forms become the same edge list, so the runs agree bit for bit; the
+    dense one against the oracle."""
+    from hyburn_gb300 import BatchHybridEngine
+    from test_parity_gpu import compare
+    dense, csr = _random_pair(seed)
+    compare(dense, 2, NATIVE, [0.0, 0.3], 40)
+    a, b = (BatchHybridEngine.from_config(c, 2).run_sweep(NATIVE, [0.0, 0.3], 40) for c in (dense, csr))
+    assert np.array_equal(a.final_states[0], b.final_states[0]) and np.array_equal(a.tavg[0], b.tavg[0])
