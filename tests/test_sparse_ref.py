@@ -136,3 +136,25 @@ def test_engine_gpu_csr_is_the_dense_matrix_it_stores(seed):
     compare(dense, 2, NATIVE, [0.0, 0.3], 40)
     a, b = (BatchHybridEngine.from_config(c, 2).run_sweep(NATIVE, [0.0, 0.3], 40) for c in (dense, csr))
     assert np.array_equal(a.final_states[0], b.final_states[0]) and np.array_equal(a.tavg[0], b.tavg[0])
+
+
+def _two_population_dense():
+    """engine.rs:1634-1690: two 2-node G2DO populations (initial state [0.1, 0.1, 0.2, 0.2], default
+    parameters), an identity dense projection from the first to the second with delay 0, Linear(1.0),
+    Euler at dt 0.1."""
+    from hyburn_gb300.config import SubnetworkConfig
+    subs = [SubnetworkConfig("Generic2dOscillator", 2, [0.1, 0.1, 0.2, 0.2], list(G2DO)) for _ in range(2)]
+    proj = ProjectionConfig(0, 1, [[1.0, 0.0], [0.0, 1.0]], delays=[0], coupling_fn="Linear", coupling_params=[1.0])
+    return SimConfig(sim_length=10.0, dt=0.1, integrator="euler", network=NetworkConfig(subs, [proj]))
+
+
+def test_batch_engine_dense_coupling_shape():  # engine.rs:1634-1690
+    r = oracle().from_config(_two_population_dense(), 2).run_sweep(NATIVE, [0.0, 0.5], 10)
+    assert r.n_sweep == 2 and len(r.tavg) == 2
+    assert all(np.isfinite(t).all() and t.size == 2 * 2 * 2 for t in r.tavg)
+
+
+@pytest.mark.gpu
+def test_engine_gpu_dense_coupling_between_populations():
+    from test_parity_gpu import compare
+    compare(_two_population_dense(), 2, NATIVE, [0.0, 0.5], 10)
