@@ -785,7 +785,8 @@ def main():
         "gpu_launches": int(sum(n for _, n in kern)),
         "clocks": clocks,
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    # the CPU baseline is timed at N = 1 only, so that no GPU of a multi-rank job idles meanwhile
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_line()
     if rank == 0:
         print(json.dumps(line), flush=True)
