@@ -20,6 +20,13 @@
  * Built twice: FP32 (HBO_REAL=float, symbols hbo_*) and an FP64 twin (HBO_REAL=double,
  * symbols hbo64_*) used to report drift against a higher-precision integration.
  * Compile with -ffp-contract=off so that no multiply-add is fused (Rust does not fuse either).
+ *
+ * Pinning: the reference's own known-answer tests (dfuns, clamps, coupling pre/post, BOLD, sweep
+ * order, ring semantics; restated in tests/test_oracle_kat.py, tests/test_config_ref.py,
+ * tests/test_integrator_ref.py, tests/test_sparse_ref.py) pin the units and the engine semantics.
+ * Whole trajectories are unpinned against the reference itself: it is Rust, no Rust toolchain is
+ * available to run it, and its TVB trajectory files are git-LFS pointers. The fixtures in
+ * tests/golden/ keep this oracle's own outputs from drifting; they are not the reference's outputs.
  */
 #include <math.h>
 #include <stdint.h>
