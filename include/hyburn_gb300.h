@@ -200,7 +200,10 @@ typedef struct hb_engine hb_engine;
 typedef struct hb_result hb_result;
 
 /* ---- library ---- */
+/* HB_ABI_VERSION of the built library (no reference counterpart: the FFI crate checks it at load). */
 int32_t     hb_abi_version(void);
+/* The calling thread's message for the last failed call: the text of the SimulationError
+ * (error.rs:6-25) that the reference would return. Valid until the thread's next call. */
 const char* hb_last_error(void);
 
 /* Number of state variables / coupling variables / parameters of a model name
@@ -213,7 +216,7 @@ hb_status hb_model_info(const char* model, int32_t* nvar, int32_t* ncvar, int32_
  * Validates the descriptor, builds the device-side projection tables and uploads them. */
 hb_status hb_engine_create(const hb_sim_desc* desc, int32_t n_sweep, hb_engine** out);
 
-/* Drop of BatchHybridEngine. Accepts NULL. */
+/* Drop of BatchHybridEngine (engine.rs:105-138; the reference frees on scope exit). Accepts NULL. */
 void hb_engine_destroy(hb_engine* engine);
 
 /* BatchHybridEngine::run_sweep / run_sweep_with_trajectory (engine.rs:477-494, 496-842).
@@ -248,12 +251,13 @@ int64_t   hb_engine_step(const hb_engine* engine);
 hb_status hb_engine_reset(hb_engine* engine);
 
 /* Milliseconds of device time of the last run's simulation kernels, measured with CUDA events
- * on the engine's stream, and the number of kernel launches of that run. */
+ * on the engine's stream, and the number of kernel launches of that run (no reference counterpart;
+ * BatchSweepResult::elapsed_ms, engine.rs:28, is the host wall time of the whole call). */
 hb_status hb_engine_last_kernel_time(const hb_engine* engine, double* ms, int64_t* launches,
                                      int32_t* kernel_kind);
 
 /* Use a caller-provided CUDA stream (cudaStream_t passed as void*) for subsequent runs; NULL
- * restores the engine's own stream. */
+ * restores the engine's own stream (no reference counterpart: Burn owns its device queue). */
 hb_status hb_engine_set_stream(hb_engine* engine, void* cuda_stream);
 
 /* Replaces an assignment to the public field `BatchHybridEngine::hybrid_integrator`
@@ -267,7 +271,8 @@ hb_status hb_engine_set_hybrid_integrator(hb_engine* engine, int32_t on);
 /* ---- device-resident runs (inputs already in HBM; used to time the kernels alone) ---- */
 
 /* Upload the sweep values and noise of a run once; later `hb_engine_execute_prepared` calls
- * reset the engine and run all steps on the device without host transfers. */
+ * reset the engine and run all steps on the device without host transfers (no reference
+ * counterpart; the same run as hb_engine_run_sweep, engine.rs:477-484, minus the copies). */
 hb_status hb_engine_prepare(hb_engine* engine, int32_t sub_idx, int32_t param_idx,
                             const float* values, int32_t n_values, int64_t n_steps,
                             uint32_t run_flags, const float* noise, int64_t noise_len);
@@ -308,11 +313,14 @@ hb_status hb_noalloc_run_csr_sweep(
 
 /* ---- grouped launch: several engines' sweeps in one kernel launch (no counterpart in the reference) ----
  * The reference runs each network size as its own BatchHybridEngine, one after the other. A grouped
- * launch runs the sweeps of several engines — different node counts, connectomes, delays, sweep
- * values and step counts, one model and coupling pre() form — as one launch of the
- * streamed-history kernel (one block per sweep point, longest points first), so short points fill
- * the SMs that long ones leave free. Every member needs one subnetwork coupled to itself through
- * one CSR projection with per-edge delays (HB_SEM_DELAY_RING) of at least 15 steps.
+ * launch runs the sweeps of several engines — different models, node counts, connectomes, delays,
+ * coupling functions, sweep values and step counts — as one launch of a persistent work-queue
+ * kernel: CTAs, or thread-block clusters (HB_RUN_STREAM_CLUSTER in the members' run flags, else
+ * chosen by the engine), take (member, point) items from a device counter, members with the most
+ * work per CTA first, so short points fill the SMs that long ones leave free; a member with at
+ * least 100 nodes per CTA runs each point split over a cluster. Every member needs one subnetwork
+ * coupled to itself through one CSR projection with per-edge delays (HB_SEM_DELAY_RING) of at
+ * least 15 steps.
  * hb_group_prepare resets every member engine, uploads its tables and noise, and captures the
  * member resets, the launch and the batch-mean BOLD reductions in a CUDA graph;
  * hb_group_execute replays it (each member restarts from its initial state) and completes the
