@@ -190,6 +190,27 @@ def workload_config(n_run=N_STEPS) -> dict:
             "l2": "flushed (512 MiB write) between timed GPU iterations"}
 
 
+# The reference's published time for its own batch-sweep benchmark, generic BatchHybridEngine on Burn
+# CUDA, 1024 points x 1000 steps: (node-steps/s, source) per population size
+RING3_PUBLISHED = {76: (6.49e8, "docs/BENCHMARK.md:16-20 (360 ms)"), 164: (1.48e9, "docs/BENCHMARK.md:30-38 (341 ms)")}
+
+
+def ring3_workload(nnodes: int, n_points: int, n_steps: int):
+    """The generic-engine workload of the reference's batch-sweep benchmark
+    (examples/bench/hyburn_bench_batch_sweep.rs:18-26, 72-150): a G2DO -> JansenRit -> WilsonCowan ring,
+    `nnodes` nodes per population from a zero state with default parameters, all-to-all Scalar weights
+    0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1; G2DO's I swept as -0.5 + i / (n - 1)."""
+    from hyburn_gb300.config import DEFAULT_PARAMS, NetworkConfig, ProjectionConfig, SimConfig, SubnetworkConfig
+    subs = [SubnetworkConfig(m, nnodes, [0.0] * (nv * nnodes), list(DEFAULT_PARAMS[m]))
+            for m, nv in (("Generic2dOscillator", 2), ("JansenRit", 6), ("WilsonCowan", 2))]
+    projs = [ProjectionConfig(s, t, 0.01, coupling_fn="Linear", coupling_params=[1.0], delays=[0])
+             for s, t in ((0, 1), (1, 2), (2, 0))]
+    cfg = SimConfig(sim_length=n_steps * 0.1, dt=0.1, integrator="heun", network=NetworkConfig(subs, projs))
+    f = np.float32
+    values = [float(f(-0.5) + f(i) * (f(1.0) / f(max(n_points - 1, 1)))) for i in range(n_points)]
+    return cfg, values
+
+
 def algorithmic_bytes_per_node_step(meta, n_points=N_POINTS) -> float:
     """Delayed reads of the coupling variable (4 B per in-edge), the ring write (4 B) and the
     shared noise draws (2 x 4 B per node per step, read once for all points)."""
@@ -563,6 +584,28 @@ def run_other_workload(args):
                                   "frac": issued / (ms / 1e3) / 1e12 / peaks_tf32(),
                                   "peak_kind": "half the measured dense bf16 burst (TF32 runs at half the bf16 rate)",
                                   "useful_tflops": useful / (ms / 1e3) / 1e12, "traffic": None}))
+        elif args.workload == "ring3":
+            # the reference's own batch-sweep benchmark (generic engine): 3-population ring, 1024 points x
+            # 1000 Heun steps, against its published Burn CUDA time
+            T, n, B = args.run_steps or 1000, args.ring_nodes, 1024
+            cfg, vals = ring3_workload(n, B, T)
+            eng = BatchHybridEngine.from_config(cfg, B)
+            eng.prepare(SweepParam(0, 1), vals, T)
+            ms, kind = _time_prepared(eng, args.steps, args.warmup)
+            eng.close()
+            ns = B * 3 * n * T
+            value = ns / (ms / 1e3)
+            pub = RING3_PUBLISHED.get(n)
+            line.update(metric="node-steps/s", value=value, unit="node-steps/s", ms_per_step=ms,
+                        vs_baseline=(value / pub[0]) if pub and T == 1000 else None,
+                        config={"workload": f"ring3-g2do-jr-wc-{n}n-per-population-{B}pt-scalar-heun-{T}steps",
+                                "kernel_kind": kind,
+                                "source": "examples/bench/hyburn_bench_batch_sweep.rs, generic BatchHybridEngine"},
+                        baseline={"published_node_steps_per_s": pub[0] if pub else None,
+                                  "backend": "Burn CUDA, generic BatchHybridEngine", "source": pub[1] if pub else None},
+                        roofline={"bound": "latency", "note": "the generic resident kernel's per-step block barrier "
+                                  "and mean-field reductions; no DRAM or tensor roof binds (no history, 1 point per CTA)",
+                                  "us_per_integration_step": ms * 1e3 / T})
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -664,8 +707,9 @@ def main():
     ap.add_argument("--dense-points", type=int, default=1024, help="dense workload: sweep points")
     ap.add_argument("--stream-npt", type=int, default=0,
                     help="streamed-history kernel: nodes per consumer thread, 1/2/4 (0: engine's choice)")
+    ap.add_argument("--ring-nodes", type=int, default=76, help="ring3 workload: nodes per population (76 or 164)")
     ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint",
-                                                          "fc", "dense"],
+                                                          "fc", "dense", "ring3"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()

@@ -131,3 +131,14 @@ def test_engine_matches_the_golden_outputs(name):
         ex = eng.run_sweep(case.param, case.values, case.n_steps, noise=case.noise, run_flags=HB_RUN_EXACT_SUMS)
         check(ex, case, case.rtol, case.atol, exact=True)
     eng.close()
+
+
+@pytest.mark.parametrize("nodes,case", [(76, "refbench_3subnet_76n"), (164, "refbench_3subnet_164n")])
+def test_bench_ring3_workload_is_the_golden_case(nodes, case):
+    """bench.py's `--workload ring3` line runs the network the golden refbench case checks (its 1024 sweep
+    values follow the same formula as the case's fewer)."""
+    import bench
+    g = load_case(case)
+    cfg, values = bench.ring3_workload(nodes, g.n_sweep, g.n_steps)
+    assert pack_config(cfg)[0] == pack_config(g.cfg)[0]
+    assert np.array_equal(np.asarray(values, np.float32), g.values)
