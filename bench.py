@@ -196,10 +196,12 @@ RING3_PUBLISHED = {76: (6.49e8, "docs/BENCHMARK.md:16-20 (360 ms)"), 164: (1.48e
 
 
 def ring3_workload(nnodes: int, n_points: int, n_steps: int):
-    """The generic-engine workload of the reference's batch-sweep benchmark
-    (examples/bench/hyburn_bench_batch_sweep.rs:18-26, 72-150): a G2DO -> JansenRit -> WilsonCowan ring,
-    `nnodes` nodes per population from a zero state with default parameters, all-to-all Scalar weights
-    0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1; G2DO's I swept as -0.5 + i / (n - 1)."""
+    """The generic-engine workload of the reference's CUDA benchmark, the one its published 3-population
+    times are for (examples/bench/hyburn_bench_generic_cuda.rs:21-56, 116-131): a G2DO -> JansenRit ->
+    WilsonCowan ring, `nnodes` nodes per population from a zero state with default parameters, all-to-all
+    Scalar weights 0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1 with the hybrid integrator
+    set after from_config (Heun for G2DO, Euler for JansenRit and WilsonCowan); G2DO's I swept as
+    -0.5 + i / (n - 1) in f32."""
     from hyburn_gb300.config import DEFAULT_PARAMS, NetworkConfig, ProjectionConfig, SimConfig, SubnetworkConfig
     subs = [SubnetworkConfig(m, nnodes, [0.0] * (nv * nnodes), list(DEFAULT_PARAMS[m]))
             for m, nv in (("Generic2dOscillator", 2), ("JansenRit", 6), ("WilsonCowan", 2))]
@@ -207,7 +209,7 @@ def ring3_workload(nnodes: int, n_points: int, n_steps: int):
              for s, t in ((0, 1), (1, 2), (2, 0))]
     cfg = SimConfig(sim_length=n_steps * 0.1, dt=0.1, integrator="heun", network=NetworkConfig(subs, projs))
     f = np.float32
-    values = [float(f(-0.5) + f(i) * (f(1.0) / f(max(n_points - 1, 1)))) for i in range(n_points)]
+    values = [float(f(-0.5) + f(i) / f(max(n_points - 1, 1))) for i in range(n_points)]
     return cfg, values
 
 
@@ -590,6 +592,7 @@ def run_other_workload(args):
             T, n, B = args.run_steps or 1000, args.ring_nodes, 1024
             cfg, vals = ring3_workload(n, B, T)
             eng = BatchHybridEngine.from_config(cfg, B)
+            eng.hybrid_integrator = True  # as the reference's benchmark sets it (hyburn_bench_generic_cuda.rs:54)
             eng.prepare(SweepParam(0, 1), vals, T)
             ms, kind = _time_prepared(eng, args.steps, args.warmup)
             eng.close()
@@ -600,9 +603,11 @@ def run_other_workload(args):
                         vs_baseline=(value / pub[0]) if pub and T == 1000 else None,
                         config={"workload": f"ring3-g2do-jr-wc-{n}n-per-population-{B}pt-scalar-heun-{T}steps",
                                 "kernel_kind": kind,
-                                "source": "examples/bench/hyburn_bench_batch_sweep.rs, generic BatchHybridEngine"},
+                                "integrator": "hybrid: Heun for G2DO, Euler for JansenRit and WilsonCowan",
+                                "source": "examples/bench/hyburn_bench_generic_cuda.rs, generic BatchHybridEngine"},
                         baseline={"published_node_steps_per_s": pub[0] if pub else None,
-                                  "backend": "Burn CUDA, generic BatchHybridEngine", "source": pub[1] if pub else None},
+                                  "backend": "Burn CUDA on an RTX 4090, generic BatchHybridEngine with the hybrid "
+                                             "integrator", "source": pub[1] if pub else None},
                         roofline={"bound": "latency", "note": "the generic resident kernel's per-step block barrier "
                                   "and mean-field reductions; no DRAM or tensor roof binds (no history, 1 point per CTA)",
                                   "us_per_integration_step": ms * 1e3 / T})

@@ -17,9 +17,9 @@ The cases are the workloads' own shapes, cut to a few hundred steps:
   frequencies omega ~ N(0, 1), 3 coupling scales, BOLD on, 80 steps;
 - ``meanfield_<model>_<integrator>``: each of the six models under Heun-stochastic and RK4, 20
   nodes, all-to-all scalar coupling, the model's native parameter swept over 4 points, 120 steps;
-- ``refbench_3subnet_*``: the generic-engine workload of the reference's batch-sweep benchmark (a
-  G2DO -> JansenRit -> WilsonCowan ring of 76 or 164 nodes per population, 1000 Heun steps), over 32
-  or 8 of its I values;
+- ``refbench_3subnet_*``: the generic-engine workload of the reference's CUDA benchmark (a
+  G2DO -> JansenRit -> WilsonCowan ring of 76 or 164 nodes per population, 1000 steps with the hybrid
+  integrator), over 32 or 8 of its I values;
 - ``example_*``: the reference's own example configurations (``examples/*.toml`` with their
   ``examples/init_*_74.npy`` initial states), loaded through this package's TOML reader, run for
   their full ``sim_length`` the way its batch-sweep command runs them (``hyburn run -c <config>
@@ -306,12 +306,14 @@ def _example(config: str, sweep: Optional[str], n_points: int):
 
 
 def _refbench(nnodes: int, n_points: int):
-    """The generic-engine workload of the reference's batch-sweep benchmark
-    (examples/bench/hyburn_bench_batch_sweep.rs:18-26, 72-150): a G2DO -> JansenRit -> WilsonCowan ring,
-    each subnetwork `nnodes` nodes from a zero state with its default parameters, all-to-all Scalar
-    weights 0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1 for 1000 steps, G2DO's I swept
-    as -0.5 + i / (n - 1) (the benchmark runs 1024 points; fewer here, with the same formula)."""
+    """The generic-engine workload of the reference's CUDA benchmark, the one its published 3-population
+    times are for (examples/bench/hyburn_bench_generic_cuda.rs:21-56, 116-131): a G2DO -> JansenRit ->
+    WilsonCowan ring, each population `nnodes` nodes from a zero state with its default parameters,
+    all-to-all Scalar weights 0.01 with Linear(1.0) coupling and no delay, Heun at dt 0.1 for 1000 steps
+    with the hybrid integrator (Heun for G2DO, Euler for the others; HB_SEM_HYBRID_INTEGRATOR), G2DO's I
+    swept as -0.5 + i / (n - 1) in f32 (the benchmark runs 256 to 1024 points; fewer here)."""
     def make():
+        from hyburn_gb300._abi import HB_SEM_HYBRID_INTEGRATOR
         from hyburn_gb300.config import DEFAULT_PARAMS
         n_steps, dt, w = 1000, 0.1, 0.01
         subs = [SubnetworkConfig(m, nnodes, [0.0] * (nv * nnodes), list(DEFAULT_PARAMS[m]))
@@ -320,10 +322,10 @@ def _refbench(nnodes: int, n_points: int):
                  for s, t in ((0, 1), (1, 2), (2, 0))]
         cfg = SimConfig(sim_length=n_steps * dt, dt=dt, integrator="heun", network=NetworkConfig(subs, projs))
         f = np.float32
-        values = [float(f(-0.5) + f(i) * (f(1.0) / f(max(n_points - 1, 1)))) for i in range(n_points)]
-        return dict(cfg=cfg, n_sweep=n_points, param=SweepParam(0, 1), values=values, n_steps=n_steps, semantics=0,
-                    noise=None, rtol=1e-5, atol=1e-6, bitwise=False, bound="fp32",
-                    source="examples/bench/hyburn_bench_batch_sweep.rs (generic BatchHybridEngine workload)")
+        values = [float(f(-0.5) + f(i) / f(max(n_points - 1, 1))) for i in range(n_points)]
+        return dict(cfg=cfg, n_sweep=n_points, param=SweepParam(0, 1), values=values, n_steps=n_steps,
+                    semantics=HB_SEM_HYBRID_INTEGRATOR, noise=None, rtol=1e-5, atol=1e-6, bitwise=False, bound="fp32",
+                    source="examples/bench/hyburn_bench_generic_cuda.rs (generic BatchHybridEngine, hybrid integrator)")
     return make
 
 

@@ -136,9 +136,12 @@ def test_engine_matches_the_golden_outputs(name):
 @pytest.mark.parametrize("nodes,case", [(76, "refbench_3subnet_76n"), (164, "refbench_3subnet_164n")])
 def test_bench_ring3_workload_is_the_golden_case(nodes, case):
     """bench.py's `--workload ring3` line runs the network the golden refbench case checks (its 1024 sweep
-    values follow the same formula as the case's fewer)."""
+    values follow the same formula as the case's fewer). The bench sets the hybrid integrator after
+    creation, as the reference's benchmark does; the case creates the engine with the same flag."""
     import bench
+    from hyburn_gb300._abi import HB_SEM_HYBRID_INTEGRATOR
     g = load_case(case)
+    assert g.semantics == HB_SEM_HYBRID_INTEGRATOR
     cfg, values = bench.ring3_workload(nodes, g.n_sweep, g.n_steps)
     assert pack_config(cfg)[0] == pack_config(g.cfg)[0]
     assert np.array_equal(np.asarray(values, np.float32), g.values)
