@@ -213,6 +213,30 @@ def ring3_workload(nnodes: int, n_points: int, n_steps: int):
     return cfg, values
 
 
+# The reference's published single-model CUDA times, 256 points x 76 nodes x 1000 steps, in ms per point
+# (docs/BENCHMARK.md:50-58; Kuramoto, listed there as ~0.30, is not in the benchmark's model loop)
+SINGLE_MODEL_PUBLISHED_MS_PER_POINT = {"G2DO": 0.28, "WC": 0.35, "MPR": 0.37, "JR": 0.41}
+SINGLE_MODELS = {"G2DO": ("Generic2dOscillator", 2), "JR": ("JansenRit", 6), "WC": ("WilsonCowan", 2),
+                 "MPR": ("MontbrioPazoRoxin", 2)}
+
+
+def single_model_workload(short: str, n_points: int = 256, nnodes: int = 76):
+    """The single-model part of the reference's CUDA benchmark (examples/bench/hyburn_bench_generic_cuda.rs:
+    60-107): one population of `nnodes` uncoupled nodes (no projection) from a zero state, default
+    parameters (MPR: [1, 1, -5, 15, 0, 1, 0]), Euler at dt 0.1; parameter 1 swept (MPR: 2) as
+    -0.5 + i / (n - 1) in f32. Only G2DO's index 1 is batch-native, so for the other models the batch engine
+    ignores the sweep (dfun.rs:49-72) and every point runs the same network, as in the reference.
+    Returns (config, SweepParam indices, values)."""
+    from hyburn_gb300.config import DEFAULT_PARAMS, NetworkConfig, SimConfig, SubnetworkConfig
+    model, nvar = SINGLE_MODELS[short]
+    params = [1.0, 1.0, -5.0, 15.0, 0.0, 1.0, 0.0] if short == "MPR" else list(DEFAULT_PARAMS[model])
+    cfg = SimConfig(sim_length=10.0, dt=0.1, integrator="euler",
+                    network=NetworkConfig([SubnetworkConfig(model, nnodes, [0.0] * (nvar * nnodes), params)], []))
+    f = np.float32
+    values = [float(f(-0.5) + f(i) / f(max(n_points - 1, 1))) for i in range(n_points)]
+    return cfg, (0, 2 if short == "MPR" else 1), values
+
+
 def algorithmic_bytes_per_node_step(meta, n_points=N_POINTS) -> float:
     """Delayed reads of the coupling variable (4 B per in-edge), the ring write (4 B) and the
     shared noise draws (2 x 4 B per node per step, read once for all points)."""
@@ -611,6 +635,28 @@ def run_other_workload(args):
                         roofline={"bound": "latency", "note": "the generic resident kernel's per-step block barrier "
                                   "and mean-field reductions; no DRAM or tensor roof binds (no history, 1 point per CTA)",
                                   "us_per_integration_step": ms * 1e3 / T})
+        elif args.workload == "single-model":
+            # the single-model part of the reference's CUDA benchmark: 256 uncoupled points x 76 nodes x
+            # 1000 Euler steps, against its published ms per point
+            T, B, n = args.run_steps or 1000, 256, 76
+            cfg, (si, pi), vals = single_model_workload(args.model, B, n)
+            eng = BatchHybridEngine.from_config(cfg, B)
+            eng.prepare(SweepParam(si, pi), vals, T)
+            ms, kind = _time_prepared(eng, args.steps, args.warmup)
+            eng.close()
+            value = B * n * T / (ms / 1e3)
+            pub_ms = SINGLE_MODEL_PUBLISHED_MS_PER_POINT[args.model]
+            pub = B * n * T / (pub_ms * B / 1e3)
+            line.update(metric="node-steps/s", value=value, unit="node-steps/s", ms_per_step=ms,
+                        vs_baseline=value / pub if T == 1000 else None,
+                        config={"workload": f"{args.model.lower()}-{n}n-{B}pt-uncoupled-euler-{T}steps",
+                                "kernel_kind": kind,
+                                "source": "examples/bench/hyburn_bench_generic_cuda.rs, single-model loop"},
+                        baseline={"published_node_steps_per_s": pub, "published_ms_per_point": pub_ms,
+                                  "backend": "Burn CUDA on an RTX 4090, generic BatchHybridEngine",
+                                  "source": "docs/BENCHMARK.md:50-58"},
+                        roofline={"bound": "latency", "note": "uncoupled nodes: per-step integration only, no "
+                                  "history, no DRAM or tensor roof binds", "us_per_integration_step": ms * 1e3 / T})
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -713,8 +759,9 @@ def main():
     ap.add_argument("--stream-npt", type=int, default=0,
                     help="streamed-history kernel: nodes per consumer thread, 1/2/4 (0: engine's choice)")
     ap.add_argument("--ring-nodes", type=int, default=76, help="ring3 workload: nodes per population (76 or 164)")
+    ap.add_argument("--model", default="G2DO", choices=sorted(SINGLE_MODELS), help="single-model workload: the model")
     ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint",
-                                                          "fc", "dense", "ring3"],
+                                                          "fc", "dense", "ring3", "single-model"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()

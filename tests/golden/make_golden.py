@@ -20,6 +20,8 @@ The cases are the workloads' own shapes, cut to a few hundred steps:
 - ``refbench_3subnet_*``: the generic-engine workload of the reference's CUDA benchmark (a
   G2DO -> JansenRit -> WilsonCowan ring of 76 or 164 nodes per population, 1000 steps with the hybrid
   integrator), over 32 or 8 of its I values;
+- ``refbench_single_*``: the single-model part of the same benchmark (76 uncoupled nodes, 1000 Euler
+  steps) for G2DO, JansenRit, WilsonCowan and MPR, 16 points;
 - ``example_*``: the reference's own example configurations (``examples/*.toml`` with their
   ``examples/init_*_74.npy`` initial states), loaded through this package's TOML reader, run for
   their full ``sim_length`` the way its batch-sweep command runs them (``hyburn run -c <config>
@@ -331,6 +333,29 @@ def _refbench(nnodes: int, n_points: int):
 
 CASES["refbench_3subnet_76n"] = _refbench(76, 32)
 CASES["refbench_3subnet_164n"] = _refbench(164, 8)
+
+
+def _refbench_single(model: str, nvar: int, n_points: int):
+    """The single-model part of the reference's CUDA benchmark (examples/bench/hyburn_bench_generic_cuda.rs:
+    60-107): 76 uncoupled nodes (no projection) from a zero state, default parameters (MPR: [1, 1, -5, 15,
+    0, 1, 0]), Euler at dt 0.1 for 1000 steps, parameter 1 (MPR: 2) swept as -0.5 + i / (n - 1) in f32;
+    only G2DO's index is batch-native, so the other models' points all run the same network."""
+    def make():
+        from hyburn_gb300.config import DEFAULT_PARAMS
+        params = [1.0, 1.0, -5.0, 15.0, 0.0, 1.0, 0.0] if model == "MontbrioPazoRoxin" else list(DEFAULT_PARAMS[model])
+        cfg = SimConfig(sim_length=10.0, dt=0.1, integrator="euler",
+                        network=NetworkConfig([SubnetworkConfig(model, 76, [0.0] * (nvar * 76), params)], []))
+        f = np.float32
+        values = [float(f(-0.5) + f(i) / f(max(n_points - 1, 1))) for i in range(n_points)]
+        return dict(cfg=cfg, n_sweep=n_points, param=SweepParam(0, 2 if model == "MontbrioPazoRoxin" else 1),
+                    values=values, n_steps=1000, semantics=0, noise=None, rtol=1e-5, atol=1e-6, bitwise=False,
+                    bound="fp32", source="examples/bench/hyburn_bench_generic_cuda.rs (single-model loop)")
+    return make
+
+
+for _short, (_m, _nv) in {"g2do": ("Generic2dOscillator", 2), "jr": ("JansenRit", 6), "wc": ("WilsonCowan", 2),
+                          "mpr": ("MontbrioPazoRoxin", 2)}.items():
+    CASES[f"refbench_single_{_short}"] = _refbench_single(_m, _nv, 16)
 
 EXAMPLES = {
     "example_g2do_sweep": ("g2do_sweep.toml", "sweep.toml", 128),

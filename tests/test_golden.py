@@ -145,3 +145,14 @@ def test_bench_ring3_workload_is_the_golden_case(nodes, case):
     cfg, values = bench.ring3_workload(nodes, g.n_sweep, g.n_steps)
     assert pack_config(cfg)[0] == pack_config(g.cfg)[0]
     assert np.array_equal(np.asarray(values, np.float32), g.values)
+
+
+@pytest.mark.parametrize("model", ["G2DO", "JR", "WC", "MPR"])
+def test_bench_single_model_workload_is_the_golden_case(model):
+    """bench.py's `--workload single-model` line runs the network the golden refbench_single case checks."""
+    import bench
+    g = load_case(f"refbench_single_{model.lower()}")
+    cfg, (si, pi), values = bench.single_model_workload(model, g.n_sweep, 76)
+    assert pack_config(cfg)[0] == pack_config(g.cfg)[0]
+    assert (si, pi) == (g.param.sub_idx, g.param.param_idx)
+    assert np.array_equal(np.asarray(values, np.float32), g.values)
