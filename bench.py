@@ -237,6 +237,23 @@ def single_model_workload(short: str, n_points: int = 256, nnodes: int = 76):
     return cfg, (0, 2 if short == "MPR" else 1), values
 
 
+# The reference's published parameter-sweep times of its example configurations on Burn CUDA (RTX 4090),
+# 128 points x 74 nodes x 10 000 steps: (node-steps/s, source); the configurations and sweep values are
+# those of the committed golden fixtures example_g2do_sweep and example_mpr_sweep
+EXAMPLE_SWEEP_PUBLISHED = {"g2do": (5.20e7, "docs/BENCHMARK_EXAMPLES.md:32 (1.82 s)"),
+                           "mpr": (3.66e7, "docs/BENCHMARK_EXAMPLES.md:33 (2.59 s)")}
+
+
+def example_sweep_case(name: str):
+    """The reference's example sweep (examples/g2do_sweep.toml with examples/sweep.toml, or
+    examples/mpr_sweep.toml with examples/sweep_mpr.toml) as stored in the golden fixture."""
+    tests = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests")
+    if tests not in sys.path:
+        sys.path.insert(0, tests)
+    from golden.make_golden import load_case
+    return load_case({"g2do": "example_g2do_sweep", "mpr": "example_mpr_sweep"}[name])
+
+
 def algorithmic_bytes_per_node_step(meta, n_points=N_POINTS) -> float:
     """Delayed reads of the coupling variable (4 B per in-edge), the ring write (4 B) and the
     shared noise draws (2 x 4 B per node per step, read once for all points)."""
@@ -657,6 +674,42 @@ def run_other_workload(args):
                                   "source": "docs/BENCHMARK.md:50-58"},
                         roofline={"bound": "latency", "note": "uncoupled nodes: per-step integration only, no "
                                   "history, no DRAM or tensor roof binds", "us_per_integration_step": ms * 1e3 / T})
+        elif args.workload == "example-sweep":
+            # the reference's example parameter sweeps, against its published Burn CUDA times; `value` is the
+            # device-resident run, `e2e` the public run_sweep call with host values and host results
+            case = example_sweep_case(args.example)
+            from hyburn_gb300._abi import MODEL_INFO
+            B, n = case.n_sweep, case.cfg.network.subnetworks[0].nnodes
+            nvar = MODEL_INFO[case.cfg.network.subnetworks[0].model][0]
+            T = args.run_steps or case.n_steps
+            eng = BatchHybridEngine.from_config(case.cfg, B)
+            eng.prepare(case.param, case.values, T)
+            ms, kind = _time_prepared(eng, args.steps, args.warmup)
+            eng.close()
+            eng2 = BatchHybridEngine.from_config(case.cfg, B)
+            for _ in range(max(1, args.warmup)):
+                eng2.reset()
+                eng2.run_sweep(case.param, case.values, T)
+            wall = []
+            for _ in range(args.steps):
+                eng2.reset()
+                t0 = time.perf_counter()
+                eng2.run_sweep(case.param, case.values, T)
+                wall.append(time.perf_counter() - t0)
+            eng2.close()
+            ns = B * n * T
+            value, pub = ns / (ms / 1e3), EXAMPLE_SWEEP_PUBLISHED[args.example]
+            line.update(metric="node-steps/s", value=value, unit="node-steps/s", ms_per_step=ms,
+                        vs_baseline=value / pub[0] if T == case.n_steps else None,
+                        e2e={"value": ns / statistics.median(wall), "unit": "node-steps/s",
+                             "h2d_bytes_per_step": 4 * B, "d2h_bytes_per_step": 2 * 4 * B * n * nvar},
+                        config={"workload": f"example-{args.example}-sweep-{n}n-{B}pt-{T}steps", "kernel_kind": kind,
+                                "source": case.source},
+                        baseline={"published_node_steps_per_s": pub[0], "backend": "Burn CUDA on an RTX 4090",
+                                  "source": pub[1]},
+                        roofline={"bound": "latency", "note": "mean-field coupling without delay: per-step work "
+                                  "of one warp per point, no history, no DRAM or tensor roof binds",
+                                  "us_per_integration_step": ms * 1e3 / T})
         elif args.workload == "fc":
             # the benchmark sweep (G2DO 74 nodes x 128 points, per-edge delays, Heun-stochastic) with its
             # trajectory kept in HBM and FC / FCD features computed there (windows of 2 000 steps, stride
@@ -760,8 +813,11 @@ def main():
                     help="streamed-history kernel: nodes per consumer thread, 1/2/4 (0: engine's choice)")
     ap.add_argument("--ring-nodes", type=int, default=76, help="ring3 workload: nodes per population (76 or 164)")
     ap.add_argument("--model", default="G2DO", choices=sorted(SINGLE_MODELS), help="single-model workload: the model")
+    ap.add_argument("--example", default="g2do", choices=sorted(EXAMPLE_SWEEP_PUBLISHED),
+                    help="example-sweep workload: the reference's example sweep")
     ap.add_argument("--workload", default="sweep", choices=["sweep", "single", "uneven", "adjoint", "kuramoto", "kuramoto-adjoint",
-                                                          "fc", "dense", "ring3", "single-model"],
+                                                          "fc", "dense", "ring3", "single-model",
+                                                          "example-sweep"],
                     help="sweep: the 128-point batched sweep (default); the others are the remaining "
                          "measured configurations, one JSON line each")
     args = ap.parse_args()
