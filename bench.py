@@ -505,7 +505,14 @@ def run_other_workload(args):
             eng = BatchHybridEngine.from_config(cfg, 1)
             eng.prepare(SweepParam(0, 1), [cfg.network.subnetworks[0].params[1]], T)
             ms, kind = _time_prepared(eng, args.steps, args.warmup)
-            line.update(metric="node-steps/s", value=74 * T / (ms / 1e3), unit="node-steps/s", ms_per_step=ms,
+            value = 74 * T / (ms / 1e3)
+            # published for examples/g2do_simple.toml, the same network and steps (its initial state from
+            # examples/init_g2do_74.npy): CUDA 4.44 s, CPU 0.67 s (docs/BENCHMARK_EXAMPLES.md:15)
+            pub_cuda, pub_cpu = 74 * 10_000 / 4.44, 74 * 10_000 / 0.67
+            line.update(metric="node-steps/s", value=value, unit="node-steps/s", ms_per_step=ms,
+                        vs_baseline=value / pub_cuda if T == 10_000 else None,
+                        baseline={"published_node_steps_per_s": pub_cuda, "backend": "Burn CUDA on an RTX 4090 (serial engine)",
+                                  "published_cpu_node_steps_per_s": pub_cpu, "source": "docs/BENCHMARK_EXAMPLES.md:15"},
                         config={"workload": f"g2do-74n-1pt-meanfield-heun-{T}steps", "kernel_kind": kind},
                         roofline={"bound": "latency", "note": "one point on one SM; no roofline fraction",
                                   "us_per_integration_step": ms * 1e3 / T})

@@ -365,6 +365,7 @@ EXAMPLES = {
     "example_two_population_coupled": ("two_population_coupled.toml", "sweep.toml", 8),
     "example_whole_brain_multi_model": ("whole_brain_multi_model.toml", "sweep.toml", 8),
     "example_wilson_cowan_ring": ("wilson_cowan_ring.toml", None, 1),
+    "example_g2do_simple": ("g2do_simple.toml", None, 1),
     "example_jansen_rit_evoked": ("jansen_rit_evoked.toml", None, 1),
 }
 for _n, (_c, _s, _p) in EXAMPLES.items():
